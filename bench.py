@@ -1,0 +1,389 @@
+#!/usr/bin/env python
+"""Walker-update benchmark: PageRank walks on an R-MAT scale-24 graph.
+
+Workload (one "step"): W = |V| walkers, one per non-isolated vertex, stop
+probability 0.15 after every move, every position counted into uint32 visit
+counts; graph = R-MAT scale 24, edge factor 16, a/b/c/d = .57/.19/.19/.05,
+seed 1, symmetrised with self-loops, duplicates and isolated vertices
+removed (synthetic, built on the device).  Each step uses a new seed.
+
+  value     walker steps/s with the graph resident in HBM (device output)
+  e2e       the same through the host-facing C ABI call ptw_pagerank,
+            counts read back into pinned host memory every step
+  roofline  random-gather bound: 64 B per move (row record + column
+            sector) + 32 B per counted visit, against the measured HBM peak
+  cpu_baseline  the oracle port (C, all host threads) on a bounded sample of
+            the same workload
+
+--impl reference times the reference's walker semantics on the host CPU
+(the oracle port; the reference's own sources do not exist on the GPU host)
+for the same metric and config.  Under torchrun, rank r runs walkers
+[r|V|, (r+1)|V|) (weak scaling; every rank replicates the graph) and the
+count vectors are summed with one NCCL all_reduce per step.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "walker steps/s (PageRank walks, R-MAT scale 24)"
+UNIT = "steps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--scale", type=int, default=24)
+    p.add_argument("--edge-factor", type=int, default=16)
+    p.add_argument("--sp", type=float, default=0.15)
+    p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--walk-len", type=int, default=80, help="DeepWalk length for the side line")
+    p.add_argument("--no-deepwalk", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-autotune", action="store_true")
+    return p.parse_args()
+
+
+def config(args, world):
+    return {"workload": "pagerank walks, R-MAT scale %d (edge factor %d, a/b/c .57/.19/.19, seed %d, "
+                        "cleaned), W=|V| one walker per vertex, sp=%g"
+                        % (args.scale, args.edge_factor, args.seed, args.sp),
+            "graph": "rmat-s%d-ef%d" % (args.scale, args.edge_factor),
+            "walkers_per_gpu": "|V|", "sp": args.sp, "parallelism": "walker-shard x%d" % world,
+            "l2": "inputs exceed L2 (CSR column array > 2 GB, L2 129 MB); no flush"}
+
+
+# ---- clocks ---------------------------------------------------------------
+
+class Clocks:
+    """nvidia-smi samples during the timed region (read-only queries)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return out
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        out.update(sm_mhz=sm[len(sm) // 2] if sm else None, sm_max_mhz=max(mx) if mx else None,
+                   reasons=sorted(reasons), samples=len(rows))
+        return out
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---- CPU baseline (oracle port) ---------------------------------------------
+
+def cpu_port_run(canon, sp, seed, n_walkers, threads):
+    import oracle
+    t0 = time.perf_counter()
+    _, moves = oracle.replay_counts(canon, 0, n_walkers, sp, seed, 0, threads=threads)
+    dt = time.perf_counter() - t0
+    return moves, dt
+
+
+def cpu_port_sample(canon, sp, seed, threads, target_s=2.0):
+    """Times the port on the first S walkers of the workload, S sized so a run
+    takes about target_s seconds of wall time (at least one calibration)."""
+    n = canon.n
+    probe = min(n, 200000)
+    moves, dt = cpu_port_run(canon, sp, seed, probe, threads)
+    S = probe
+    if dt > 0:
+        S = int(min(n, max(probe, probe * target_s / dt)))
+    if S > probe:
+        moves, dt = cpu_port_run(canon, sp, seed, S, threads)
+    return S, moves, dt
+
+
+# ---- reference arm ------------------------------------------------------------
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return 0
+    import oracle
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    canon = oracle.rmat_clean_csr(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed, threads)
+    build_s = time.perf_counter() - t0
+    S, _, _ = cpu_port_sample(canon, args.sp, args.seed, threads, target_s=2.0)
+    for k in range(args.warmup):
+        cpu_port_run(canon, args.sp, 1000 + k, S, threads)
+    tot_moves, tot_s = 0, 0.0
+    for k in range(args.steps):
+        mv, dt = cpu_port_run(canon, args.sp, 2000 + k, S, threads)
+        tot_moves += mv
+        tot_s += dt
+    value = tot_moves / tot_s
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * tot_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": config(args, world), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "first %d of %d walkers per step (per-vertex starts) of the same "
+                                   "workload; graph built on the host in %.1f s"
+                                   % (S, canon.n, build_s)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---- our arm ----------------------------------------------------------------------
+
+def tune_cache_path():
+    return os.path.join(ROOT, "ptwalker_gb300", "_lib", "tune_cache.json")
+
+
+def get_tune(G, ptw, args, dev_name):
+    key = "%s|s%d|ef%d|seed%d|n%d|m%d|sp%g" % (dev_name, args.scale, args.edge_factor, args.seed,
+                                               G.n, G.m, args.sp)
+    path = tune_cache_path()
+    cache = {}
+    if os.path.exists(path):
+        try:
+            cache = json.load(open(path))
+        except Exception:
+            cache = {}
+    if key in cache:
+        G.tune = ptw.Tune(**cache[key])
+        return G.tune, "cache"
+    if args.no_autotune:
+        return G.tune, "default"
+    t = G.autotune(args.sp, 0)
+    cache[key] = t.as_dict()
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        with open(path, "w") as f:
+            json.dump(cache, f, indent=1)
+    except Exception:
+        pass
+    return t, "autotune"
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import ptwalker_gb300 as ptw
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev_name = torch.cuda.get_device_name(local)
+
+    t0 = time.perf_counter()
+    G = ptw.Graph.rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, seed=args.seed, clean=True)
+    build_s = time.perf_counter() - t0
+    tune, tune_src = get_tune(G, ptw, args, dev_name)
+    stream = torch.cuda.Stream()
+    G.set_stream(stream)
+    n = G.n
+    first = rank * n
+    d_counts = torch.empty(G.id_bound, dtype=torch.int32, device="cuda")
+    seeds = [args.seed * 7919 + 100 + k for k in range(args.steps)]
+
+    def step(seed, out):
+        ptw.pagerank(G, n, args.sp, seed, "per_vertex", out=out, first_walker=first)
+        if world > 1:
+            with torch.cuda.stream(stream):
+                dist.all_reduce(d_counts)
+
+    for k in range(args.warmup):
+        step(10 + k, d_counts)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+
+    clocks = Clocks(local)
+    clocks.start()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    evs[0].record(stream)
+    for k in range(args.steps):
+        step(seeds[k], d_counts)
+        evs[k + 1].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    per_step = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    t_ms = evs[0].elapsed_time(evs[-1])
+    if world > 1:
+        tt = torch.tensor([t_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+
+    # moves of each timed step (a pure function of the seed: re-run with stats)
+    moves, kern_ms = [], []
+    for k in range(args.steps):
+        _, st = ptw.pagerank(G, n, args.sp, seeds[k], "per_vertex", out=d_counts,
+                             first_walker=first, stats=True)
+        moves.append(st.moves)
+        kern_ms.append(st.kernel_ms)
+    total_moves = sum(moves) * world
+    value = total_moves / (t_ms / 1000.0)
+
+    # roofline of the walk kernel: 64 B per move + 32 B per counted visit
+    bytes_per_launch = [64 * mv + 32 * (n + mv) for mv in moves]
+    launch_ms = sum(per_step) / len(per_step)
+    achieved = (sum(bytes_per_launch) / len(bytes_per_launch)) / (launch_ms / 1000.0) / 1e9
+    peak, peak_kind = measured_peaks()
+
+    # e2e through the host-facing call: counts copied into pinned host memory
+    e2e = None
+    if world == 1:
+        host = torch.empty(G.id_bound, dtype=torch.int32, pin_memory=True)
+        for k in range(2):
+            ptw.pagerank(G, n, args.sp, 10 + k, "per_vertex", out=host)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        e0.record(stream)
+        for k in range(args.steps):
+            ptw.pagerank(G, n, args.sp, seeds[k], "per_vertex", out=host)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+        e_ms = e0.elapsed_time(e1)
+        e2e = {"value": sum(moves) / (e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": 0,
+               "d2h_bytes_per_step": 4 * G.id_bound, "host_wall_value": sum(moves) / wall}
+
+    # DeepWalk side line: one walker per vertex, L = walk_len, paths in HBM
+    deepwalk = None
+    if not args.no_deepwalk and world == 1:
+        L = args.walk_len
+        paths = torch.empty((n, L), dtype=torch.int32, device="cuda")
+        ptw.deepwalk(G, n, L, 5, out=paths)
+        d0 = torch.cuda.Event(enable_timing=True)
+        d1 = torch.cuda.Event(enable_timing=True)
+        reps = max(2, min(args.steps, 5))
+        torch.cuda.synchronize()
+        d0.record(stream)
+        for k in range(reps):
+            ptw.deepwalk(G, n, L, 50 + k, out=paths)
+        d1.record(stream)
+        torch.cuda.synchronize()
+        dms = d0.elapsed_time(d1) / reps
+        dsteps = n * (L - 1)
+        dbytes = 64 * dsteps + 4 * n * L
+        deepwalk = {"walk_len": L, "walkers": n, "steps_per_s": dsteps / (dms / 1000.0),
+                    "ms_per_step": dms, "achieved_gbs": dbytes / (dms / 1000.0) / 1e9,
+                    "frac": dbytes / (dms / 1000.0) / 1e9 / peak,
+                    "path_bytes": 4 * n * L}
+        del paths
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        names, row_ptr, col = G.export_csr()
+        import oracle
+        canon = oracle.CanonicalGraph(names=names, row_ptr=row_ptr, col=col)
+        threads = os.cpu_count() or 1
+        S, mv, dt = cpu_port_sample(canon, args.sp, 4242, threads, target_s=3.0)
+        cpu = {"value": mv / dt, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "first %d of %d walkers (per-vertex starts) of the same workload, %d moves "
+                         "in %.2f s" % (S, n, mv, dt)}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": config(args, world),
+        "e2e": e2e,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_kind": peak_kind,
+                     "bytes_per_launch": sum(bytes_per_launch) / len(bytes_per_launch),
+                     "launch_ms": launch_ms, "walk_kernel_ms": sum(kern_ms) / len(kern_ms)},
+        "cpu_baseline": cpu,
+        "gpu_launches": args.steps * 2,  # k_walk + k_counts_by_name per step
+        "clocks": clk,
+        "graph": {"vertices": n, "edges": G.m, "max_degree": G.max_degree, "build_s": build_s,
+                  "device_bytes": G.device_bytes},
+        "tune": dict(tune.as_dict(), source=tune_src),
+        "moves_per_step": sum(moves) / len(moves),
+        "deepwalk": deepwalk,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    G.set_stream(None)
+    G.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,185 @@
+/*
+ * ptw.h -- C ABI of the GB300 random-walk engine (libptw.so).
+ *
+ * The reference (PTWalker, a FlashMob fork) has no C ABI: its "plugin API" is
+ * the compile-time app template passed to
+ *     walk(FMobSolver*, uint64_t walker_num, int walk_len, uint64_t mem_quota,
+ *          Alg& myapp, uint16_t walker_size)          src/core/solver.hpp:1049-1074
+ * with the graph from
+ *     Graph::load(path, GraphFormat, as_undirected, degree_boundary)
+ *                                                      src/core/graph.hpp:277
+ * and the apps pagerank (src/core/pagerank.cpp:10-90), PPR
+ * (src/core/ppr.cpp:10-118), RWR (src/core/RWR.cpp:15-106) and DeepWalk
+ * (src/core/deepwalk.cpp:10-41).  Each entry point below replaces one of
+ * those pieces; the citation is on the declaration.
+ *
+ * Conventions
+ *   - Status codes: PTW_OK (0) or a negative PTW_E* value; the message of the
+ *     last failure on the calling thread is returned by ptw_last_error().
+ *     No entry point aborts the process (the reference CHECK-aborts).
+ *   - Vertex names are the u32 ids of the edge list.  Outputs indexed "by
+ *     name" have id_bound = (largest name + 1) entries; names that do not
+ *     occur in the graph read 0.
+ *   - A ptw_graph owns its device memory and one CUDA stream.  A handle must
+ *     not be used from two host threads at once.
+ *   - Pointers named h_* are host memory; pointers named d_* are device
+ *     memory on the graph's device.  Any host buffer works; pinned buffers
+ *     copy faster.
+ */
+#ifndef PTW_H
+#define PTW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PTW_OK 0
+#define PTW_EINVAL (-1)   /* invalid argument */
+#define PTW_ENOMEM (-2)   /* device or host allocation refused */
+#define PTW_ECUDA (-3)    /* CUDA runtime error */
+#define PTW_ETIMEOUT (-4) /* a bounded device-side wait gave up */
+#define PTW_EIO (-5)      /* file could not be read or parsed */
+#define PTW_EFULL (-6)    /* a device table has no free capacity */
+
+#define PTW_FMT_BINARY 0  /* raw Edge{u32 src; u32 dst}[]   include/io.hpp:39-53 */
+#define PTW_FMT_TEXT 1    /* "%u %u" lines, '#' comments    include/io.hpp:76-90 */
+
+#define PTW_START_PER_VERTEX 0 /* walker w starts at the (w mod n)-th vertex by ascending name */
+#define PTW_START_UNIFORM 1    /* uniform over vertices, with replacement (pagerank.cpp:70-80) */
+#define PTW_START_SOURCES 2    /* uniform over a source list; one source = PPR (ppr.cpp:91-108) */
+
+typedef struct ptw_graph ptw_graph;
+
+typedef struct ptw_graph_info {
+    uint32_t n_vertices;   /* distinct names in the edge list */
+    uint32_t id_bound;     /* largest name + 1 */
+    uint64_t n_edges;      /* CSR entries (directed edges after as_undirected) */
+    uint32_t max_degree;
+    uint32_t reserved;
+    uint64_t device_bytes; /* resident device memory held by the graph */
+} ptw_graph_info;
+
+/* Walk configuration: the flag set -w / --sp / -l of the reference
+ * (include/option.hpp:227-302) plus a seed and a start mode. */
+typedef struct ptw_walk_cfg {
+    uint64_t n_walkers;        /* -w */
+    double sp;                 /* --sp: stop probability after each move, 0 < sp <= 1 */
+    uint64_t seed;
+    int32_t start_mode;        /* PTW_START_* */
+    uint32_t max_moves;        /* 0 = unbounded (geometric length only) */
+    const uint32_t *h_sources; /* names, for PTW_START_SOURCES */
+    uint32_t n_sources;
+    uint32_t reserved;
+    uint64_t first_walker;     /* global id of the first walker: walkers are
+                                  first_walker .. first_walker + n_walkers - 1.
+                                  Every draw depends on the global id only, so
+                                  a run split into shards equals the whole run;
+                                  PPR query q uses first_walker = q << 32. */
+} ptw_walk_cfg;
+
+typedef struct ptw_walk_stats {
+    uint64_t walkers;  /* walkers run */
+    uint64_t moves;    /* edge traversals (walker steps) */
+    uint64_t visits;   /* counted positions = walkers + moves for count apps */
+    float kernel_ms;   /* device time of the walk kernel */
+    float total_ms;    /* device time of the whole call, copies included */
+} ptw_walk_stats;
+
+/* Launch parameters of the walk kernels (chosen by ptw_autotune). */
+typedef struct ptw_tune {
+    int32_t block;         /* threads per block (multiple of 32) */
+    int32_t ilp;           /* walkers held per thread: 1, 2 or 4 */
+    int32_t chunk;         /* walker ids taken per warp refill */
+    int32_t hot_k;         /* vertex ids < hot_k counted in shared memory (0 = off) */
+    int32_t blocks_per_sm; /* 0 = as many as fit */
+    int32_t reserved;
+} ptw_tune;
+
+const char *ptw_last_error(void);
+const char *ptw_version(void);
+
+/* ---- graph ------------------------------------------------------------ */
+
+/* Replaces Graph::load (src/core/graph.hpp:277-785) with read_text_graph /
+ * read_binary_graph (include/io.hpp:39-90).  Builds a degree-sorted device
+ * CSR in place of the NUMA/cache partitioner. */
+int ptw_graph_load(const char *path, int32_t fmt, int32_t as_undirected, ptw_graph **out);
+
+/* Same as ptw_graph_load from in-memory edge arrays (graph.hpp:284-318). */
+int ptw_graph_from_edges(const uint32_t *h_src, const uint32_t *h_dst, uint64_t m,
+                         int32_t as_undirected, ptw_graph **out);
+
+/* Synthetic R-MAT graph built on the device (no reference counterpart; the
+ * reference reads files only).  2^scale * edge_factor raw edges with
+ * quadrant probabilities a, b, c, 1-a-b-c; clean != 0 symmetrises, drops
+ * self-loops, duplicates and isolated vertices and renames vertices 0..n-1. */
+int ptw_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                   uint64_t seed, int32_t clean, ptw_graph **out);
+
+int ptw_graph_get_info(const ptw_graph *g, ptw_graph_info *info);
+
+/* Canonical CSR: vertex i = i-th smallest name, rows list neighbour
+ * indices ascending.  Any output pointer may be NULL. */
+int ptw_graph_export_csr(const ptw_graph *g, uint32_t *h_names /*[n]*/,
+                         uint64_t *h_row_ptr /*[n+1]*/, uint32_t *h_col /*[m]*/);
+
+/* Sorted edge list by (src, dst) name: the text/binary writer input
+ * (include/io.hpp:55-74, :92-105). */
+int ptw_graph_export_edges(const ptw_graph *g, uint32_t *h_src, uint32_t *h_dst);
+
+void ptw_graph_free(ptw_graph *g);
+
+int ptw_graph_set_tune(ptw_graph *g, const ptw_tune *t);
+int ptw_graph_get_tune(const ptw_graph *g, ptw_tune *t);
+
+/* ---- walks ------------------------------------------------------------ */
+
+/* Visit counting: pagerank (src/core/pagerank.cpp:86-89) and single-source
+ * PPR (src/core/ppr.cpp:114-117) driven by the solver loop
+ * (src/core/solver.hpp:242-263).  Counts every position, start included,
+ * into h_counts[id_bound] by name. */
+int ptw_pagerank(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_counts,
+                 ptw_walk_stats *stats);
+
+/* Device variant: d_counts[id_bound] receives the counts by name.  Runs on
+ * the graph's stream and does not synchronise unless stats != NULL. */
+int ptw_pagerank_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_counts,
+                     ptw_walk_stats *stats);
+
+/* RWR endpoint app (src/core/RWR.cpp:76-105, type=1 loop at
+ * src/core/solver.hpp:284-306): h_pairs[2*w] = start name, h_pairs[2*w+1] =
+ * name after the last move, for w in [0, n_walkers). */
+int ptw_rwr(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_pairs, ptw_walk_stats *stats);
+int ptw_rwr_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_pairs, ptw_walk_stats *stats);
+
+/* DeepWalk (src/core/deepwalk.cpp:25-37): n_walkers walks of L vertices
+ * (L-1 moves), written as names into h_paths[n_walkers * L] (row-major,
+ * int32).  A walk that reaches a vertex without out-edges is padded with -1.
+ * cfg->sp and cfg->max_moves are ignored. */
+int ptw_deepwalk(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *h_paths,
+                 ptw_walk_stats *stats);
+int ptw_deepwalk_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *d_paths,
+                     ptw_walk_stats *stats);
+
+/* Synchronise the graph's stream. */
+int ptw_graph_sync(ptw_graph *g);
+
+/* Run the graph's work on a caller-owned cudaStream_t from now on (NULL
+ * returns to the graph's own stream), so callers can order and time it with
+ * their own events.  No reference counterpart (the reference is CPU-only). */
+int ptw_graph_set_stream(ptw_graph *g, void *cuda_stream);
+
+/* Autotuner (the idea of the sampler micro-benchmark cache,
+ * src/core/mini_bmk.hpp:62-117): times the count walk over candidate
+ * launch parameters on this graph and device, stores the fastest in the
+ * graph and returns it. n_walkers = 0 means one walker per vertex. */
+int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tune *best);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PTW_H */

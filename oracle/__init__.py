@@ -1,0 +1,46 @@
+"""CPU oracle for the walker-update path -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this package, and only as a checker.  The GPU engine in
+``ptwalker_gb300`` never imports it.
+
+Contents
+  * ``oracle.c`` (built to ``oracle/_build/liboracle.so``): Philox4x32-10,
+    raw R-MAT edges, walker replay for counts / endpoints / paths.
+  * ``graph.py``: canonical graph layout (names, CSR in index space) and the
+    R-MAT clean-up pipeline, restating the reference loader's semantics.
+  * ``power.py``: FP64 power iteration and the exact expected-visit formulas.
+
+Parity pins: Philox is checked against the SC'11 known-answer vector and,
+on the GPU, against cuRAND's Philox4_32_10; the walker semantics are checked
+statistically against the reference binary built from its own sources
+(``oracle/ref``) and against the FP64 expectation.
+"""
+from .lib import load_lib, build_lib  # noqa: F401
+from .graph import (  # noqa: F401
+    CanonicalGraph,
+    canonical_from_edges,
+    rmat_raw_edges,
+    rmat_clean_edges,
+    rmat_clean_csr,
+    rmat_thresholds,
+    read_edge_file,
+    write_text_edges,
+    write_binary_edges,
+)
+from .replay import (  # noqa: F401
+    philox4x32_10,
+    replay_counts,
+    replay_pairs,
+    replay_paths,
+    sp_threshold,
+    TAG_WALK,
+    TAG_START,
+    TAG_RMAT,
+)
+from .power import (  # noqa: F401
+    ppr_vector,
+    expected_visits_from_source,
+    expected_visits_per_vertex_start,
+    expected_endpoint_from_source,
+)

@@ -1,0 +1,87 @@
+"""Python wrappers over the C walker replay (test infrastructure).
+
+The semantics are documented at the top of ``oracle/oracle.c``.  All
+results are in canonical index space (see ``oracle/graph.py``).
+"""
+import ctypes
+
+import numpy as np
+
+from .lib import load_lib
+
+TAG_WALK = 0x57414C4B
+TAG_START = 0x53545254
+TAG_RMAT = 0x524D4154
+
+START_PER_VERTEX, START_UNIFORM, START_SOURCES = 0, 1, 2
+
+
+def sp_threshold(sp):
+    """Stop after a move iff the 32-bit draw is below floor(sp * 2^32)."""
+    return min(int(sp * 4294967296.0), 1 << 32)
+
+
+def _p(arr, ctype):
+    if arr is None:
+        return None
+    return arr.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def philox4x32_10(ctr, key):
+    lib = load_lib()
+    c = np.asarray(ctr, dtype=np.uint32)
+    k = np.asarray(key, dtype=np.uint32)
+    out = np.zeros(4, dtype=np.uint32)
+    lib.ora_philox4x32_10(_p(c, ctypes.c_uint32), _p(k, ctypes.c_uint32), _p(out, ctypes.c_uint32))
+    return out
+
+
+def _sources_arg(g, start_mode, sources):
+    if start_mode != START_SOURCES:
+        return None, 0
+    idx = g.name_to_index(sources)
+    return np.ascontiguousarray(idx, dtype=np.uint32), int(idx.shape[0])
+
+
+def replay_counts(g, w_begin, w_end, sp, seed, start_mode=START_PER_VERTEX,
+                  sources=None, max_moves=0, threads=1):
+    """Visit counts over vertex indices and the total number of moves."""
+    lib = load_lib()
+    counts = np.zeros(g.n, dtype=np.uint32)
+    src_arr, n_src = _sources_arg(g, start_mode, sources)
+    total = lib.ora_replay_walks(
+        _p(g.row_ptr, ctypes.c_uint64), _p(g.col, ctypes.c_uint32), g.n,
+        w_begin, w_end, sp_threshold(sp), seed, start_mode,
+        _p(src_arr, ctypes.c_uint32), n_src, max_moves,
+        _p(counts, ctypes.c_uint32), None, None, threads)
+    return counts, int(total)
+
+
+def replay_pairs(g, w_begin, w_end, sp, seed, start_mode=START_PER_VERTEX,
+                 sources=None, max_moves=0, threads=1):
+    """(start, end) vertex indices per walker and the move count per walker."""
+    lib = load_lib()
+    nw = w_end - w_begin
+    pairs = np.zeros((nw, 2), dtype=np.uint32)
+    moves = np.zeros(nw, dtype=np.uint32)
+    src_arr, n_src = _sources_arg(g, start_mode, sources)
+    lib.ora_replay_walks(
+        _p(g.row_ptr, ctypes.c_uint64), _p(g.col, ctypes.c_uint32), g.n,
+        w_begin, w_end, sp_threshold(sp), seed, start_mode,
+        _p(src_arr, ctypes.c_uint32), n_src, max_moves,
+        None, _p(pairs, ctypes.c_uint32), _p(moves, ctypes.c_uint32), threads)
+    return pairs, moves
+
+
+def replay_paths(g, w_begin, w_end, L, seed, start_mode=START_PER_VERTEX,
+                 sources=None, threads=1):
+    """[walkers, L] int32 vertex indices (-1 after a dead end)."""
+    lib = load_lib()
+    nw = w_end - w_begin
+    paths = np.zeros((nw, L), dtype=np.int32)
+    src_arr, n_src = _sources_arg(g, start_mode, sources)
+    lib.ora_replay_paths(
+        _p(g.row_ptr, ctypes.c_uint64), _p(g.col, ctypes.c_uint32), g.n,
+        w_begin, w_end, L, seed, start_mode, _p(src_arr, ctypes.c_uint32), n_src,
+        _p(paths, ctypes.c_int32), threads)
+    return paths

@@ -1,0 +1,25 @@
+"""GB300-native random-walk engine with PTWalker's app surface.
+
+The walker-update path (neighbour pick, geometric / fixed-length
+termination, visit counting, endpoint and path recording) runs as
+hand-written sm_103a CUDA kernels in libptw.so behind the C ABI in
+include/ptw.h; this package is the Python host mirror of that ABI.
+"""
+from ._capi import PTWError, load as load_library, lib_path  # noqa: F401
+from .api import (  # noqa: F401
+    Graph,
+    Tune,
+    WalkStats,
+    pagerank,
+    ppr,
+    rwr,
+    deepwalk,
+    PageRankApp,
+    PPRApp,
+    RWRApp,
+    DeepWalkApp,
+    Solver,
+    walk,
+)
+
+__version__ = "0.1.0"

@@ -1,0 +1,121 @@
+"""ctypes binding of libptw.so (declarations mirror include/ptw.h)."""
+import ctypes
+import os
+
+from . import _build
+
+PTW_OK = 0
+PTW_EINVAL = -1
+PTW_ENOMEM = -2
+PTW_ECUDA = -3
+PTW_ETIMEOUT = -4
+PTW_EIO = -5
+PTW_EFULL = -6
+
+PTW_FMT_BINARY = 0
+PTW_FMT_TEXT = 1
+
+PTW_START_PER_VERTEX = 0
+PTW_START_UNIFORM = 1
+PTW_START_SOURCES = 2
+
+_ERRNAMES = {PTW_EINVAL: "PTW_EINVAL", PTW_ENOMEM: "PTW_ENOMEM", PTW_ECUDA: "PTW_ECUDA",
+             PTW_ETIMEOUT: "PTW_ETIMEOUT", PTW_EIO: "PTW_EIO", PTW_EFULL: "PTW_EFULL"}
+
+
+class GraphInfo(ctypes.Structure):
+    _fields_ = [("n_vertices", ctypes.c_uint32), ("id_bound", ctypes.c_uint32),
+                ("n_edges", ctypes.c_uint64), ("max_degree", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64)]
+
+
+class WalkCfg(ctypes.Structure):
+    _fields_ = [("n_walkers", ctypes.c_uint64), ("sp", ctypes.c_double),
+                ("seed", ctypes.c_uint64), ("start_mode", ctypes.c_int32),
+                ("max_moves", ctypes.c_uint32), ("h_sources", ctypes.POINTER(ctypes.c_uint32)),
+                ("n_sources", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("first_walker", ctypes.c_uint64)]
+
+
+class WalkStats(ctypes.Structure):
+    _fields_ = [("walkers", ctypes.c_uint64), ("moves", ctypes.c_uint64),
+                ("visits", ctypes.c_uint64), ("kernel_ms", ctypes.c_float),
+                ("total_ms", ctypes.c_float)]
+
+
+class Tune(ctypes.Structure):
+    _fields_ = [("block", ctypes.c_int32), ("ilp", ctypes.c_int32), ("chunk", ctypes.c_int32),
+                ("hot_k", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+# Every symbol include/ptw.h declares: (name, restype, argtypes).
+_vp = ctypes.c_void_p
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_G = ctypes.c_void_p
+_GP = ctypes.POINTER(ctypes.c_void_p)
+SIGNATURES = [
+    ("ptw_last_error", ctypes.c_char_p, []),
+    ("ptw_version", ctypes.c_char_p, []),
+    ("ptw_graph_load", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, _GP]),
+    ("ptw_graph_from_edges", ctypes.c_int, [_u32p, _u32p, ctypes.c_uint64, ctypes.c_int32, _GP]),
+    ("ptw_graph_rmat", ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                      ctypes.c_int32, _GP]),
+    ("ptw_graph_get_info", ctypes.c_int, [_G, ctypes.POINTER(GraphInfo)]),
+    ("ptw_graph_export_csr", ctypes.c_int, [_G, _u32p, _u64p, _u32p]),
+    ("ptw_graph_export_edges", ctypes.c_int, [_G, _u32p, _u32p]),
+    ("ptw_graph_free", None, [_G]),
+    ("ptw_graph_set_tune", ctypes.c_int, [_G, ctypes.POINTER(Tune)]),
+    ("ptw_graph_get_tune", ctypes.c_int, [_G, ctypes.POINTER(Tune)]),
+    ("ptw_pagerank", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, ctypes.POINTER(WalkStats)]),
+    ("ptw_pagerank_dev", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, ctypes.POINTER(WalkStats)]),
+    ("ptw_rwr", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, ctypes.POINTER(WalkStats)]),
+    ("ptw_rwr_dev", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, ctypes.POINTER(WalkStats)]),
+    ("ptw_deepwalk", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), ctypes.c_uint32, _vp,
+                                    ctypes.POINTER(WalkStats)]),
+    ("ptw_deepwalk_dev", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), ctypes.c_uint32, _vp,
+                                        ctypes.POINTER(WalkStats)]),
+    ("ptw_graph_sync", ctypes.c_int, [_G]),
+    ("ptw_graph_set_stream", ctypes.c_int, [_G, _vp]),
+    ("ptw_autotune", ctypes.c_int, [_G, ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(Tune)]),
+]
+
+_lib = None
+
+
+def lib_path():
+    return _build.SO
+
+
+def load(build_if_missing=True):
+    """Loads libptw.so; builds it first when it is missing or stale."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing and not _build.up_to_date():
+        _build.build()
+    if not os.path.exists(_build.SO):
+        raise ImportError("libptw.so is not built; run ptwalker_gb300._build.build()")
+    lib = ctypes.CDLL(_build.SO)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class PTWError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (_ERRNAMES.get(code, "PTW_ERR"), code, msg))
+        self.code = code
+
+
+def check(rc):
+    if rc != PTW_OK:
+        msg = load().ptw_last_error().decode("utf-8", "replace")
+        raise PTWError(rc, msg)
+    return rc

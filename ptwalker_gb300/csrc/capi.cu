@@ -1,0 +1,592 @@
+// C ABI of libptw: argument checking, host<->device staging and the
+// edge-list loader.  See include/ptw.h for the reference interface each entry
+// point replaces.
+#include <cuda_runtime.h>
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ptw_internal.cuh"
+
+namespace ptw {
+
+static thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    const int code = (e == cudaErrorMemoryAllocation) ? PTW_ENOMEM : PTW_ECUDA;
+    cudaGetLastError();  // clear a sticky-free error so later calls can run
+    return fail(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+// ---- edge-list parsing (include/io.hpp:39-90) -------------------------------
+
+struct ParseChunk {
+    std::vector<uint32_t> src, dst;
+    uint64_t bad_line = 0;  // 1-based line number inside the chunk, 0 = ok
+    uint64_t lines = 0;
+};
+
+inline bool is_space(char c) { return c == ' ' || c == '\t' || c == '\r'; }
+
+// Parses [b, e) that starts at a line start.  Comment lines start with '#'.
+// Blank lines are skipped; any other line must start with two unsigned
+// decimal integers that fit in 32 bits.
+void parse_range(const char *b, const char *e, ParseChunk *out)
+{
+    const char *p = b;
+    while (p < e) {
+        ++out->lines;
+        const char *le = (const char *)memchr(p, '\n', (size_t)(e - p));
+        if (!le) le = e;
+        const char *q = p;
+        while (q < le && is_space(*q)) ++q;
+        if (q < le && *p != '#') {
+            uint64_t v[2];
+            bool ok = true;
+            for (int k = 0; k < 2 && ok; ++k) {
+                while (q < le && is_space(*q)) ++q;
+                if (q >= le || *q < '0' || *q > '9') { ok = false; break; }
+                uint64_t x = 0;
+                while (q < le && *q >= '0' && *q <= '9') {
+                    x = x * 10 + (uint64_t)(*q - '0');
+                    if (x > 0xFFFFFFFFull) { ok = false; break; }
+                    ++q;
+                }
+                v[k] = x;
+            }
+            if (!ok) {
+                if (!out->bad_line) out->bad_line = out->lines;
+                return;
+            }
+            out->src.push_back((uint32_t)v[0]);
+            out->dst.push_back((uint32_t)v[1]);
+        }
+        p = le + 1;
+    }
+}
+
+int read_edges(const char *path, int fmt, std::vector<uint32_t> &src, std::vector<uint32_t> &dst)
+{
+    const int fd = open(path, O_RDONLY);
+    if (fd < 0) return fail(PTW_EIO, std::string("cannot open ") + path);
+    struct stat stt;
+    if (fstat(fd, &stt) != 0) {
+        close(fd);
+        return fail(PTW_EIO, std::string("cannot stat ") + path);
+    }
+    const size_t size = (size_t)stt.st_size;
+    if (size == 0) {
+        close(fd);
+        return fail(PTW_EIO, std::string("empty edge file ") + path);
+    }
+    void *map = mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);
+    close(fd);
+    if (map == MAP_FAILED) return fail(PTW_EIO, std::string("cannot map ") + path);
+    const char *data = (const char *)map;
+    int rc = PTW_OK;
+    if (fmt == PTW_FMT_BINARY) {
+        if (size % 8 != 0) {
+            rc = fail(PTW_EIO, "binary edge file size is not a multiple of 8 bytes");
+        } else {
+            const uint64_t m = size / 8;
+            src.resize(m);
+            dst.resize(m);
+            const uint32_t *w = (const uint32_t *)data;
+            for (uint64_t i = 0; i < m; ++i) {
+                src[i] = w[2 * i];
+                dst[i] = w[2 * i + 1];
+            }
+        }
+    } else {
+        unsigned nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+        if (size < (1u << 20)) nt = 1;
+        std::vector<size_t> cut(nt + 1, size);
+        cut[0] = 0;
+        for (unsigned t = 1; t < nt; ++t) {
+            size_t c = size * t / nt;
+            while (c < size && data[c - 1] != '\n') ++c;
+            cut[t] = std::max(c, cut[t - 1]);
+        }
+        std::vector<ParseChunk> parts(nt);
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < nt; ++t)
+            th.emplace_back(parse_range, data + cut[t], data + cut[t + 1], &parts[t]);
+        for (auto &x : th) x.join();
+        uint64_t line0 = 0, total = 0;
+        for (unsigned t = 0; t < nt && rc == PTW_OK; ++t) {
+            if (parts[t].bad_line) {
+                rc = fail(PTW_EIO, std::string("malformed edge at line ") +
+                                       std::to_string(line0 + parts[t].bad_line) + " of " + path);
+            }
+            line0 += parts[t].lines;
+            total += parts[t].src.size();
+        }
+        if (rc == PTW_OK) {
+            src.reserve(total);
+            dst.reserve(total);
+            for (auto &pc : parts) {
+                src.insert(src.end(), pc.src.begin(), pc.src.end());
+                dst.insert(dst.end(), pc.dst.begin(), pc.dst.end());
+            }
+        }
+    }
+    munmap(map, size);
+    return rc;
+}
+
+int upload_and_build(const uint32_t *h_src, const uint32_t *h_dst, uint64_t m, bool undirected,
+                     ptw_graph **out)
+{
+    if (!out) return fail(PTW_EINVAL, "null output handle");
+    *out = nullptr;
+    if (m == 0) return fail(PTW_EINVAL, "edge list is empty");
+    if (!h_src || !h_dst) return fail(PTW_EINVAL, "null edge arrays");
+    ptw_graph *g = new (std::nothrow) ptw_graph();
+    if (!g) return fail(PTW_ENOMEM, "host allocation failed");
+    int rc = graph_init_handle(g);
+    uint32_t *d_src = nullptr, *d_dst = nullptr;
+    if (rc == PTW_OK) {
+        cudaError_t e = cudaMallocAsync(&d_src, m * 4, g->stream);
+        if (e == cudaSuccess) e = cudaMallocAsync(&d_dst, m * 4, g->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_src, h_src, m * 4, cudaMemcpyHostToDevice, g->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_dst, h_dst, m * 4, cudaMemcpyHostToDevice, g->stream);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "edge upload");
+            if (d_src) cudaFreeAsync(d_src, g->stream);
+            if (d_dst) cudaFreeAsync(d_dst, g->stream);
+        } else {
+            rc = build_graph_from_device_edges(g, d_src, d_dst, m, undirected, false, false);
+        }
+    }
+    if (rc != PTW_OK) {
+        graph_release(g);
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return PTW_OK;
+}
+
+int check_cfg(const ptw_graph *g, const ptw_walk_cfg *cfg, bool needs_sp)
+{
+    if (!g) return fail(PTW_EINVAL, "null graph");
+    if (!cfg) return fail(PTW_EINVAL, "null walk configuration");
+    if (needs_sp) {
+        if (!(cfg->sp >= 0.0 && cfg->sp <= 1.0))
+            return fail(PTW_EINVAL, "sp must be in [0, 1]");
+        if (cfg->sp == 0.0 && cfg->max_moves == 0)
+            return fail(PTW_EINVAL, "sp = 0 needs max_moves > 0 (walks would never end)");
+    }
+    if (cfg->start_mode < PTW_START_PER_VERTEX || cfg->start_mode > PTW_START_SOURCES)
+        return fail(PTW_EINVAL, "unknown start_mode");
+    if (cfg->start_mode == PTW_START_SOURCES && (cfg->n_sources == 0 || !cfg->h_sources))
+        return fail(PTW_EINVAL, "PTW_START_SOURCES needs at least one source");
+    if (cfg->n_walkers > ~0ull - cfg->first_walker) return fail(PTW_EINVAL, "walker ids overflow 64 bits");
+    return PTW_OK;
+}
+
+// Maps source names to internal ids and uploads them to the scratch table.
+int upload_sources(ptw_graph *g, const ptw_walk_cfg *cfg)
+{
+    if (cfg->start_mode != PTW_START_SOURCES) return PTW_OK;
+    const uint32_t n = g->dg.n;
+    std::vector<uint32_t> ids(cfg->n_sources);
+    for (uint32_t i = 0; i < cfg->n_sources; ++i) {
+        const uint32_t nm = cfg->h_sources[i];
+        const uint32_t *p = std::lower_bound(g->h_names, g->h_names + n, nm);
+        if (p == g->h_names + n || *p != nm)
+            return fail(PTW_EINVAL, "source " + std::to_string(nm) + " is not a vertex of the graph");
+        ids[i] = g->h_idx2int[p - g->h_names];
+    }
+    if (g->sc.sources_cap < cfg->n_sources) {
+        cudaFree(g->sc.sources);
+        g->sc.sources = nullptr;
+        g->sc.sources_cap = 0;
+        PTW_CUDA(cudaMalloc(&g->sc.sources, (uint64_t)cfg->n_sources * 4));
+        g->sc.sources_cap = cfg->n_sources;
+    }
+    PTW_CUDA(cudaMemcpyAsync(g->sc.sources, ids.data(), (uint64_t)cfg->n_sources * 4,
+                             cudaMemcpyHostToDevice, g->stream));
+    // ids must outlive the copy
+    PTW_CUDA(cudaStreamSynchronize(g->stream));
+    return PTW_OK;
+}
+
+int stage_bytes(ptw_graph *g, size_t bytes, void **out)
+{
+    if (g->sc.out_stage_bytes < bytes) {
+        cudaFree(g->sc.out_stage);
+        g->sc.out_stage = nullptr;
+        g->sc.out_stage_bytes = 0;
+        PTW_CUDA(cudaMalloc(&g->sc.out_stage, std::max<size_t>(bytes, 256)));
+        g->sc.out_stage_bytes = std::max<size_t>(bytes, 256);
+    }
+    *out = g->sc.out_stage;
+    return PTW_OK;
+}
+
+uint64_t threshold(double sp)
+{
+    if (sp >= 1.0) return 1ull << 32;
+    return (uint64_t)(sp * 4294967296.0);
+}
+
+WalkLaunch make_launch(const ptw_walk_cfg *cfg)
+{
+    WalkLaunch wl;
+    wl.w_begin = cfg->first_walker;
+    wl.w_end = wl.w_begin + cfg->n_walkers;
+    wl.thr = threshold(cfg->sp);
+    wl.seed = cfg->seed;
+    wl.start_mode = cfg->start_mode;
+    wl.n_sources = cfg->start_mode == PTW_START_SOURCES ? cfg->n_sources : 0;
+    wl.max_moves = cfg->max_moves;
+    return wl;
+}
+
+int finish_stats(ptw_graph *g, ptw_walk_stats *stats, uint64_t walkers, bool count_app)
+{
+    if (!stats) return PTW_OK;
+    unsigned long long moves = 0;
+    PTW_CUDA(cudaMemcpyAsync(&moves, g->sc.ctrl + 1, sizeof(moves), cudaMemcpyDeviceToHost, g->stream));
+    PTW_CUDA(cudaStreamSynchronize(g->stream));
+    stats->walkers = walkers;
+    stats->moves = moves;
+    stats->visits = count_app ? walkers + moves : 0;
+    float ms = 0;
+    PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]));
+    stats->kernel_ms = ms;
+    PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[3], g->ev[2]));
+    stats->total_ms = ms;
+    return PTW_OK;
+}
+
+// Runs the count walk into g->sc.counts and scatters the result by name
+// into d_by_name.  Events: ev0 before, ev1 after the kernel.
+int run_count(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_by_name)
+{
+    int rc = upload_sources(g, cfg);
+    if (rc) return rc;
+    PTW_CUDA(cudaEventRecord(g->ev[3], g->stream));
+    PTW_CUDA(cudaMemsetAsync(g->sc.counts, 0, (uint64_t)g->dg.n * 4, g->stream));
+    PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
+    if (cfg->n_walkers) {
+        rc = launch_walk(g, make_launch(cfg), g->tune);
+        if (rc) return rc;
+    } else {
+        PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 2 * sizeof(unsigned long long), g->stream));
+    }
+    PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
+    return launch_counts_by_name(g, d_by_name);
+}
+
+int run_endpoint(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_pairs)
+{
+    int rc = upload_sources(g, cfg);
+    if (rc) return rc;
+    PTW_CUDA(cudaEventRecord(g->ev[3], g->stream));
+    PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
+    if (cfg->n_walkers) {
+        WalkLaunch wl = make_launch(cfg);
+        wl.endpoint = true;
+        wl.pairs = d_pairs;
+        rc = launch_walk(g, wl, g->tune);
+        if (rc) return rc;
+    } else {
+        PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 2 * sizeof(unsigned long long), g->stream));
+    }
+    PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
+    return PTW_OK;
+}
+
+int run_paths(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *d_paths)
+{
+    int rc = upload_sources(g, cfg);
+    if (rc) return rc;
+    PTW_CUDA(cudaEventRecord(g->ev[3], g->stream));
+    PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 2 * sizeof(unsigned long long), g->stream));
+    PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
+    if (cfg->n_walkers && L) {
+        const uint64_t w0 = cfg->first_walker;
+        rc = launch_paths(g, w0, w0 + cfg->n_walkers, L, cfg->seed, cfg->start_mode,
+                          cfg->start_mode == PTW_START_SOURCES ? cfg->n_sources : 0, d_paths);
+        if (rc) return rc;
+    }
+    PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
+    return PTW_OK;
+}
+
+}  // namespace
+}  // namespace ptw
+
+using namespace ptw;
+
+extern "C" const char *ptw_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" const char *ptw_version(void) { return "ptwalker_gb300 0.1 (sm_103a)"; }
+
+extern "C" int ptw_graph_load(const char *path, int32_t fmt, int32_t as_undirected, ptw_graph **out)
+{
+    if (!path || !out) return fail(PTW_EINVAL, "null argument");
+    if (fmt != PTW_FMT_BINARY && fmt != PTW_FMT_TEXT) return fail(PTW_EINVAL, "unknown graph format");
+    std::vector<uint32_t> src, dst;
+    int rc = read_edges(path, fmt, src, dst);
+    if (rc) return rc;
+    return upload_and_build(src.data(), dst.data(), src.size(), as_undirected != 0, out);
+}
+
+extern "C" int ptw_graph_from_edges(const uint32_t *h_src, const uint32_t *h_dst, uint64_t m,
+                                    int32_t as_undirected, ptw_graph **out)
+{
+    return upload_and_build(h_src, h_dst, m, as_undirected != 0, out);
+}
+
+extern "C" int ptw_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                              uint64_t seed, int32_t clean, ptw_graph **out)
+{
+    if (!out) return fail(PTW_EINVAL, "null output handle");
+    *out = nullptr;
+    if (scale < 1 || scale > 31) return fail(PTW_EINVAL, "scale must be in [1, 31]");
+    if (edge_factor < 1) return fail(PTW_EINVAL, "edge_factor must be >= 1");
+    if (!(a >= 0 && b >= 0 && c >= 0 && a + b + c <= 1.0))
+        return fail(PTW_EINVAL, "R-MAT probabilities must be >= 0 with a + b + c <= 1");
+    const uint64_t m = (uint64_t)edge_factor << scale;
+    if (m >= (1ull << 32)) return fail(PTW_EINVAL, "2^scale * edge_factor must be < 2^32");
+    auto thr = [](double p) -> uint32_t {
+        const double x = p * 4294967296.0;
+        return x >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)x;
+    };
+    ptw_graph *g = new (std::nothrow) ptw_graph();
+    if (!g) return fail(PTW_ENOMEM, "host allocation failed");
+    int rc = graph_init_handle(g);
+    uint32_t *d_src = nullptr, *d_dst = nullptr;
+    if (rc == PTW_OK) {
+        cudaError_t e = cudaMallocAsync(&d_src, m * 4, g->stream);
+        if (e == cudaSuccess) e = cudaMallocAsync(&d_dst, m * 4, g->stream);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "R-MAT edge buffers");
+            if (d_src) cudaFreeAsync(d_src, g->stream);
+        } else {
+            rc = rmat_generate_device(scale, m, thr(a), thr(a + b), thr(a + b + c), seed, d_src, d_dst,
+                                      g->stream);
+            if (rc == PTW_OK)
+                rc = build_graph_from_device_edges(g, d_src, d_dst, m, clean != 0, clean != 0, clean != 0);
+        }
+    }
+    if (rc != PTW_OK) {
+        graph_release(g);
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return PTW_OK;
+}
+
+extern "C" void ptw_graph_free(ptw_graph *g)
+{
+    if (!g) return;
+    cudaSetDevice(g->device);
+    graph_release(g);
+    delete g;
+}
+
+extern "C" int ptw_graph_set_tune(ptw_graph *g, const ptw_tune *t)
+{
+    if (!g || !t) return fail(PTW_EINVAL, "null argument");
+    int rc = check_tune(*t);
+    if (rc) return rc;
+    g->tune = *t;
+    return PTW_OK;
+}
+
+extern "C" int ptw_graph_get_tune(const ptw_graph *g, ptw_tune *t)
+{
+    if (!g || !t) return fail(PTW_EINVAL, "null argument");
+    *t = g->tune;
+    return PTW_OK;
+}
+
+extern "C" int ptw_pagerank_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_counts,
+                                ptw_walk_stats *stats)
+{
+    int rc = check_cfg(g, cfg, true);
+    if (rc) return rc;
+    if (!d_counts) return fail(PTW_EINVAL, "null counts buffer");
+    PTW_CUDA(cudaSetDevice(g->device));
+    rc = run_count(g, cfg, d_counts);
+    if (rc) return rc;
+    PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    return finish_stats(g, stats, cfg->n_walkers, true);
+}
+
+extern "C" int ptw_pagerank(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_counts,
+                            ptw_walk_stats *stats)
+{
+    int rc = check_cfg(g, cfg, true);
+    if (rc) return rc;
+    if (!h_counts) return fail(PTW_EINVAL, "null counts buffer");
+    PTW_CUDA(cudaSetDevice(g->device));
+    if (!g->sc.by_name) PTW_CUDA(cudaMalloc(&g->sc.by_name, (uint64_t)g->dg.id_bound * 4));
+    rc = run_count(g, cfg, g->sc.by_name);
+    if (rc) return rc;
+    PTW_CUDA(cudaMemcpyAsync(h_counts, g->sc.by_name, (uint64_t)g->dg.id_bound * 4,
+                             cudaMemcpyDeviceToHost, g->stream));
+    PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    PTW_CUDA(cudaStreamSynchronize(g->stream));
+    return finish_stats(g, stats, cfg->n_walkers, true);
+}
+
+extern "C" int ptw_rwr_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_pairs,
+                           ptw_walk_stats *stats)
+{
+    int rc = check_cfg(g, cfg, true);
+    if (rc) return rc;
+    if (!d_pairs && cfg->n_walkers) return fail(PTW_EINVAL, "null pairs buffer");
+    if ((uintptr_t)d_pairs % 8) return fail(PTW_EINVAL, "pairs buffer must be 8-byte aligned");
+    PTW_CUDA(cudaSetDevice(g->device));
+    rc = run_endpoint(g, cfg, d_pairs);
+    if (rc) return rc;
+    PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    return finish_stats(g, stats, cfg->n_walkers, false);
+}
+
+extern "C" int ptw_rwr(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_pairs, ptw_walk_stats *stats)
+{
+    int rc = check_cfg(g, cfg, true);
+    if (rc) return rc;
+    if (!h_pairs && cfg->n_walkers) return fail(PTW_EINVAL, "null pairs buffer");
+    PTW_CUDA(cudaSetDevice(g->device));
+    void *stage = nullptr;
+    rc = stage_bytes(g, cfg->n_walkers * 8, &stage);
+    if (rc) return rc;
+    rc = run_endpoint(g, cfg, (uint32_t *)stage);
+    if (rc) return rc;
+    if (cfg->n_walkers)
+        PTW_CUDA(cudaMemcpyAsync(h_pairs, stage, cfg->n_walkers * 8, cudaMemcpyDeviceToHost, g->stream));
+    PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    PTW_CUDA(cudaStreamSynchronize(g->stream));
+    return finish_stats(g, stats, cfg->n_walkers, false);
+}
+
+extern "C" int ptw_deepwalk_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *d_paths,
+                                ptw_walk_stats *stats)
+{
+    int rc = check_cfg(g, cfg, false);
+    if (rc) return rc;
+    if (!d_paths && cfg->n_walkers && L) return fail(PTW_EINVAL, "null paths buffer");
+    if (g->dg.id_bound > 0x80000000u) return fail(PTW_EINVAL, "names above 2^31-1 do not fit int32 paths");
+    PTW_CUDA(cudaSetDevice(g->device));
+    rc = run_paths(g, cfg, L, d_paths);
+    if (rc) return rc;
+    PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    if (stats) {
+        PTW_CUDA(cudaStreamSynchronize(g->stream));
+        stats->walkers = cfg->n_walkers;
+        stats->moves = L ? cfg->n_walkers * (uint64_t)(L - 1) : 0;  // dead ends excluded below
+        stats->visits = 0;
+        float ms = 0;
+        PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]));
+        stats->kernel_ms = ms;
+        PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[3], g->ev[2]));
+        stats->total_ms = ms;
+    }
+    return PTW_OK;
+}
+
+extern "C" int ptw_deepwalk(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *h_paths,
+                            ptw_walk_stats *stats)
+{
+    int rc = check_cfg(g, cfg, false);
+    if (rc) return rc;
+    if (!h_paths && cfg->n_walkers && L) return fail(PTW_EINVAL, "null paths buffer");
+    if (g->dg.id_bound > 0x80000000u) return fail(PTW_EINVAL, "names above 2^31-1 do not fit int32 paths");
+    PTW_CUDA(cudaSetDevice(g->device));
+    const uint64_t bytes = cfg->n_walkers * (uint64_t)L * 4;
+    void *stage = nullptr;
+    rc = stage_bytes(g, bytes, &stage);
+    if (rc) return rc;
+    rc = run_paths(g, cfg, L, (int32_t *)stage);
+    if (rc) return rc;
+    if (bytes) PTW_CUDA(cudaMemcpyAsync(h_paths, stage, bytes, cudaMemcpyDeviceToHost, g->stream));
+    PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    PTW_CUDA(cudaStreamSynchronize(g->stream));
+    if (stats) {
+        stats->walkers = cfg->n_walkers;
+        stats->moves = L ? cfg->n_walkers * (uint64_t)(L - 1) : 0;
+        stats->visits = 0;
+        float ms = 0;
+        PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]));
+        stats->kernel_ms = ms;
+        PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[3], g->ev[2]));
+        stats->total_ms = ms;
+    }
+    return PTW_OK;
+}
+
+extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tune *best)
+{
+    if (!g) return fail(PTW_EINVAL, "null graph");
+    if (!(sp > 0.0 && sp <= 1.0)) return fail(PTW_EINVAL, "sp must be in (0, 1]");
+    PTW_CUDA(cudaSetDevice(g->device));
+    ptw_walk_cfg cfg{};
+    cfg.n_walkers = n_walkers ? n_walkers : g->dg.n;
+    cfg.sp = sp;
+    cfg.seed = 0x5eedull;
+    cfg.start_mode = PTW_START_PER_VERTEX;
+    const ptw_tune saved = g->tune;
+    ptw_tune bt = saved;
+    float bms = 1e30f;
+    const int blocks[] = {128, 256, 512};
+    const int ilps[] = {1, 2, 4};
+    const int chunks[] = {64, 256, 1024};
+    const int hots[] = {0, 8192};
+    WalkLaunch wl = make_launch(&cfg);
+    for (int hk : hots)
+        for (int bl : blocks)
+            for (int il : ilps)
+                for (int ch : chunks) {
+                    ptw_tune t{};
+                    t.block = bl;
+                    t.ilp = il;
+                    t.chunk = ch;
+                    t.hot_k = hk;
+                    t.blocks_per_sm = 0;
+                    float tot = 0;
+                    bool ok = true;
+                    for (int rep = 0; rep < 3 && ok; ++rep) {
+                        PTW_CUDA(cudaMemsetAsync(g->sc.counts, 0, (uint64_t)g->dg.n * 4, g->stream));
+                        PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
+                        if (launch_walk(g, wl, t) != PTW_OK) ok = false;
+                        PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
+                        PTW_CUDA(cudaEventSynchronize(g->ev[1]));
+                        float ms = 0;
+                        PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]));
+                        if (rep) tot += ms;  // first run warms up
+                    }
+                    if (ok && tot < bms) {
+                        bms = tot;
+                        bt = t;
+                    }
+                }
+    g->tune = bt;
+    if (best) *best = bt;
+    return PTW_OK;
+}

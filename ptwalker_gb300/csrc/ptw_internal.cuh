@@ -1,0 +1,116 @@
+// Internal declarations shared by the libptw translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/ptw.h"
+
+// Philox counter words that separate the purposes of a draw.
+#define PTW_TAG_WALK 0x57414C4Bu  // "WALK": one draw per move
+#define PTW_TAG_START 0x53545254u // "STRT": start-vertex draw
+#define PTW_TAG_RMAT 0x524D4154u  // "RMAT": synthetic edge generation
+
+namespace ptw {
+
+// Records msg as the calling thread's last error and returns code.
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define PTW_CUDA(call)                                   \
+    do {                                                 \
+        cudaError_t _e = (call);                         \
+        if (_e != cudaSuccess) return ptw::cuda_fail(_e, #call); \
+    } while (0)
+
+// Philox4x32-10 (Salmon et al., SC'11): ten rounds of the 4x32 S-box,
+// multipliers 0xD2511F53 / 0xCD9E8D57, Weyl key increments 0x9E3779B9 /
+// 0xBB67AE85.  ctr = (x, y, z, w), key = (k0, k1).
+__device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Device-resident graph.  Internal vertex ids are ranks by descending
+// degree (ties by ascending name), so the hottest rows, counters and column
+// blocks sit at the low end of every array and stay in L2.
+struct DeviceGraph {
+    uint32_t n = 0;
+    uint64_t m = 0;
+    uint32_t id_bound = 0;
+    uint32_t max_degree = 0;
+    uint2 *adj = nullptr;        // [n] {first column, degree} by internal id
+    uint32_t *col = nullptr;     // [m] neighbour internal ids; row order = name order
+    uint32_t *int2name = nullptr; // [n]
+    uint32_t *idx2int = nullptr;  // [n] canonical index (name rank) -> internal
+    uint32_t *int2idx = nullptr;  // [n] internal -> canonical index
+};
+
+// Scratch owned by a graph handle and reused by every call.
+struct Scratch {
+    uint32_t *counts = nullptr;           // [n] visit counts by internal id
+    unsigned long long *ctrl = nullptr;   // [8]: walker cursor, moves, error flags
+    uint32_t *sources = nullptr;          // source internal ids
+    uint32_t sources_cap = 0;
+    uint32_t *by_name = nullptr;          // [id_bound] staging for host-output calls
+    void *out_stage = nullptr;            // device staging for host-output calls
+    size_t out_stage_bytes = 0;
+};
+
+}  // namespace ptw
+
+struct ptw_graph {
+    ptw::DeviceGraph dg;
+    ptw::Scratch sc;
+    uint32_t *h_names = nullptr;   // [n] ascending, for host-side name lookups
+    uint32_t *h_idx2int = nullptr; // [n] canonical index -> internal id
+    cudaStream_t stream = nullptr;     // stream all work is issued on
+    cudaStream_t own_stream = nullptr; // created with the handle
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    int device = 0;
+    int num_sms = 0;
+    ptw_tune tune{};
+    uint64_t device_bytes = 0;
+};
+
+namespace ptw {
+
+// Builds a canonical + degree-sorted device graph from device edge arrays
+// (consumes them).  Implemented in graph.cu.
+int build_graph_from_device_edges(ptw_graph *g, uint32_t *d_src, uint32_t *d_dst, uint64_t m,
+                                  bool as_undirected, bool clean, bool compact_names);
+int rmat_generate_device(uint32_t scale, uint64_t m, uint32_t ta, uint32_t tab, uint32_t tabc,
+                         uint64_t seed, uint32_t *d_src, uint32_t *d_dst, cudaStream_t st);
+int graph_init_handle(ptw_graph *g);
+void graph_release(ptw_graph *g);
+
+// Walk launchers (walk.cu).
+struct WalkLaunch {
+    uint64_t w_begin = 0, w_end = 0;
+    uint64_t thr = 0;
+    uint64_t seed = 0;
+    int start_mode = 0;
+    uint32_t n_sources = 0;
+    uint32_t max_moves = 0;
+    bool endpoint = false;     // RWR endpoint app instead of counting
+    uint32_t *pairs = nullptr; // endpoint output by walker (names)
+};
+int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t);
+int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
+                 int start_mode, uint32_t n_sources, int32_t *paths);
+int launch_counts_by_name(ptw_graph *g, uint32_t *d_out);
+int check_tune(const ptw_tune &t);
+
+}  // namespace ptw

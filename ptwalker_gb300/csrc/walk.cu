@@ -1,0 +1,400 @@
+// Walker-update kernels for sm_103a.
+//
+// K1/K2 k_walk: persistent walker pool.  Replaces the reference's per-thread
+// walker containers, partition sweeps and migrations
+// (src/core/solver.hpp:194-498, :850-1028) and the direct sampler
+// (src/core/sampler.hpp:214-217).  Each lane holds ILP walkers.  A lane whose
+// walker ended is refilled from a warp-private range of walker ids: the warp
+// ballots the empty lanes, ranks them with a popcount prefix and takes ids
+// from its range, drawing a new range of `chunk` ids from one global cursor
+// when it runs dry.  Every draw is a pure function of (seed, walker id, step),
+// so scheduling never changes a result.
+//
+// Per move (count apps, pagerank.cpp:86-89 / ppr.cpp:114-117):
+//   {off, deg} = adj[v]                      one 8-byte random load
+//   u = Philox4x32-10(key=seed, ctr=(wid_lo, wid_hi, step, "WALK"))
+//   v = col[off + mulhi(u.x, deg)]           one 4-byte random load
+//   counts[v] += 1                           one fire-and-forget reduction
+//   stop iff u.y < floor(sp * 2^32)
+//
+// K3 k_paths: DeepWalk (src/core/deepwalk.cpp:25-28).  One walker per lane,
+// all walks the same length, so a warp stays converged.  Each warp stages the
+// next 32 path positions of its 32 walkers in shared memory and writes them
+// out row by row, so every store instruction writes 32 consecutive int32 of
+// one path row.
+#include <algorithm>
+
+#include "ptw_internal.cuh"
+
+namespace ptw {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ uint64_t umin64(uint64_t x, uint64_t y) { return x < y ? x : y; }
+
+struct WalkArgs {
+    const uint2 *__restrict__ adj;
+    const uint32_t *__restrict__ col;
+    const uint32_t *__restrict__ start_map;  // canonical index -> internal
+    const uint32_t *__restrict__ sources;    // internal ids
+    const uint32_t *__restrict__ int2name;
+    uint32_t *__restrict__ counts;
+    uint32_t *__restrict__ pairs;            // endpoint app: [2 * walkers] names
+    unsigned long long *__restrict__ ctrl;   // [0] cursor, [1] moves
+    uint64_t w_begin;
+    uint64_t n_walk;
+    uint64_t thr;
+    uint32_t n;
+    uint32_t key0, key1;
+    uint32_t n_sources;
+    uint32_t max_moves;
+    uint32_t chunk;
+    uint32_t hot_k;
+    int start_mode;
+};
+
+__device__ __forceinline__ uint32_t start_vertex(const WalkArgs &a, uint64_t wid)
+{
+    if (a.start_mode == PTW_START_PER_VERTEX) {
+        const uint32_t idx = wid < a.n ? (uint32_t)wid : (uint32_t)(wid % a.n);
+        return a.start_map[idx];
+    }
+    if (a.start_mode == PTW_START_SOURCES && a.n_sources == 1) return a.sources[0];
+    const uint4 r = philox(make_uint4((uint32_t)wid, (uint32_t)(wid >> 32), 0u, PTW_TAG_START),
+                           a.key0, a.key1);
+    if (a.start_mode == PTW_START_UNIFORM) return a.start_map[__umulhi(r.x, a.n)];
+    return a.sources[__umulhi(r.x, a.n_sources)];
+}
+
+template <bool HOT>
+__device__ __forceinline__ void count_visit(const WalkArgs &a, uint32_t *s_hot, uint32_t v)
+{
+    if (HOT && v < a.hot_k) atomicAdd(&s_hot[v], 1u);
+    else atomicAdd(&a.counts[v], 1u);
+}
+
+template <bool ENDPOINT, int ILP, bool HOT>
+__global__ void k_walk(const WalkArgs a)
+{
+    extern __shared__ uint32_t s_hot[];
+    if (HOT) {
+        for (uint32_t i = threadIdx.x; i < a.hot_k; i += blockDim.x) s_hot[i] = 0;
+        __syncthreads();
+    }
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+
+    uint64_t wid[ILP];
+    uint32_t v[ILP], step[ILP], s0[ILP];
+    bool act[ILP];
+#pragma unroll
+    for (int k = 0; k < ILP; ++k) {
+        act[k] = false;
+        wid[k] = 0;
+        v[k] = step[k] = s0[k] = 0;
+    }
+    // Warp-uniform walker-id range [next, end) relative to w_begin.
+    uint64_t next = 0, end = 0;
+    bool exhausted = false;
+    unsigned long long moves = 0;
+
+    for (;;) {
+        // ---- refill empty slots ------------------------------------------
+#pragma unroll
+        for (int k = 0; k < ILP; ++k) {
+            const unsigned need = __ballot_sync(kFull, !act[k]);
+            if (need == 0 || exhausted) continue;
+            const uint32_t n_need = __popc(need);
+            const uint32_t rank = __popc(need & lt_mask);
+            uint64_t my = ~0ull;
+            const uint64_t avail = end - next;
+            const uint32_t took = (uint32_t)umin64(n_need, avail);
+            if (!act[k] && rank < took) my = next + rank;
+            next += took;
+            if (took < n_need) {
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd(&a.ctrl[0], (unsigned long long)a.chunk);
+                base = __shfl_sync(kFull, base, 0);
+                if (base >= a.n_walk) {
+                    exhausted = true;
+                    next = end = a.n_walk;
+                } else {
+                    next = base;
+                    end = umin64(base + a.chunk, a.n_walk);
+                    const uint32_t take2 = (uint32_t)umin64(n_need - took, end - next);
+                    if (!act[k] && rank >= took && rank - took < take2) my = next + (rank - took);
+                    next += take2;
+                }
+            }
+            if (my != ~0ull) {
+                wid[k] = a.w_begin + my;
+                v[k] = start_vertex(a, wid[k]);
+                s0[k] = v[k];
+                step[k] = 0;
+                act[k] = true;
+                if (!ENDPOINT) count_visit<HOT>(a, s_hot, v[k]);
+            }
+        }
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < ILP; ++k) any |= act[k];
+        if (!__any_sync(kFull, any)) break;
+
+        // ---- one move for every active slot --------------------------------
+        uint2 rec[ILP];
+#pragma unroll
+        for (int k = 0; k < ILP; ++k)
+            if (act[k]) rec[k] = __ldg(&a.adj[v[k]]);
+        uint4 r[ILP];
+#pragma unroll
+        for (int k = 0; k < ILP; ++k)
+            if (act[k])
+                r[k] = philox(make_uint4((uint32_t)wid[k], (uint32_t)(wid[k] >> 32), step[k], PTW_TAG_WALK),
+                              a.key0, a.key1);
+        uint32_t nb[ILP];
+#pragma unroll
+        for (int k = 0; k < ILP; ++k)
+            if (act[k] && rec[k].y != 0) nb[k] = __ldg(&a.col[rec[k].x + __umulhi(r[k].x, rec[k].y)]);
+#pragma unroll
+        for (int k = 0; k < ILP; ++k) {
+            if (!act[k]) continue;
+            bool done;
+            if (rec[k].y == 0) {
+                done = true;  // no out-edge: the walk ends here
+            } else {
+                v[k] = nb[k];
+                ++step[k];
+                ++moves;
+                if (!ENDPOINT) count_visit<HOT>(a, s_hot, v[k]);
+                done = (uint64_t)r[k].y < a.thr || (a.max_moves && step[k] >= a.max_moves);
+            }
+            if (done) {
+                if (ENDPOINT) {
+                    const uint64_t j = wid[k] - a.w_begin;
+                    *reinterpret_cast<uint2 *>(&a.pairs[2 * j]) =
+                        make_uint2(a.int2name[s0[k]], a.int2name[v[k]]);
+                }
+                act[k] = false;
+            }
+        }
+    }
+
+    // ---- flush ------------------------------------------------------------
+#pragma unroll
+    for (int o = 16; o; o >>= 1) moves += __shfl_xor_sync(kFull, moves, o);
+    if (lane == 0 && moves) atomicAdd(&a.ctrl[1], moves);
+    if (HOT) {
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < a.hot_k; i += blockDim.x)
+            if (s_hot[i]) atomicAdd(&a.counts[i], s_hot[i]);
+    }
+}
+
+struct PathArgs {
+    const uint2 *__restrict__ adj;
+    const uint32_t *__restrict__ col;
+    const uint32_t *__restrict__ start_map;
+    const uint32_t *__restrict__ sources;
+    const uint32_t *__restrict__ int2name;
+    int32_t *__restrict__ paths;
+    uint64_t w_begin, n_walk;
+    uint32_t n, L;
+    uint32_t key0, key1;
+    uint32_t n_sources;
+    int start_mode;
+};
+
+constexpr int kPathWarps = 8;  // warps per block
+
+__global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
+{
+    __shared__ int32_t stage[kPathWarps][32][33];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t wib = threadIdx.x >> 5;
+    int32_t(*buf)[33] = stage[wib];
+    const uint64_t n_groups = (a.n_walk + 31) / 32;
+    const uint64_t warps = (uint64_t)gridDim.x * kPathWarps;
+
+    WalkArgs sa;  // start-vertex helper view
+    sa.start_map = a.start_map;
+    sa.sources = a.sources;
+    sa.n = a.n;
+    sa.key0 = a.key0;
+    sa.key1 = a.key1;
+    sa.n_sources = a.n_sources;
+    sa.start_mode = a.start_mode;
+
+    for (uint64_t grp = blockIdx.x * (uint64_t)kPathWarps + wib; grp < n_groups; grp += warps) {
+        const uint64_t j = grp * 32 + lane;  // walker offset
+        const bool valid = j < a.n_walk;
+        const uint64_t wid = a.w_begin + j;
+        const uint32_t rows = (uint32_t)umin64(32, a.n_walk - grp * 32);
+        uint32_t v = valid ? start_vertex(sa, wid) : 0;
+        bool dead = !valid;
+        buf[lane][0] = valid ? (int32_t)a.int2name[v] : -1;
+        uint32_t c0 = 0;  // path position of buf column 0
+        for (uint32_t p = 1; p <= a.L; ++p) {
+            if (p == a.L || (p & 31) == 0) {
+                // flush columns [c0, p) of the 32 rows
+                __syncwarp();
+                const uint32_t cols = p - c0;
+                for (uint32_t rr = 0; rr < rows; ++rr)
+                    if (lane < cols)
+                        a.paths[(grp * 32 + rr) * (uint64_t)a.L + c0 + lane] = buf[rr][lane];
+                __syncwarp();
+                c0 = p;
+                if (p == a.L) break;
+            }
+            int32_t out = -1;
+            if (!dead) {
+                const uint2 rec = __ldg(&a.adj[v]);
+                if (rec.y == 0) {
+                    dead = true;
+                } else {
+                    const uint4 r = philox(make_uint4((uint32_t)wid, (uint32_t)(wid >> 32), p - 1, PTW_TAG_WALK),
+                                           a.key0, a.key1);
+                    v = __ldg(&a.col[rec.x + __umulhi(r.x, rec.y)]);
+                    out = (int32_t)__ldg(&a.int2name[v]);
+                }
+            }
+            buf[lane][p - c0] = out;
+        }
+    }
+}
+
+__global__ void k_counts_by_name(const uint32_t *counts, const uint32_t *int2name, uint32_t n,
+                                 uint32_t *out)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[int2name[i]] = counts[i];
+}
+
+template <bool E, int ILP, bool H> void *walk_fn() { return (void *)k_walk<E, ILP, H>; }
+
+void *pick_walk(bool endpoint, int ilp, bool hot)
+{
+    if (endpoint) {
+        switch (ilp) {
+        case 1: return walk_fn<true, 1, false>();
+        case 4: return walk_fn<true, 4, false>();
+        default: return walk_fn<true, 2, false>();
+        }
+    }
+    if (hot) {
+        switch (ilp) {
+        case 1: return walk_fn<false, 1, true>();
+        case 4: return walk_fn<false, 4, true>();
+        default: return walk_fn<false, 2, true>();
+        }
+    }
+    switch (ilp) {
+    case 1: return walk_fn<false, 1, false>();
+    case 4: return walk_fn<false, 4, false>();
+    default: return walk_fn<false, 2, false>();
+    }
+}
+
+}  // namespace
+
+int check_tune(const ptw_tune &t)
+{
+    if (t.block < 32 || t.block > 1024 || t.block % 32)
+        return fail(PTW_EINVAL, "tune.block must be a multiple of 32 in [32, 1024]");
+    if (t.ilp != 1 && t.ilp != 2 && t.ilp != 4) return fail(PTW_EINVAL, "tune.ilp must be 1, 2 or 4");
+    if (t.chunk < 1 || t.chunk > (1 << 20)) return fail(PTW_EINVAL, "tune.chunk must be in [1, 2^20]");
+    if (t.hot_k < 0 || t.hot_k > 48 * 1024)
+        return fail(PTW_EINVAL, "tune.hot_k must be in [0, 49152]");
+    if (t.blocks_per_sm < 0 || t.blocks_per_sm > 64) return fail(PTW_EINVAL, "tune.blocks_per_sm out of range");
+    return PTW_OK;
+}
+
+int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t)
+{
+    int rc = check_tune(t);
+    if (rc) return rc;
+    const DeviceGraph &dg = g->dg;
+    WalkArgs a;
+    a.adj = dg.adj;
+    a.col = dg.col;
+    a.start_map = dg.idx2int;
+    a.sources = g->sc.sources;
+    a.int2name = dg.int2name;
+    a.counts = g->sc.counts;
+    a.pairs = wl.pairs;
+    a.ctrl = g->sc.ctrl;
+    a.w_begin = wl.w_begin;
+    a.n_walk = wl.w_end - wl.w_begin;
+    a.thr = wl.thr;
+    a.n = dg.n;
+    a.key0 = (uint32_t)wl.seed;
+    a.key1 = (uint32_t)(wl.seed >> 32);
+    a.n_sources = wl.n_sources;
+    a.max_moves = wl.max_moves;
+    a.chunk = (uint32_t)t.chunk;
+    const bool hot = !wl.endpoint && t.hot_k > 0;
+    a.hot_k = hot ? std::min<uint32_t>((uint32_t)t.hot_k, dg.n) : 0;
+    a.start_mode = wl.start_mode;
+
+    void *fn = pick_walk(wl.endpoint, t.ilp, hot);
+    const size_t smem = hot ? (size_t)a.hot_k * 4 : 0;
+    if (smem > 48 * 1024)
+        PTW_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, t.block, smem));
+    if (per_sm < 1) return fail(PTW_EINVAL, "walk kernel does not fit on an SM with this tune");
+    if (t.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)t.blocks_per_sm);
+    uint64_t grid = (uint64_t)g->num_sms * per_sm;
+    // No more warps than walker ranges to hand out.
+    const uint64_t warps_needed = (a.n_walk + (uint64_t)a.chunk - 1) / a.chunk;
+    const uint64_t max_blocks = std::max<uint64_t>(1, (warps_needed + t.block / 32 - 1) / (t.block / 32));
+    grid = std::min(grid, max_blocks);
+
+    PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 2 * sizeof(unsigned long long), g->stream));
+    void *args[] = {&a};
+    PTW_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(t.block), args, smem, g->stream));
+    return PTW_OK;
+}
+
+int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
+                 int start_mode, uint32_t n_sources, int32_t *paths)
+{
+    const DeviceGraph &dg = g->dg;
+    PathArgs a;
+    a.adj = dg.adj;
+    a.col = dg.col;
+    a.start_map = dg.idx2int;
+    a.sources = g->sc.sources;
+    a.int2name = dg.int2name;
+    a.paths = paths;
+    a.w_begin = w_begin;
+    a.n_walk = w_end - w_begin;
+    a.n = dg.n;
+    a.L = L;
+    a.key0 = (uint32_t)seed;
+    a.key1 = (uint32_t)(seed >> 32);
+    a.n_sources = n_sources;
+    a.start_mode = start_mode;
+    int per_sm = 0;
+    PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_paths, kPathWarps * 32, 0));
+    per_sm = std::max(per_sm, 1);
+    const uint64_t groups = (a.n_walk + 31) / 32;
+    uint64_t grid = std::min<uint64_t>((uint64_t)g->num_sms * per_sm, (groups + kPathWarps - 1) / kPathWarps);
+    grid = std::max<uint64_t>(grid, 1);
+    k_paths<<<(unsigned)grid, kPathWarps * 32, 0, g->stream>>>(a);
+    PTW_CUDA(cudaGetLastError());
+    return PTW_OK;
+}
+
+int launch_counts_by_name(ptw_graph *g, uint32_t *d_out)
+{
+    const DeviceGraph &dg = g->dg;
+    if (dg.id_bound != dg.n)
+        PTW_CUDA(cudaMemsetAsync(d_out, 0, (uint64_t)dg.id_bound * 4, g->stream));
+    const unsigned grid = (unsigned)std::min<uint64_t>((dg.n + 255) / 256, (uint64_t)g->num_sms * 16);
+    k_counts_by_name<<<std::max(grid, 1u), 256, 0, g->stream>>>(g->sc.counts, dg.int2name, dg.n, d_out);
+    PTW_CUDA(cudaGetLastError());
+    return PTW_OK;
+}
+
+}  // namespace ptw

@@ -1,0 +1,106 @@
+"""CPU checks of the C ABI: libptw.so builds for sm_103a, loads, and exports
+every entry point include/ptw.h declares; the Python binding covers exactly
+that set.  No compute calls (no GPU here)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from ptwalker_gb300 import _build, _capi
+from ptwalker_gb300 import api
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "ptw.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ptw_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_builds_and_exports_header_symbols():
+    so = _build.build()
+    lib = ctypes.CDLL(so)
+    names = header_functions()
+    assert len(names) >= 18
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_matches_header():
+    bound = sorted(n for n, _, _ in _capi.SIGNATURES)
+    assert bound == header_functions()
+
+
+def test_struct_layouts(tmp_path):
+    """ctypes structs match the C compiler's layout of include/ptw.h."""
+    structs = {"ptw_graph_info": _capi.GraphInfo, "ptw_walk_cfg": _capi.WalkCfg,
+               "ptw_walk_stats": _capi.WalkStats, "ptw_tune": _capi.Tune}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ptw.h"', "int main(void){"]
+    for cname, py in structs.items():
+        lines.append('printf("%%zu\\n", sizeof(%s));' % cname)
+        for fname, _ in py._fields_:
+            lines.append('printf("%%zu\\n", offsetof(%s, %s));' % (cname, fname))
+    lines.append("return 0;}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    import subprocess
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = [int(x) for x in subprocess.check_output([str(exe)]).split()]
+    want = []
+    for py in structs.values():
+        want.append(ctypes.sizeof(py))
+        want.extend(getattr(py, f).offset for f, _ in py._fields_)
+    assert got == want
+
+
+def test_version_and_errors_without_gpu():
+    lib = _capi.load()
+    assert b"sm_103a" in lib.ptw_version()
+    # argument checks run before any device call
+    rc = lib.ptw_graph_from_edges(None, None, 0, 0, ctypes.byref(ctypes.c_void_p()))
+    assert rc == _capi.PTW_EINVAL
+    assert b"empty" in lib.ptw_last_error()
+    rc = lib.ptw_graph_load(b"/nonexistent/file", _capi.PTW_FMT_TEXT, 0, ctypes.byref(ctypes.c_void_p()))
+    assert rc == _capi.PTW_EIO
+    rc = lib.ptw_graph_load(b"x", 7, 0, ctypes.byref(ctypes.c_void_p()))
+    assert rc == _capi.PTW_EINVAL
+    rc = lib.ptw_graph_rmat(0, 16, 0.57, 0.19, 0.19, 1, 1, ctypes.byref(ctypes.c_void_p()))
+    assert rc == _capi.PTW_EINVAL
+    rc = lib.ptw_graph_rmat(10, 16, 0.6, 0.3, 0.3, 1, 1, ctypes.byref(ctypes.c_void_p()))
+    assert rc == _capi.PTW_EINVAL
+    cfg = _capi.WalkCfg()
+    rc = lib.ptw_pagerank(None, ctypes.byref(cfg), None, None)
+    assert rc == _capi.PTW_EINVAL
+    err = _capi.PTWError(rc, "x")
+    assert "PTW_EINVAL" in str(err)
+
+
+def test_malformed_text_edge_list_is_an_io_error(tmp_path):
+    lib = _capi.load()
+    p = tmp_path / "bad.txt"
+    p.write_text("# comment\n0 1\n1 x\n")
+    rc = lib.ptw_graph_load(str(p).encode(), _capi.PTW_FMT_TEXT, 0, ctypes.byref(ctypes.c_void_p()))
+    assert rc == _capi.PTW_EIO
+    assert b"line 3" in lib.ptw_last_error()
+    p.write_bytes(b"\x00" * 12)
+    rc = lib.ptw_graph_load(str(p).encode(), _capi.PTW_FMT_BINARY, 0, ctypes.byref(ctypes.c_void_p()))
+    assert rc == _capi.PTW_EIO
+
+
+def test_cfg_builder():
+    cfg, keep = api._cfg(10, 0.15, -1, "sources", [3, 4], 0, first_walker=7 << 32)
+    assert cfg.seed == 0xFFFFFFFFFFFFFFFF
+    assert cfg.start_mode == _capi.PTW_START_SOURCES and cfg.n_sources == 2
+    assert list(keep) == [3, 4] and cfg.first_walker == 7 << 32
+    with pytest.raises(ValueError):
+        api._cfg(10, 0.15, 0, "uniform", [1], 0)
+    with pytest.raises(KeyError):
+        api._cfg(10, 0.15, 0, "nope", None, 0)
+    t = api.Tune(block=128, ilp=4, chunk=64, hot_k=1024)
+    assert api.Tune.from_c(t.to_c()).as_dict() == t.as_dict()
+    with pytest.raises(ValueError):
+        api._host_ptr(np.zeros(4, dtype=np.uint32)[::2])
