@@ -63,7 +63,32 @@ def build(force=False, verbose=False, extra_flags=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, SO)
+    build_cli()
     return SO
+
+
+CLI_SRC = os.path.join(HERE, "cli", "ptw_cli.cpp")
+BIN_DIR = os.path.join(OUT, "bin")
+APPS = ("pagerank", "ppr", "rwr", "deepwalk")
+
+
+def build_cli():
+    """C++ command-line apps linked against libptw.so (rpath to _lib)."""
+    os.makedirs(BIN_DIR, exist_ok=True)
+    exe = os.path.join(BIN_DIR, "ptw_cli")
+    tmp = exe + ".tmp%d" % os.getpid()
+    cmd = ["g++", "-O2", "-std=c++17", CLI_SRC, "-o", tmp, "-L", OUT, "-lptw",
+           "-Wl,-rpath,$ORIGIN/.."]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("CLI build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(tmp, exe)
+    for app in APPS:
+        link = os.path.join(BIN_DIR, app)
+        if os.path.lexists(link):
+            os.unlink(link)
+        os.symlink("ptw_cli", link)
+    return exe
 
 
 if __name__ == "__main__":
