@@ -172,6 +172,23 @@ int ptw_graph_sync(ptw_graph *g);
  * their own events.  No reference counterpart (the reference is CPU-only). */
 int ptw_graph_set_stream(ptw_graph *g, void *cuda_stream);
 
+/* Count walk that allocates no device memory.  No counterpart in the
+ * reference.  For callers that cannot call cudaMalloc when they run (a host
+ * whose pool allocator owns all device memory, or a context where an
+ * allocation or its implied synchronisation is not allowed).  Same results
+ * as ptw_pagerank_dev: counts by name into the caller's d_counts[id_bound],
+ * issued on cuda_stream (NULL = the graph's stream), asynchronous.
+ * Limits: graphs of at most PTW_NOALLOC_MAX_VERTICES vertices (PTW_EINVAL
+ * beyond), per-vertex or uniform starts only.  The per-vertex counters and
+ * the walker cursor live in one fixed device array inside the library
+ * (about 16 MiB on every GPU that loads it, held until exit).  The first call
+ * on a device looks up that array's address: make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race
+ * and must be serialised. */
+#define PTW_NOALLOC_MAX_VERTICES (1u << 22)
+int ptw_pagerank_noalloc(const ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_counts,
+                         void *cuda_stream);
+
 /* Autotuner (the idea of the sampler micro-benchmark cache,
  * src/core/mini_bmk.hpp:62-117): times the count walk over candidate
  * launch parameters on this graph and device, stores the fastest in the

@@ -81,7 +81,10 @@ SIGNATURES = [
     ("ptw_graph_sync", ctypes.c_int, [_G]),
     ("ptw_graph_set_stream", ctypes.c_int, [_G, _vp]),
     ("ptw_autotune", ctypes.c_int, [_G, ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(Tune)]),
+    ("ptw_pagerank_noalloc", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, _vp]),
 ]
+
+PTW_NOALLOC_MAX_VERTICES = 1 << 22
 
 _lib = None
 
