@@ -32,14 +32,14 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "walker steps/s (PageRank walks, R-MAT scale 24)"
+METRIC = "walker steps/s (PageRank walks on R-MAT)"
 UNIT = "steps/s"
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--scale", type=int, default=24)
@@ -50,6 +50,9 @@ def parse():
     p.add_argument("--no-deepwalk", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
+    p.add_argument("--tune", default=None,
+                   help="block,ilp,chunk,hot_k[,min_blocks[,paths_ilp]]: fixed launch parameters "
+                        "(skips the autotuner)")
     return p.parse_args()
 
 
@@ -196,6 +199,11 @@ def tune_cache_path():
 def get_tune(G, ptw, args, dev_name):
     key = "%s|s%d|ef%d|seed%d|n%d|m%d|sp%g" % (dev_name, args.scale, args.edge_factor, args.seed,
                                                G.n, G.m, args.sp)
+    if args.tune:
+        v = [int(x) for x in args.tune.split(",")]
+        names = ["block", "ilp", "chunk", "hot_k", "min_blocks", "paths_ilp"]
+        G.tune = ptw.Tune(**dict(zip(names, v)))
+        return G.tune, "fixed"
     path = tune_cache_path()
     cache = {}
     if os.path.exists(path):

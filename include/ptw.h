@@ -95,6 +95,8 @@ typedef struct ptw_tune {
     int32_t chunk;         /* walker ids taken per warp refill */
     int32_t hot_k;         /* vertex ids < hot_k counted in shared memory (0 = off) */
     int32_t blocks_per_sm; /* 0 = as many as fit */
+    int32_t min_blocks;    /* 2 = cap registers so two 512-thread blocks fit per SM; 0 = no cap */
+    int32_t paths_ilp;     /* DeepWalk: groups of 32 walkers per warp, 1, 2 or 4 */
     int32_t reserved;
 } ptw_tune;
 

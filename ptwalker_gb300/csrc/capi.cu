@@ -558,7 +558,9 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
     const int ilps[] = {1, 2, 4};
     const int chunks[] = {64, 256, 1024};
     const int hots[] = {0, 8192};
+    const int minbs[] = {0, 2};
     WalkLaunch wl = make_launch(&cfg);
+    for (int mb : minbs)
     for (int hk : hots)
         for (int bl : blocks)
             for (int il : ilps)
@@ -569,6 +571,7 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
                     t.chunk = ch;
                     t.hot_k = hk;
                     t.blocks_per_sm = 0;
+                    t.min_blocks = mb;
                     float tot = 0;
                     bool ok = true;
                     for (int rep = 0; rep < 3 && ok; ++rep) {
@@ -586,6 +589,35 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
                         bt = t;
                     }
                 }
+    // DeepWalk groups per warp: time a short fixed-length walk for each.
+    {
+        const uint64_t W = std::min<uint64_t>(g->dg.n, 1u << 20);
+        const uint32_t L = 16;
+        void *buf = nullptr;
+        int rc = stage_bytes(g, W * L * 4, &buf);
+        if (rc) return rc;
+        float best_ms = 1e30f;
+        bt.paths_ilp = 2;
+        for (int G : {1, 2, 4}) {
+            g->tune = bt;
+            g->tune.paths_ilp = G;
+            float tot = 0;
+            for (int rep = 0; rep < 3; ++rep) {
+                PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
+                rc = launch_paths(g, 0, W, L, 0x5eedull + rep, PTW_START_PER_VERTEX, 0, (int32_t *)buf);
+                if (rc) return rc;
+                PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
+                PTW_CUDA(cudaEventSynchronize(g->ev[1]));
+                float ms = 0;
+                PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]));
+                if (rep) tot += ms;
+            }
+            if (tot < best_ms) {
+                best_ms = tot;
+                bt.paths_ilp = G;
+            }
+        }
+    }
     g->tune = bt;
     if (best) *best = bt;
     return PTW_OK;

@@ -255,6 +255,8 @@ int graph_init_handle(ptw_graph *g)
     g->tune.chunk = 256;
     g->tune.hot_k = 0;
     g->tune.blocks_per_sm = 0;
+    g->tune.min_blocks = 0;
+    g->tune.paths_ilp = 2;
     return PTW_OK;
 }
 

@@ -75,9 +75,8 @@ __device__ __forceinline__ void count_visit(const WalkArgs &a, uint32_t *s_hot, 
 }
 
 template <bool ENDPOINT, int ILP, bool HOT>
-__global__ void k_walk(const WalkArgs a)
+__device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
 {
-    extern __shared__ uint32_t s_hot[];
     if (HOT) {
         for (uint32_t i = threadIdx.x; i < a.hot_k; i += blockDim.x) s_hot[i] = 0;
         __syncthreads();
@@ -191,6 +190,24 @@ __global__ void k_walk(const WalkArgs a)
     }
 }
 
+// Register budget chosen by the compiler (ILP=4: 72 registers, one
+// 512-thread block per SM).
+template <bool ENDPOINT, int ILP, bool HOT>
+__global__ void k_walk(const WalkArgs a)
+{
+    extern __shared__ uint32_t s_hot[];
+    walk_body<ENDPOINT, ILP, HOT>(a, s_hot);
+}
+
+// At most 64 registers so two 512-thread blocks fit on an SM: twice the
+// walkers in flight for the latency-bound gathers.
+template <bool ENDPOINT, int ILP, bool HOT>
+__global__ void __launch_bounds__(512, 2) k_walk_b2(const WalkArgs a)
+{
+    extern __shared__ uint32_t s_hot[];
+    walk_body<ENDPOINT, ILP, HOT>(a, s_hot);
+}
+
 struct PathArgs {
     const uint2 *__restrict__ adj;
     const uint32_t *__restrict__ col;
@@ -205,14 +222,19 @@ struct PathArgs {
     int start_mode;
 };
 
-constexpr int kPathWarps = 8;  // warps per block
+constexpr int kPathWarps = 4;  // warps per block
 
+// G groups of 32 consecutive walkers per warp (one walker of each group per
+// lane), stepped together so a lane has G gathers in flight.
+template <int G>
 __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
 {
-    __shared__ int32_t stage[kPathWarps][32][33];
+    // C path positions are staged per walker before a flush; rows are padded
+    // to C+1 words so the per-lane column writes do not conflict on banks.
+    constexpr uint32_t C = G == 1 ? 32 : 16;
+    __shared__ int32_t stage[kPathWarps][G][32][C + 1];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t wib = threadIdx.x >> 5;
-    int32_t(*buf)[33] = stage[wib];
     const uint64_t n_groups = (a.n_walk + 31) / 32;
     const uint64_t warps = (uint64_t)gridDim.x * kPathWarps;
 
@@ -225,40 +247,58 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
     sa.n_sources = a.n_sources;
     sa.start_mode = a.start_mode;
 
-    for (uint64_t grp = blockIdx.x * (uint64_t)kPathWarps + wib; grp < n_groups; grp += warps) {
-        const uint64_t j = grp * 32 + lane;  // walker offset
-        const bool valid = j < a.n_walk;
-        const uint64_t wid = a.w_begin + j;
-        const uint32_t rows = (uint32_t)umin64(32, a.n_walk - grp * 32);
-        uint32_t v = valid ? start_vertex(sa, wid) : 0;
-        bool dead = !valid;
-        buf[lane][0] = valid ? (int32_t)a.int2name[v] : -1;
-        uint32_t c0 = 0;  // path position of buf column 0
+    for (uint64_t g0 = (blockIdx.x * (uint64_t)kPathWarps + wib) * G; g0 < n_groups; g0 += warps * G) {
+        uint64_t wid[G];
+        uint32_t v[G], rows[G];
+        bool dead[G];
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const uint64_t grp = g0 + g;
+            const uint64_t j = grp * 32 + lane;  // walker offset
+            const bool valid = j < a.n_walk;
+            wid[g] = a.w_begin + j;
+            rows[g] = grp < n_groups ? (uint32_t)umin64(32, a.n_walk - grp * 32) : 0;
+            v[g] = valid ? start_vertex(sa, wid[g]) : 0;
+            dead[g] = !valid;
+            stage[wib][g][lane][0] = valid ? (int32_t)a.int2name[v[g]] : -1;
+        }
+        uint32_t c0 = 0;  // path position of stage column 0
         for (uint32_t p = 1; p <= a.L; ++p) {
-            if (p == a.L || (p & 31) == 0) {
-                // flush columns [c0, p) of the 32 rows
+            if (p == a.L || p % C == 0) {
+                // flush columns [c0, p) of every group's rows; consecutive
+                // lanes write consecutive positions of one path row
                 __syncwarp();
                 const uint32_t cols = p - c0;
-                for (uint32_t rr = 0; rr < rows; ++rr)
-                    if (lane < cols)
-                        a.paths[(grp * 32 + rr) * (uint64_t)a.L + c0 + lane] = buf[rr][lane];
+#pragma unroll
+                for (int g = 0; g < G; ++g)
+                    for (uint32_t idx = lane; idx < rows[g] * cols; idx += 32) {
+                        const uint32_t rr = idx / cols, cc = idx - rr * cols;
+                        a.paths[((g0 + g) * 32 + rr) * (uint64_t)a.L + c0 + cc] = stage[wib][g][rr][cc];
+                    }
                 __syncwarp();
                 c0 = p;
                 if (p == a.L) break;
             }
-            int32_t out = -1;
-            if (!dead) {
-                const uint2 rec = __ldg(&a.adj[v]);
-                if (rec.y == 0) {
-                    dead = true;
-                } else {
-                    const uint4 r = philox(make_uint4((uint32_t)wid, (uint32_t)(wid >> 32), p - 1, PTW_TAG_WALK),
-                                           a.key0, a.key1);
-                    v = __ldg(&a.col[rec.x + __umulhi(r.x, rec.y)]);
-                    out = (int32_t)__ldg(&a.int2name[v]);
+            uint2 rec[G];
+#pragma unroll
+            for (int g = 0; g < G; ++g)
+                if (!dead[g]) rec[g] = __ldg(&a.adj[v[g]]);
+            uint4 r[G];
+#pragma unroll
+            for (int g = 0; g < G; ++g)
+                if (!dead[g])
+                    r[g] = philox(make_uint4((uint32_t)wid[g], (uint32_t)(wid[g] >> 32), p - 1, PTW_TAG_WALK),
+                                  a.key0, a.key1);
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                if (!dead[g]) {
+                    if (rec[g].y == 0) dead[g] = true;
+                    else v[g] = __ldg(&a.col[rec[g].x + __umulhi(r[g].x, rec[g].y)]);
                 }
             }
-            buf[lane][p - c0] = out;
+#pragma unroll
+            for (int g = 0; g < G; ++g)
+                stage[wib][g][lane][p - c0] = dead[g] ? -1 : (int32_t)__ldg(&a.int2name[v[g]]);
         }
     }
 }
@@ -271,9 +311,34 @@ __global__ void k_counts_by_name(const uint32_t *counts, const uint32_t *int2nam
 }
 
 template <bool E, int ILP, bool H> void *walk_fn() { return (void *)k_walk<E, ILP, H>; }
+template <bool E, int ILP, bool H> void *walk_fn_b2() { return (void *)k_walk_b2<E, ILP, H>; }
 
-void *pick_walk(bool endpoint, int ilp, bool hot)
+void *pick_walk_b2(bool endpoint, int ilp, bool hot)
 {
+    if (endpoint) {
+        switch (ilp) {
+        case 1: return walk_fn_b2<true, 1, false>();
+        case 4: return walk_fn_b2<true, 4, false>();
+        default: return walk_fn_b2<true, 2, false>();
+        }
+    }
+    if (hot) {
+        switch (ilp) {
+        case 1: return walk_fn_b2<false, 1, true>();
+        case 4: return walk_fn_b2<false, 4, true>();
+        default: return walk_fn_b2<false, 2, true>();
+        }
+    }
+    switch (ilp) {
+    case 1: return walk_fn_b2<false, 1, false>();
+    case 4: return walk_fn_b2<false, 4, false>();
+    default: return walk_fn_b2<false, 2, false>();
+    }
+}
+
+void *pick_walk(bool endpoint, int ilp, bool hot, int min_blocks)
+{
+    if (min_blocks == 2) return pick_walk_b2(endpoint, ilp, hot);
     if (endpoint) {
         switch (ilp) {
         case 1: return walk_fn<true, 1, false>();
@@ -306,6 +371,12 @@ int check_tune(const ptw_tune &t)
     if (t.hot_k < 0 || t.hot_k > 48 * 1024)
         return fail(PTW_EINVAL, "tune.hot_k must be in [0, 49152]");
     if (t.blocks_per_sm < 0 || t.blocks_per_sm > 64) return fail(PTW_EINVAL, "tune.blocks_per_sm out of range");
+    if (t.min_blocks != 0 && t.min_blocks != 1 && t.min_blocks != 2)
+        return fail(PTW_EINVAL, "tune.min_blocks must be 0, 1 or 2");
+    if (t.min_blocks == 2 && t.block > 512)
+        return fail(PTW_EINVAL, "tune.min_blocks = 2 needs tune.block <= 512");
+    if (t.paths_ilp != 0 && t.paths_ilp != 1 && t.paths_ilp != 2 && t.paths_ilp != 4)
+        return fail(PTW_EINVAL, "tune.paths_ilp must be 1, 2 or 4 (0 = default)");
     return PTW_OK;
 }
 
@@ -336,7 +407,7 @@ int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t)
     a.hot_k = hot ? std::min<uint32_t>((uint32_t)t.hot_k, dg.n) : 0;
     a.start_mode = wl.start_mode;
 
-    void *fn = pick_walk(wl.endpoint, t.ilp, hot);
+    void *fn = pick_walk(wl.endpoint, t.ilp, hot, t.min_blocks);
     const size_t smem = hot ? (size_t)a.hot_k * 4 : 0;
     if (smem > 48 * 1024)
         PTW_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -375,14 +446,18 @@ int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uin
     a.key1 = (uint32_t)(seed >> 32);
     a.n_sources = n_sources;
     a.start_mode = start_mode;
+    const int G = g->tune.paths_ilp == 1 || g->tune.paths_ilp == 4 ? g->tune.paths_ilp : 2;
+    const void *fn = G == 1 ? (const void *)k_paths<1> : G == 4 ? (const void *)k_paths<4>
+                                                                : (const void *)k_paths<2>;
     int per_sm = 0;
-    PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_paths, kPathWarps * 32, 0));
+    PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPathWarps * 32, 0));
     per_sm = std::max(per_sm, 1);
     const uint64_t groups = (a.n_walk + 31) / 32;
-    uint64_t grid = std::min<uint64_t>((uint64_t)g->num_sms * per_sm, (groups + kPathWarps - 1) / kPathWarps);
+    const uint64_t per_block = (uint64_t)kPathWarps * G;
+    uint64_t grid = std::min<uint64_t>((uint64_t)g->num_sms * per_sm, (groups + per_block - 1) / per_block);
     grid = std::max<uint64_t>(grid, 1);
-    k_paths<<<(unsigned)grid, kPathWarps * 32, 0, g->stream>>>(a);
-    PTW_CUDA(cudaGetLastError());
+    void *args[] = {&a};
+    PTW_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kPathWarps * 32), args, 0, g->stream));
     return PTW_OK;
 }
 

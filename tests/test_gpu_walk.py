@@ -66,6 +66,9 @@ def test_ppr_sources_and_query_ids(gpu, G16, s16_canon, sources, W, qid):
     dict(block=256, ilp=4, chunk=4096, hot_k=0),
     dict(block=1024, ilp=2, chunk=256, hot_k=40000),
     dict(block=512, ilp=4, chunk=64, hot_k=8192, blocks_per_sm=1),
+    dict(block=512, ilp=4, chunk=256, hot_k=8192, min_blocks=2),
+    dict(block=256, ilp=1, chunk=64, hot_k=0, min_blocks=2),
+    dict(block=128, ilp=2, chunk=7, hot_k=100, min_blocks=2),
 ])
 def test_launch_parameters_do_not_change_results(gpu, G16, s16_canon, tune):
     saved = G16.tune
@@ -102,6 +105,43 @@ def test_deepwalk_paths_bit_exact(gpu, G16, s16_canon, L, W, start):
     W = G16.n if W is None else W
     got = gpu.deepwalk(G16, W, L, 13, start)
     want = oracle.replay_paths(s16_canon, 0, W, L, 13, MODES[start])
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("paths_ilp", [1, 2, 4])
+def test_deepwalk_groups_per_warp(gpu, G16, s16_canon, paths_ilp):
+    saved = G16.tune
+    try:
+        t = G16.tune
+        t.paths_ilp = paths_ilp
+        G16.tune = t
+        for W, L in ((G16.n, 40), (4096 + 33, 7), (65, 33)):
+            got = gpu.deepwalk(G16, W, L, 17)
+            assert np.array_equal(got, oracle.replay_paths(s16_canon, 0, W, L, 17, START_PER_VERTEX))
+    finally:
+        G16.tune = saved
+
+
+def test_rwr_with_register_capped_kernel(gpu, G16, s16_canon):
+    saved = G16.tune
+    try:
+        G16.tune = gpu.Tune(block=512, ilp=4, chunk=128, hot_k=0, min_blocks=2)
+        got = gpu.rwr(G16, 3 * G16.n, 0.3, 23, "uniform")
+    finally:
+        G16.tune = saved
+    want, _ = oracle.replay_pairs(s16_canon, 0, 3 * G16.n, 0.3, 23, START_UNIFORM)
+    assert np.array_equal(got, want)
+
+
+def test_autotune_keeps_results(gpu, G16, s16_canon):
+    saved = G16.tune
+    try:
+        t = G16.autotune(0.15)
+        assert t.ilp in (1, 2, 4) and t.paths_ilp in (1, 2, 4) and t.min_blocks in (0, 2)
+        got = gpu.pagerank(G16, G16.n, 0.15, 99)
+    finally:
+        G16.tune = saved
+    want, _ = oracle.replay_counts(s16_canon, 0, G16.n, 0.15, 99, START_PER_VERTEX)
     assert np.array_equal(got, want)
 
 
