@@ -97,7 +97,8 @@ typedef struct ptw_tune {
     int32_t blocks_per_sm; /* 0 = as many as fit */
     int32_t min_blocks;    /* 2 = cap registers so two 512-thread blocks fit per SM; 0 = no cap */
     int32_t paths_ilp;     /* DeepWalk: groups of 32 walkers per warp, 1, 2 or 4 */
-    int32_t reserved;
+    int32_t cache_hints;   /* 1 = L2 evict_last for row records and counters, evict_first
+                              for the column array; 0 = default L2 policy */
 } ptw_tune;
 
 const char *ptw_last_error(void);
@@ -173,6 +174,52 @@ int ptw_graph_sync(ptw_graph *g);
  * returns to the graph's own stream), so callers can order and time it with
  * their own events.  No reference counterpart (the reference is CPU-only). */
 int ptw_graph_set_stream(ptw_graph *g, void *cuda_stream);
+
+/* ---- batched PPR / RWR ------------------------------------------------- */
+
+/* One single-source query.  Its walkers have ids (query_id << 32) + j,
+ * j < budget, so its result is the same alone or in any batch. */
+typedef struct ptw_query {
+    uint32_t source;   /* vertex name */
+    uint32_t query_id;
+    uint64_t budget;   /* walkers, 1 .. 2^28 */
+} ptw_query;
+
+#define PTW_APP_VISITS 0   /* count every position (PPR: src/core/ppr.cpp:114-117) */
+#define PTW_APP_ENDPOINT 1 /* count the vertex after the last move (RWR: src/core/RWR.cpp:99-105) */
+
+typedef struct ptw_batch_cfg {
+    double sp;            /* stop probability after each move */
+    uint64_t seed;
+    int32_t app;          /* PTW_APP_* */
+    uint32_t max_moves;   /* 0 = unbounded */
+    uint64_t table_bytes; /* device memory for the count tables of one wave; 0 = 1/4 of free */
+    double table_factor;  /* table slots per expected counted position; 0 = 2.  A query whose
+                             table fills is run again with 2n slots, so results never depend on it */
+} ptw_batch_cfg;
+
+typedef struct ptw_batch ptw_batch; /* the sparse results of one batch (host memory) */
+
+/* Runs nq queries: the reference runs one source per process
+ * (src/core/ppr.cpp:121-138 hard-codes internal id 0); here a device query
+ * table feeds one persistent walker launch per wave of queries, waves sized
+ * so their per-query hash tables fit table_bytes.  Results are kept sparse:
+ * (vertex name, count) pairs per query, sorted by name. */
+int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t nq, const ptw_batch_cfg *cfg,
+                  ptw_batch **out);
+/* Number of queries, total (name, count) entries, and walk statistics. */
+int ptw_batch_info(const ptw_batch *b, uint32_t *nq, uint64_t *entries, ptw_walk_stats *stats);
+/* h_offsets[nq + 1]: query i owns entries [h_offsets[i], h_offsets[i+1]).
+ * Any pointer may be NULL. */
+int ptw_batch_export(const ptw_batch *b, uint64_t *h_offsets, uint32_t *h_names, uint32_t *h_counts);
+void ptw_batch_free(ptw_batch *b);
+
+/* FP64 oracle on the device: for each source name, the exact expected count
+ * vector of the app (visits: pi_s / (sp (1-sp)) - sp/(1-sp) e_s; endpoint:
+ * (pi_s - sp e_s) / (1-sp)) by power iteration until the added mass is below
+ * tol, and the L1 distance between it and the normalised sparse counts of
+ * query i of batch b (both normalised to sum 1).  h_l1[nq]. */
+int ptw_batch_l1(ptw_graph *g, const ptw_batch *b, double sp, int32_t app, double tol, double *h_l1);
 
 /* Count walk that allocates no device memory.  No counterpart in the
  * reference.  For callers that cannot call cudaMalloc when they run (a host

@@ -22,4 +22,6 @@ from .api import (  # noqa: F401
     walk,
 )
 
+from .batch import BatchResult, ppr_batch  # noqa: F401,E402
+
 __version__ = "0.1.0"

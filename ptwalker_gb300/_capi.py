@@ -43,11 +43,25 @@ class WalkStats(ctypes.Structure):
                 ("total_ms", ctypes.c_float)]
 
 
+class Query(ctypes.Structure):
+    _fields_ = [("source", ctypes.c_uint32), ("query_id", ctypes.c_uint32), ("budget", ctypes.c_uint64)]
+
+
+class BatchCfg(ctypes.Structure):
+    _fields_ = [("sp", ctypes.c_double), ("seed", ctypes.c_uint64), ("app", ctypes.c_int32),
+                ("max_moves", ctypes.c_uint32), ("table_bytes", ctypes.c_uint64),
+                ("table_factor", ctypes.c_double)]
+
+
+PTW_APP_VISITS = 0
+PTW_APP_ENDPOINT = 1
+
+
 class Tune(ctypes.Structure):
     _fields_ = [("block", ctypes.c_int32), ("ilp", ctypes.c_int32), ("chunk", ctypes.c_int32),
                 ("hot_k", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("min_blocks", ctypes.c_int32), ("paths_ilp", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("cache_hints", ctypes.c_int32)]
 
 
 # Every symbol include/ptw.h declares: (name, restype, argtypes).
@@ -83,6 +97,14 @@ SIGNATURES = [
     ("ptw_graph_set_stream", ctypes.c_int, [_G, _vp]),
     ("ptw_autotune", ctypes.c_int, [_G, ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(Tune)]),
     ("ptw_pagerank_noalloc", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, _vp]),
+    ("ptw_ppr_batch", ctypes.c_int, [_G, ctypes.POINTER(Query), ctypes.c_uint32,
+                                     ctypes.POINTER(BatchCfg), _GP]),
+    ("ptw_batch_info", ctypes.c_int, [_G, ctypes.POINTER(ctypes.c_uint32), _u64p,
+                                      ctypes.POINTER(WalkStats)]),
+    ("ptw_batch_export", ctypes.c_int, [_G, _u64p, _u32p, _u32p]),
+    ("ptw_batch_free", None, [_G]),
+    ("ptw_batch_l1", ctypes.c_int, [_G, _G, ctypes.c_double, ctypes.c_int32, ctypes.c_double,
+                                    ctypes.POINTER(ctypes.c_double)]),
 ]
 
 PTW_NOALLOC_MAX_VERTICES = 1 << 22

@@ -55,23 +55,24 @@ class Tune:
     """Launch parameters of the walk kernels (see ptw_tune in include/ptw.h)."""
 
     def __init__(self, block=256, ilp=2, chunk=256, hot_k=0, blocks_per_sm=0, min_blocks=0,
-                 paths_ilp=2):
+                 paths_ilp=2, cache_hints=0):
         self.block, self.ilp, self.chunk = block, ilp, chunk
         self.hot_k, self.blocks_per_sm, self.min_blocks = hot_k, blocks_per_sm, min_blocks
-        self.paths_ilp = paths_ilp
+        self.paths_ilp, self.cache_hints = paths_ilp, cache_hints
 
     def to_c(self):
         return C.Tune(self.block, self.ilp, self.chunk, self.hot_k, self.blocks_per_sm,
-                      self.min_blocks, self.paths_ilp, 0)
+                      self.min_blocks, self.paths_ilp, self.cache_hints)
 
     @classmethod
     def from_c(cls, t):
-        return cls(t.block, t.ilp, t.chunk, t.hot_k, t.blocks_per_sm, t.min_blocks, t.paths_ilp)
+        return cls(t.block, t.ilp, t.chunk, t.hot_k, t.blocks_per_sm, t.min_blocks, t.paths_ilp,
+                   t.cache_hints)
 
     def as_dict(self):
         return dict(block=self.block, ilp=self.ilp, chunk=self.chunk, hot_k=self.hot_k,
                     blocks_per_sm=self.blocks_per_sm, min_blocks=self.min_blocks,
-                    paths_ilp=self.paths_ilp)
+                    paths_ilp=self.paths_ilp, cache_hints=self.cache_hints)
 
     def __repr__(self):
         return "Tune(%s)" % ", ".join("%s=%s" % kv for kv in self.as_dict().items())

@@ -554,12 +554,14 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
     const ptw_tune saved = g->tune;
     ptw_tune bt = saved;
     float bms = 1e30f;
-    const int blocks[] = {128, 256, 512};
-    const int ilps[] = {1, 2, 4};
-    const int chunks[] = {64, 256, 1024};
+    const int blocks[] = {256, 512};
+    const int ilps[] = {2, 4};
+    const int chunks[] = {64, 256};
     const int hots[] = {0, 8192};
     const int minbs[] = {0, 2};
+    const int hintss[] = {0, 1};
     WalkLaunch wl = make_launch(&cfg);
+    for (int hn : hintss)
     for (int mb : minbs)
     for (int hk : hots)
         for (int bl : blocks)
@@ -572,6 +574,8 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
                     t.hot_k = hk;
                     t.blocks_per_sm = 0;
                     t.min_blocks = mb;
+                    t.cache_hints = hn;
+                    t.paths_ilp = 2;
                     float tot = 0;
                     bool ok = true;
                     for (int rep = 0; rep < 3 && ok; ++rep) {

@@ -43,6 +43,37 @@ __device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1)
     return c;
 }
 
+// L2 eviction-priority policies (PTX createpolicy) for the gathers:
+// kind 0 = normal, 1 = evict_last (keep: row records, visit counters),
+// 2 = evict_first (stream: the column array).
+__device__ __forceinline__ uint64_t l2_policy(int kind)
+{
+    uint64_t p;
+    if (kind == 1) asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    else if (kind == 2) asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    else asm("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ uint2 ld_hint_u2(const uint2 *p, uint64_t pol)
+{
+    uint2 r;
+    asm("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;" : "=r"(r.x), "=r"(r.y) : "l"(p), "l"(pol));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t ld_hint_u32(const uint32_t *p, uint64_t pol)
+{
+    uint32_t r;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+    return r;
+}
+
+__device__ __forceinline__ void red_add_hint(uint32_t *p, uint32_t v, uint64_t pol)
+{
+    asm volatile("red.global.add.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+
 // Device-resident graph.  Internal vertex ids are ranks by descending
 // degree (ties by ascending name), so the hottest rows, counters and column
 // blocks sit at the low end of every array and stay in L2.
@@ -112,5 +143,8 @@ int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uin
                  int start_mode, uint32_t n_sources, int32_t *paths);
 int launch_counts_by_name(ptw_graph *g, uint32_t *d_out);
 int check_tune(const ptw_tune &t);
+
+// The query table a batch was run with (batch.cu).
+const ptw_query *batch_queries(const ptw_batch *b);
 
 }  // namespace ptw

@@ -52,6 +52,7 @@ struct WalkArgs {
     uint32_t chunk;
     uint32_t hot_k;
     int start_mode;
+    int hints;  // L2 eviction priorities on (see l2_policy)
 };
 
 __device__ __forceinline__ uint32_t start_vertex(const WalkArgs &a, uint64_t wid)
@@ -68,10 +69,10 @@ __device__ __forceinline__ uint32_t start_vertex(const WalkArgs &a, uint64_t wid
 }
 
 template <bool HOT>
-__device__ __forceinline__ void count_visit(const WalkArgs &a, uint32_t *s_hot, uint32_t v)
+__device__ __forceinline__ void count_visit(const WalkArgs &a, uint32_t *s_hot, uint32_t v, uint64_t pol)
 {
     if (HOT && v < a.hot_k) atomicAdd(&s_hot[v], 1u);
-    else atomicAdd(&a.counts[v], 1u);
+    else red_add_hint(&a.counts[v], 1u, pol);
 }
 
 template <bool ENDPOINT, int ILP, bool HOT>
@@ -81,6 +82,8 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
         for (uint32_t i = threadIdx.x; i < a.hot_k; i += blockDim.x) s_hot[i] = 0;
         __syncthreads();
     }
+    const uint64_t pol_keep = l2_policy(a.hints ? 1 : 0);   // row records, counters
+    const uint64_t pol_stream = l2_policy(a.hints ? 2 : 0); // column array
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt_mask = (1u << lane) - 1u;
 
@@ -132,7 +135,7 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
                 s0[k] = v[k];
                 step[k] = 0;
                 act[k] = true;
-                if (!ENDPOINT) count_visit<HOT>(a, s_hot, v[k]);
+                if (!ENDPOINT) count_visit<HOT>(a, s_hot, v[k], pol_keep);
             }
         }
         bool any = false;
@@ -144,7 +147,7 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
         uint2 rec[ILP];
 #pragma unroll
         for (int k = 0; k < ILP; ++k)
-            if (act[k]) rec[k] = __ldg(&a.adj[v[k]]);
+            if (act[k]) rec[k] = ld_hint_u2(&a.adj[v[k]], pol_keep);
         uint4 r[ILP];
 #pragma unroll
         for (int k = 0; k < ILP; ++k)
@@ -154,7 +157,8 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
         uint32_t nb[ILP];
 #pragma unroll
         for (int k = 0; k < ILP; ++k)
-            if (act[k] && rec[k].y != 0) nb[k] = __ldg(&a.col[rec[k].x + __umulhi(r[k].x, rec[k].y)]);
+            if (act[k] && rec[k].y != 0)
+                nb[k] = ld_hint_u32(&a.col[rec[k].x + __umulhi(r[k].x, rec[k].y)], pol_stream);
 #pragma unroll
         for (int k = 0; k < ILP; ++k) {
             if (!act[k]) continue;
@@ -165,8 +169,8 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
                 v[k] = nb[k];
                 ++step[k];
                 ++moves;
-                if (!ENDPOINT) count_visit<HOT>(a, s_hot, v[k]);
-                done = (uint64_t)r[k].y < a.thr || (a.max_moves && step[k] >= a.max_moves);
+                if (!ENDPOINT) count_visit<HOT>(a, s_hot, v[k], pol_keep);
+                done =(uint64_t)r[k].y < a.thr || (a.max_moves && step[k] >= a.max_moves);
             }
             if (done) {
                 if (ENDPOINT) {
@@ -220,6 +224,7 @@ struct PathArgs {
     uint32_t key0, key1;
     uint32_t n_sources;
     int start_mode;
+    int hints;
 };
 
 constexpr int kPathWarps = 4;  // warps per block
@@ -246,6 +251,8 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
     sa.key1 = a.key1;
     sa.n_sources = a.n_sources;
     sa.start_mode = a.start_mode;
+    const uint64_t pol_keep = l2_policy(a.hints ? 1 : 0);   // row records, names
+    const uint64_t pol_stream = l2_policy(a.hints ? 2 : 0); // column array
 
     for (uint64_t g0 = (blockIdx.x * (uint64_t)kPathWarps + wib) * G; g0 < n_groups; g0 += warps * G) {
         uint64_t wid[G];
@@ -282,7 +289,7 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
             uint2 rec[G];
 #pragma unroll
             for (int g = 0; g < G; ++g)
-                if (!dead[g]) rec[g] = __ldg(&a.adj[v[g]]);
+                if (!dead[g]) rec[g] = ld_hint_u2(&a.adj[v[g]], pol_keep);
             uint4 r[G];
 #pragma unroll
             for (int g = 0; g < G; ++g)
@@ -293,12 +300,12 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
             for (int g = 0; g < G; ++g) {
                 if (!dead[g]) {
                     if (rec[g].y == 0) dead[g] = true;
-                    else v[g] = __ldg(&a.col[rec[g].x + __umulhi(r[g].x, rec[g].y)]);
+                    else v[g] = ld_hint_u32(&a.col[rec[g].x + __umulhi(r[g].x, rec[g].y)], pol_stream);
                 }
             }
 #pragma unroll
             for (int g = 0; g < G; ++g)
-                stage[wib][g][lane][p - c0] = dead[g] ? -1 : (int32_t)__ldg(&a.int2name[v[g]]);
+                stage[wib][g][lane][p - c0] = dead[g] ? -1 : (int32_t)ld_hint_u32(&a.int2name[v[g]], pol_keep);
         }
     }
 }
@@ -377,6 +384,7 @@ int check_tune(const ptw_tune &t)
         return fail(PTW_EINVAL, "tune.min_blocks = 2 needs tune.block <= 512");
     if (t.paths_ilp != 0 && t.paths_ilp != 1 && t.paths_ilp != 2 && t.paths_ilp != 4)
         return fail(PTW_EINVAL, "tune.paths_ilp must be 1, 2 or 4 (0 = default)");
+    if (t.cache_hints != 0 && t.cache_hints != 1) return fail(PTW_EINVAL, "tune.cache_hints must be 0 or 1");
     return PTW_OK;
 }
 
@@ -406,6 +414,7 @@ int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t)
     const bool hot = !wl.endpoint && t.hot_k > 0;
     a.hot_k = hot ? std::min<uint32_t>((uint32_t)t.hot_k, dg.n) : 0;
     a.start_mode = wl.start_mode;
+    a.hints = t.cache_hints;
 
     void *fn = pick_walk(wl.endpoint, t.ilp, hot, t.min_blocks);
     const size_t smem = hot ? (size_t)a.hot_k * 4 : 0;
@@ -446,7 +455,8 @@ int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uin
     a.key1 = (uint32_t)(seed >> 32);
     a.n_sources = n_sources;
     a.start_mode = start_mode;
-    const int G = g->tune.paths_ilp == 1 || g->tune.paths_ilp == 4 ? g->tune.paths_ilp : 2;
+    a.hints = g->tune.cache_hints;
+    const int G =g->tune.paths_ilp == 1 || g->tune.paths_ilp == 4 ? g->tune.paths_ilp : 2;
     const void *fn = G == 1 ? (const void *)k_paths<1> : G == 4 ? (const void *)k_paths<4>
                                                                 : (const void *)k_paths<2>;
     int per_sm = 0;

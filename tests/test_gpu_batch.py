@@ -1,0 +1,119 @@
+"""Batched PPR / RWR: per-query sparse counts vs the oracle replay of each
+query alone (bit-exact), independence from batch composition and wave
+sizing, table-overflow recovery, and the device FP64 L1 oracle vs the CPU
+FP64 oracle."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle.replay import START_SOURCES
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def G16(gpu):
+    G = gpu.Graph.rmat(16, 16, 0.57, 0.19, 0.19, seed=1, clean=True)
+    yield G
+    G.close()
+
+
+def replay_query(canon, src, qid, budget, sp, seed, app, max_moves=0):
+    w0 = qid << 32
+    if app == "visits":
+        c, _ = oracle.replay_counts(canon, w0, w0 + budget, sp, seed, START_SOURCES, [src],
+                                    max_moves=max_moves)
+        return c
+    pairs, _ = oracle.replay_pairs(canon, w0, w0 + budget, sp, seed, START_SOURCES, [src],
+                                   max_moves=max_moves)
+    return np.bincount(pairs[:, 1], minlength=canon.n).astype(np.uint32)
+
+
+def sparse_equal(res, i, dense):
+    names, counts = res.query(i)
+    nz = np.nonzero(dense)[0]
+    return np.array_equal(names, nz.astype(np.uint32)) and np.array_equal(counts, dense[nz])
+
+
+@pytest.mark.parametrize("app", ["visits", "endpoint"])
+def test_batch_bit_exact_per_query(gpu, G16, s16_canon, app):
+    rng = np.random.default_rng(5)
+    nq = 24
+    sources = rng.integers(0, G16.n, nq)
+    budgets = rng.integers(1, 20000, nq)
+    budgets[0] = 1
+    qids = rng.permutation(1000)[:nq]
+    res = gpu.ppr_batch(G16, sources, budgets, sp=0.2, seed=9, app=app, query_ids=qids)
+    assert res.nq == nq and res.walkers == int(budgets.sum())
+    tot_moves = 0
+    for i in range(nq):
+        want = replay_query(s16_canon, int(sources[i]), int(qids[i]), int(budgets[i]), 0.2, 9, app)
+        assert sparse_equal(res, i, want), i
+        if app == "visits":
+            tot_moves += int(want.sum()) - int(budgets[i])
+    if app == "visits":
+        assert res.moves == tot_moves
+
+
+def test_query_alone_equals_query_in_batch_and_across_waves(gpu, G16):
+    sources = [3, 77, 77, 1024, 46000]
+    budgets = [5000, 3000, 3000, 7000, 100]
+    full = gpu.ppr_batch(G16, sources, budgets, sp=0.15, seed=4, query_ids=[10, 11, 12, 13, 14])
+    alone = gpu.ppr_batch(G16, [1024], [7000], sp=0.15, seed=4, query_ids=[13])
+    assert np.array_equal(full.dense(3), alone.dense(0))
+    # one table per wave: every query in its own wave
+    waves = gpu.ppr_batch(G16, sources, budgets, sp=0.15, seed=4, query_ids=[10, 11, 12, 13, 14],
+                          table_bytes=1)
+    for i in range(5):
+        assert np.array_equal(full.dense(i), waves.dense(i))
+    # the same source under two query ids draws two different walker streams
+    assert not np.array_equal(full.dense(1), full.dense(2))
+    # a query equals the single-source PPR call with first_walker = qid << 32
+    single = gpu.ppr(G16, 1024, 7000, 0.15, 4, query_id=13)
+    assert np.array_equal(single, alone.dense(0))
+
+
+def test_table_overflow_rerun_is_exact(gpu, G16, s16_canon):
+    # tiny tables force the probe limit; the rerun with 2n slots must give
+    # the same counts as the replay
+    sources = [0, 5, 9]
+    budgets = [20000, 20000, 20000]
+    res = gpu.ppr_batch(G16, sources, budgets, sp=0.2, seed=3, query_ids=[0, 1, 2], table_factor=0.001)
+    for i in range(3):
+        want = replay_query(s16_canon, sources[i], i, budgets[i], 0.2, 3, "visits")
+        assert sparse_equal(res, i, want)
+
+
+def test_batch_max_moves_and_errors(gpu, G16, s16_canon):
+    res = gpu.ppr_batch(G16, [8, 9], [3000, 4000], sp=0.0001, seed=2, query_ids=[1, 2], max_moves=3)
+    for i, (s, b, q) in enumerate(((8, 3000, 1), (9, 4000, 2))):
+        want = replay_query(s16_canon, s, q, b, 0.0001, 2, "visits", max_moves=3)
+        assert sparse_equal(res, i, want)
+    with pytest.raises(gpu.PTWError):
+        gpu.ppr_batch(G16, [10 ** 8], [10])
+    with pytest.raises(gpu.PTWError):
+        gpu.ppr_batch(G16, [1], [0])
+    with pytest.raises(gpu.PTWError):
+        gpu.ppr_batch(G16, [1], [10], sp=0.0)
+    empty = gpu.ppr_batch(G16, [], [])
+    assert empty.nq == 0 and empty.entries == 0
+
+
+@pytest.mark.parametrize("app", ["visits", "endpoint"])
+def test_device_fp64_l1_matches_cpu_oracle(gpu, G16, s16_canon, app):
+    sp = 0.2
+    sources = [0, 17, 500, 46878]
+    res = gpu.ppr_batch(G16, sources, [20000] * 4, sp=sp, seed=12, app=app)
+    l1_dev = res.l1(tol=1e-12)
+    from oracle.power import _transition_T
+    PT = _transition_T(s16_canon)
+    for i, s in enumerate(sources):
+        idx = s16_canon.name_to_index([s])[0]
+        if app == "visits":
+            exp = oracle.expected_visits_from_source(s16_canon, sp, idx, tol=1e-13, PT=PT)
+        else:
+            exp = oracle.expected_endpoint_from_source(s16_canon, sp, idx, tol=1e-13, PT=PT)
+        c = res.dense(i).astype(np.float64)
+        l1_cpu = np.abs(c / c.sum() - exp / exp.sum()).sum()
+        assert abs(l1_dev[i] - l1_cpu) < 1e-8, (i, l1_dev[i], l1_cpu)
+        assert l1_dev[i] < 0.5

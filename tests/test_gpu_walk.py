@@ -69,6 +69,8 @@ def test_ppr_sources_and_query_ids(gpu, G16, s16_canon, sources, W, qid):
     dict(block=512, ilp=4, chunk=256, hot_k=8192, min_blocks=2),
     dict(block=256, ilp=1, chunk=64, hot_k=0, min_blocks=2),
     dict(block=128, ilp=2, chunk=7, hot_k=100, min_blocks=2),
+    dict(block=512, ilp=4, chunk=256, hot_k=8192, cache_hints=1),
+    dict(block=256, ilp=2, chunk=64, hot_k=0, min_blocks=2, cache_hints=1),
 ])
 def test_launch_parameters_do_not_change_results(gpu, G16, s16_canon, tune):
     saved = G16.tune
@@ -108,12 +110,13 @@ def test_deepwalk_paths_bit_exact(gpu, G16, s16_canon, L, W, start):
     assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("paths_ilp", [1, 2, 4])
-def test_deepwalk_groups_per_warp(gpu, G16, s16_canon, paths_ilp):
+@pytest.mark.parametrize("paths_ilp,hints", [(1, 0), (2, 0), (4, 0), (2, 1), (4, 1)])
+def test_deepwalk_groups_per_warp(gpu, G16, s16_canon, paths_ilp, hints):
     saved = G16.tune
     try:
         t = G16.tune
         t.paths_ilp = paths_ilp
+        t.cache_hints = hints
         G16.tune = t
         for W, L in ((G16.n, 40), (4096 + 33, 7), (65, 33)):
             got = gpu.deepwalk(G16, W, L, 17)
