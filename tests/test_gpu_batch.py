@@ -116,4 +116,4 @@ def test_device_fp64_l1_matches_cpu_oracle(gpu, G16, s16_canon, app):
         c = res.dense(i).astype(np.float64)
         l1_cpu = np.abs(c / c.sum() - exp / exp.sum()).sum()
         assert abs(l1_dev[i] - l1_cpu) < 1e-8, (i, l1_dev[i], l1_cpu)
-        assert l1_dev[i] < 0.5
+        assert 0.0 < l1_dev[i] < 2.0
