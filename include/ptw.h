@@ -221,6 +221,61 @@ void ptw_batch_free(ptw_batch *b);
  * query i of batch b (both normalised to sum 1).  h_l1[nq]. */
 int ptw_batch_l1(ptw_graph *g, const ptw_batch *b, double sp, int32_t app, double tol, double *h_l1);
 
+/* ---- serving loop with continuous batching ----------------------------- */
+
+/* No counterpart in the reference (one query per process).  Queries are
+ * submitted as they arrive; each ptw_serve_step admits waiting queries while
+ * their count tables fit the device table arena (admission by device
+ * memory) and free query slots remain, then runs one tick: every active
+ * query gets a share of tick_walkers walkers, all in one launch, so queries
+ * that arrived while others were running share the GPU with them.  A query
+ * completes when all its walkers have run; its sparse result is then
+ * compacted and kept on the host until taken.  The tick's copy-in, walk
+ * kernel and copy-out are one CUDA graph, replayed with new parameters. */
+typedef struct ptw_server ptw_server;
+
+typedef struct ptw_serve_cfg {
+    double sp;
+    uint64_t seed;
+    int32_t app;            /* PTW_APP_* */
+    uint32_t max_moves;
+    uint64_t table_bytes;   /* device arena for count tables; 0 = 1/4 of free memory */
+    uint64_t tick_walkers;  /* walkers started per tick over all active queries; 0 = 2^22 */
+    uint32_t max_active;    /* query slots; 0 = 4096 */
+    uint32_t use_graph;     /* 1 = replay the tick as a CUDA graph */
+    double table_factor;    /* as in ptw_batch_cfg */
+} ptw_serve_cfg;
+
+typedef struct ptw_serve_result {
+    uint32_t query_id;
+    uint32_t source;
+    uint64_t budget;
+    uint64_t n_entries;     /* (name, count) pairs */
+    double submit_s;        /* host clock (s since open) at submission */
+    double admit_s;         /* ... when its table was allocated */
+    double done_s;          /* ... when its result reached the host */
+} ptw_serve_result;
+
+int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server **out);
+/* Queues one query (validated now: unknown source or bad budget = PTW_EINVAL). */
+int ptw_serve_submit(ptw_server *s, const ptw_query *q);
+/* Admits, runs one tick, collects completed queries; *n_active and
+ * *n_pending (may be NULL) report the state after the tick. */
+int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_active, uint32_t *n_pending);
+/* Oldest completed, not yet taken result: 1 and *r filled, or 0 if none. */
+int ptw_serve_poll(ptw_server *s, ptw_serve_result *r);
+/* Copies the polled result's entries (n_entries each) and drops it. */
+int ptw_serve_take(ptw_server *s, uint32_t *h_names, uint32_t *h_counts);
+/* Seconds since ptw_serve_open on the server's clock. */
+double ptw_serve_clock(const ptw_server *s);
+void ptw_serve_close(ptw_server *s);
+
+/* Synthetic Chung-Lu power-law graph built on the device: n vertices with
+ * expected degrees proportional to (i + 1)^(-1/(gamma-1)), mean degree
+ * mean_degree; symmetrised, self-loops, duplicates and isolated vertices
+ * removed, names 0..n'-1.  No reference counterpart. */
+int ptw_graph_chung_lu(uint32_t n, double gamma, double mean_degree, uint64_t seed, ptw_graph **out);
+
 /* Count walk that allocates no device memory.  No counterpart in the
  * reference.  For callers that cannot call cudaMalloc when they run (a host
  * whose pool allocator owns all device memory, or a context where an

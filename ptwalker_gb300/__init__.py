@@ -23,5 +23,6 @@ from .api import (  # noqa: F401
 )
 
 from .batch import BatchResult, ppr_batch  # noqa: F401,E402
+from .serving import Server, open_loop  # noqa: F401,E402
 
 __version__ = "0.1.0"

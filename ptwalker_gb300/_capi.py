@@ -57,6 +57,19 @@ PTW_APP_VISITS = 0
 PTW_APP_ENDPOINT = 1
 
 
+class ServeCfg(ctypes.Structure):
+    _fields_ = [("sp", ctypes.c_double), ("seed", ctypes.c_uint64), ("app", ctypes.c_int32),
+                ("max_moves", ctypes.c_uint32), ("table_bytes", ctypes.c_uint64),
+                ("tick_walkers", ctypes.c_uint64), ("max_active", ctypes.c_uint32),
+                ("use_graph", ctypes.c_uint32), ("table_factor", ctypes.c_double)]
+
+
+class ServeResult(ctypes.Structure):
+    _fields_ = [("query_id", ctypes.c_uint32), ("source", ctypes.c_uint32), ("budget", ctypes.c_uint64),
+                ("n_entries", ctypes.c_uint64), ("submit_s", ctypes.c_double),
+                ("admit_s", ctypes.c_double), ("done_s", ctypes.c_double)]
+
+
 class Tune(ctypes.Structure):
     _fields_ = [("block", ctypes.c_int32), ("ilp", ctypes.c_int32), ("chunk", ctypes.c_int32),
                 ("hot_k", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
@@ -105,6 +118,15 @@ SIGNATURES = [
     ("ptw_batch_free", None, [_G]),
     ("ptw_batch_l1", ctypes.c_int, [_G, _G, ctypes.c_double, ctypes.c_int32, ctypes.c_double,
                                     ctypes.POINTER(ctypes.c_double)]),
+    ("ptw_serve_open", ctypes.c_int, [_G, ctypes.POINTER(ServeCfg), _GP]),
+    ("ptw_serve_submit", ctypes.c_int, [_G, ctypes.POINTER(Query)]),
+    ("ptw_serve_step", ctypes.c_int, [_G, _u32p, _u32p, _u32p]),
+    ("ptw_serve_poll", ctypes.c_int, [_G, ctypes.POINTER(ServeResult)]),
+    ("ptw_serve_take", ctypes.c_int, [_G, _u32p, _u32p]),
+    ("ptw_serve_clock", ctypes.c_double, [_G]),
+    ("ptw_serve_close", None, [_G]),
+    ("ptw_graph_chung_lu", ctypes.c_int, [ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_uint64, _GP]),
 ]
 
 PTW_NOALLOC_MAX_VERTICES = 1 << 22

@@ -131,6 +131,14 @@ class Graph:
         C.check(lib.ptw_graph_rmat(scale, edge_factor, a, b, c, seed, int(bool(clean)), ctypes.byref(h)))
         return cls(h)
 
+    @classmethod
+    def chung_lu(cls, n, gamma=2.1, mean_degree=32.0, seed=1):
+        """Chung-Lu power-law graph (symmetrised, cleaned, names 0..n'-1)."""
+        lib = C.load()
+        h = ctypes.c_void_p()
+        C.check(lib.ptw_graph_chung_lu(int(n), float(gamma), float(mean_degree), int(seed), ctypes.byref(h)))
+        return cls(h)
+
     # -- lifetime ----------------------------------------------------------
     def close(self):
         if self._h:

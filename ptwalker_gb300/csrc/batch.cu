@@ -1,4 +1,4 @@
-// Batched single-source PPR / RWR (K4) and the device FP64 oracle (K7/K8).
+// Batched single-source PPR / RWR (K4).
 //
 // The reference answers one source per process (src/core/ppr.cpp:121-138,
 // source hard-coded to internal id 0; RWR.cpp:109-128 records (start, end)
@@ -26,7 +26,7 @@
 #include <cstring>
 #include <vector>
 
-#include "ptw_internal.cuh"
+#include "batch_kernels.cuh"
 
 struct ptw_batch {
     uint32_t nq = 0;
@@ -39,245 +39,7 @@ struct ptw_batch {
 namespace ptw {
 namespace {
 
-constexpr unsigned kFull = 0xffffffffu;
-constexpr uint32_t kProbeLimit = 256;
 constexpr uint64_t kMaxBudget = 1ull << 28;
-
-__device__ __forceinline__ uint32_t mix32(uint32_t x)
-{
-    // MurmurHash3 32-bit finaliser (Appleby, public domain)
-    x ^= x >> 16;
-    x *= 0x85ebca6bu;
-    x ^= x >> 13;
-    x *= 0xc2b2ae35u;
-    x ^= x >> 16;
-    return x;
-}
-
-// Adds inc to the count of key in the table at slots[0 .. mask].
-__device__ __forceinline__ void tab_add(unsigned long long *slots, uint32_t mask, uint32_t key, uint32_t inc,
-                                        uint32_t *flag)
-{
-    const unsigned long long tag = (unsigned long long)(key + 1) << 32;
-    uint32_t h = mix32(key) & mask;
-    for (uint32_t probe = 0; probe < kProbeLimit && probe <= mask; ++probe) {
-        unsigned long long *s = slots + h;
-        unsigned long long cur = *(volatile unsigned long long *)s;
-        if ((cur & 0xFFFFFFFF00000000ull) == tag) {
-            atomicAdd(s, (unsigned long long)inc);
-            return;
-        }
-        if (cur == 0) {
-            const unsigned long long prev = atomicCAS(s, 0ull, tag | inc);
-            if (prev == 0) return;
-            if ((prev & 0xFFFFFFFF00000000ull) == tag) {
-                atomicAdd(s, (unsigned long long)inc);
-                return;
-            }
-        }
-        h = (h + 1) & mask;
-    }
-    atomicOr(flag, 1u);
-}
-
-struct BatchArgs {
-    const uint2 *__restrict__ adj;
-    const uint32_t *__restrict__ col;
-    const unsigned long long *__restrict__ q_off;  // [nq + 1]
-    const uint32_t *__restrict__ q_src;
-    const uint32_t *__restrict__ q_qid;
-    const unsigned long long *__restrict__ q_tab;
-    const uint32_t *__restrict__ q_mask;
-    uint32_t *q_flag;
-    unsigned long long *slots;
-    unsigned long long *ctrl;  // [0] cursor, [1] moves
-    uint64_t total;
-    uint64_t thr;
-    uint32_t nq, key0, key1, max_moves, chunk;
-    int app;
-};
-
-__device__ __forceinline__ uint32_t find_query(const unsigned long long *q_off, uint32_t nq, uint64_t g)
-{
-    uint32_t lo = 0, hi = nq;  // q_off[lo] <= g < q_off[hi]
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (q_off[mid] <= g) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
-constexpr int kBatchIlp = 2;
-
-__global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
-{
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t lt_mask = (1u << lane) - 1u;
-    uint32_t q[kBatchIlp], v[kBatchIlp], step[kBatchIlp], j[kBatchIlp], qid[kBatchIlp], mask[kBatchIlp];
-    unsigned long long *tab[kBatchIlp];
-    bool act[kBatchIlp];
-#pragma unroll
-    for (int k = 0; k < kBatchIlp; ++k) {
-        act[k] = false;
-        q[k] = v[k] = step[k] = j[k] = qid[k] = mask[k] = 0;
-        tab[k] = nullptr;
-    }
-    uint64_t next = 0, end = 0;
-    bool exhausted = false;
-    unsigned long long moves = 0;
-    for (;;) {
-#pragma unroll
-        for (int k = 0; k < kBatchIlp; ++k) {
-            const unsigned need = __ballot_sync(kFull, !act[k]);
-            if (need == 0 || exhausted) continue;
-            const uint32_t n_need = __popc(need);
-            const uint32_t rank = __popc(need & lt_mask);
-            uint64_t my = ~0ull;
-            const uint64_t avail = end - next;
-            const uint32_t took = (uint32_t)(n_need < avail ? n_need : avail);
-            if (!act[k] && rank < took) my = next + rank;
-            next += took;
-            if (took < n_need) {
-                unsigned long long base = 0;
-                if (lane == 0) base = atomicAdd(&a.ctrl[0], (unsigned long long)a.chunk);
-                base = __shfl_sync(kFull, base, 0);
-                if (base >= a.total) {
-                    exhausted = true;
-                    next = end = a.total;
-                } else {
-                    next = base;
-                    end = base + a.chunk < a.total ? base + a.chunk : a.total;
-                    const uint64_t rem = end - next;
-                    const uint32_t take2 = (uint32_t)((n_need - took) < rem ? (n_need - took) : rem);
-                    if (!act[k] && rank >= took && rank - took < take2) my = next + (rank - took);
-                    next += take2;
-                }
-            }
-            const bool got = my != ~0ull;
-            if (got) {
-                const uint32_t qq = find_query(a.q_off, a.nq, my);
-                q[k] = qq;
-                j[k] = (uint32_t)(my - a.q_off[qq]);
-                qid[k] = a.q_qid[qq];
-                v[k] = a.q_src[qq];
-                tab[k] = a.slots + a.q_tab[qq];
-                mask[k] = a.q_mask[qq];
-                step[k] = 0;
-                act[k] = true;
-            }
-            if (a.app == PTW_APP_VISITS) {
-                // Start visits: one table update per (warp, query) group.
-                const unsigned gm = __ballot_sync(kFull, got);
-                if (got) {
-                    const unsigned grp = __match_any_sync(gm, q[k]);
-                    if ((grp & lt_mask) == 0) tab_add(tab[k], mask[k], v[k], __popc(grp), &a.q_flag[q[k]]);
-                }
-            }
-        }
-        bool any = false;
-#pragma unroll
-        for (int k = 0; k < kBatchIlp; ++k) any |= act[k];
-        if (!__any_sync(kFull, any)) break;
-
-        uint2 rec[kBatchIlp];
-#pragma unroll
-        for (int k = 0; k < kBatchIlp; ++k)
-            if (act[k]) rec[k] = __ldg(&a.adj[v[k]]);
-        uint4 r[kBatchIlp];
-#pragma unroll
-        for (int k = 0; k < kBatchIlp; ++k)
-            if (act[k]) r[k] = philox(make_uint4(j[k], qid[k], step[k], PTW_TAG_WALK), a.key0, a.key1);
-        uint32_t nb[kBatchIlp];
-#pragma unroll
-        for (int k = 0; k < kBatchIlp; ++k)
-            if (act[k] && rec[k].y != 0) nb[k] = __ldg(&a.col[rec[k].x + __umulhi(r[k].x, rec[k].y)]);
-#pragma unroll
-        for (int k = 0; k < kBatchIlp; ++k) {
-            if (!act[k]) continue;
-            bool done;
-            if (rec[k].y == 0) {
-                done = true;
-            } else {
-                v[k] = nb[k];
-                ++step[k];
-                ++moves;
-                if (a.app == PTW_APP_VISITS) tab_add(tab[k], mask[k], v[k], 1u, &a.q_flag[q[k]]);
-                done = (uint64_t)r[k].y < a.thr || (a.max_moves && step[k] >= a.max_moves);
-            }
-            if (done) {
-                if (a.app == PTW_APP_ENDPOINT) tab_add(tab[k], mask[k], v[k], 1u, &a.q_flag[q[k]]);
-                act[k] = false;
-            }
-        }
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) moves += __shfl_xor_sync(kFull, moves, o);
-    if (lane == 0 && moves) atomicAdd(&a.ctrl[1], moves);
-}
-
-// Slot s of the wave belongs to the query q with q_tab[q] <= s < q_tab[q+1].
-__device__ __forceinline__ uint32_t slot_query(const unsigned long long *q_tab, uint32_t nq, uint64_t s)
-{
-    uint32_t lo = 0, hi = nq;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (q_tab[mid] <= s) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
-// Per-query number of occupied slots (warp-aggregated per query).
-__global__ void k_tab_count(const unsigned long long *slots, uint64_t n_slots,
-                            const unsigned long long *q_tab, uint32_t nq, unsigned long long *cnt)
-{
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t s0 = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); s0 < n_slots; s0 += stride) {
-        const uint64_t s = s0 + lane;
-        const bool occ = s < n_slots && slots[s] != 0;
-        const unsigned om = __ballot_sync(kFull, occ);
-        if (occ) {
-            const uint32_t qq = slot_query(q_tab, nq, s);
-            const unsigned grp = __match_any_sync(om, qq);
-            if ((grp & ((1u << lane) - 1u)) == 0) atomicAdd(&cnt[qq], (unsigned long long)__popc(grp));
-        }
-    }
-}
-
-// Writes each occupied slot as (name, count) into its query's segment.
-__global__ void k_tab_emit(const unsigned long long *slots, uint64_t n_slots, const unsigned long long *q_tab,
-                           uint32_t nq, const unsigned long long *seg_off, unsigned long long *fill,
-                           const uint32_t *int2name, uint32_t *out_name, uint32_t *out_cnt)
-{
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t s0 = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); s0 < n_slots; s0 += stride) {
-        const uint64_t s = s0 + lane;
-        const unsigned long long w = s < n_slots ? slots[s] : 0ull;
-        const bool occ = w != 0;
-        const unsigned om = __ballot_sync(kFull, occ);
-        if (occ) {
-            const uint32_t qq = slot_query(q_tab, nq, s);
-            const unsigned grp = __match_any_sync(om, qq);
-            const int leader = __ffs(grp) - 1;
-            unsigned long long base = 0;
-            if (lane == (uint32_t)leader) base = atomicAdd(&fill[qq], (unsigned long long)__popc(grp));
-            base = __shfl_sync(grp, base, leader);
-            const uint64_t pos = seg_off[qq] + base + __popc(grp & ((1u << lane) - 1u));
-            out_name[pos] = int2name[(uint32_t)(w >> 32) - 1];
-            out_cnt[pos] = (uint32_t)(w & 0xFFFFFFFFull);
-        }
-    }
-}
-
-uint64_t next_pow2(uint64_t x)
-{
-    uint64_t p = 1;
-    while (p < x) p <<= 1;
-    return p;
-}
 
 struct DevBuf {
     cudaStream_t st;
@@ -318,7 +80,7 @@ struct WaveQuery {
     uint64_t cap;    // table slots (power of two)
 };
 
-// Runs one wave; appends each query's sorted entries to per-query host lists.
+// Runs one wave; stores each query's sorted entries in per-query host lists.
 int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg *cfg, uint64_t thr,
              std::vector<std::vector<uint32_t>> &names, std::vector<std::vector<uint32_t>> &cnts,
              std::vector<uint32_t> &overflow, uint64_t *moves_out)
@@ -326,17 +88,18 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     cudaStream_t st = g->stream;
     const uint32_t nq = (uint32_t)wq.size();
     std::vector<unsigned long long> h_off(nq + 1), h_tab(nq + 1);
-    std::vector<uint32_t> h_src(nq), h_qid(nq), h_mask(nq);
+    std::vector<uint32_t> h_src(nq), h_qid(nq), h_mask(nq), h_cap(nq);
     for (uint32_t i = 0; i < nq; ++i) {
         h_off[i + 1] = h_off[i] + wq[i].budget;
         h_tab[i + 1] = h_tab[i] + wq[i].cap;
         h_src[i] = wq[i].src;
         h_qid[i] = wq[i].qid;
         h_mask[i] = (uint32_t)(wq[i].cap - 1);
+        h_cap[i] = (uint32_t)wq[i].cap;
     }
     const uint64_t total = h_off[nq], n_slots = h_tab[nq];
     DevBuf db(st);
-    unsigned long long *d_off, *d_tab, *d_slots, *d_ctrl, *d_cnt, *d_seg, *d_fill;
+    unsigned long long *d_off, *d_tab, *d_slots, *d_ctrl;
     uint32_t *d_src, *d_qid, *d_mask, *d_flag;
     PTW_CUDA(db.alloc(&d_off, nq + 1));
     PTW_CUDA(db.alloc(&d_tab, nq + 1));
@@ -345,9 +108,6 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     PTW_CUDA(db.alloc(&d_mask, nq));
     PTW_CUDA(db.alloc(&d_flag, nq));
     PTW_CUDA(db.alloc(&d_ctrl, 2));
-    PTW_CUDA(db.alloc(&d_cnt, nq));
-    PTW_CUDA(db.alloc(&d_seg, nq + 1));
-    PTW_CUDA(db.alloc(&d_fill, nq));
     PTW_CUDA(db.alloc(&d_slots, n_slots));
     PTW_CUDA(cudaMemcpyAsync(d_off, h_off.data(), (nq + 1) * 8ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_tab, h_tab.data(), (nq + 1) * 8ull, cudaMemcpyHostToDevice, st));
@@ -356,14 +116,13 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     PTW_CUDA(cudaMemcpyAsync(d_mask, h_mask.data(), nq * 4ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemsetAsync(d_flag, 0, nq * 4ull, st));
     PTW_CUDA(cudaMemsetAsync(d_ctrl, 0, 16, st));
-    PTW_CUDA(cudaMemsetAsync(d_cnt, 0, nq * 8ull, st));
-    PTW_CUDA(cudaMemsetAsync(d_fill, 0, nq * 8ull, st));
     PTW_CUDA(cudaMemsetAsync(d_slots, 0, n_slots * 8, st));
 
     BatchArgs a;
     a.adj = g->dg.adj;
     a.col = g->dg.col;
     a.q_off = d_off;
+    a.q_j0 = nullptr;
     a.q_src = d_src;
     a.q_qid = d_qid;
     a.q_tab = d_tab;
@@ -385,57 +144,112 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     grid = std::min<uint64_t>(grid, std::max<uint64_t>(1, (total + a.chunk * 8 - 1) / (a.chunk * 8)));
     k_batch<<<(unsigned)grid, 256, 0, st>>>(a);
     PTW_CUDA(cudaGetLastError());
-
-    const unsigned sgrid = (unsigned)std::min<uint64_t>((n_slots + 255) / 256, (uint64_t)g->num_sms * 32);
-    k_tab_count<<<std::max(sgrid, 1u), 256, 0, st>>>(d_slots, n_slots, d_tab, nq, d_cnt);
-    PTW_CUDA(cudaMemsetAsync(d_seg, 0, 8, st));
-    PTW_CUDA(cub_call([&](void *t, size_t &b) {
-        return cub::DeviceScan::InclusiveSum(t, b, d_cnt, d_seg + 1, (int64_t)nq, st);
-    }, st));
-    std::vector<unsigned long long> h_seg(nq + 1);
     std::vector<uint32_t> h_flag(nq);
     unsigned long long h_moves = 0;
-    PTW_CUDA(cudaMemcpyAsync(h_seg.data(), d_seg, (nq + 1) * 8ull, cudaMemcpyDeviceToHost, st));
     PTW_CUDA(cudaMemcpyAsync(h_flag.data(), d_flag, nq * 4ull, cudaMemcpyDeviceToHost, st));
     PTW_CUDA(cudaMemcpyAsync(&h_moves, d_ctrl + 1, 8, cudaMemcpyDeviceToHost, st));
-    PTW_CUDA(cudaStreamSynchronize(st));
-    *moves_out += h_moves;
-    const uint64_t n_ent = h_seg[nq];
-    uint32_t *e_name, *e_cnt, *s_name, *s_cnt;
-    PTW_CUDA(db.alloc(&e_name, n_ent));
-    PTW_CUDA(db.alloc(&e_cnt, n_ent));
-    PTW_CUDA(db.alloc(&s_name, n_ent));
-    PTW_CUDA(db.alloc(&s_cnt, n_ent));
-    if (n_ent) {
-        k_tab_emit<<<std::max(sgrid, 1u), 256, 0, st>>>(d_slots, n_slots, d_tab, nq, d_seg, d_fill,
-                                                        g->dg.int2name, e_name, e_cnt);
-        PTW_CUDA(cudaGetLastError());
-        PTW_CUDA(cub_call([&](void *t, size_t &b) {
-            return cub::DeviceSegmentedSort::SortPairs(t, b, e_name, s_name, e_cnt, s_cnt, (int64_t)n_ent,
-                                                      (int64_t)nq, d_seg, d_seg + 1, st);
-        }, st));
-    }
-    std::vector<uint32_t> h_name(n_ent), h_cnt(n_ent);
-    if (n_ent) {
-        PTW_CUDA(cudaMemcpyAsync(h_name.data(), s_name, n_ent * 4, cudaMemcpyDeviceToHost, st));
-        PTW_CUDA(cudaMemcpyAsync(h_cnt.data(), s_cnt, n_ent * 4, cudaMemcpyDeviceToHost, st));
-    }
-    PTW_CUDA(cudaStreamSynchronize(st));
+    std::vector<std::vector<uint32_t> *> out_n(nq), out_c(nq);
     for (uint32_t i = 0; i < nq; ++i) {
-        const uint32_t qi = wq[i].index;
-        if (h_flag[i]) {
-            overflow.push_back(qi);
-            continue;
-        }
-        names[qi].assign(h_name.begin() + h_seg[i], h_name.begin() + h_seg[i + 1]);
-        cnts[qi].assign(h_cnt.begin() + h_seg[i], h_cnt.begin() + h_seg[i + 1]);
+        out_n[i] = &names[wq[i].index];
+        out_c[i] = &cnts[wq[i].index];
     }
+    int rc = compact_tables(g, d_slots, h_tab.data(), h_cap.data(), nq, out_n.data(), out_c.data());
+    if (rc) return rc;
+    *moves_out += h_moves;
+    for (uint32_t i = 0; i < nq; ++i)
+        if (h_flag[i]) {
+            overflow.push_back(wq[i].index);
+            names[wq[i].index].clear();
+            cnts[wq[i].index].clear();
+        }
     return PTW_OK;
+}
+
+uint64_t next_pow2(uint64_t x)
+{
+    uint64_t p = 1;
+    while (p < x) p <<= 1;
+    return p;
 }
 
 }  // namespace
 
 const ptw_query *batch_queries(const ptw_batch *b) { return b->queries.data(); }
+
+int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned long long *h_base,
+                   const uint32_t *h_cap, uint32_t nt, std::vector<uint32_t> **names,
+                   std::vector<uint32_t> **counts)
+{
+    if (nt == 0) return PTW_OK;
+    cudaStream_t st = g->stream;
+    DevBuf db(st);
+    unsigned long long *d_base, *d_cnt, *d_seg, *d_fill;
+    uint32_t *d_cap;
+    PTW_CUDA(db.alloc(&d_base, nt));
+    PTW_CUDA(db.alloc(&d_cap, nt));
+    PTW_CUDA(db.alloc(&d_cnt, nt));
+    PTW_CUDA(db.alloc(&d_seg, nt + 1));
+    PTW_CUDA(db.alloc(&d_fill, nt));
+    PTW_CUDA(cudaMemcpyAsync(d_base, h_base, nt * 8ull, cudaMemcpyHostToDevice, st));
+    PTW_CUDA(cudaMemcpyAsync(d_cap, h_cap, nt * 4ull, cudaMemcpyHostToDevice, st));
+    PTW_CUDA(cudaMemsetAsync(d_cnt, 0, nt * 8ull, st));
+    PTW_CUDA(cudaMemsetAsync(d_fill, 0, nt * 8ull, st));
+    PTW_CUDA(cudaMemsetAsync(d_seg, 0, 8, st));
+    uint32_t max_cap = 0;
+    for (uint32_t i = 0; i < nt; ++i) max_cap = std::max(max_cap, h_cap[i]);
+    const unsigned gx = (unsigned)std::min<uint64_t>(256, (max_cap + 2047) / 2048);
+    for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
+        const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
+        k_tabs_count<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(d_slots, d_base + t0, d_cap + t0, d_cnt + t0);
+    }
+    PTW_CUDA(cudaGetLastError());
+    PTW_CUDA(cub_call([&](void *t, size_t &b) {
+        return cub::DeviceScan::InclusiveSum(t, b, d_cnt, d_seg + 1, (int64_t)nt, st);
+    }, st));
+    std::vector<unsigned long long> h_seg(nt + 1);
+    PTW_CUDA(cudaMemcpyAsync(h_seg.data(), d_seg, (nt + 1) * 8ull, cudaMemcpyDeviceToHost, st));
+    PTW_CUDA(cudaStreamSynchronize(st));
+    const uint64_t n_ent = h_seg[nt];
+    std::vector<uint32_t> h_name(n_ent), h_cnt(n_ent);
+    if (n_ent) {
+        uint32_t *e_name, *e_cnt, *s_name, *s_cnt;
+        PTW_CUDA(db.alloc(&e_name, n_ent));
+        PTW_CUDA(db.alloc(&e_cnt, n_ent));
+        PTW_CUDA(db.alloc(&s_name, n_ent));
+        PTW_CUDA(db.alloc(&s_cnt, n_ent));
+        for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
+            const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
+            k_tabs_emit<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(d_slots, d_base + t0, d_cap + t0, d_seg + t0,
+                                                                   d_fill + t0, g->dg.int2name, e_name, e_cnt);
+        }
+        PTW_CUDA(cudaGetLastError());
+        PTW_CUDA(cub_call([&](void *t, size_t &b) {
+            return cub::DeviceSegmentedSort::SortPairs(t, b, e_name, s_name, e_cnt, s_cnt, (int64_t)n_ent,
+                                                      (int64_t)nt, d_seg, d_seg + 1, st);
+        }, st));
+        PTW_CUDA(cudaMemcpyAsync(h_name.data(), s_name, n_ent * 4, cudaMemcpyDeviceToHost, st));
+        PTW_CUDA(cudaMemcpyAsync(h_cnt.data(), s_cnt, n_ent * 4, cudaMemcpyDeviceToHost, st));
+        PTW_CUDA(cudaStreamSynchronize(st));
+    }
+    for (uint32_t i = 0; i < nt; ++i) {
+        names[i]->assign(h_name.begin() + h_seg[i], h_name.begin() + h_seg[i + 1]);
+        counts[i]->assign(h_cnt.begin() + h_seg[i], h_cnt.begin() + h_seg[i + 1]);
+    }
+    return PTW_OK;
+}
+
+uint64_t table_slots(double sp, uint32_t max_moves, int32_t app, double factor, uint64_t budget, uint32_t n)
+{
+    const double len = max_moves ? std::min(1.0 / std::max(sp, 1e-12), (double)max_moves)
+                                 : 1.0 / std::max(sp, 1e-12);
+    const double per_walker = app == PTW_APP_VISITS ? len + 1.0 : 1.0;
+    const double f = factor > 0 ? factor : 2.0;
+    const double expect = std::ceil(f * per_walker * (double)budget) + 64.0;
+    const uint64_t full_cap = next_pow2(2ull * n);
+    return std::min(full_cap, std::max<uint64_t>(256, next_pow2((uint64_t)std::min(expect, 4e18))));
+}
+
+uint64_t full_table_slots(uint32_t n) { return next_pow2(2ull * n); }
 
 }  // namespace ptw
 
@@ -453,12 +267,7 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
     if (cfg->app != PTW_APP_VISITS && cfg->app != PTW_APP_ENDPOINT) return fail(PTW_EINVAL, "unknown app");
     PTW_CUDA(cudaSetDevice(g->device));
     const uint32_t n = g->dg.n;
-    // Queries -> internal sources and table sizes.
     std::vector<WaveQuery> all(nq);
-    const double len = cfg->max_moves ? std::min(1.0 / std::max(cfg->sp, 1e-12), (double)cfg->max_moves)
-                                      : 1.0 / std::max(cfg->sp, 1e-12);
-    const double per_walker = cfg->app == PTW_APP_VISITS ? len + 1.0 : 1.0;
-    const uint64_t full_cap = next_pow2(2ull * n);
     for (uint32_t i = 0; i < nq; ++i) {
         const ptw_query &q = h_queries[i];
         if (q.budget < 1 || q.budget > kMaxBudget)
@@ -471,9 +280,7 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
         all[i].src = g->h_idx2int[p - g->h_names];
         all[i].qid = q.query_id;
         all[i].budget = q.budget;
-        const double factor = cfg->table_factor > 0 ? cfg->table_factor : 2.0;
-        const double expect = std::ceil(factor * per_walker * (double)q.budget) + 64.0;
-        all[i].cap = std::min(full_cap, std::max<uint64_t>(256, next_pow2((uint64_t)expect)));
+        all[i].cap = table_slots(cfg->sp, cfg->max_moves, cfg->app, cfg->table_factor, q.budget, n);
     }
     uint64_t budget_bytes = cfg->table_bytes;
     if (budget_bytes == 0) {
@@ -495,8 +302,7 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
     for (uint32_t i = 0; i < nq && rc == PTW_OK;) {
         std::vector<WaveQuery> wave;
         uint64_t bytes = 0;
-        while (i < nq && (wave.empty() || bytes + all[i].cap * 8 <= budget_bytes) &&
-               wave.size() < (1u << 20)) {
+        while (i < nq && (wave.empty() || bytes + all[i].cap * 8 <= budget_bytes) && wave.size() < (1u << 20)) {
             bytes += all[i].cap * 8;
             wave.push_back(all[i++]);
         }
@@ -507,7 +313,7 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
     again.swap(overflow);
     for (size_t k = 0; k < again.size() && rc == PTW_OK; ++k) {
         WaveQuery w = all[again[k]];
-        w.cap = full_cap;
+        w.cap = full_table_slots(n);
         uint64_t m2 = 0;
         rc = run_wave(g, {w}, cfg, thr, names, cnts, overflow, &m2);
         if (rc == PTW_OK && !overflow.empty()) rc = fail(PTW_EFULL, "count table overflow at 2n slots");

@@ -400,6 +400,40 @@ extern "C" int ptw_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, do
     return PTW_OK;
 }
 
+extern "C" int ptw_graph_chung_lu(uint32_t n, double gamma, double mean_degree, uint64_t seed, ptw_graph **out)
+{
+    if (!out) return fail(PTW_EINVAL, "null output handle");
+    *out = nullptr;
+    if (n < 2) return fail(PTW_EINVAL, "n must be >= 2");
+    if (!(gamma > 1.0)) return fail(PTW_EINVAL, "gamma must be > 1");
+    if (!(mean_degree > 0.0)) return fail(PTW_EINVAL, "mean_degree must be > 0");
+    const double md = std::ceil((double)n * mean_degree / 2.0);
+    if (md >= 2147483648.0) return fail(PTW_EINVAL, "n * mean_degree / 2 must be < 2^31");
+    const uint64_t m = (uint64_t)md;
+    ptw_graph *g = new (std::nothrow) ptw_graph();
+    if (!g) return fail(PTW_ENOMEM, "host allocation failed");
+    int rc = graph_init_handle(g);
+    uint32_t *d_src = nullptr, *d_dst = nullptr;
+    if (rc == PTW_OK) {
+        cudaError_t e = cudaMallocAsync(&d_src, m * 4, g->stream);
+        if (e == cudaSuccess) e = cudaMallocAsync(&d_dst, m * 4, g->stream);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "Chung-Lu edge buffers");
+            if (d_src) cudaFreeAsync(d_src, g->stream);
+        } else {
+            rc = chung_lu_generate_device(n, gamma, m, seed, d_src, d_dst, g->stream);
+            if (rc == PTW_OK) rc = build_graph_from_device_edges(g, d_src, d_dst, m, true, true, true);
+        }
+    }
+    if (rc != PTW_OK) {
+        graph_release(g);
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return PTW_OK;
+}
+
 extern "C" void ptw_graph_free(ptw_graph *g)
 {
     if (!g) return;

@@ -193,6 +193,41 @@ __global__ void k_rmat(uint32_t scale, uint64_t m, uint32_t ta, uint32_t tab, ui
     }
 }
 
+// Chung-Lu: vertex i has weight (i + 1)^(-expo), expo = 1 / (gamma - 1);
+// both endpoints of an edge are drawn proportionally to weight by inverse
+// CDF (binary search over the inclusive prefix sums).
+__global__ void k_cl_weights(uint32_t n, double expo, double *w)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        w[i] = pow((double)i + 1.0, -expo);
+}
+
+__device__ __forceinline__ uint32_t cdf_pick(const double *cdf, uint32_t n, double x)
+{
+    uint32_t lo = 0, hi = n - 1;  // first i with cdf[i] > x
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (cdf[mid] > x) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+__global__ void k_cl_edges(uint64_t m, const double *cdf, uint32_t n, uint32_t k0, uint32_t k1, uint32_t *src,
+                           uint32_t *dst)
+{
+    const double total = cdf[n - 1];
+    const double inv53 = 1.0 / 9007199254740992.0;  // 2^-53
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 r = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), 0u, PTW_TAG_CHUNGLU), k0, k1);
+        const double u1 = (double)(((uint64_t)(r.x >> 5) << 26) | (r.y >> 6)) * inv53;
+        const double u2 = (double)(((uint64_t)(r.z >> 5) << 26) | (r.w >> 6)) * inv53;
+        src[e] = cdf_pick(cdf, n, u1 * total);
+        dst[e] = cdf_pick(cdf, n, u2 * total);
+    }
+}
+
 // Frees every pointer on scope exit (stream-ordered).
 struct AsyncBufs {
     cudaStream_t st;
@@ -288,6 +323,23 @@ int rmat_generate_device(uint32_t scale, uint64_t m, uint32_t ta, uint32_t tab, 
     k_rmat<<<grid_for(m), kThreads, 0, st>>>(scale, m, ta, tab, tabc, (uint32_t)seed,
                                              (uint32_t)(seed >> 32), d_src, d_dst);
     PTW_CUDA(cudaGetLastError());
+    return PTW_OK;
+}
+
+int chung_lu_generate_device(uint32_t n, double gamma, uint64_t m, uint64_t seed, uint32_t *d_src,
+                             uint32_t *d_dst, cudaStream_t st)
+{
+    AsyncBufs tmp(st);
+    double *w = nullptr, *cdf = nullptr;
+    PTW_CUDA(tmp.alloc(&w, n));
+    PTW_CUDA(tmp.alloc(&cdf, n));
+    k_cl_weights<<<grid_for(n), kThreads, 0, st>>>(n, 1.0 / (gamma - 1.0), w);
+    PTW_CUDA(cub_call([&](void *t, size_t &b) {
+        return cub::DeviceScan::InclusiveSum(t, b, w, cdf, (int64_t)n, st);
+    }, st));
+    k_cl_edges<<<grid_for(m), kThreads, 0, st>>>(m, cdf, n, (uint32_t)seed, (uint32_t)(seed >> 32), d_src, d_dst);
+    PTW_CUDA(cudaGetLastError());
+    PTW_CUDA(cudaStreamSynchronize(st));
     return PTW_OK;
 }
 

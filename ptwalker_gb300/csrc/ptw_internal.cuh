@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/ptw.h"
 
@@ -12,6 +13,7 @@
 #define PTW_TAG_WALK 0x57414C4Bu  // "WALK": one draw per move
 #define PTW_TAG_START 0x53545254u // "STRT": start-vertex draw
 #define PTW_TAG_RMAT 0x524D4154u  // "RMAT": synthetic edge generation
+#define PTW_TAG_CHUNGLU 0x43484C55u // "CHLU": Chung-Lu endpoints
 
 namespace ptw {
 
@@ -124,6 +126,8 @@ int build_graph_from_device_edges(ptw_graph *g, uint32_t *d_src, uint32_t *d_dst
                                   bool as_undirected, bool clean, bool compact_names);
 int rmat_generate_device(uint32_t scale, uint64_t m, uint32_t ta, uint32_t tab, uint32_t tabc,
                          uint64_t seed, uint32_t *d_src, uint32_t *d_dst, cudaStream_t st);
+int chung_lu_generate_device(uint32_t n, double gamma, uint64_t m, uint64_t seed, uint32_t *d_src,
+                             uint32_t *d_dst, cudaStream_t st);
 int graph_init_handle(ptw_graph *g);
 void graph_release(ptw_graph *g);
 
@@ -146,5 +150,14 @@ int check_tune(const ptw_tune &t);
 
 // The query table a batch was run with (batch.cu).
 const ptw_query *batch_queries(const ptw_batch *b);
+
+// Compacts nt count tables (slots [h_base[i], h_base[i] + h_cap[i]) of
+// d_slots) into (name, count) lists sorted by name (batch.cu).
+int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned long long *h_base,
+                   const uint32_t *h_cap, uint32_t nt, std::vector<uint32_t> **names,
+                   std::vector<uint32_t> **counts);
+// Count-table size for a query of `budget` walkers, and the size that cannot fill.
+uint64_t table_slots(double sp, uint32_t max_moves, int32_t app, double factor, uint64_t budget, uint32_t n);
+uint64_t full_table_slots(uint32_t n);
 
 }  // namespace ptw

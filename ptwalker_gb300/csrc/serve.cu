@@ -1,0 +1,465 @@
+// Serving runtime: continuous batching of PPR / RWR queries (no reference
+// counterpart; the reference runs one query per process).
+//
+// State that stays resident between ticks:
+//   - the graph (owned by the ptw_graph handle);
+//   - a device arena of count-table slots, carved by a buddy allocator into
+//     power-of-two tables, one per active query (admission by device memory);
+//   - a device plan block (the tick's query table) and its pinned host mirror.
+// A tick gives every active query a share of the tick's walkers (its walker
+// ranks j0 .. j0+share-1) and runs them all in one k_batch launch; walkers
+// finish within the tick, so a query is done once all its ranks have run.
+// Draws depend on (query id, rank) only: a query's counts are the same
+// however its ranks are split across ticks and whatever runs beside it.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <vector>
+
+#include "batch_kernels.cuh"
+
+namespace ptw {
+namespace {
+
+// Buddy allocator over [0, 2^max_order) slots, minimum block 2^min_order.
+class Buddy {
+public:
+    void init(uint64_t total_slots, int min_order)
+    {
+        min_order_ = min_order;
+        max_order_ = min_order;
+        while ((2ull << max_order_) <= total_slots) ++max_order_;
+        if ((1ull << max_order_) > total_slots) max_order_ = -1;  // arena smaller than one block
+        free_.assign(64, {});
+        if (max_order_ >= min_order_) free_[max_order_].push_back(0);
+    }
+    bool alloc(uint64_t slots, uint64_t *off)
+    {
+        int o = min_order_;
+        while ((1ull << o) < slots) ++o;
+        if (max_order_ < 0 || o > max_order_) return false;
+        int k = o;
+        while (k <= max_order_ && free_[k].empty()) ++k;
+        if (k > max_order_) return false;
+        uint64_t b = free_[k].back();
+        free_[k].pop_back();
+        while (k > o) {
+            --k;
+            free_[k].push_back(b + (1ull << k));  // upper half stays free
+        }
+        *off = b;
+        used_[b] = o;
+        return true;
+    }
+    void release(uint64_t off)
+    {
+        auto it = used_.find(off);
+        if (it == used_.end()) return;
+        int o = it->second;
+        used_.erase(it);
+        uint64_t b = off;
+        while (o < max_order_) {
+            const uint64_t buddy = b ^ (1ull << o);
+            auto &fl = free_[o];
+            auto f = std::find(fl.begin(), fl.end(), buddy);
+            if (f == fl.end()) break;
+            fl.erase(f);
+            b = std::min(b, buddy);
+            ++o;
+        }
+        free_[o].push_back(b);
+    }
+    uint64_t capacity() const { return max_order_ < 0 ? 0 : 1ull << max_order_; }
+
+private:
+    int min_order_ = 8, max_order_ = -1;
+    std::vector<std::vector<uint64_t>> free_;
+    std::map<uint64_t, int> used_;
+};
+
+struct Pending {
+    ptw_query q;
+    uint32_t src;  // internal id
+    double submit_s;
+    bool full;     // re-run with a table that cannot fill
+};
+
+struct Active {
+    Pending p;
+    uint64_t cap, off;  // table slots, arena offset
+    uint64_t started;   // ranks run so far
+    double admit_s;
+};
+
+struct Done {
+    ptw_serve_result r;
+    std::vector<uint32_t> names, counts;
+};
+
+}  // namespace
+}  // namespace ptw
+
+struct ptw_server {
+    ptw_graph *g = nullptr;
+    ptw_serve_cfg cfg{};
+    uint64_t thr = 0;
+    std::chrono::steady_clock::time_point t0;
+    ptw::Buddy buddy;
+    unsigned long long *arena = nullptr;
+    uint32_t S = 0;                  // plan capacity (max_active)
+    void *d_plan = nullptr, *h_plan = nullptr;
+    size_t plan_bytes = 0, ret_off = 0, ret_bytes = 0;
+    std::deque<ptw::Pending> pending;
+    std::vector<ptw::Active> active;
+    std::deque<ptw::Done> done;
+    ptw::BatchArgs args{};
+    unsigned grid = 1;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t knode = nullptr;
+    cudaKernelNodeParams kparams{};
+    uint64_t ticks = 0, moves = 0;
+};
+
+namespace ptw {
+namespace {
+
+double now_s(const ptw_server *s)
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - s->t0).count();
+}
+
+// Plan block layout (identical on host and device):
+//   off[S+1] u64 | j0[S] u64 | tab[S] u64 | src[S] u32 | qid[S] u32 | mask[S] u32 |
+//   flag[S] u32 | ctrl[2] u64
+struct PlanView {
+    unsigned long long *off, *j0, *tab, *ctrl;
+    uint32_t *src, *qid, *mask, *flag;
+};
+
+PlanView view(void *base, uint32_t S)
+{
+    PlanView v;
+    char *p = (char *)base;
+    v.off = (unsigned long long *)p;
+    p += 8ull * (S + 1);
+    v.j0 = (unsigned long long *)p;
+    p += 8ull * S;
+    v.tab = (unsigned long long *)p;
+    p += 8ull * S;
+    v.src = (uint32_t *)p;
+    p += 4ull * S;
+    v.qid = (uint32_t *)p;
+    p += 4ull * S;
+    v.mask = (uint32_t *)p;
+    p += 4ull * S;
+    v.flag = (uint32_t *)p;
+    p += 4ull * S;
+    p = (char *)(((uintptr_t)p + 15) & ~(uintptr_t)15);
+    v.ctrl = (unsigned long long *)p;
+    return v;
+}
+
+size_t plan_size(uint32_t S)
+{
+    size_t b = 8ull * (S + 1) + 16ull * S + 8ull * S + 16ull * S;
+    return ((b + 15) & ~(size_t)15) + 16;
+}
+
+int build_tick_graph(ptw_server *s)
+{
+    cudaStream_t st = s->g->stream;
+    PTW_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e1 = cudaMemcpyAsync(s->d_plan, s->h_plan, s->plan_bytes, cudaMemcpyHostToDevice, st);
+    k_batch<<<s->grid, 256, 0, st>>>(s->args);
+    cudaError_t e2 = cudaGetLastError();
+    cudaError_t e3 = cudaMemcpyAsync((char *)s->h_plan + s->ret_off, (char *)s->d_plan + s->ret_off,
+                                     s->ret_bytes, cudaMemcpyDeviceToHost, st);
+    cudaError_t e4 = cudaStreamEndCapture(st, &s->graph);
+    if (e1 != cudaSuccess) return cuda_fail(e1, "tick graph copy-in");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "tick graph kernel");
+    if (e3 != cudaSuccess) return cuda_fail(e3, "tick graph copy-out");
+    if (e4 != cudaSuccess) return cuda_fail(e4, "cudaStreamEndCapture");
+    size_t nn = 0;
+    PTW_CUDA(cudaGraphGetNodes(s->graph, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    PTW_CUDA(cudaGraphGetNodes(s->graph, nodes.data(), &nn));
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        PTW_CUDA(cudaGraphNodeGetType(nd, &t));
+        if (t == cudaGraphNodeTypeKernel) s->knode = nd;
+    }
+    if (!s->knode) return fail(PTW_ECUDA, "tick graph has no kernel node");
+    PTW_CUDA(cudaGraphKernelNodeGetParams(s->knode, &s->kparams));
+    PTW_CUDA(cudaGraphInstantiate(&s->exec, s->graph, 0));
+    return PTW_OK;
+}
+
+// Turns the tables of finished queries (indices into s->active) into results
+// and releases the tables; the caller removes them from s->active.
+int collect(ptw_server *s, const std::vector<size_t> &fin)
+{
+    if (fin.empty()) return PTW_OK;
+    std::vector<unsigned long long> base(fin.size());
+    std::vector<uint32_t> cap(fin.size());
+    std::vector<Done> out(fin.size());
+    std::vector<std::vector<uint32_t> *> pn(fin.size()), pc(fin.size());
+    for (size_t i = 0; i < fin.size(); ++i) {
+        base[i] = s->active[fin[i]].off;
+        cap[i] = (uint32_t)s->active[fin[i]].cap;
+        pn[i] = &out[i].names;
+        pc[i] = &out[i].counts;
+    }
+    int rc = compact_tables(s->g, s->arena, base.data(), cap.data(), (uint32_t)fin.size(), pn.data(), pc.data());
+    if (rc) return rc;
+    const double t = now_s(s);
+    for (size_t i = 0; i < fin.size(); ++i) {
+        const Active &a = s->active[fin[i]];
+        out[i].r.query_id = a.p.q.query_id;
+        out[i].r.source = a.p.q.source;
+        out[i].r.budget = a.p.q.budget;
+        out[i].r.n_entries = out[i].names.size();
+        out[i].r.submit_s = a.p.submit_s;
+        out[i].r.admit_s = a.admit_s;
+        out[i].r.done_s = t;
+        s->buddy.release(a.off);
+        s->done.push_back(std::move(out[i]));
+    }
+    return PTW_OK;
+}
+
+}  // namespace
+}  // namespace ptw
+
+using namespace ptw;
+
+extern "C" int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server **out)
+{
+    if (!g || !cfg || !out) return fail(PTW_EINVAL, "null argument");
+    *out = nullptr;
+    if (!(cfg->sp >= 0.0 && cfg->sp <= 1.0)) return fail(PTW_EINVAL, "sp must be in [0, 1]");
+    if (cfg->sp == 0.0 && cfg->max_moves == 0)
+        return fail(PTW_EINVAL, "sp = 0 needs max_moves > 0 (walks would never end)");
+    if (cfg->app != PTW_APP_VISITS && cfg->app != PTW_APP_ENDPOINT) return fail(PTW_EINVAL, "unknown app");
+    PTW_CUDA(cudaSetDevice(g->device));
+    ptw_server *s = new (std::nothrow) ptw_server();
+    if (!s) return fail(PTW_ENOMEM, "host allocation failed");
+    s->g = g;
+    s->cfg = *cfg;
+    if (!s->cfg.tick_walkers) s->cfg.tick_walkers = 1ull << 22;
+    if (!s->cfg.max_active) s->cfg.max_active = 4096;
+    s->S = s->cfg.max_active;
+    s->thr = cfg->sp >= 1.0 ? (1ull << 32) : (uint64_t)(cfg->sp * 4294967296.0);
+    s->t0 = std::chrono::steady_clock::now();
+    uint64_t bytes = cfg->table_bytes;
+    if (!bytes) {
+        size_t fr = 0, tot = 0;
+        cudaError_t e = cudaMemGetInfo(&fr, &tot);
+        if (e != cudaSuccess) {
+            delete s;
+            return cuda_fail(e, "cudaMemGetInfo");
+        }
+        bytes = fr / 4;
+    }
+    s->buddy.init(bytes / 8, 8);
+    int rc = PTW_OK;
+    cudaError_t e = cudaMalloc(&s->arena, std::max<uint64_t>(s->buddy.capacity(), 1) * 8);
+    s->plan_bytes = plan_size(s->S);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_plan, s->plan_bytes);
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_plan, s->plan_bytes);
+    if (e != cudaSuccess) {
+        rc = cuda_fail(e, "server allocation");
+    } else {
+        std::memset(s->h_plan, 0, s->plan_bytes);
+        PlanView dv = view(s->d_plan, s->S);
+        PlanView hv = view(s->h_plan, s->S);
+        s->ret_off = (char *)hv.flag - (char *)s->h_plan;
+        s->ret_bytes = s->plan_bytes - s->ret_off;
+        BatchArgs &a = s->args;
+        a.adj = g->dg.adj;
+        a.col = g->dg.col;
+        a.q_off = dv.off;
+        a.q_j0 = dv.j0;
+        a.q_src = dv.src;
+        a.q_qid = dv.qid;
+        a.q_tab = dv.tab;
+        a.q_mask = dv.mask;
+        a.q_flag = dv.flag;
+        a.slots = s->arena;
+        a.ctrl = dv.ctrl;
+        a.total = 0;
+        a.thr = s->thr;
+        a.nq = 1;
+        a.key0 = (uint32_t)cfg->seed;
+        a.key1 = (uint32_t)(cfg->seed >> 32);
+        a.max_moves = cfg->max_moves;
+        a.chunk = 256;
+        a.app = cfg->app;
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, 256, 0);
+        if (e != cudaSuccess) rc = cuda_fail(e, "occupancy");
+        s->grid = (unsigned)std::max(1, g->num_sms * std::max(per_sm, 1));
+        if (rc == PTW_OK && cfg->use_graph) rc = build_tick_graph(s);
+    }
+    if (rc != PTW_OK) {
+        ptw_serve_close(s);
+        return rc;
+    }
+    *out = s;
+    return PTW_OK;
+}
+
+extern "C" int ptw_serve_submit(ptw_server *s, const ptw_query *q)
+{
+    if (!s || !q) return fail(PTW_EINVAL, "null argument");
+    if (q->budget < 1 || q->budget > (1ull << 28)) return fail(PTW_EINVAL, "budget must be in [1, 2^28]");
+    const uint32_t n = s->g->dg.n;
+    const uint32_t *p = std::lower_bound(s->g->h_names, s->g->h_names + n, q->source);
+    if (p == s->g->h_names + n || *p != q->source)
+        return fail(PTW_EINVAL, "source " + std::to_string(q->source) + " is not a vertex of the graph");
+    Pending pd;
+    pd.q = *q;
+    pd.src = s->g->h_idx2int[p - s->g->h_names];
+    pd.submit_s = now_s(s);
+    pd.full = false;
+    s->pending.push_back(pd);
+    return PTW_OK;
+}
+
+extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_active, uint32_t *n_pending)
+{
+    if (!s) return fail(PTW_EINVAL, "null server");
+    PTW_CUDA(cudaSetDevice(s->g->device));
+    cudaStream_t st = s->g->stream;
+    const uint32_t n = s->g->dg.n;
+    const size_t done_before = s->done.size();
+    // 1. admission: FIFO while a slot and a table fit
+    while (!s->pending.empty() && s->active.size() < s->S) {
+        Pending &pd = s->pending.front();
+        const uint64_t cap = pd.full ? full_table_slots(n)
+                                     : table_slots(s->cfg.sp, s->cfg.max_moves, s->cfg.app,
+                                                   s->cfg.table_factor, pd.q.budget, n);
+        uint64_t off = 0;
+        if (!s->buddy.alloc(cap, &off)) {
+            if (s->active.empty() && cap > s->buddy.capacity())
+                return fail(PTW_ENOMEM, "a query's count table is larger than the whole table arena");
+            break;
+        }
+        PTW_CUDA(cudaMemsetAsync(s->arena + off, 0, cap * 8, st));
+        Active a;
+        a.p = pd;
+        a.cap = cap;
+        a.off = off;
+        a.started = 0;
+        a.admit_s = now_s(s);
+        s->active.push_back(a);
+        s->pending.pop_front();
+    }
+    uint32_t nd = 0;
+    if (!s->active.empty()) {
+        // 2. plan: a fair share of the tick's walkers per active query
+        PlanView hv = view(s->h_plan, s->S);
+        const uint32_t na = (uint32_t)s->active.size();
+        const uint64_t share = std::max<uint64_t>(1024, s->cfg.tick_walkers / na);
+        hv.off[0] = 0;
+        for (uint32_t i = 0; i < na; ++i) {
+            const Active &a = s->active[i];
+            const uint64_t take = std::min<uint64_t>(share, a.p.q.budget - a.started);
+            hv.off[i + 1] = hv.off[i] + take;
+            hv.j0[i] = a.started;
+            hv.tab[i] = a.off;
+            hv.src[i] = a.p.src;
+            hv.qid[i] = a.p.q.query_id;
+            hv.mask[i] = (uint32_t)(a.cap - 1);
+            hv.flag[i] = 0;
+        }
+        hv.ctrl[0] = hv.ctrl[1] = 0;
+        s->args.nq = na;
+        s->args.total = hv.off[na];
+        // 3. the tick
+        if (s->exec) {
+            void *kp[] = {&s->args};
+            cudaKernelNodeParams p = s->kparams;
+            p.kernelParams = kp;
+            PTW_CUDA(cudaGraphExecKernelNodeSetParams(s->exec, s->knode, &p));
+            PTW_CUDA(cudaGraphLaunch(s->exec, st));
+        } else {
+            PTW_CUDA(cudaMemcpyAsync(s->d_plan, s->h_plan, s->plan_bytes, cudaMemcpyHostToDevice, st));
+            k_batch<<<s->grid, 256, 0, st>>>(s->args);
+            PTW_CUDA(cudaGetLastError());
+            PTW_CUDA(cudaMemcpyAsync((char *)s->h_plan + s->ret_off, (char *)s->d_plan + s->ret_off,
+                                     s->ret_bytes, cudaMemcpyDeviceToHost, st));
+        }
+        PTW_CUDA(cudaStreamSynchronize(st));
+        ++s->ticks;
+        s->moves += hv.ctrl[1];
+        // 4. progress; completed queries become results; a query whose table
+        //    filled is queued again (first) with a table that cannot fill
+        std::vector<size_t> fin;
+        std::vector<char> drop(na, 0);
+        std::vector<Pending> retry;
+        for (uint32_t i = 0; i < na; ++i) {
+            Active &a = s->active[i];
+            if (hv.flag[i]) {
+                retry.push_back(a.p);
+                retry.back().full = true;
+                s->buddy.release(a.off);
+                drop[i] = 1;
+                continue;
+            }
+            a.started += hv.off[i + 1] - hv.off[i];
+            if (a.started == a.p.q.budget) {
+                fin.push_back(i);
+                drop[i] = 1;
+            }
+        }
+        int rc = collect(s, fin);
+        if (rc) return rc;
+        std::vector<Active> keep;
+        for (uint32_t i = 0; i < na; ++i)
+            if (!drop[i]) keep.push_back(s->active[i]);
+        s->active.swap(keep);
+        for (auto it = retry.rbegin(); it != retry.rend(); ++it) s->pending.push_front(*it);
+        nd = (uint32_t)(s->done.size() - done_before);
+    }
+    if (n_done) *n_done = nd;
+    if (n_active) *n_active = (uint32_t)s->active.size();
+    if (n_pending) *n_pending = (uint32_t)s->pending.size();
+    return PTW_OK;
+}
+
+extern "C" int ptw_serve_poll(ptw_server *s, ptw_serve_result *r)
+{
+    if (!s || !r) return fail(PTW_EINVAL, "null argument");
+    if (s->done.empty()) return 0;
+    *r = s->done.front().r;
+    return 1;
+}
+
+extern "C" int ptw_serve_take(ptw_server *s, uint32_t *h_names, uint32_t *h_counts)
+{
+    if (!s) return fail(PTW_EINVAL, "null server");
+    if (s->done.empty()) return fail(PTW_EINVAL, "no completed result");
+    Done &d = s->done.front();
+    if (h_names && !d.names.empty()) std::memcpy(h_names, d.names.data(), d.names.size() * 4);
+    if (h_counts && !d.counts.empty()) std::memcpy(h_counts, d.counts.data(), d.counts.size() * 4);
+    s->done.pop_front();
+    return PTW_OK;
+}
+
+extern "C" double ptw_serve_clock(const ptw_server *s) { return s ? now_s(s) : 0.0; }
+
+extern "C" void ptw_serve_close(ptw_server *s)
+{
+    if (!s) return;
+    cudaSetDevice(s->g->device);
+    cudaStreamSynchronize(s->g->stream);
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    cudaFree(s->arena);
+    cudaFree(s->d_plan);
+    if (s->h_plan) cudaFreeHost(s->h_plan);
+    delete s;
+}

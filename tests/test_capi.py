@@ -37,7 +37,9 @@ def test_binding_matches_header():
 def test_struct_layouts(tmp_path):
     """ctypes structs match the C compiler's layout of include/ptw.h."""
     structs = {"ptw_graph_info": _capi.GraphInfo, "ptw_walk_cfg": _capi.WalkCfg,
-               "ptw_walk_stats": _capi.WalkStats, "ptw_tune": _capi.Tune}
+               "ptw_walk_stats": _capi.WalkStats, "ptw_tune": _capi.Tune,
+               "ptw_query": _capi.Query, "ptw_batch_cfg": _capi.BatchCfg,
+               "ptw_serve_cfg": _capi.ServeCfg, "ptw_serve_result": _capi.ServeResult}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ptw.h"', "int main(void){"]
     for cname, py in structs.items():
         lines.append('printf("%%zu\\n", sizeof(%s));' % cname)

@@ -1,0 +1,130 @@
+"""Serving loop: continuous batching must not change any result.
+
+Each query's sparse counts from the server equal the oracle replay of that
+query alone, whether it ran alone or mixed with queries that arrived while
+it was on the GPU, in CUDA-graph or plain-launch mode, under a small table
+arena that forces admission to wait for memory, and when a table overflows.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from oracle.replay import START_SOURCES
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def G16(gpu):
+    G = gpu.Graph.rmat(16, 16, 0.57, 0.19, 0.19, seed=1, clean=True)
+    yield G
+    G.close()
+
+
+def replay(canon, src, qid, budget, sp, seed, app="visits"):
+    w0 = qid << 32
+    if app == "visits":
+        c, _ = oracle.replay_counts(canon, w0, w0 + budget, sp, seed, START_SOURCES, [src])
+        return c
+    pairs, _ = oracle.replay_pairs(canon, w0, w0 + budget, sp, seed, START_SOURCES, [src])
+    return np.bincount(pairs[:, 1], minlength=canon.n).astype(np.uint32)
+
+
+def check(r, canon, sp, seed, app="visits"):
+    want = replay(canon, r["source"], r["query_id"], r["budget"], sp, seed, app)
+    nz = np.nonzero(want)[0].astype(np.uint32)
+    assert np.array_equal(r["names"], nz), r["query_id"]
+    assert np.array_equal(r["counts"], want[nz]), r["query_id"]
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_alone_and_in_the_mix(gpu, G16, s16_canon, use_graph):
+    sp, seed = 0.2, 31
+    # alone
+    with gpu.Server(G16, sp=sp, seed=seed, tick_walkers=4096, use_graph=use_graph) as srv:
+        srv.submit(1234, 20000, 7)
+        alone = srv.drain()
+    assert len(alone) == 1
+    check(alone[0], s16_canon, sp, seed)
+    # in a mix: the same query arrives while others are running and others
+    # arrive while it runs (tick_walkers 4096 spreads it over several ticks)
+    rng = np.random.default_rng(2)
+    with gpu.Server(G16, sp=sp, seed=seed, tick_walkers=4096, use_graph=use_graph) as srv:
+        got = {}
+        for k in range(5):
+            srv.submit(int(rng.integers(0, G16.n)), int(rng.integers(100, 30000)), 100 + k)
+        for r in srv.step():
+            got[r["query_id"]] = r
+        srv.submit(1234, 20000, 7)
+        for k in range(5, 40):
+            srv.submit(int(rng.integers(0, G16.n)), int(rng.integers(100, 30000)), 100 + k)
+            for r in srv.step():
+                got[r["query_id"]] = r
+        for r in srv.drain():
+            got[r["query_id"]] = r
+    assert len(got) == 41
+    assert np.array_equal(got[7]["names"], alone[0]["names"])
+    assert np.array_equal(got[7]["counts"], alone[0]["counts"])
+    for qid in (100, 104, 120, 139):
+        check(got[qid], s16_canon, sp, seed)
+    assert got[7]["submit_s"] <= got[7]["admit_s"] <= got[7]["done_s"]
+
+
+def test_admission_waits_for_table_memory(gpu, G16, s16_canon):
+    sp, seed = 0.25, 5
+    # arena of 2^17 slots: one 20000-walker query (table 2^18 > arena? no: 2^17)
+    with gpu.Server(G16, sp=sp, seed=seed, tick_walkers=8192, table_bytes=8 << 17) as srv:
+        for k in range(8):
+            srv.submit(100 + k, 5000, k)  # table 2^16 slots each: two fit at once
+        seen_active = []
+        res = []
+        while True:
+            res += srv.step()
+            seen_active.append(srv.n_active)
+            if srv.n_active == 0 and srv.n_pending == 0:
+                break
+    assert max(seen_active) <= 2
+    assert len(res) == 8
+    for r in res:
+        check(r, s16_canon, sp, seed)
+
+
+def test_overflow_and_endpoint_app(gpu, G16, s16_canon):
+    with gpu.Server(G16, sp=0.2, seed=8, tick_walkers=50000, table_factor=0.001) as srv:
+        for k in range(3):
+            srv.submit(7 * k, 40000, k)
+        res = srv.drain()
+    assert len(res) == 3
+    for r in res:
+        check(r, s16_canon, 0.2, 8)
+    with gpu.Server(G16, sp=0.5, seed=9, app="endpoint", tick_walkers=3000) as srv:
+        srv.submit(42, 10000, 3)
+        srv.submit(43, 777, 4)
+        res = srv.drain()
+    for r in res:
+        check(r, s16_canon, 0.5, 9, "endpoint")
+
+
+def test_submit_errors_and_open_loop(gpu, G16):
+    with gpu.Server(G16, sp=0.2) as srv:
+        with pytest.raises(gpu.PTWError):
+            srv.submit(10 ** 8, 10, 0)
+        with pytest.raises(gpu.PTWError):
+            srv.submit(1, 0, 0)
+        rng = np.random.default_rng(0)
+        out = gpu.open_loop(srv, rng.integers(0, G16.n, 200), rng.integers(1000, 5000, 200), rate=2000.0)
+    assert out["n"] == 200 and out["p99_ms"] >= out["p50_ms"] > 0 and out["qps"] > 0
+
+
+def test_chung_lu_graph(gpu):
+    with gpu.Graph.chung_lu(20000, 2.1, 16.0, seed=3) as G:
+        names, row_ptr, col = G.export_csr()
+        deg = np.diff(row_ptr)
+        assert deg.min() >= 1 and G.n <= 20000
+        assert deg.max() > 20 * deg.mean()  # heavy tail
+        s, d = G.export_edges()
+        fwd = np.sort((s.astype(np.uint64) << np.uint64(32)) | d)
+        rev = np.sort((d.astype(np.uint64) << np.uint64(32)) | s)
+        assert np.array_equal(fwd, rev) and np.all(s != d)  # symmetric, no loops
+        with gpu.Graph.chung_lu(20000, 2.1, 16.0, seed=3) as G2:
+            assert np.array_equal(G2.export_csr()[2], col)  # deterministic
