@@ -276,6 +276,39 @@ void ptw_serve_close(ptw_server *s);
  * removed, names 0..n'-1.  No reference counterpart. */
 int ptw_graph_chung_lu(uint32_t n, double gamma, double mean_degree, uint64_t seed, ptw_graph **out);
 
+/* ---- learned walker budgets --------------------------------------------- */
+
+/* No counterpart in the reference, which gives every query the same walker
+ * count.  Eight cheap features per source (K5), one warp per source:
+ *   0 log(1+deg)        1 mean log(1+deg(u))   2 max log(1+deg(u))
+ *   3 min log(1+deg(u)) 4 log(1+sum deg(u))    5 std log(1+deg(u))
+ *   6 fraction of neighbours of degree 1      7 log(1+sum deg(u)/deg)
+ * over the out-neighbours u of the source.  h_feat[ns * 8]. */
+int ptw_source_features(ptw_graph *g, const uint32_t *h_sources, uint32_t ns, float *h_feat);
+
+/* FP32 MLP 8 -> 64 -> 64 -> 1 (ReLU) trained with MSE and Adam on the GPU by
+ * hand-written forward / backward / update kernels (K6).  Inputs are
+ * standardised with mean / std taken from the training data; so is the
+ * target.  Parameter order: W1[8][64], b1[64], W2[64][64], b2[64], w3[64], b3.
+ * h_norm: mu[8], sigma[8], target mu, target sigma. */
+#define PTW_MLP_IN 8
+#define PTW_MLP_HIDDEN 64
+#define PTW_MLP_NPARAMS 4801
+#define PTW_MLP_NNORM 18
+typedef struct ptw_mlp ptw_mlp;
+int ptw_mlp_create(uint64_t seed, ptw_mlp **out);
+int ptw_mlp_set_params(ptw_mlp *m, const float *h_params, const float *h_norm);
+int ptw_mlp_get_params(const ptw_mlp *m, float *h_params, float *h_norm);
+/* h_y[B]: de-standardised predictions. */
+int ptw_mlp_forward(ptw_mlp *m, const float *h_x, uint32_t B, float *h_y);
+/* Loss on standardised targets and its gradient (h_grad may be NULL). */
+int ptw_mlp_grad(ptw_mlp *m, const float *h_x, const float *h_t, uint32_t B, double *h_loss, float *h_grad);
+/* Sets the standardisation from (h_x, h_t), then runs `epochs` passes of
+ * mini-batch Adam; h_loss_curve[epochs] (may be NULL) gets the mean loss. */
+int ptw_mlp_train(ptw_mlp *m, const float *h_x, const float *h_t, uint32_t N, uint32_t batch, uint32_t epochs,
+                  float lr, uint64_t seed, float *h_loss_curve);
+void ptw_mlp_free(ptw_mlp *m);
+
 /* Count walk that allocates no device memory.  No counterpart in the
  * reference.  For callers that cannot call cudaMalloc when they run (a host
  * whose pool allocator owns all device memory, or a context where an

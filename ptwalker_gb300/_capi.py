@@ -82,6 +82,7 @@ _vp = ctypes.c_void_p
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 _i32p = ctypes.POINTER(ctypes.c_int32)
+_f32p = ctypes.POINTER(ctypes.c_float)
 _G = ctypes.c_void_p
 _GP = ctypes.POINTER(ctypes.c_void_p)
 SIGNATURES = [
@@ -127,7 +128,22 @@ SIGNATURES = [
     ("ptw_serve_close", None, [_G]),
     ("ptw_graph_chung_lu", ctypes.c_int, [ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_uint64, _GP]),
+    ("ptw_source_features", ctypes.c_int, [_G, _u32p, ctypes.c_uint32, _f32p]),
+    ("ptw_mlp_create", ctypes.c_int, [ctypes.c_uint64, _GP]),
+    ("ptw_mlp_set_params", ctypes.c_int, [_G, _f32p, _f32p]),
+    ("ptw_mlp_get_params", ctypes.c_int, [_G, _f32p, _f32p]),
+    ("ptw_mlp_forward", ctypes.c_int, [_G, _f32p, ctypes.c_uint32, _f32p]),
+    ("ptw_mlp_grad", ctypes.c_int, [_G, _f32p, _f32p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_double),
+                                    _f32p]),
+    ("ptw_mlp_train", ctypes.c_int, [_G, _f32p, _f32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                     ctypes.c_float, ctypes.c_uint64, _f32p]),
+    ("ptw_mlp_free", None, [_G]),
 ]
+
+PTW_MLP_IN = 8
+PTW_MLP_HIDDEN = 64
+PTW_MLP_NPARAMS = 4801
+PTW_MLP_NNORM = 18
 
 PTW_NOALLOC_MAX_VERTICES = 1 << 22
 

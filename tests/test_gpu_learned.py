@@ -1,0 +1,89 @@
+"""Learned walker budgets: device features and MLP kernels against the FP64
+CPU oracle, training on the GPU, and what the trained network gains over the
+plain fixed budget at equal FP64-oracle L1 error."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import mlp as omlp
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def G16(gpu):
+    G = gpu.Graph.rmat(16, 16, 0.57, 0.19, 0.19, seed=1, clean=True)
+    yield G
+    G.close()
+
+
+def test_features_match_oracle(gpu, G16, s16_canon):
+    from ptwalker_gb300 import learned
+    rng = np.random.default_rng(0)
+    src = rng.integers(0, G16.n, 300).astype(np.uint32)
+    src[:3] = [0, 1, G16.n - 1]
+    got = learned.source_features(G16, src)
+    want = omlp.source_features(s16_canon, src)
+    np.testing.assert_allclose(got, want, rtol=2e-6, atol=2e-6)
+
+
+def test_mlp_forward_and_gradient_match_fp64_oracle(gpu):
+    from ptwalker_gb300 import learned
+    rng = np.random.default_rng(1)
+    m = learned.MLP(seed=3)
+    p, _ = m.params()
+    p = p + rng.normal(0, 0.05, p.shape).astype(np.float32)  # non-zero biases too
+    norm = np.concatenate([rng.normal(0, 1, 8), rng.uniform(0.5, 2, 8), [0.3, 1.7]]).astype(np.float32)
+    m.set_params(p, norm)
+    x = rng.normal(0, 1.5, (333, 8)).astype(np.float32)
+    t = rng.normal(0, 2, 333).astype(np.float32)
+    loss, g = m.grad(x, t)
+    loss64, g64, y64 = omlp.forward_backward(p, norm, x, t)
+    assert abs(loss - loss64) <= 1e-5 * max(1.0, loss64)
+    scale = np.abs(g64).max()
+    np.testing.assert_allclose(g, g64, rtol=1e-3, atol=1e-5 * scale)
+    y = m.forward(x)
+    np.testing.assert_allclose(y, y64 * norm[17] + norm[16], rtol=1e-4, atol=1e-4)
+    m.close()
+
+
+def test_training_on_gpu_reduces_loss(gpu):
+    from ptwalker_gb300 import learned
+    rng = np.random.default_rng(2)
+    x = rng.normal(0, 1, (4000, 8)).astype(np.float32)
+    t = (np.sin(x[:, 0]) + 0.5 * x[:, 1] * x[:, 2] + 0.1 * x[:, 3]).astype(np.float32)
+    m = learned.MLP(seed=5)
+    curve = m.train(x, t, epochs=60, batch=256, lr=3e-3, seed=1)
+    assert curve[-1] < 0.1 * curve[0], curve[[0, -1]]
+    pred = m.forward(x)
+    assert np.mean((pred - t) ** 2) < 0.1 * np.var(t)
+    m.close()
+
+
+def test_learned_budgets_beat_fixed_budget(gpu, G16, s16_canon):
+    """Held-out queries reach the fixed budget's 90th-percentile FP64 L1 with
+    fewer total walker steps when budgets come from the trained network."""
+    from ptwalker_gb300 import learned
+    rng = np.random.default_rng(7)
+    s, d = G16.export_edges()
+    # sources drawn degree-proportionally: the endpoint of a uniform edge
+    train_src = d[rng.integers(0, len(d), 768)]
+    test_src = d[rng.integers(0, len(d), 256)]
+    sp, b_fix = 0.2, 40000
+    log_c, _ = learned.error_constants(G16, train_src, b0=2000, mult=16, sp=sp, seed=11)
+    model = learned.BudgetModel(seed=0)
+    model.fit(G16, train_src, np.log(log_c), epochs=300, coverage=0.9)
+
+    fixed = gpu.ppr_batch(G16, test_src, b_fix, sp=sp, seed=12, query_ids=np.arange(10000, 10256))
+    l1_fixed = fixed.l1(tol=1e-10)
+    eps = float(np.quantile(l1_fixed, 0.9))
+    budgets = model.budgets(G16, test_src, eps, b_min=500, b_max=b_fix, fallback=b_fix)
+    learned_run = gpu.ppr_batch(G16, test_src, budgets, sp=sp, seed=12, query_ids=np.arange(10000, 10256))
+    l1_learned = learned_run.l1(tol=1e-10)
+    gain = fixed.moves / learned_run.moves
+    print("fixed p90 L1 %.4f learned p90 L1 %.4f steps fixed %d learned %d gain %.2fx"
+          % (eps, np.quantile(l1_learned, 0.9), fixed.moves, learned_run.moves, gain))
+    assert np.quantile(l1_learned, 0.9) <= 1.1 * eps
+    assert gain >= 1.3
+    # fallback: without a model every query gets the plain budget
+    assert np.all(learned.plain_budgets(5, b_fix) == b_fix)

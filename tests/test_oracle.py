@@ -170,3 +170,21 @@ def test_reference_binary_s16_calibrated(s16_canon):
     ref_z = np.max([maxz(ref, r) for r in runs])
     assert ref_l1 <= 1.5 * np.percentile(pair_l1, 99), (ref_l1, np.percentile(pair_l1, 99))
     assert ref_z <= 1.5 * np.percentile(pair_z, 99), (ref_z, np.percentile(pair_z, 99))
+
+
+def test_mlp_oracle_gradient_finite_differences():
+    from oracle import mlp as omlp
+    rng = np.random.default_rng(0)
+    p = rng.normal(0, 0.3, omlp.NPARAMS)
+    norm = np.concatenate([rng.normal(0, 1, 8), rng.uniform(0.5, 2, 8), [0.2, 1.5]])
+    x = rng.normal(0, 1, (50, 8))
+    t = rng.normal(0, 1, 50)
+    loss, g, _ = omlp.forward_backward(p, norm, x, t)
+    for k in rng.choice(omlp.NPARAMS, 40, replace=False):
+        h = 1e-6
+        pp = p.copy()
+        pp[k] += h
+        pm = p.copy()
+        pm[k] -= h
+        fd = (omlp.forward_backward(pp, norm, x, t)[0] - omlp.forward_backward(pm, norm, x, t)[0]) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-6 + 1e-4 * abs(g[k])
