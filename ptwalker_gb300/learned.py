@@ -1,21 +1,22 @@
 """Learned walker budgets for PPR queries.
 
-The Monte Carlo PPR estimate of a source s with b walkers has an L1 error
-close to C_s / sqrt(b), where C_s depends on how widely s's PPR mass spreads.
-The engine measures C_s on its own runs, learns it from cheap source
-features, and sizes each query's budget for a target error:
+Each query needs a different number of walkers to reach a target L1 error:
+a source whose PPR mass spreads widely needs more than one whose mass stays
+near it.  The engine measures that need on its own runs, learns it from
+cheap source features, and sizes each query's budget from the prediction.
 
-  labels   C_s = L1(est_b0, est_B) / sqrt(1/b0 - 1/B): a budget-b0 run is the
-           first b0 walkers of the budget-B run of the same query id (the
-           draws depend on (query id, walker rank) only), so both come from
-           one nested pair of runs of the method itself;
+  labels   for a training query, the budget-b estimates on a log grid of b
+           are prefixes of one high-budget run of the same query id (draws
+           depend on (query id, walker rank) only); the label is the budget
+           b* at which L1(est_b, est_high) falls to the target eps, log-log
+           interpolated on the grid (extrapolated with the 1/sqrt(b) law
+           outside it);
   model    the 8 -> 64 -> 64 -> 1 MLP of libptw (ptw_mlp_*), trained on the
-           GPU on log C_s from the features of ptw_source_features;
-  budget   b_s = clamp(kappa * (C_s_predicted / eps)^2, b_min, b_max), with
-           kappa calibrated on the training queries so that a chosen share
-           of them gets at least the budget they need; a fixed plain budget
-           is the fallback when no model is given or a prediction is not
-           finite.
+           GPU on log b* from the features of ptw_source_features;
+  budget   b = clamp(kappa * exp(prediction), b_min, b_max), kappa set on the
+           training queries so that a chosen share of them gets at least its
+           b*; a fixed plain budget is the fallback when no model is given or
+           a prediction is not finite.
 """
 import ctypes
 
@@ -94,54 +95,80 @@ class MLP:
 
 def sparse_l1(names_a, counts_a, names_b, counts_b):
     """L1 between two sparse count vectors (sorted names), each normalised."""
-    ca = counts_a.astype(np.float64) / max(counts_a.sum(), 1)
-    cb = counts_b.astype(np.float64) / max(counts_b.sum(), 1)
+    ca = counts_a.astype(np.float64) / max(int(counts_a.sum()), 1)
+    cb = counts_b.astype(np.float64) / max(int(counts_b.sum()), 1)
+    if len(names_b) == 0:
+        return float(ca.sum())
     pos = np.searchsorted(names_b, names_a)
-    pos_c = np.minimum(pos, max(len(names_b) - 1, 0))
-    hit = (pos < len(names_b)) & (names_b[pos_c] == names_a) if len(names_b) else np.zeros(len(names_a), bool)
-    l1 = np.abs(ca - np.where(hit, cb[pos_c] if len(names_b) else 0.0, 0.0)).sum()
+    pos_c = np.minimum(pos, len(names_b) - 1)
+    hit = (pos < len(names_b)) & (names_b[pos_c] == names_a)
+    l1 = np.abs(ca - np.where(hit, cb[pos_c], 0.0)).sum()
     only_b = np.ones(len(names_b), bool)
     only_b[pos_c[hit]] = False
     return float(l1 + cb[only_b].sum())
 
 
-def error_constants(graph, sources, b0=2000, mult=16, sp=0.2, seed=0, query_id0=0, table_bytes=0):
-    """Measured C_s per source from one nested pair of runs (see module doc)."""
+def grid_errors(graph, sources, grid, ref_budget, sp=0.2, seed=0, query_id0=0, chunk=256):
+    """L1(est_b, est_ref) for every source and grid budget b; returns [ns, len(grid)]
+    and the total moves spent.  The budget-b run of a query id is the first b
+    walkers of its ref run."""
     sources = np.atleast_1d(np.asarray(sources, dtype=np.uint32))
-    qids = np.arange(query_id0, query_id0 + len(sources), dtype=np.uint32)
-    lo = ppr_batch(graph, sources, b0, sp=sp, seed=seed, query_ids=qids, table_bytes=table_bytes)
-    hi = ppr_batch(graph, sources, b0 * mult, sp=sp, seed=seed, query_ids=qids, table_bytes=table_bytes)
-    scale = 1.0 / np.sqrt(1.0 / b0 - 1.0 / (b0 * mult))
-    out = np.empty(len(sources))
-    for i in range(len(sources)):
-        na, ca = lo.query(i)
-        nb, cb = hi.query(i)
-        out[i] = sparse_l1(na, ca, nb, cb) * scale
-    return out, lo.moves + hi.moves
+    out = np.empty((len(sources), len(grid)))
+    moves = 0
+    for c0 in range(0, len(sources), chunk):
+        src = sources[c0:c0 + chunk]
+        qids = np.arange(query_id0 + c0, query_id0 + c0 + len(src), dtype=np.uint32)
+        ref = ppr_batch(graph, src, ref_budget, sp=sp, seed=seed, query_ids=qids)
+        moves += ref.moves
+        for k, b in enumerate(grid):
+            run = ppr_batch(graph, src, int(b), sp=sp, seed=seed, query_ids=qids)
+            moves += run.moves
+            for i in range(len(src)):
+                out[c0 + i, k] = sparse_l1(*run.query(i), *ref.query(i))
+            run.close()
+        ref.close()
+    return out, moves
+
+
+def needed_budget(errors, grid, eps):
+    """Budget at which each row of errors (over the log grid) reaches eps."""
+    grid = np.asarray(grid, dtype=np.float64)
+    lg = np.log(grid)
+    out = np.empty(errors.shape[0])
+    for i, e in enumerate(errors):
+        le = np.log(np.maximum(e, 1e-12))
+        below = np.nonzero(e <= eps)[0]
+        if len(below) == 0:  # beyond the grid: 1/sqrt(b) from the last point
+            out[i] = lg[-1] + 2.0 * (le[-1] - np.log(eps))
+        elif below[0] == 0:  # already below at the smallest budget
+            out[i] = lg[0] - 2.0 * (np.log(eps) - le[0])
+        else:
+            k = below[0]
+            t = (np.log(eps) - le[k - 1]) / (le[k] - le[k - 1]) if le[k] != le[k - 1] else 1.0
+            out[i] = lg[k - 1] + t * (lg[k] - lg[k - 1])
+    return out  # log budgets
 
 
 class BudgetModel:
-    """Features -> predicted log C_s -> walker budget for a target L1."""
+    """Features -> predicted log b* -> walker budget."""
 
     def __init__(self, seed=0):
         self.mlp = MLP(seed)
         self.kappa = 1.0
 
-    def fit(self, graph, sources, log_c, epochs=300, batch=256, lr=3e-3, seed=0, coverage=0.9):
+    def fit(self, graph, sources, log_budget, epochs=300, batch=256, lr=3e-3, seed=0, coverage=0.9):
         x = source_features(graph, sources)
-        curve = self.mlp.train(x, np.asarray(log_c, np.float32), epochs, batch, lr, seed)
+        curve = self.mlp.train(x, np.asarray(log_budget, np.float32), epochs, batch, lr, seed)
         pred = self.mlp.forward(x).astype(np.float64)
-        # kappa: the share `coverage` of training queries gets >= its need
-        ratio2 = np.exp(2.0 * (np.asarray(log_c, np.float64) - pred))
-        self.kappa = float(np.quantile(ratio2, coverage))
+        # kappa: the share `coverage` of training queries gets >= its b*
+        self.kappa = float(np.quantile(np.exp(np.asarray(log_budget, np.float64) - pred), coverage))
         return curve
 
-    def predict_log_c(self, graph, sources):
+    def predict_log_budget(self, graph, sources):
         return self.mlp.forward(source_features(graph, sources)).astype(np.float64)
 
-    def budgets(self, graph, sources, eps, b_min=1000, b_max=1_000_000, fallback=1_000_000):
-        pred = self.predict_log_c(graph, sources)
-        b = self.kappa * np.exp(2.0 * pred) / (eps * eps)
+    def budgets(self, graph, sources, b_min=1000, b_max=1_000_000, fallback=1_000_000):
+        b = self.kappa * np.exp(self.predict_log_budget(graph, sources))
         b = np.where(np.isfinite(b), np.clip(b, b_min, b_max), fallback)
         return b.astype(np.int64)
 
@@ -149,3 +176,35 @@ class BudgetModel:
 def plain_budgets(n, fixed=1_000_000):
     """The fallback / baseline: the same budget for every query."""
     return np.full(n, int(fixed), dtype=np.int64)
+
+
+def evaluate(graph, train_src, test_src, b_fix, sp=0.2, seed=0, grid_points=7, ref_mult=8, coverage=0.9,
+             epochs=300, b_min=None, l1_tol=1e-10):
+    """Learned budgets vs the fixed budget b_fix on held-out queries at equal
+    FP64-oracle L1 (90th percentile).  The target eps is the fixed budget's
+    90th-percentile error on the training queries (measured against their
+    high-budget runs).  Returns a dict of the measured figures."""
+    grid = np.unique(np.geomspace(b_fix / 2 ** (grid_points - 1), b_fix * 2, grid_points + 1).astype(np.int64))
+    ref_budget = int(b_fix * ref_mult)
+    errs, label_moves = grid_errors(graph, train_src, grid, ref_budget, sp, seed, query_id0=1 << 20)
+    k_fix = int(np.argmin(np.abs(grid - b_fix)))
+    eps = float(np.quantile(errs[:, k_fix], 0.9))
+    log_b = needed_budget(errs, grid, eps)
+    model = BudgetModel(seed=seed)
+    curve = model.fit(graph, train_src, log_b, epochs=epochs, coverage=coverage)
+    b_min = b_min or int(grid[0])
+    qids = np.arange(len(test_src), dtype=np.uint32) + (1 << 24)
+    fixed = ppr_batch(graph, test_src, b_fix, sp=sp, seed=seed + 1, query_ids=qids)
+    budgets = model.budgets(graph, test_src, b_min=b_min, b_max=4 * b_fix, fallback=b_fix)
+    learned = ppr_batch(graph, test_src, budgets, sp=sp, seed=seed + 1, query_ids=qids)
+    l1_f = fixed.l1(tol=l1_tol)
+    l1_l = learned.l1(tol=l1_tol)
+    return dict(eps_train=eps, fixed_budget=int(b_fix), fixed_moves=int(fixed.moves),
+                learned_moves=int(learned.moves), gain=fixed.moves / max(learned.moves, 1),
+                fixed_l1_p50=float(np.median(l1_f)), fixed_l1_p90=float(np.quantile(l1_f, 0.9)),
+                learned_l1_p50=float(np.median(l1_l)), learned_l1_p90=float(np.quantile(l1_l, 0.9)),
+                fixed_l1_mean=float(l1_f.mean()), learned_l1_mean=float(l1_l.mean()),
+                budget_min=int(budgets.min()), budget_max=int(budgets.max()),
+                budget_mean=float(budgets.mean()), label_moves=int(label_moves),
+                train_loss=[float(curve[0]), float(curve[-1])], kappa=model.kappa,
+                n_train=int(len(train_src)), n_test=int(len(test_src)))

@@ -93,6 +93,25 @@ def test_malformed_text_edge_list_is_an_io_error(tmp_path):
     assert rc == _capi.PTW_EIO
 
 
+def test_cli_rejects_bad_flags_without_a_gpu(tmp_path):
+    import subprocess
+    _build.build()
+    exe = os.path.join(_build.BIN_DIR, "pagerank")
+    r = subprocess.run([exe, "-f", "text", "-g", "x", "-w", "5", "--sp", "0.1", "--bogus", "1"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "unknown flag --bogus" in r.stderr
+    r = subprocess.run([exe, "-f", "text", "-g", "x", "-w", "5"], capture_output=True, text=True)
+    assert r.returncode == 1 and "--sp is required" in r.stderr
+    r = subprocess.run([exe, "-f", "text", "-g", "x", "-w", "5", "-e", "2", "--sp", "0.1"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "exactly one of -w and -e" in r.stderr
+    bad = tmp_path / "bad.txt"
+    bad.write_text("0 1\nfoo\n")
+    r = subprocess.run([exe, "-f", "text", "-g", str(bad), "-w", "5", "--sp", "0.1"],
+                       capture_output=True, text=True)
+    assert r.returncode == 2 and "malformed edge at line 2" in r.stderr
+
+
 def test_cfg_builder():
     cfg, keep = api._cfg(10, 0.15, -1, "sources", [3, 4], 0, first_walker=7 << 32)
     assert cfg.seed == 0xFFFFFFFFFFFFFFFF
