@@ -53,6 +53,14 @@ def parse():
     p.add_argument("--tune", default=None,
                    help="block,ilp,chunk,hot_k[,min_blocks[,paths_ilp]]: fixed launch parameters "
                         "(skips the autotuner)")
+    p.add_argument("--no-batch", action="store_true", help="skip the batched-PPR side line")
+    p.add_argument("--no-serve", action="store_true", help="skip the serving side line")
+    p.add_argument("--learned", action="store_true", help="add the learned-budget side line (minutes)")
+    p.add_argument("--batch-scale", type=int, default=22)
+    p.add_argument("--batch-queries", type=int, default=4096)
+    p.add_argument("--serve-n", type=int, default=8_400_000)
+    p.add_argument("--serve-rates", default="1000,10000,50000")
+    p.add_argument("--serve-queries", type=int, default=3000)
     return p.parse_args()
 
 
@@ -188,6 +196,80 @@ def run_reference(args):
     }
     print(json.dumps(line))
     return 0
+
+
+# ---- side lines: batched PPR, serving, learned budgets -------------------------------
+
+def degree_sources(G, n, seed):
+    """Sources drawn degree-proportionally: the endpoint of a uniform edge."""
+    import numpy as np
+    names, row_ptr, col = G.export_csr()
+    rng = np.random.default_rng(seed)
+    e = rng.integers(0, G.m, n)
+    return names[col[e]]
+
+
+def loguniform_budgets(n, lo, hi, seed):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), n)).astype(np.int64)
+
+
+def bench_batch(args, ptw):
+    """Config: R-MAT scale 22, 4096 degree-proportional sources (seed 2),
+    budgets log-uniform in [1e3, 1e6] (seed 3), sp 0.2, one batch call."""
+    import numpy as np
+    G = ptw.Graph.rmat(args.batch_scale, 16, 0.57, 0.19, 0.19, seed=1, clean=True)
+    src = degree_sources(G, args.batch_queries, 2)
+    bud = loguniform_budgets(args.batch_queries, 1e3, 1e6, 3)
+    ptw.ppr_batch(G, src[:64], bud[:64], sp=0.2, seed=7).close()  # warm-up
+    t0 = time.perf_counter()
+    res = ptw.ppr_batch(G, src, bud, sp=0.2, seed=7)
+    wall = time.perf_counter() - t0
+    sub = np.arange(0, args.batch_queries, max(1, args.batch_queries // 64))[:64]
+    one = ptw.ppr_batch(G, src[sub], bud[sub], sp=0.2, seed=7, query_ids=sub.astype(np.uint32))
+    l1 = one.l1(tol=1e-10)
+    out = {"graph": "rmat-s%d" % args.batch_scale, "vertices": G.n, "edges": G.m,
+           "queries": int(args.batch_queries), "walkers": int(res.walkers), "moves": int(res.moves),
+           "entries": int(res.entries), "seconds": wall, "queries_per_s": args.batch_queries / wall,
+           "steps_per_s": res.moves / wall, "device_ms": res.ms, "walk_kernel_ms": res.kernel_ms,
+           "walk_kernel_steps_per_s": res.moves / (res.kernel_ms / 1000.0),
+           "fp64_l1_sample": {"queries": int(len(sub)), "p50": float(np.median(l1)),
+                              "p90": float(np.quantile(l1, 0.9)), "max": float(l1.max())}}
+    res.close()
+    one.close()
+    G.close()
+    return out
+
+
+def bench_serve(args, ptw):
+    """Config: Chung-Lu power-law graph (8.4M vertices, exponent 2.1, mean
+    degree 32), Poisson arrivals at each rate, random sources, budgets
+    log-uniform in [1e3, 1e5] (fixed plain budgets), sp 0.2."""
+    import numpy as np
+    G = ptw.Graph.chung_lu(args.serve_n, 2.1, 32.0, seed=1)
+    rng = np.random.default_rng(4)
+    out = {"graph": "chung-lu n=%d gamma=2.1 mean_degree=32" % args.serve_n, "vertices": G.n, "edges": G.m,
+           "rates": []}
+    for k, rate in enumerate(float(r) for r in args.serve_rates.split(",")):
+        src = rng.integers(0, G.n, args.serve_queries)
+        bud = loguniform_budgets(args.serve_queries, 1e3, 1e5, 10 + k)
+        with ptw.Server(G, sp=0.2, seed=3, tick_walkers=1 << 21, use_graph=True) as srv:
+            r = ptw.open_loop(srv, src, bud, rate=rate, seed=k, query_id0=k << 20)
+        out["rates"].append({kk: r[kk] for kk in ("rate", "n", "qps", "p50_ms", "p99_ms", "mean_ms")})
+    G.close()
+    return out
+
+
+def bench_learned(args, ptw):
+    import numpy as np
+    from ptwalker_gb300 import learned
+    G = ptw.Graph.rmat(args.batch_scale, 16, 0.57, 0.19, 0.19, seed=1, clean=True)
+    train = degree_sources(G, 1024, 21)
+    test = degree_sources(G, 512, 22)
+    r = learned.evaluate(G, train, test, b_fix=100000, sp=0.2, seed=5, epochs=300)
+    G.close()
+    return r
 
 
 # ---- our arm ----------------------------------------------------------------------
@@ -377,10 +459,19 @@ def run_ours(args):
         "moves_per_step": sum(moves) / len(moves),
         "deepwalk": deepwalk,
     }
-    if rank == 0:
-        print(json.dumps(line))
     G.set_stream(None)
     G.close()
+    if rank == 0 and world == 1:
+        for key, flag, fn in (("batched_ppr", args.no_batch, bench_batch), ("serving", args.no_serve, bench_serve),
+                              ("learned_budgets", not args.learned, bench_learned)):
+            if flag:
+                continue
+            try:
+                line[key] = fn(args, ptw)
+            except Exception as e:  # a side line must not cost the headline
+                line[key] = {"error": "%s: %s" % (type(e).__name__, e)}
+    if rank == 0:
+        print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
     return 0

@@ -212,6 +212,10 @@ int ptw_batch_info(const ptw_batch *b, uint32_t *nq, uint64_t *entries, ptw_walk
 /* h_offsets[nq + 1]: query i owns entries [h_offsets[i], h_offsets[i+1]).
  * Any pointer may be NULL. */
 int ptw_batch_export(const ptw_batch *b, uint64_t *h_offsets, uint32_t *h_names, uint32_t *h_counts);
+/* The same arrays without a copy: pointers into the batch's own host memory,
+ * valid until ptw_batch_free. */
+int ptw_batch_view(const ptw_batch *b, const uint64_t **offsets, const uint32_t **names,
+                   const uint32_t **counts);
 void ptw_batch_free(ptw_batch *b);
 
 /* FP64 oracle on the device: for each source name, the exact expected count

@@ -116,6 +116,8 @@ SIGNATURES = [
     ("ptw_batch_info", ctypes.c_int, [_G, ctypes.POINTER(ctypes.c_uint32), _u64p,
                                       ctypes.POINTER(WalkStats)]),
     ("ptw_batch_export", ctypes.c_int, [_G, _u64p, _u32p, _u32p]),
+    ("ptw_batch_view", ctypes.c_int, [_G, ctypes.POINTER(_u64p), ctypes.POINTER(_u32p),
+                                      ctypes.POINTER(_u32p)]),
     ("ptw_batch_free", None, [_G]),
     ("ptw_batch_l1", ctypes.c_int, [_G, _G, ctypes.c_double, ctypes.c_int32, ctypes.c_double,
                                     ctypes.POINTER(ctypes.c_double)]),

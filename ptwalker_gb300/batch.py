@@ -32,13 +32,19 @@ class BatchResult:
         self.nq, self.entries = int(nq.value), int(ne.value)
         self.walkers, self.moves, self.visits = int(st.walkers), int(st.moves), int(st.visits)
         self.ms = float(st.total_ms)
-        self.offsets = np.empty(self.nq + 1, dtype=np.uint64)
-        self.names = np.empty(self.entries, dtype=np.uint32)
-        self.counts = np.empty(self.entries, dtype=np.uint32)
-        C.check(self._lib.ptw_batch_export(
-            self._h, self.offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
-            self.names.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
-            self.counts.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
+        self.kernel_ms = float(st.kernel_ms)
+        # zero-copy views of the batch's host arrays (valid until close())
+        po = ctypes.POINTER(ctypes.c_uint64)()
+        pn = ctypes.POINTER(ctypes.c_uint32)()
+        pc = ctypes.POINTER(ctypes.c_uint32)()
+        C.check(self._lib.ptw_batch_view(self._h, ctypes.byref(po), ctypes.byref(pn), ctypes.byref(pc)))
+        self.offsets = np.ctypeslib.as_array(po, shape=(self.nq + 1,))
+        if self.entries:
+            self.names = np.ctypeslib.as_array(pn, shape=(self.entries,))
+            self.counts = np.ctypeslib.as_array(pc, shape=(self.entries,))
+        else:
+            self.names = np.empty(0, dtype=np.uint32)
+            self.counts = np.empty(0, dtype=np.uint32)
 
     def query(self, i):
         a, b = int(self.offsets[i]), int(self.offsets[i + 1])
@@ -59,7 +65,9 @@ class BatchResult:
         return out
 
     def close(self):
+        """Frees the results; the arrays of this object are no longer valid."""
         if self._h:
+            self.offsets = self.names = self.counts = None
             self._lib.ptw_batch_free(self._h)
             self._h = None
 

@@ -22,7 +22,10 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -32,9 +35,21 @@ struct ptw_batch {
     uint32_t nq = 0;
     std::vector<ptw_query> queries;
     std::vector<uint64_t> offsets;  // [nq + 1]
-    std::vector<uint32_t> names, counts;
+    std::unique_ptr<uint32_t[]> names, counts;
     ptw_walk_stats stats{};
 };
+
+namespace ptw {
+namespace {
+// Result of one wave: its queries (caller indices, in wave order), their
+// compacted entries, and which of them overflowed (entries to be replaced).
+struct WaveResult {
+    std::vector<uint32_t> idx;
+    Compacted c;
+    std::vector<char> overflow;
+};
+}  // namespace
+}  // namespace ptw
 
 namespace ptw {
 namespace {
@@ -80,40 +95,69 @@ struct WaveQuery {
     uint64_t cap;    // table slots (power of two)
 };
 
+}  // namespace
+
+// Splits [j0, j0 + count) of every entry into descriptors of at most
+// kDescWalkers ranks, ordered round-robin over the entries.
+void interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<uint64_t> &count,
+                            std::vector<uint3> &desc)
+{
+    desc.clear();
+    std::vector<uint32_t> live;
+    for (uint32_t i = 0; i < count.size(); ++i)
+        if (count[i]) live.push_back(i);
+    for (uint64_t r = 0; !live.empty(); ++r) {
+        size_t keep = 0;
+        for (uint32_t i : live) {
+            const uint64_t off = r * kDescWalkers;
+            const uint64_t c = std::min<uint64_t>(kDescWalkers, count[i] - off);
+            desc.push_back(make_uint3(i, (uint32_t)(j0[i] + off), (uint32_t)c));
+            if (off + c < count[i]) live[keep++] = i;
+        }
+        live.resize(keep);
+    }
+}
+
+namespace {
+
 // Runs one wave; stores each query's sorted entries in per-query host lists.
 int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg *cfg, uint64_t thr,
-             std::vector<std::vector<uint32_t>> &names, std::vector<std::vector<uint32_t>> &cnts,
-             std::vector<uint32_t> &overflow, uint64_t *moves_out)
+             std::vector<WaveResult> &waves, std::vector<uint32_t> &overflow, uint64_t *moves_out,
+             float *walk_ms)
 {
     cudaStream_t st = g->stream;
     const uint32_t nq = (uint32_t)wq.size();
-    std::vector<unsigned long long> h_off(nq + 1), h_tab(nq + 1);
+    std::vector<unsigned long long> h_tab(nq + 1);
     std::vector<uint32_t> h_src(nq), h_qid(nq), h_mask(nq), h_cap(nq);
+    std::vector<uint64_t> j0(nq, 0), cnt(nq);
     for (uint32_t i = 0; i < nq; ++i) {
-        h_off[i + 1] = h_off[i] + wq[i].budget;
         h_tab[i + 1] = h_tab[i] + wq[i].cap;
         h_src[i] = wq[i].src;
         h_qid[i] = wq[i].qid;
         h_mask[i] = (uint32_t)(wq[i].cap - 1);
         h_cap[i] = (uint32_t)wq[i].cap;
+        cnt[i] = wq[i].budget;
     }
-    const uint64_t total = h_off[nq], n_slots = h_tab[nq];
+    std::vector<uint3> h_desc;
+    interleave_descriptors(j0, cnt, h_desc);
+    const uint64_t n_slots = h_tab[nq], nd = h_desc.size();
     DevBuf db(st);
-    unsigned long long *d_off, *d_tab, *d_slots, *d_ctrl;
+    unsigned long long *d_tab, *d_slots, *d_ctrl;
     uint32_t *d_src, *d_qid, *d_mask, *d_flag;
-    PTW_CUDA(db.alloc(&d_off, nq + 1));
+    uint3 *d_desc;
     PTW_CUDA(db.alloc(&d_tab, nq + 1));
     PTW_CUDA(db.alloc(&d_src, nq));
     PTW_CUDA(db.alloc(&d_qid, nq));
     PTW_CUDA(db.alloc(&d_mask, nq));
     PTW_CUDA(db.alloc(&d_flag, nq));
     PTW_CUDA(db.alloc(&d_ctrl, 2));
+    PTW_CUDA(db.alloc(&d_desc, nd));
     PTW_CUDA(db.alloc(&d_slots, n_slots));
-    PTW_CUDA(cudaMemcpyAsync(d_off, h_off.data(), (nq + 1) * 8ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_tab, h_tab.data(), (nq + 1) * 8ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_src, h_src.data(), nq * 4ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_qid, h_qid.data(), nq * 4ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_mask, h_mask.data(), nq * 4ull, cudaMemcpyHostToDevice, st));
+    PTW_CUDA(cudaMemcpyAsync(d_desc, h_desc.data(), nd * sizeof(uint3), cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemsetAsync(d_flag, 0, nq * 4ull, st));
     PTW_CUDA(cudaMemsetAsync(d_ctrl, 0, 16, st));
     PTW_CUDA(cudaMemsetAsync(d_slots, 0, n_slots * 8, st));
@@ -121,8 +165,7 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     BatchArgs a;
     a.adj = g->dg.adj;
     a.col = g->dg.col;
-    a.q_off = d_off;
-    a.q_j0 = nullptr;
+    a.desc = d_desc;
     a.q_src = d_src;
     a.q_qid = d_qid;
     a.q_tab = d_tab;
@@ -130,38 +173,87 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     a.q_flag = d_flag;
     a.slots = d_slots;
     a.ctrl = d_ctrl;
-    a.total = total;
+    a.ndesc = (uint32_t)nd;
     a.thr = thr;
-    a.nq = nq;
     a.key0 = (uint32_t)cfg->seed;
     a.key1 = (uint32_t)(cfg->seed >> 32);
     a.max_moves = cfg->max_moves;
-    a.chunk = 256;
     a.app = cfg->app;
+    if (nd >= (1ull << 32)) return fail(PTW_EINVAL, "wave too large");
     int per_sm = 0;
     PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, 256, 0));
     uint64_t grid = (uint64_t)g->num_sms * std::max(per_sm, 1);
-    grid = std::min<uint64_t>(grid, std::max<uint64_t>(1, (total + a.chunk * 8 - 1) / (a.chunk * 8)));
+    grid = std::min<uint64_t>(grid, std::max<uint64_t>(1, (nd + 7) / 8));
+    PTW_CUDA(cudaEventRecord(g->ev[0], st));
     k_batch<<<(unsigned)grid, 256, 0, st>>>(a);
+    PTW_CUDA(cudaEventRecord(g->ev[1], st));
     PTW_CUDA(cudaGetLastError());
     std::vector<uint32_t> h_flag(nq);
     unsigned long long h_moves = 0;
     PTW_CUDA(cudaMemcpyAsync(h_flag.data(), d_flag, nq * 4ull, cudaMemcpyDeviceToHost, st));
     PTW_CUDA(cudaMemcpyAsync(&h_moves, d_ctrl + 1, 8, cudaMemcpyDeviceToHost, st));
-    std::vector<std::vector<uint32_t> *> out_n(nq), out_c(nq);
-    for (uint32_t i = 0; i < nq; ++i) {
-        out_n[i] = &names[wq[i].index];
-        out_c[i] = &cnts[wq[i].index];
-    }
-    int rc = compact_tables(g, d_slots, h_tab.data(), h_cap.data(), nq, out_n.data(), out_c.data());
+    WaveResult wr;
+    int rc = compact_tables(g, d_slots, h_tab.data(), h_cap.data(), nq, &wr.c);
     if (rc) return rc;
+    float ms = 0;
+    PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]));
+    *walk_ms += ms;
     *moves_out += h_moves;
-    for (uint32_t i = 0; i < nq; ++i)
+    if (std::getenv("PTW_TIMING"))
+        std::fprintf(stderr, "[ptw] wave of %u queries, %llu descriptors, %llu slots: walk kernel %.1f ms\n", nq,
+                     (unsigned long long)nd, (unsigned long long)n_slots, ms);
+    wr.idx.resize(nq);
+    wr.overflow.assign(nq, 0);
+    for (uint32_t i = 0; i < nq; ++i) {
+        wr.idx[i] = wq[i].index;
         if (h_flag[i]) {
             overflow.push_back(wq[i].index);
-            names[wq[i].index].clear();
-            cnts[wq[i].index].clear();
+            wr.overflow[i] = 1;
         }
+    }
+    waves.push_back(std::move(wr));
+    return PTW_OK;
+}
+
+// Concatenates the waves' entries in caller query order.  One wave holding
+// every query in order (the common case) is adopted without a copy.
+int assemble(ptw_batch *b, std::vector<WaveResult> &waves)
+{
+    const uint32_t nq = b->nq;
+    std::vector<const WaveResult *> src_w(nq, nullptr);
+    std::vector<uint32_t> src_i(nq, 0);
+    for (const WaveResult &w : waves)
+        for (uint32_t k = 0; k < w.idx.size(); ++k)
+            if (!w.overflow[k]) {
+                src_w[w.idx[k]] = &w;
+                src_i[w.idx[k]] = k;
+            }
+    b->offsets.assign(nq + 1, 0);
+    for (uint32_t i = 0; i < nq; ++i) {
+        const WaveResult *w = src_w[i];
+        const uint64_t len = w ? w->c.seg[src_i[i] + 1] - w->c.seg[src_i[i]] : 0;
+        b->offsets[i + 1] = b->offsets[i] + len;
+    }
+    const uint64_t total = b->offsets[nq];
+    bool adopt = waves.size() == 1 && waves[0].idx.size() == nq;
+    if (adopt)
+        for (uint32_t k = 0; k < nq; ++k) adopt = adopt && waves[0].idx[k] == k && !waves[0].overflow[k];
+    if (adopt) {
+        b->names = std::move(waves[0].c.names);
+        b->counts = std::move(waves[0].c.counts);
+        return PTW_OK;
+    }
+    if (!total) return PTW_OK;
+    b->names.reset(new (std::nothrow) uint32_t[total]);
+    b->counts.reset(new (std::nothrow) uint32_t[total]);
+    if (!b->names || !b->counts) return fail(PTW_ENOMEM, "host allocation of batch results failed");
+    for (uint32_t i = 0; i < nq; ++i) {
+        const WaveResult *w = src_w[i];
+        if (!w) continue;
+        const uint64_t a = w->c.seg[src_i[i]], len = b->offsets[i + 1] - b->offsets[i];
+        std::memcpy(b->names.get() + b->offsets[i], w->c.names.get() + a, len * 4);
+        std::memcpy(b->counts.get() + b->offsets[i], w->c.counts.get() + a, len * 4);
+    }
     return PTW_OK;
 }
 
@@ -177,11 +269,18 @@ uint64_t next_pow2(uint64_t x)
 const ptw_query *batch_queries(const ptw_batch *b) { return b->queries.data(); }
 
 int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned long long *h_base,
-                   const uint32_t *h_cap, uint32_t nt, std::vector<uint32_t> **names,
-                   std::vector<uint32_t> **counts)
+                   const uint32_t *h_cap, uint32_t nt, Compacted *out)
 {
+    out->n = 0;
+    out->seg.assign(nt + 1, 0);
+    out->names.reset();
+    out->counts.reset();
     if (nt == 0) return PTW_OK;
     cudaStream_t st = g->stream;
+    const bool timing = std::getenv("PTW_TIMING") != nullptr;
+    auto clk = [] { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
+    const double t0 = timing ? (cudaStreamSynchronize(st), clk()) : 0.0;
+    double t1 = 0, t2 = 0;
     DevBuf db(st);
     unsigned long long *d_base, *d_cnt, *d_seg, *d_fill;
     uint32_t *d_cap;
@@ -206,35 +305,51 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     PTW_CUDA(cub_call([&](void *t, size_t &b) {
         return cub::DeviceScan::InclusiveSum(t, b, d_cnt, d_seg + 1, (int64_t)nt, st);
     }, st));
-    std::vector<unsigned long long> h_seg(nt + 1);
-    PTW_CUDA(cudaMemcpyAsync(h_seg.data(), d_seg, (nt + 1) * 8ull, cudaMemcpyDeviceToHost, st));
+    PTW_CUDA(cudaMemcpyAsync(out->seg.data(), d_seg, (nt + 1) * 8ull, cudaMemcpyDeviceToHost, st));
     PTW_CUDA(cudaStreamSynchronize(st));
-    const uint64_t n_ent = h_seg[nt];
-    std::vector<uint32_t> h_name(n_ent), h_cnt(n_ent);
+    const uint64_t n_ent = out->seg[nt];
+    out->n = n_ent;
     if (n_ent) {
-        uint32_t *e_name, *e_cnt, *s_name, *s_cnt;
-        PTW_CUDA(db.alloc(&e_name, n_ent));
+        out->names.reset(new (std::nothrow) uint32_t[n_ent]);  // no value-initialisation
+        out->counts.reset(new (std::nothrow) uint32_t[n_ent]);
+        if (!out->names || !out->counts) return fail(PTW_ENOMEM, "host allocation of batch results failed");
+        int name_bits = 1, q_bits = 1;
+        while (name_bits < 32 && (1ull << name_bits) < g->dg.id_bound) ++name_bits;
+        while ((1ull << q_bits) < nt) ++q_bits;
+        unsigned long long *e_key, *s_key;
+        uint32_t *e_cnt, *s_cnt, *s_name;
+        PTW_CUDA(db.alloc(&e_key, n_ent));
+        PTW_CUDA(db.alloc(&s_key, n_ent));
         PTW_CUDA(db.alloc(&e_cnt, n_ent));
-        PTW_CUDA(db.alloc(&s_name, n_ent));
         PTW_CUDA(db.alloc(&s_cnt, n_ent));
         for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
             const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
             k_tabs_emit<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(d_slots, d_base + t0, d_cap + t0, d_seg + t0,
-                                                                   d_fill + t0, g->dg.int2name, e_name, e_cnt);
+                                                                   d_fill + t0, g->dg.int2name, t0, name_bits,
+                                                                   e_key, e_cnt);
         }
         PTW_CUDA(cudaGetLastError());
+        // one radix sort over (table, name): tables stay in their segments
         PTW_CUDA(cub_call([&](void *t, size_t &b) {
-            return cub::DeviceSegmentedSort::SortPairs(t, b, e_name, s_name, e_cnt, s_cnt, (int64_t)n_ent,
-                                                      (int64_t)nt, d_seg, d_seg + 1, st);
+            return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_ent, 0,
+                                                   name_bits + q_bits, st);
         }, st));
-        PTW_CUDA(cudaMemcpyAsync(h_name.data(), s_name, n_ent * 4, cudaMemcpyDeviceToHost, st));
-        PTW_CUDA(cudaMemcpyAsync(h_cnt.data(), s_cnt, n_ent * 4, cudaMemcpyDeviceToHost, st));
+        s_name = (uint32_t *)e_key;  // reuse the unsorted-key buffer
+        const unsigned kg = (unsigned)std::min<uint64_t>((n_ent + 255) / 256, (uint64_t)g->num_sms * 32);
+        k_key_names<<<std::max(kg, 1u), 256, 0, st>>>(s_key, n_ent, (1ull << name_bits) - 1, s_name);
+        PTW_CUDA(cudaGetLastError());
+        if (timing) {
+            PTW_CUDA(cudaStreamSynchronize(st));
+            t1 = clk();
+        }
+        PTW_CUDA(cudaMemcpyAsync(out->names.get(), s_name, n_ent * 4, cudaMemcpyDeviceToHost, st));
+        PTW_CUDA(cudaMemcpyAsync(out->counts.get(), s_cnt, n_ent * 4, cudaMemcpyDeviceToHost, st));
         PTW_CUDA(cudaStreamSynchronize(st));
+        if (timing) t2 = clk();
     }
-    for (uint32_t i = 0; i < nt; ++i) {
-        names[i]->assign(h_name.begin() + h_seg[i], h_name.begin() + h_seg[i + 1]);
-        counts[i]->assign(h_cnt.begin() + h_seg[i], h_cnt.begin() + h_seg[i + 1]);
-    }
+    if (timing)
+        std::fprintf(stderr, "[ptw] compact %u tables, %llu entries: device %.1f ms, d2h %.1f ms\n", nt,
+                     (unsigned long long)n_ent, 1e3 * (t1 - t0), 1e3 * (t2 - t1));
     return PTW_OK;
 }
 
@@ -292,10 +407,11 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
     if (!b) return fail(PTW_ENOMEM, "host allocation failed");
     b->nq = nq;
     b->queries.assign(h_queries, h_queries + nq);
-    std::vector<std::vector<uint32_t>> names(nq), cnts(nq);
+    std::vector<WaveResult> waves;
     std::vector<uint32_t> overflow;
     const uint64_t thr = cfg->sp >= 1.0 ? (1ull << 32) : (uint64_t)(cfg->sp * 4294967296.0);
     uint64_t moves = 0;
+    float walk_ms = 0;
     PTW_CUDA(cudaEventRecord(g->ev[3], g->stream));
     int rc = PTW_OK;
     // Waves in query order, admitted while their tables fit the budget.
@@ -306,7 +422,7 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
             bytes += all[i].cap * 8;
             wave.push_back(all[i++]);
         }
-        rc = run_wave(g, wave, cfg, thr, names, cnts, overflow, &moves);
+        rc = run_wave(g, wave, cfg, thr, waves, overflow, &moves, &walk_ms);
     }
     // Queries whose table filled run again with 2n slots (they cannot fill).
     std::vector<uint32_t> again;
@@ -315,32 +431,25 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
         WaveQuery w = all[again[k]];
         w.cap = full_table_slots(n);
         uint64_t m2 = 0;
-        rc = run_wave(g, {w}, cfg, thr, names, cnts, overflow, &m2);
+        rc = run_wave(g, {w}, cfg, thr, waves, overflow, &m2, &walk_ms);
         if (rc == PTW_OK && !overflow.empty()) rc = fail(PTW_EFULL, "count table overflow at 2n slots");
     }
+    if (rc == PTW_OK) rc = assemble(b, waves);
     if (rc != PTW_OK) {
         delete b;
         return rc;
     }
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
     PTW_CUDA(cudaEventSynchronize(g->ev[2]));
-    b->offsets.assign(nq + 1, 0);
-    for (uint32_t i = 0; i < nq; ++i) b->offsets[i + 1] = b->offsets[i] + names[i].size();
-    b->names.reserve(b->offsets[nq]);
-    b->counts.reserve(b->offsets[nq]);
     uint64_t walkers = 0;
-    for (uint32_t i = 0; i < nq; ++i) {
-        b->names.insert(b->names.end(), names[i].begin(), names[i].end());
-        b->counts.insert(b->counts.end(), cnts[i].begin(), cnts[i].end());
-        walkers += all[i].budget;
-    }
+    for (uint32_t i = 0; i < nq; ++i) walkers += all[i].budget;
     b->stats.walkers = walkers;
     b->stats.moves = moves;
     b->stats.visits = cfg->app == PTW_APP_VISITS ? walkers + moves : walkers;
     float ms = 0;
     PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[3], g->ev[2]));
     b->stats.total_ms = ms;
-    b->stats.kernel_ms = ms;
+    b->stats.kernel_ms = walk_ms;  // walker kernels only; total_ms includes compaction and copies
     *out = b;
     return PTW_OK;
 }
@@ -357,9 +466,20 @@ extern "C" int ptw_batch_info(const ptw_batch *b, uint32_t *nq, uint64_t *entrie
 extern "C" int ptw_batch_export(const ptw_batch *b, uint64_t *h_offsets, uint32_t *h_names, uint32_t *h_counts)
 {
     if (!b) return fail(PTW_EINVAL, "null batch");
+    const uint64_t n = b->offsets.empty() ? 0 : b->offsets.back();
     if (h_offsets) std::memcpy(h_offsets, b->offsets.data(), b->offsets.size() * 8);
-    if (h_names && !b->names.empty()) std::memcpy(h_names, b->names.data(), b->names.size() * 4);
-    if (h_counts && !b->counts.empty()) std::memcpy(h_counts, b->counts.data(), b->counts.size() * 4);
+    if (h_names && n) std::memcpy(h_names, b->names.get(), n * 4);
+    if (h_counts && n) std::memcpy(h_counts, b->counts.get(), n * 4);
+    return PTW_OK;
+}
+
+extern "C" int ptw_batch_view(const ptw_batch *b, const uint64_t **offsets, const uint32_t **names,
+                              const uint32_t **counts)
+{
+    if (!b) return fail(PTW_EINVAL, "null batch");
+    if (offsets) *offsets = b->offsets.data();
+    if (names) *names = b->names.get();
+    if (counts) *counts = b->counts.get();
     return PTW_OK;
 }
 

@@ -49,39 +49,46 @@ __device__ __forceinline__ void tab_add(unsigned long long *slots, uint32_t mask
     atomicOr(flag, 1u);
 }
 
-// Query table of one launch: entry q runs walkers q_j0[q] .. q_j0[q] +
-// (q_off[q+1] - q_off[q]) - 1 of query q_qid[q] from source q_src[q], counting
-// into the table at slots + q_tab[q] (q_mask[q] + 1 slots).
+// Work of one launch: descriptor d runs walker ranks desc[d].y ..
+// desc[d].y + desc[d].z - 1 of query entry q = desc[d].x, whose walker ids
+// are (q_qid[q] << 32) + rank, source q_src[q], count table at slots +
+// q_tab[q] (q_mask[q] + 1 slots).  Descriptors are ordered round-robin over
+// the queries (the host builds them so), and a warp takes one descriptor at
+// a time, so the walkers in flight belong to many queries at once and no
+// single query's hot slots serialise the whole GPU.
 struct BatchArgs {
     const uint2 *__restrict__ adj;
     const uint32_t *__restrict__ col;
-    const unsigned long long *__restrict__ q_off;  // [nq + 1]
-    const unsigned long long *__restrict__ q_j0;   // [nq] or null (= 0)
+    const uint3 *__restrict__ desc;  // [ndesc] {entry, first rank, count}
     const uint32_t *__restrict__ q_src;
     const uint32_t *__restrict__ q_qid;
     const unsigned long long *__restrict__ q_tab;
     const uint32_t *__restrict__ q_mask;
     uint32_t *q_flag;
     unsigned long long *slots;
-    unsigned long long *ctrl;  // [0] cursor, [1] moves
-    uint64_t total;
+    unsigned long long *ctrl;  // [0] descriptor cursor, [1] moves
+    uint32_t ndesc;
     uint64_t thr;
-    uint32_t nq, key0, key1, max_moves, chunk;
+    uint32_t key0, key1, max_moves;
     int app;
 };
 
-__device__ __forceinline__ uint32_t find_entry(const unsigned long long *off, uint32_t nq, uint64_t g)
-{
-    uint32_t lo = 0, hi = nq;  // off[lo] <= g < off[hi]
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (off[mid] <= g) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
+// Walker ranks per descriptor (host side splits queries into chunks of it).
+constexpr uint32_t kDescWalkers = 256;
 
 constexpr int kBatchIlp = 2;
+
+// Counts one visit of key v in query entry q's table, aggregated over the
+// lanes of the warp that visit the same (query, vertex) now.
+__device__ __forceinline__ void visit_agg(unsigned mask_active, bool on, uint32_t q, uint32_t v,
+                                          unsigned long long *tab, uint32_t tmask, uint32_t *flag, uint32_t lane)
+{
+    const unsigned m = __ballot_sync(mask_active, on);
+    if (!on) return;
+    const unsigned long long key = ((unsigned long long)q << 32) | v;
+    const unsigned grp = __match_any_sync(m, key);
+    if ((grp & ((1u << lane) - 1u)) == 0) tab_add(tab, tmask, v, __popc(grp), flag);
+}
 
 __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
 {
@@ -96,56 +103,56 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
         q[k] = v[k] = step[k] = j[k] = qid[k] = mask[k] = 0;
         tab[k] = nullptr;
     }
-    uint64_t next = 0, end = 0;
+    // Warp-uniform current descriptor: entry dq, ranks [dnext, dend).
+    uint32_t dq = 0, dnext = 0, dend = 0;
     bool exhausted = false;
     unsigned long long moves = 0;
     for (;;) {
 #pragma unroll
         for (int k = 0; k < kBatchIlp; ++k) {
             const unsigned need = __ballot_sync(kBFull, !act[k]);
-            if (need == 0 || exhausted) continue;
-            const uint32_t n_need = __popc(need);
-            const uint32_t rank = __popc(need & lt_mask);
-            uint64_t my = ~0ull;
-            const uint64_t avail = end - next;
-            const uint32_t took = (uint32_t)(n_need < avail ? n_need : avail);
-            if (!act[k] && rank < took) my = next + rank;
-            next += took;
-            if (took < n_need) {
-                unsigned long long base = 0;
-                if (lane == 0) base = atomicAdd(&a.ctrl[0], (unsigned long long)a.chunk);
-                base = __shfl_sync(kBFull, base, 0);
-                if (base >= a.total) {
-                    exhausted = true;
-                    next = end = a.total;
-                } else {
-                    next = base;
-                    end = base + a.chunk < a.total ? base + a.chunk : a.total;
-                    const uint64_t rem = end - next;
-                    const uint32_t take2 = (uint32_t)((n_need - took) < rem ? (n_need - took) : rem);
-                    if (!act[k] && rank >= took && rank - took < take2) my = next + (rank - took);
-                    next += take2;
+            bool got = false;
+            if (need != 0 && !exhausted) {
+                uint32_t n_need = __popc(need);
+                uint32_t rank = __popc(need & lt_mask);
+                uint32_t done_before = 0;  // lanes served from earlier descriptors
+                // Serve the needing lanes from the current descriptor, then
+                // from newly taken ones, until all are served or work ends.
+                while (n_need > done_before) {
+                    const uint32_t avail = dend - dnext;
+                    const uint32_t take = n_need - done_before < avail ? n_need - done_before : avail;
+                    if (!act[k] && rank >= done_before && rank < done_before + take) {
+                        q[k] = dq;
+                        j[k] = dnext + (rank - done_before);
+                        got = true;
+                    }
+                    dnext += take;
+                    done_before += take;
+                    if (done_before == n_need) break;
+                    unsigned long long d = 0;
+                    if (lane == 0) d = atomicAdd(&a.ctrl[0], 1ull);
+                    d = __shfl_sync(kBFull, d, 0);
+                    if (d >= a.ndesc) {
+                        exhausted = true;
+                        break;
+                    }
+                    const uint3 ds = a.desc[d];
+                    dq = ds.x;
+                    dnext = ds.y;
+                    dend = ds.y + ds.z;
                 }
             }
-            const bool got = my != ~0ull;
             if (got) {
-                const uint32_t qq = find_entry(a.q_off, a.nq, my);
-                q[k] = qq;
-                j[k] = (uint32_t)(my - a.q_off[qq] + (a.q_j0 ? a.q_j0[qq] : 0ull));
-                qid[k] = a.q_qid[qq];
-                v[k] = a.q_src[qq];
-                tab[k] = a.slots + a.q_tab[qq];
-                mask[k] = a.q_mask[qq];
+                qid[k] = a.q_qid[q[k]];
+                v[k] = a.q_src[q[k]];
+                tab[k] = a.slots + a.q_tab[q[k]];
+                mask[k] = a.q_mask[q[k]];
                 step[k] = 0;
                 act[k] = true;
             }
             if (a.app == PTW_APP_VISITS) {
                 // Start visits: one table update per (warp, query) group.
-                const unsigned gm = __ballot_sync(kBFull, got);
-                if (got) {
-                    const unsigned grp = __match_any_sync(gm, q[k]);
-                    if ((grp & lt_mask) == 0) tab_add(tab[k], mask[k], v[k], __popc(grp), &a.q_flag[q[k]]);
-                }
+                visit_agg(kBFull, got, q[k], v[k], tab[k], mask[k], &a.q_flag[q[k]], lane);
             }
         }
         bool any = false;
@@ -167,21 +174,17 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
             if (act[k] && rec[k].y != 0) nb[k] = __ldg(&a.col[rec[k].x + __umulhi(r[k].x, rec[k].y)]);
 #pragma unroll
         for (int k = 0; k < kBatchIlp; ++k) {
-            if (!act[k]) continue;
-            bool done;
-            if (rec[k].y == 0) {
-                done = true;
-            } else {
+            // every lane runs the aggregation calls (warp-collective)
+            const bool moved = act[k] && rec[k].y != 0;
+            if (moved) {
                 v[k] = nb[k];
                 ++step[k];
                 ++moves;
-                if (a.app == PTW_APP_VISITS) tab_add(tab[k], mask[k], v[k], 1u, &a.q_flag[q[k]]);
-                done = (uint64_t)r[k].y < a.thr || (a.max_moves && step[k] >= a.max_moves);
             }
-            if (done) {
-                if (a.app == PTW_APP_ENDPOINT) tab_add(tab[k], mask[k], v[k], 1u, &a.q_flag[q[k]]);
-                act[k] = false;
-            }
+            if (a.app == PTW_APP_VISITS) visit_agg(kBFull, moved, q[k], v[k], tab[k], mask[k], &a.q_flag[q[k]], lane);
+            const bool done = act[k] && (!moved || (uint64_t)r[k].y < a.thr || (a.max_moves && step[k] >= a.max_moves));
+            if (a.app == PTW_APP_ENDPOINT) visit_agg(kBFull, done, q[k], v[k], tab[k], mask[k], &a.q_flag[q[k]], lane);
+            if (done) act[k] = false;
         }
     }
 #pragma unroll
@@ -204,9 +207,13 @@ __global__ void k_tabs_count(const unsigned long long *slots, const unsigned lon
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(&cnt[i], (unsigned long long)c);
 }
 
+// Writes each occupied slot of table i (= t_index0 + blockIdx.y) into the
+// table's segment as key (i << name_bits | name) and count, so one radix
+// sort of the keys orders every table's entries by name in place.
 __global__ void k_tabs_emit(const unsigned long long *slots, const unsigned long long *t_base,
                             const uint32_t *t_cap, const unsigned long long *seg_off, unsigned long long *fill,
-                            const uint32_t *int2name, uint32_t *out_name, uint32_t *out_cnt)
+                            const uint32_t *int2name, uint32_t t_index0, int name_bits,
+                            unsigned long long *out_key, uint32_t *out_cnt)
 {
     const uint32_t i = blockIdx.y;
     const unsigned long long *s = slots + t_base[i];
@@ -223,10 +230,16 @@ __global__ void k_tabs_emit(const unsigned long long *slots, const unsigned long
         base = __shfl_sync(kBFull, base, 0);
         if (w) {
             const uint64_t pos = seg_off[i] + base + __popc(om & ((1u << lane) - 1u));
-            out_name[pos] = int2name[(uint32_t)(w >> 32) - 1];
+            out_key[pos] = ((unsigned long long)(t_index0 + i) << name_bits) | int2name[(uint32_t)(w >> 32) - 1];
             out_cnt[pos] = (uint32_t)(w & 0xFFFFFFFFull);
         }
     }
+}
+
+__global__ void k_key_names(const unsigned long long *key, uint64_t n, unsigned long long mask, uint32_t *name)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        name[i] = (uint32_t)(key[i] & mask);
 }
 
 }  // namespace

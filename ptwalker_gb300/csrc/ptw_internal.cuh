@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -151,13 +152,23 @@ int check_tune(const ptw_tune &t);
 // The query table a batch was run with (batch.cu).
 const ptw_query *batch_queries(const ptw_batch *b);
 
+// (name, count) lists of nt tables in host memory: table i owns entries
+// [seg[i], seg[i+1]), sorted by name.
+struct Compacted {
+    uint64_t n = 0;
+    std::vector<uint64_t> seg;
+    std::unique_ptr<uint32_t[]> names, counts;
+};
 // Compacts nt count tables (slots [h_base[i], h_base[i] + h_cap[i]) of
-// d_slots) into (name, count) lists sorted by name (batch.cu).
+// d_slots) into *out (batch.cu).
 int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned long long *h_base,
-                   const uint32_t *h_cap, uint32_t nt, std::vector<uint32_t> **names,
-                   std::vector<uint32_t> **counts);
+                   const uint32_t *h_cap, uint32_t nt, Compacted *out);
 // Count-table size for a query of `budget` walkers, and the size that cannot fill.
 uint64_t table_slots(double sp, uint32_t max_moves, int32_t app, double factor, uint64_t budget, uint32_t n);
 uint64_t full_table_slots(uint32_t n);
+// Splits [j0[i], j0[i] + count[i]) of every query entry i into walker
+// descriptors {entry, first rank, count}, ordered round-robin over entries.
+void interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<uint64_t> &count,
+                            std::vector<uint3> &desc);
 
 }  // namespace ptw

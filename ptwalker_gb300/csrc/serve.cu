@@ -109,6 +109,8 @@ struct ptw_server {
     ptw::Buddy buddy;
     unsigned long long *arena = nullptr;
     uint32_t S = 0;                  // plan capacity (max_active)
+    uint32_t D = 0;                  // descriptor capacity per tick
+    std::vector<uint64_t> take;      // walker ranks given to each active query this tick
     void *d_plan = nullptr, *h_plan = nullptr;
     size_t plan_bytes = 0, ret_off = 0, ret_bytes = 0;
     std::deque<ptw::Pending> pending;
@@ -131,22 +133,21 @@ double now_s(const ptw_server *s)
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - s->t0).count();
 }
 
-// Plan block layout (identical on host and device):
-//   off[S+1] u64 | j0[S] u64 | tab[S] u64 | src[S] u32 | qid[S] u32 | mask[S] u32 |
-//   flag[S] u32 | ctrl[2] u64
+// Plan block layout (identical on host and device), S query slots and D
+// walker descriptors:
+//   tab[S] u64 | src[S] u32 | qid[S] u32 | mask[S] u32 | desc[D] uint3 |
+//   flag[S] u32 | (pad to 16) ctrl[2] u64
+// The tail from flag on is what a tick copies back.
 struct PlanView {
-    unsigned long long *off, *j0, *tab, *ctrl;
+    unsigned long long *tab, *ctrl;
     uint32_t *src, *qid, *mask, *flag;
+    uint3 *desc;
 };
 
-PlanView view(void *base, uint32_t S)
+PlanView view(void *base, uint32_t S, uint32_t D)
 {
     PlanView v;
     char *p = (char *)base;
-    v.off = (unsigned long long *)p;
-    p += 8ull * (S + 1);
-    v.j0 = (unsigned long long *)p;
-    p += 8ull * S;
     v.tab = (unsigned long long *)p;
     p += 8ull * S;
     v.src = (uint32_t *)p;
@@ -155,6 +156,8 @@ PlanView view(void *base, uint32_t S)
     p += 4ull * S;
     v.mask = (uint32_t *)p;
     p += 4ull * S;
+    v.desc = (uint3 *)p;
+    p += sizeof(uint3) * (size_t)D;
     v.flag = (uint32_t *)p;
     p += 4ull * S;
     p = (char *)(((uintptr_t)p + 15) & ~(uintptr_t)15);
@@ -162,9 +165,9 @@ PlanView view(void *base, uint32_t S)
     return v;
 }
 
-size_t plan_size(uint32_t S)
+size_t plan_size(uint32_t S, uint32_t D)
 {
-    size_t b = 8ull * (S + 1) + 16ull * S + 8ull * S + 16ull * S;
+    size_t b = 20ull * S + sizeof(uint3) * (size_t)D + 4ull * S;
     return ((b + 15) & ~(size_t)15) + 16;
 }
 
@@ -205,15 +208,17 @@ int collect(ptw_server *s, const std::vector<size_t> &fin)
     std::vector<unsigned long long> base(fin.size());
     std::vector<uint32_t> cap(fin.size());
     std::vector<Done> out(fin.size());
-    std::vector<std::vector<uint32_t> *> pn(fin.size()), pc(fin.size());
     for (size_t i = 0; i < fin.size(); ++i) {
         base[i] = s->active[fin[i]].off;
         cap[i] = (uint32_t)s->active[fin[i]].cap;
-        pn[i] = &out[i].names;
-        pc[i] = &out[i].counts;
     }
-    int rc = compact_tables(s->g, s->arena, base.data(), cap.data(), (uint32_t)fin.size(), pn.data(), pc.data());
+    Compacted c;
+    int rc = compact_tables(s->g, s->arena, base.data(), cap.data(), (uint32_t)fin.size(), &c);
     if (rc) return rc;
+    for (size_t i = 0; i < fin.size(); ++i) {
+        out[i].names.assign(c.names.get() + c.seg[i], c.names.get() + c.seg[i + 1]);
+        out[i].counts.assign(c.counts.get() + c.seg[i], c.counts.get() + c.seg[i + 1]);
+    }
     const double t = now_s(s);
     for (size_t i = 0; i < fin.size(); ++i) {
         const Active &a = s->active[fin[i]];
@@ -266,22 +271,23 @@ extern "C" int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server
     s->buddy.init(bytes / 8, 8);
     int rc = PTW_OK;
     cudaError_t e = cudaMalloc(&s->arena, std::max<uint64_t>(s->buddy.capacity(), 1) * 8);
-    s->plan_bytes = plan_size(s->S);
+    // every query's share splits into at most share/kDescWalkers + 1 descriptors
+    s->D = (uint32_t)std::min<uint64_t>(0xFFFFFFFFull, s->cfg.tick_walkers / kDescWalkers + 2ull * s->S + 1);
+    s->plan_bytes = plan_size(s->S, s->D);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_plan, s->plan_bytes);
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_plan, s->plan_bytes);
     if (e != cudaSuccess) {
         rc = cuda_fail(e, "server allocation");
     } else {
         std::memset(s->h_plan, 0, s->plan_bytes);
-        PlanView dv = view(s->d_plan, s->S);
-        PlanView hv = view(s->h_plan, s->S);
+        PlanView dv = view(s->d_plan, s->S, s->D);
+        PlanView hv = view(s->h_plan, s->S, s->D);
         s->ret_off = (char *)hv.flag - (char *)s->h_plan;
         s->ret_bytes = s->plan_bytes - s->ret_off;
         BatchArgs &a = s->args;
         a.adj = g->dg.adj;
         a.col = g->dg.col;
-        a.q_off = dv.off;
-        a.q_j0 = dv.j0;
+        a.desc = dv.desc;
         a.q_src = dv.src;
         a.q_qid = dv.qid;
         a.q_tab = dv.tab;
@@ -289,13 +295,11 @@ extern "C" int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server
         a.q_flag = dv.flag;
         a.slots = s->arena;
         a.ctrl = dv.ctrl;
-        a.total = 0;
+        a.ndesc = 0;
         a.thr = s->thr;
-        a.nq = 1;
         a.key0 = (uint32_t)cfg->seed;
         a.key1 = (uint32_t)(cfg->seed >> 32);
         a.max_moves = cfg->max_moves;
-        a.chunk = 256;
         a.app = cfg->app;
         int per_sm = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, 256, 0);
@@ -360,24 +364,37 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
     uint32_t nd = 0;
     if (!s->active.empty()) {
         // 2. plan: a fair share of the tick's walkers per active query
-        PlanView hv = view(s->h_plan, s->S);
+        PlanView hv = view(s->h_plan, s->S, s->D);
         const uint32_t na = (uint32_t)s->active.size();
-        const uint64_t share = std::max<uint64_t>(1024, s->cfg.tick_walkers / na);
-        hv.off[0] = 0;
+        // a fair share per query, rounded to whole descriptors so the plan
+        // never holds more than D of them
+        uint64_t share = std::max<uint64_t>(1024, s->cfg.tick_walkers / na);
+        share = (share + kDescWalkers - 1) / kDescWalkers * kDescWalkers;
+        std::vector<uint64_t> j0(na);
+        s->take.assign(na, 0);
         for (uint32_t i = 0; i < na; ++i) {
             const Active &a = s->active[i];
-            const uint64_t take = std::min<uint64_t>(share, a.p.q.budget - a.started);
-            hv.off[i + 1] = hv.off[i] + take;
-            hv.j0[i] = a.started;
+            s->take[i] = std::min<uint64_t>(share, a.p.q.budget - a.started);
+            j0[i] = a.started;
             hv.tab[i] = a.off;
             hv.src[i] = a.p.src;
             hv.qid[i] = a.p.q.query_id;
             hv.mask[i] = (uint32_t)(a.cap - 1);
             hv.flag[i] = 0;
         }
+        std::vector<uint3> desc;
+        interleave_descriptors(j0, s->take, desc);
+        if (desc.size() > s->D) {
+            // more active queries than the plan holds descriptors for: keep
+            // the first D (whole queries stay consistent: trim their takes)
+            desc.resize(s->D);
+            std::vector<uint64_t> got(na, 0);
+            for (const uint3 &d : desc) got[d.x] += d.z;
+            s->take = got;
+        }
+        std::memcpy(hv.desc, desc.data(), desc.size() * sizeof(uint3));
         hv.ctrl[0] = hv.ctrl[1] = 0;
-        s->args.nq = na;
-        s->args.total = hv.off[na];
+        s->args.ndesc = (uint32_t)desc.size();
         // 3. the tick
         if (s->exec) {
             void *kp[] = {&s->args};
@@ -409,7 +426,7 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
                 drop[i] = 1;
                 continue;
             }
-            a.started += hv.off[i + 1] - hv.off[i];
+            a.started += s->take[i];
             if (a.started == a.p.q.budget) {
                 fin.push_back(i);
                 drop[i] = 1;
