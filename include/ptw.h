@@ -99,6 +99,10 @@ typedef struct ptw_tune {
     int32_t paths_ilp;     /* DeepWalk: groups of 32 walkers per warp, 1, 2 or 4 */
     int32_t cache_hints;   /* 1 = L2 evict_last for row records and counters, evict_first
                               for the column array; 0 = default L2 policy */
+    int32_t paths_named;   /* DeepWalk: 1 = keep a {neighbour, name} column copy (8 bytes per
+                              CSR entry, built on the first path walk) so a move needs no
+                              separate name lookup; 0 = look names up per move */
+    int32_t reserved;
 } ptw_tune;
 
 const char *ptw_last_error(void);

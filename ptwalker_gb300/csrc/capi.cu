@@ -636,9 +636,13 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
         if (rc) return rc;
         float best_ms = 1e30f;
         bt.paths_ilp = 2;
-        for (int G : {1, 2, 4}) {
+        bt.paths_named = saved.paths_named;
+        for (int cfg_i = 0; cfg_i < 6; ++cfg_i) {
+            const int G = cfg_i % 3 == 0 ? 1 : cfg_i % 3 == 1 ? 2 : 4;
+            const int named = cfg_i < 3 ? 1 : 0;
             g->tune = bt;
             g->tune.paths_ilp = G;
+            g->tune.paths_named = named;
             float tot = 0;
             for (int rep = 0; rep < 3; ++rep) {
                 PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
@@ -653,6 +657,7 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
             if (tot < best_ms) {
                 best_ms = tot;
                 bt.paths_ilp = G;
+                bt.paths_named = named;
             }
         }
     }

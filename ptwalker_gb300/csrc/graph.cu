@@ -292,6 +292,8 @@ int graph_init_handle(ptw_graph *g)
     g->tune.blocks_per_sm = 0;
     g->tune.min_blocks = 0;
     g->tune.paths_ilp = 2;
+    g->tune.cache_hints = 1;
+    g->tune.paths_named = 1;
     return PTW_OK;
 }
 
@@ -304,6 +306,7 @@ void graph_release(ptw_graph *g)
     cudaFree(g->dg.int2name);
     cudaFree(g->dg.idx2int);
     cudaFree(g->dg.int2idx);
+    cudaFree(g->dg.col_named);
     cudaFree(g->sc.counts);
     cudaFree(g->sc.ctrl);
     cudaFree(g->sc.sources);

@@ -90,6 +90,7 @@ struct DeviceGraph {
     uint32_t *int2name = nullptr; // [n]
     uint32_t *idx2int = nullptr;  // [n] canonical index (name rank) -> internal
     uint32_t *int2idx = nullptr;  // [n] internal -> canonical index
+    uint2 *col_named = nullptr;   // [m] {neighbour internal id, its name}; built on first path walk
 };
 
 // Scratch owned by a graph handle and reused by every call.

@@ -215,6 +215,7 @@ __global__ void __launch_bounds__(512, 2) k_walk_b2(const WalkArgs a)
 struct PathArgs {
     const uint2 *__restrict__ adj;
     const uint32_t *__restrict__ col;
+    const uint2 *__restrict__ col_named;  // {internal id, name} per column entry
     const uint32_t *__restrict__ start_map;
     const uint32_t *__restrict__ sources;
     const uint32_t *__restrict__ int2name;
@@ -230,8 +231,10 @@ struct PathArgs {
 constexpr int kPathWarps = 4;  // warps per block
 
 // G groups of 32 consecutive walkers per warp (one walker of each group per
-// lane), stepped together so a lane has G gathers in flight.
-template <int G>
+// lane), stepped together so a lane has G gathers in flight.  NAMED reads
+// {internal id, name} pairs from col_named, so a move costs two random reads
+// (row record, column pair) instead of three (plus the name lookup).
+template <int G, bool NAMED>
 __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
 {
     // C path positions are staged per walker before a flush; rows are padded
@@ -296,17 +299,36 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
                 if (!dead[g])
                     r[g] = philox(make_uint4((uint32_t)wid[g], (uint32_t)(wid[g] >> 32), p - 1, PTW_TAG_WALK),
                                   a.key0, a.key1);
+            uint32_t nm[G];
 #pragma unroll
             for (int g = 0; g < G; ++g) {
                 if (!dead[g]) {
-                    if (rec[g].y == 0) dead[g] = true;
-                    else v[g] = ld_hint_u32(&a.col[rec[g].x + __umulhi(r[g].x, rec[g].y)], pol_stream);
+                    if (rec[g].y == 0) {
+                        dead[g] = true;
+                    } else if (NAMED) {
+                        const uint2 cn = ld_hint_u2(&a.col_named[rec[g].x + __umulhi(r[g].x, rec[g].y)], pol_stream);
+                        v[g] = cn.x;
+                        nm[g] = cn.y;
+                    } else {
+                        v[g] = ld_hint_u32(&a.col[rec[g].x + __umulhi(r[g].x, rec[g].y)], pol_stream);
+                    }
                 }
             }
 #pragma unroll
-            for (int g = 0; g < G; ++g)
-                stage[wib][g][lane][p - c0] = dead[g] ? -1 : (int32_t)ld_hint_u32(&a.int2name[v[g]], pol_keep);
+            for (int g = 0; g < G; ++g) {
+                int32_t out = -1;
+                if (!dead[g]) out = NAMED ? (int32_t)nm[g] : (int32_t)ld_hint_u32(&a.int2name[v[g]], pol_keep);
+                stage[wib][g][lane][p - c0] = out;
+            }
         }
+    }
+}
+
+__global__ void k_name_columns(const uint32_t *col, const uint32_t *int2name, uint64_t m, uint2 *col_named)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = col[e];
+        col_named[e] = make_uint2(c, int2name[c]);
     }
 }
 
@@ -385,6 +407,7 @@ int check_tune(const ptw_tune &t)
     if (t.paths_ilp != 0 && t.paths_ilp != 1 && t.paths_ilp != 2 && t.paths_ilp != 4)
         return fail(PTW_EINVAL, "tune.paths_ilp must be 1, 2 or 4 (0 = default)");
     if (t.cache_hints != 0 && t.cache_hints != 1) return fail(PTW_EINVAL, "tune.cache_hints must be 0 or 1");
+    if (t.paths_named != 0 && t.paths_named != 1) return fail(PTW_EINVAL, "tune.paths_named must be 0 or 1");
     return PTW_OK;
 }
 
@@ -456,9 +479,31 @@ int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uin
     a.n_sources = n_sources;
     a.start_mode = start_mode;
     a.hints = g->tune.cache_hints;
-    const int G =g->tune.paths_ilp == 1 || g->tune.paths_ilp == 4 ? g->tune.paths_ilp : 2;
-    const void *fn = G == 1 ? (const void *)k_paths<1> : G == 4 ? (const void *)k_paths<4>
-                                                                : (const void *)k_paths<2>;
+    // Name-paired columns: built once on the first path walk (8 bytes per
+    // CSR entry); without them the kernel looks names up per move.
+    bool named = g->tune.paths_named != 0;
+    if (named && !g->dg.col_named) {
+        uint2 *cn = nullptr;
+        if (cudaMalloc(&cn, std::max<uint64_t>(dg.m, 1) * sizeof(uint2)) == cudaSuccess) {
+            const unsigned grid = (unsigned)std::min<uint64_t>((dg.m + 255) / 256, (uint64_t)g->num_sms * 64);
+            k_name_columns<<<std::max(grid, 1u), 256, 0, g->stream>>>(dg.col, dg.int2name, dg.m, cn);
+            PTW_CUDA(cudaGetLastError());
+            g->dg.col_named = cn;
+            g->device_bytes += dg.m * sizeof(uint2);
+        } else {
+            cudaGetLastError();  // no room: walk with per-move name lookups
+            named = false;
+        }
+    }
+    a.col_named = g->dg.col_named;
+    const int G = g->tune.paths_ilp == 1 || g->tune.paths_ilp == 4 ? g->tune.paths_ilp : 2;
+    const void *fn;
+    if (named)
+        fn = G == 1 ? (const void *)k_paths<1, true> : G == 4 ? (const void *)k_paths<4, true>
+                                                              : (const void *)k_paths<2, true>;
+    else
+        fn = G == 1 ? (const void *)k_paths<1, false> : G == 4 ? (const void *)k_paths<4, false>
+                                                               : (const void *)k_paths<2, false>;
     int per_sm = 0;
     PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPathWarps * 32, 0));
     per_sm = std::max(per_sm, 1);

@@ -110,13 +110,15 @@ def test_deepwalk_paths_bit_exact(gpu, G16, s16_canon, L, W, start):
     assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("paths_ilp,hints", [(1, 0), (2, 0), (4, 0), (2, 1), (4, 1)])
-def test_deepwalk_groups_per_warp(gpu, G16, s16_canon, paths_ilp, hints):
+@pytest.mark.parametrize("paths_ilp,hints,named", [(1, 0, 0), (2, 0, 0), (4, 0, 1), (2, 1, 1), (4, 1, 0),
+                                                   (1, 1, 1)])
+def test_deepwalk_groups_per_warp(gpu, G16, s16_canon, paths_ilp, hints, named):
     saved = G16.tune
     try:
         t = G16.tune
         t.paths_ilp = paths_ilp
         t.cache_hints = hints
+        t.paths_named = named
         G16.tune = t
         for W, L in ((G16.n, 40), (4096 + 33, 7), (65, 33)):
             got = gpu.deepwalk(G16, W, L, 17)
