@@ -61,6 +61,11 @@ def parse():
     p.add_argument("--serve-n", type=int, default=8_400_000)
     p.add_argument("--serve-rates", default="1000,10000,50000")
     p.add_argument("--serve-queries", type=int, default=3000)
+    p.add_argument("--serve-budget-max", type=float, default=1e6)
+    p.add_argument("--serve-tick", type=int, default=1 << 21, help="walkers per serving tick")
+    p.add_argument("--serve-top-k", type=int, default=1000,
+                   help="entries returned per query (largest counts); 0 = full vectors.  With k > 0 one "
+                        "extra run at the second rate returns full vectors")
     return p.parse_args()
 
 
@@ -209,6 +214,24 @@ def degree_sources(G, n, seed):
     return names[col[e]]
 
 
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_walk_dram_bytes_rmat-s24.md")
+
+
+def traffic_per_move(scale):
+    """DRAM bytes per move of the walk kernel from the committed ncu summary
+    (its line `dram_bytes_per_move: X`), for the scale it was captured at."""
+    if scale != 24 or not os.path.exists(TRAFFIC_PROFILE):
+        return None
+    for ln in open(TRAFFIC_PROFILE):
+        if ln.startswith("dram_bytes_per_move:"):
+            return float(ln.split(":", 1)[1])
+    return None
+
+
+def per_move_src(scale):
+    return "ncu dram__bytes_read.sum + dram__bytes_write.sum per move, %s" % os.path.relpath(TRAFFIC_PROFILE, ROOT)
+
+
 def loguniform_budgets(n, lo, hi, seed):
     import numpy as np
     rng = np.random.default_rng(seed)
@@ -244,19 +267,32 @@ def bench_batch(args, ptw):
 
 def bench_serve(args, ptw):
     """Config: Chung-Lu power-law graph (8.4M vertices, exponent 2.1, mean
-    degree 32), Poisson arrivals at each rate, random sources, budgets
-    log-uniform in [1e3, 1e5] (fixed plain budgets), sp 0.2."""
+    degree 32), Poisson arrivals at each rate, random sources, fixed budgets
+    log-uniform in [1e3, serve_budget_max], sp 0.2.  Each rate line carries
+    the server's own counters: ticks, walk moves, and where the host time of
+    the steps went (device time of the ticks, result collection)."""
     import numpy as np
     G = ptw.Graph.chung_lu(args.serve_n, 2.1, 32.0, seed=1)
     rng = np.random.default_rng(4)
     out = {"graph": "chung-lu n=%d gamma=2.1 mean_degree=32" % args.serve_n, "vertices": G.n, "edges": G.m,
-           "rates": []}
-    for k, rate in enumerate(float(r) for r in args.serve_rates.split(",")):
+           "budgets": "log-uniform [1e3, %.0e]" % args.serve_budget_max, "sp": 0.2,
+           "tick_walkers": args.serve_tick, "rates": []}
+    out["top_k"] = args.serve_top_k
+    runs = [(float(r), args.serve_top_k) for r in args.serve_rates.split(",")]
+    if args.serve_top_k:
+        runs.append((float(args.serve_rates.split(",")[1 if "," in args.serve_rates else 0]), 0))
+    for k, (rate, top_k) in enumerate(runs):
         src = rng.integers(0, G.n, args.serve_queries)
-        bud = loguniform_budgets(args.serve_queries, 1e3, 1e5, 10 + k)
-        with ptw.Server(G, sp=0.2, seed=3, tick_walkers=1 << 21, use_graph=True) as srv:
+        bud = loguniform_budgets(args.serve_queries, 1e3, args.serve_budget_max, 10 + k)
+        with ptw.Server(G, sp=0.2, seed=3, tick_walkers=args.serve_tick, use_graph=True, top_k=top_k) as srv:
             r = ptw.open_loop(srv, src, bud, rate=rate, seed=k, query_id0=k << 20)
-        out["rates"].append({kk: r[kk] for kk in ("rate", "n", "qps", "p50_ms", "p99_ms", "mean_ms")})
+            st = srv.stats()
+        line = {kk: r[kk] for kk in ("rate", "n", "qps", "p50_ms", "p99_ms", "mean_ms")}
+        line["top_k"] = top_k
+        line["steps_per_s"] = st["moves"] / r["span_s"]
+        line["server"] = {kk: st[kk] for kk in ("ticks", "moves", "walkers", "entries", "retries", "step_ms",
+                                                 "device_ms", "collect_ms")}
+        out["rates"].append(line)
     G.close()
     return out
 
@@ -428,6 +464,22 @@ def run_ours(args):
                     "path_bytes": 4 * n * L}
         del paths
 
+    # DRAM bytes per walk launch: the ncu capture's bytes per move at this
+    # workload (committed summary) times this run's moves per launch.
+    traffic, traffic_src = None, None
+    per_move = traffic_per_move(args.scale)
+    if per_move:
+        traffic = per_move * sum(moves) / len(moves)
+        traffic_src = per_move_src(args.scale)
+    # Random-gather ceiling measured on this GPU: a move is one dependent
+    # random gather into the column array (2 GB > L2), so moves/s over this
+    # rate is the kernel's share of what random access can deliver.
+    gather = None
+    if rank == 0:
+        g_rate = ptw.probe_gather(2 << 30, 8)
+        gather = {"loads_per_s": g_rate, "array_bytes": 2 << 30,
+                  "moves_per_s_over_loads_per_s": value / world / g_rate}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         names, row_ptr, col = G.export_csr()
@@ -446,8 +498,10 @@ def run_ours(args):
         "config": config(args, world),
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": traffic,
+                     "traffic_source": traffic_src,
                      "peak_kind": peak_kind,
+                     "gather_peak": gather,
                      "bytes_per_launch": sum(bytes_per_launch) / len(bytes_per_launch),
                      "launch_ms": launch_ms, "walk_kernel_ms": sum(kern_ms) / len(kern_ms)},
         "cpu_baseline": cpu,

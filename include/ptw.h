@@ -119,6 +119,17 @@ int ptw_graph_load(const char *path, int32_t fmt, int32_t as_undirected, ptw_gra
 int ptw_graph_from_edges(const uint32_t *h_src, const uint32_t *h_dst, uint64_t m,
                          int32_t as_undirected, ptw_graph **out);
 
+/* Same from a CSR, the inverse of ptw_graph_export_csr: row i of the n rows
+ * is vertex h_names[i] (vertex i when h_names is NULL) and lists its out-
+ * neighbours as row indices h_col[h_row_ptr[i] .. h_row_ptr[i+1]).  Replaces
+ * the CSR half of Graph::load (graph.hpp:715-769).  Duplicates and
+ * self-loops are kept; a row with no entries whose vertex is no one's
+ * neighbour is not a vertex of the graph, as in an edge list.  PTW_EINVAL
+ * for row_ptr[0] != 0, a decreasing row_ptr, a column index >= n, repeated
+ * names or no entries. */
+int ptw_graph_from_csr(const uint64_t *h_row_ptr /*[n+1]*/, const uint32_t *h_col /*[row_ptr[n]]*/,
+                       uint32_t n, const uint32_t *h_names /*[n] or NULL*/, ptw_graph **out);
+
 /* Synthetic R-MAT graph built on the device (no reference counterpart; the
  * reference reads files only).  2^scale * edge_factor raw edges with
  * quadrant probabilities a, b, c, 1-a-b-c; clean != 0 symmetrises, drops
@@ -200,6 +211,9 @@ typedef struct ptw_batch_cfg {
     uint64_t table_bytes; /* device memory for the count tables of one wave; 0 = 1/4 of free */
     double table_factor;  /* table slots per expected counted position; 0 = 2.  A query whose
                              table fills is run again with 2n slots, so results never depend on it */
+    uint32_t top_k;       /* 0 = every visited vertex, by name; k > 0 = each query's k largest
+                             counts, by count descending then name (selected on the device) */
+    uint32_t reserved;
 } ptw_batch_cfg;
 
 typedef struct ptw_batch ptw_batch; /* the sparse results of one batch (host memory) */
@@ -226,7 +240,8 @@ void ptw_batch_free(ptw_batch *b);
  * vector of the app (visits: pi_s / (sp (1-sp)) - sp/(1-sp) e_s; endpoint:
  * (pi_s - sp e_s) / (1-sp)) by power iteration until the added mass is below
  * tol, and the L1 distance between it and the normalised sparse counts of
- * query i of batch b (both normalised to sum 1).  h_l1[nq]. */
+ * query i of batch b (both normalised to sum 1).  h_l1[nq].  PTW_EINVAL for
+ * a batch run with top_k > 0 (its lists are truncated). */
 int ptw_batch_l1(ptw_graph *g, const ptw_batch *b, double sp, int32_t app, double tol, double *h_l1);
 
 /* ---- serving loop with continuous batching ----------------------------- */
@@ -252,6 +267,8 @@ typedef struct ptw_serve_cfg {
     uint32_t max_active;    /* query slots; 0 = 4096 */
     uint32_t use_graph;     /* 1 = replay the tick as a CUDA graph */
     double table_factor;    /* as in ptw_batch_cfg */
+    uint32_t top_k;         /* as in ptw_batch_cfg */
+    uint32_t reserved;
 } ptw_serve_cfg;
 
 typedef struct ptw_serve_result {
@@ -272,8 +289,30 @@ int ptw_serve_submit(ptw_server *s, const ptw_query *q);
 int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_active, uint32_t *n_pending);
 /* Oldest completed, not yet taken result: 1 and *r filled, or 0 if none. */
 int ptw_serve_poll(ptw_server *s, ptw_serve_result *r);
-/* Copies the polled result's entries (n_entries each) and drops it. */
+/* Copies the polled result's entries (n_entries each) and drops it; NULL
+ * outputs drop it without copying. */
 int ptw_serve_take(ptw_server *s, uint32_t *h_names, uint32_t *h_counts);
+/* Zero-copy view of the polled result's entries: pinned host memory the
+ * device wrote them to, valid until that result is taken or the server is
+ * closed. */
+int ptw_serve_view(const ptw_server *s, const uint32_t **names, const uint32_t **counts);
+
+typedef struct ptw_serve_stats {
+    uint64_t ticks;         /* steps that ran a tick */
+    uint64_t moves;         /* walker moves run */
+    uint64_t walkers;       /* walkers run */
+    uint64_t completed;     /* queries completed */
+    uint64_t entries;       /* (name, count) entries produced */
+    uint64_t retries;       /* queries re-run with a table that cannot fill */
+    uint64_t pinned_bytes;  /* pinned host staging held for results */
+    uint32_t active;        /* queries holding a table now */
+    uint32_t pending;       /* queries waiting for admission now */
+    double step_ms;         /* host wall time inside ptw_serve_step */
+    double device_ms;       /* device time of the ticks: plan copy-in, walk, flag copy-out */
+    double collect_ms;      /* compaction and copy-out of completed queries */
+} ptw_serve_stats;
+/* Counters since ptw_serve_open. */
+int ptw_serve_get_stats(const ptw_server *s, ptw_serve_stats *out);
 /* Seconds since ptw_serve_open on the server's clock. */
 double ptw_serve_clock(const ptw_server *s);
 void ptw_serve_close(ptw_server *s);
@@ -339,6 +378,13 @@ int ptw_pagerank_noalloc(const ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *
  * launch parameters on this graph and device, stores the fastest in the
  * graph and returns it. n_walkers = 0 means one walker per vertex. */
 int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tune *best);
+
+/* Measurement only: random 4-byte gathers per second that the current GPU
+ * serves from an array of array_bytes (filled with hashed values), each of
+ * `chains` (1, 2, 4 or 8) independent chains per thread loading at an index
+ * hashed from its previous value.  Above L2 size this is the ceiling of a
+ * walk move's dependent gather, which a streaming copy peak overstates. */
+int ptw_probe_gather(uint64_t array_bytes, uint32_t chains, double *loads_per_s);
 
 #ifdef __cplusplus
 }

@@ -20,6 +20,7 @@ from .api import (  # noqa: F401
     DeepWalkApp,
     Solver,
     walk,
+    probe_gather,
 )
 
 from .batch import BatchResult, ppr_batch  # noqa: F401,E402

@@ -50,7 +50,14 @@ class Query(ctypes.Structure):
 class BatchCfg(ctypes.Structure):
     _fields_ = [("sp", ctypes.c_double), ("seed", ctypes.c_uint64), ("app", ctypes.c_int32),
                 ("max_moves", ctypes.c_uint32), ("table_bytes", ctypes.c_uint64),
-                ("table_factor", ctypes.c_double)]
+                ("table_factor", ctypes.c_double), ("top_k", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("ticks", ctypes.c_uint64), ("moves", ctypes.c_uint64), ("walkers", ctypes.c_uint64),
+                ("completed", ctypes.c_uint64), ("entries", ctypes.c_uint64), ("retries", ctypes.c_uint64),
+                ("pinned_bytes", ctypes.c_uint64), ("active", ctypes.c_uint32), ("pending", ctypes.c_uint32),
+                ("step_ms", ctypes.c_double), ("device_ms", ctypes.c_double), ("collect_ms", ctypes.c_double)]
 
 
 PTW_APP_VISITS = 0
@@ -61,7 +68,8 @@ class ServeCfg(ctypes.Structure):
     _fields_ = [("sp", ctypes.c_double), ("seed", ctypes.c_uint64), ("app", ctypes.c_int32),
                 ("max_moves", ctypes.c_uint32), ("table_bytes", ctypes.c_uint64),
                 ("tick_walkers", ctypes.c_uint64), ("max_active", ctypes.c_uint32),
-                ("use_graph", ctypes.c_uint32), ("table_factor", ctypes.c_double)]
+                ("use_graph", ctypes.c_uint32), ("table_factor", ctypes.c_double),
+                ("top_k", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class ServeResult(ctypes.Structure):
@@ -91,6 +99,7 @@ SIGNATURES = [
     ("ptw_version", ctypes.c_char_p, []),
     ("ptw_graph_load", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, _GP]),
     ("ptw_graph_from_edges", ctypes.c_int, [_u32p, _u32p, ctypes.c_uint64, ctypes.c_int32, _GP]),
+    ("ptw_graph_from_csr", ctypes.c_int, [_u64p, _u32p, ctypes.c_uint32, _u32p, _GP]),
     ("ptw_graph_rmat", ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
                                       ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                       ctypes.c_int32, _GP]),
@@ -111,6 +120,7 @@ SIGNATURES = [
     ("ptw_graph_sync", ctypes.c_int, [_G]),
     ("ptw_graph_set_stream", ctypes.c_int, [_G, _vp]),
     ("ptw_autotune", ctypes.c_int, [_G, ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(Tune)]),
+    ("ptw_probe_gather", ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(ctypes.c_double)]),
     ("ptw_pagerank_noalloc", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, _vp]),
     ("ptw_ppr_batch", ctypes.c_int, [_G, ctypes.POINTER(Query), ctypes.c_uint32,
                                      ctypes.POINTER(BatchCfg), _GP]),
@@ -127,6 +137,8 @@ SIGNATURES = [
     ("ptw_serve_step", ctypes.c_int, [_G, _u32p, _u32p, _u32p]),
     ("ptw_serve_poll", ctypes.c_int, [_G, ctypes.POINTER(ServeResult)]),
     ("ptw_serve_take", ctypes.c_int, [_G, _u32p, _u32p]),
+    ("ptw_serve_view", ctypes.c_int, [_G, ctypes.POINTER(_u32p), ctypes.POINTER(_u32p)]),
+    ("ptw_serve_get_stats", ctypes.c_int, [_G, ctypes.POINTER(ServeStats)]),
     ("ptw_serve_clock", ctypes.c_double, [_G]),
     ("ptw_serve_close", None, [_G]),
     ("ptw_graph_chung_lu", ctypes.c_int, [ctypes.c_uint32, ctypes.c_double, ctypes.c_double,

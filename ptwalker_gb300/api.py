@@ -126,6 +126,28 @@ class Graph:
         return cls(h)
 
     @classmethod
+    def from_csr(cls, row_ptr, col, names=None):
+        """Graph from a CSR (row_ptr[n+1], col[row_ptr[n]] row indices, optional names[n]):
+        the inverse of export_csr."""
+        lib = C.load()
+        r = np.ascontiguousarray(row_ptr, dtype=np.uint64)
+        c = np.ascontiguousarray(col, dtype=np.uint32)
+        if r.ndim != 1 or r.shape[0] < 2:
+            raise ValueError("row_ptr needs n + 1 >= 2 entries")
+        n = r.shape[0] - 1
+        if c.shape[0] != int(r[-1]):
+            raise ValueError("col has %d entries, row_ptr[n] = %d" % (c.shape[0], int(r[-1])))
+        nm = None
+        if names is not None:
+            nm = np.ascontiguousarray(names, dtype=np.uint32)
+            if nm.shape[0] != n:
+                raise ValueError("names has %d entries for %d rows" % (nm.shape[0], n))
+        h = ctypes.c_void_p()
+        C.check(lib.ptw_graph_from_csr(_ptr(r, ctypes.c_uint64), _ptr(c), n,
+                                       _ptr(nm) if nm is not None else None, ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
     def rmat(cls, scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, clean=True):
         lib = C.load()
         h = ctypes.c_void_p()
@@ -239,6 +261,15 @@ def _cfg(n_walkers, sp, seed, start, sources, max_moves, first_walker=0):
             raise ValueError("sources given but start mode is not 'sources'")
     cfg.first_walker = int(first_walker)
     return cfg, keep
+
+
+def probe_gather(array_bytes=2 << 30, chains=8):
+    """Random 4-byte gathers per second the current GPU serves from an array
+    of array_bytes (ptw_probe_gather): the ceiling of a walk move's dependent
+    gather once the array exceeds L2."""
+    out = ctypes.c_double()
+    C.check(C.load().ptw_probe_gather(int(array_bytes), int(chains), ctypes.byref(out)))
+    return float(out.value)
 
 
 def pagerank(graph, n_walkers=None, sp=0.15, seed=0, start="per_vertex", sources=None,

@@ -79,7 +79,7 @@ class BatchResult:
 
 
 def ppr_batch(graph, sources, budgets, sp=0.2, seed=0, app="visits", query_ids=None, max_moves=0,
-              table_bytes=0, table_factor=0.0):
+              table_bytes=0, table_factor=0.0, top_k=0):
     sources = np.atleast_1d(np.asarray(sources, dtype=np.uint32))
     budgets = np.broadcast_to(np.asarray(budgets, dtype=np.uint64), sources.shape).copy()
     if query_ids is None:
@@ -92,7 +92,7 @@ def ppr_batch(graph, sources, budgets, sp=0.2, seed=0, app="visits", query_ids=N
         qs[i].query_id = int(query_ids[i])
         qs[i].budget = int(budgets[i])
     cfg = C.BatchCfg(float(sp), int(seed) & 0xFFFFFFFFFFFFFFFF, APPS[app], int(max_moves),
-                     int(table_bytes), float(table_factor))
+                     int(table_bytes), float(table_factor), int(top_k))
     h = ctypes.c_void_p()
     C.check(graph._lib.ptw_ppr_batch(graph.handle, qs, nq, ctypes.byref(cfg), ctypes.byref(h)))
     return BatchResult(graph, h, sources, budgets, query_ids, sp, app)

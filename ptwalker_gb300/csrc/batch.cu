@@ -37,6 +37,7 @@ struct ptw_batch {
     std::vector<uint64_t> offsets;  // [nq + 1]
     std::unique_ptr<uint32_t[]> names, counts;
     ptw_walk_stats stats{};
+    uint32_t top_k = 0;  // results hold each query's top_k largest counts only
 };
 
 namespace ptw {
@@ -63,7 +64,7 @@ struct DevBuf {
     template <typename T> cudaError_t alloc(T **p, uint64_t count)
     {
         void *q = nullptr;
-        cudaError_t e = cudaMallocAsync(&q, std::max<uint64_t>(count, 1) * sizeof(T), st);
+        cudaError_t e = pooled_alloc_async(&q, std::max<uint64_t>(count, 1) * sizeof(T), st);
         if (e == cudaSuccess) ptrs.push_back(q);
         *p = (T *)q;
         return e;
@@ -80,7 +81,7 @@ template <typename F> cudaError_t cub_call(F f, cudaStream_t st)
     cudaError_t e = f(nullptr, bytes);
     if (e != cudaSuccess) return e;
     void *tmp = nullptr;
-    e = cudaMallocAsync(&tmp, std::max<size_t>(bytes, 16), st);
+    e = pooled_alloc_async(&tmp, std::max<size_t>(bytes, 16), st);
     if (e != cudaSuccess) return e;
     e = f(tmp, bytes);
     cudaFreeAsync(tmp, st);
@@ -193,6 +194,7 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     PTW_CUDA(cudaMemcpyAsync(h_flag.data(), d_flag, nq * 4ull, cudaMemcpyDeviceToHost, st));
     PTW_CUDA(cudaMemcpyAsync(&h_moves, d_ctrl + 1, 8, cudaMemcpyDeviceToHost, st));
     WaveResult wr;
+    wr.c.top_k = cfg->top_k;
     int rc = compact_tables(g, d_slots, h_tab.data(), h_cap.data(), nq, &wr.c);
     if (rc) return rc;
     float ms = 0;
@@ -267,6 +269,7 @@ uint64_t next_pow2(uint64_t x)
 }  // namespace
 
 const ptw_query *batch_queries(const ptw_batch *b) { return b->queries.data(); }
+uint32_t batch_top_k(const ptw_batch *b) { return b->top_k; }
 
 int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned long long *h_base,
                    const uint32_t *h_cap, uint32_t nt, Compacted *out)
@@ -275,6 +278,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     out->seg.assign(nt + 1, 0);
     out->names.reset();
     out->counts.reset();
+    out->h_names = out->h_counts = nullptr;
     if (nt == 0) return PTW_OK;
     cudaStream_t st = g->stream;
     const bool timing = std::getenv("PTW_TIMING") != nullptr;
@@ -308,11 +312,30 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     PTW_CUDA(cudaMemcpyAsync(out->seg.data(), d_seg, (nt + 1) * 8ull, cudaMemcpyDeviceToHost, st));
     PTW_CUDA(cudaStreamSynchronize(st));
     const uint64_t n_ent = out->seg[nt];
-    out->n = n_ent;
+    // top-k: every table keeps its min(k, entries) largest counts
+    const uint32_t k = out->top_k;
+    std::vector<uint64_t> kseg;
+    uint64_t n_out = n_ent;
+    if (k && n_ent) {
+        kseg.assign(nt + 1, 0);
+        for (uint32_t i = 0; i < nt; ++i)
+            kseg[i + 1] = kseg[i] + std::min<uint64_t>(k, out->seg[i + 1] - out->seg[i]);
+        n_out = kseg[nt];
+    }
+    out->n = n_out;
     if (n_ent) {
-        out->names.reset(new (std::nothrow) uint32_t[n_ent]);  // no value-initialisation
-        out->counts.reset(new (std::nothrow) uint32_t[n_ent]);
-        if (!out->names || !out->counts) return fail(PTW_ENOMEM, "host allocation of batch results failed");
+        if (out->sink) {
+            uint32_t *base = out->sink(n_out);
+            if (!base) return fail(PTW_ENOMEM, "host staging of results failed");
+            out->h_names = base;
+            out->h_counts = base + n_out;
+        } else {
+            out->names.reset(new (std::nothrow) uint32_t[n_out]);  // no value-initialisation
+            out->counts.reset(new (std::nothrow) uint32_t[n_out]);
+            if (!out->names || !out->counts) return fail(PTW_ENOMEM, "host allocation of batch results failed");
+            out->h_names = out->names.get();
+            out->h_counts = out->counts.get();
+        }
         int name_bits = 1, q_bits = 1;
         while (name_bits < 32 && (1ull << name_bits) < g->dg.id_bound) ++name_bits;
         while ((1ull << q_bits) < nt) ++q_bits;
@@ -322,28 +345,69 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
         PTW_CUDA(db.alloc(&s_key, n_ent));
         PTW_CUDA(db.alloc(&e_cnt, n_ent));
         PTW_CUDA(db.alloc(&s_cnt, n_ent));
+        // top-k with (table, ~count, name) in 64 bits: one sort, keys only
+        const bool packed = k && q_bits + 32 + name_bits <= 64;
         for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
             const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
             k_tabs_emit<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(d_slots, d_base + t0, d_cap + t0, d_seg + t0,
                                                                    d_fill + t0, g->dg.int2name, t0, name_bits,
-                                                                   e_key, e_cnt);
+                                                                   packed, e_key, e_cnt);
         }
         PTW_CUDA(cudaGetLastError());
-        // one radix sort over (table, name): tables stay in their segments
-        PTW_CUDA(cub_call([&](void *t, size_t &b) {
-            return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_ent, 0,
-                                                   name_bits + q_bits, st);
-        }, st));
-        s_name = (uint32_t *)e_key;  // reuse the unsorted-key buffer
         const unsigned kg = (unsigned)std::min<uint64_t>((n_ent + 255) / 256, (uint64_t)g->num_sms * 32);
-        k_key_names<<<std::max(kg, 1u), 256, 0, st>>>(s_key, n_ent, (1ull << name_bits) - 1, s_name);
-        PTW_CUDA(cudaGetLastError());
+        uint32_t *o_name = nullptr, *o_cnt = nullptr;
+        if (packed) {
+            PTW_CUDA(cub_call([&](void *t, size_t &b) {
+                return cub::DeviceRadixSort::SortKeys(t, b, e_key, s_key, (int64_t)n_ent, 0,
+                                                      q_bits + 32 + name_bits, st);
+            }, st));
+        } else {
+            // one radix sort over (table, name): tables stay in their segments
+            PTW_CUDA(cub_call([&](void *t, size_t &b) {
+                return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_ent, 0,
+                                                       name_bits + q_bits, st);
+            }, st));
+        }
+        if (packed) {
+            unsigned long long *d_kseg;
+            PTW_CUDA(db.alloc(&d_kseg, nt + 1));
+            PTW_CUDA(db.alloc(&o_name, n_out));
+            PTW_CUDA(db.alloc(&o_cnt, n_out));
+            PTW_CUDA(cudaMemcpyAsync(d_kseg, kseg.data(), (nt + 1) * 8ull, cudaMemcpyHostToDevice, st));
+            k_topk_copy_packed<<<std::max(kg, 1u), 256, 0, st>>>(s_key, n_ent, name_bits, d_seg, d_kseg, k, o_name,
+                                                                 o_cnt);
+            PTW_CUDA(cudaGetLastError());
+            out->seg = kseg;
+        } else if (k) {
+            // re-key by (table, count descending) with the name as value; the
+            // radix sort is stable, so equal counts stay in name order
+            k_count_keys<<<std::max(kg, 1u), 256, 0, st>>>(s_key, s_cnt, n_ent, name_bits, e_key, e_cnt);
+            PTW_CUDA(cudaGetLastError());
+            PTW_CUDA(cub_call([&](void *t, size_t &b) {
+                return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_ent, 0,
+                                                       32 + q_bits, st);
+            }, st));
+            unsigned long long *d_kseg;
+            PTW_CUDA(db.alloc(&d_kseg, nt + 1));
+            PTW_CUDA(db.alloc(&o_name, n_out));
+            PTW_CUDA(db.alloc(&o_cnt, n_out));
+            PTW_CUDA(cudaMemcpyAsync(d_kseg, kseg.data(), (nt + 1) * 8ull, cudaMemcpyHostToDevice, st));
+            k_topk_copy<<<std::max(kg, 1u), 256, 0, st>>>(s_key, s_cnt, n_ent, d_seg, d_kseg, k, o_name, o_cnt);
+            PTW_CUDA(cudaGetLastError());
+            out->seg = kseg;
+        } else {
+            s_name = (uint32_t *)e_key;  // reuse the unsorted-key buffer
+            k_key_names<<<std::max(kg, 1u), 256, 0, st>>>(s_key, n_ent, (1ull << name_bits) - 1, s_name);
+            PTW_CUDA(cudaGetLastError());
+            o_name = s_name;
+            o_cnt = s_cnt;
+        }
         if (timing) {
             PTW_CUDA(cudaStreamSynchronize(st));
             t1 = clk();
         }
-        PTW_CUDA(cudaMemcpyAsync(out->names.get(), s_name, n_ent * 4, cudaMemcpyDeviceToHost, st));
-        PTW_CUDA(cudaMemcpyAsync(out->counts.get(), s_cnt, n_ent * 4, cudaMemcpyDeviceToHost, st));
+        PTW_CUDA(cudaMemcpyAsync(out->h_names, o_name, n_out * 4, cudaMemcpyDeviceToHost, st));
+        PTW_CUDA(cudaMemcpyAsync(out->h_counts, o_cnt, n_out * 4, cudaMemcpyDeviceToHost, st));
         PTW_CUDA(cudaStreamSynchronize(st));
         if (timing) t2 = clk();
     }
@@ -443,6 +507,7 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
     PTW_CUDA(cudaEventSynchronize(g->ev[2]));
     uint64_t walkers = 0;
     for (uint32_t i = 0; i < nq; ++i) walkers += all[i].budget;
+    b->top_k = cfg->top_k;
     b->stats.walkers = walkers;
     b->stats.moves = moves;
     b->stats.visits = cfg->app == PTW_APP_VISITS ? walkers + moves : walkers;

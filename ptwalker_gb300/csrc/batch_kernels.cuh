@@ -209,30 +209,66 @@ __global__ void k_tabs_count(const unsigned long long *slots, const unsigned lon
 
 // Writes each occupied slot of table i (= t_index0 + blockIdx.y) into the
 // table's segment as key (i << name_bits | name) and count, so one radix
-// sort of the keys orders every table's entries by name in place.
-__global__ void k_tabs_emit(const unsigned long long *slots, const unsigned long long *t_base,
+// sort of the keys orders every table's entries by name in place.  Each
+// block owns one contiguous chunk of the table: it counts the chunk's
+// occupied slots, reserves that many positions with a single atomic on the
+// table's fill cursor, then writes them (warp offsets through shared
+// memory).  One atomic per block instead of one per 32 slots keeps warps from
+// queueing on the cursor of a large table.  Launch with 256 threads.
+__global__ void __launch_bounds__(256) k_tabs_emit(const unsigned long long *slots, const unsigned long long *t_base,
                             const uint32_t *t_cap, const unsigned long long *seg_off, unsigned long long *fill,
-                            const uint32_t *int2name, uint32_t t_index0, int name_bits,
+                            const uint32_t *int2name, uint32_t t_index0, int name_bits, bool by_count,
                             unsigned long long *out_key, uint32_t *out_cnt)
 {
+    __shared__ uint32_t warp_n[8];
+    __shared__ unsigned long long base_s;
     const uint32_t i = blockIdx.y;
     const unsigned long long *s = slots + t_base[i];
     const uint32_t cap = t_cap[i];
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t x0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); x0 < cap; x0 += stride) {
-        const uint32_t x = x0 + lane;
-        const unsigned long long w = x < cap ? s[x] : 0ull;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t per = (cap + gridDim.x - 1) / gridDim.x;
+    per = (per + 255u) & ~255u;
+    const uint64_t lo = (uint64_t)blockIdx.x * per;
+    const uint64_t hi = lo + per < cap ? lo + per : cap;
+    if (lo >= hi) return;  // whole block leaves together
+    // pass 1: occupied slots of the chunk
+    uint32_t c = 0;
+    for (uint64_t x = lo + threadIdx.x; x < hi; x += 256) c += s[x] != 0;
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kBFull, c, o);
+    if (lane == 0) warp_n[warp] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < 8; ++w) t += warp_n[w];
+        base_s = t ? atomicAdd(&fill[i], (unsigned long long)t) : 0ull;
+    }
+    __syncthreads();
+    unsigned long long pos0 = seg_off[i] + base_s;
+    // by_count: key (table, ~count, name) so one sort orders each table by
+    // count descending, then name (the caller checks that it fits 64 bits)
+    const unsigned long long tagged = (unsigned long long)(t_index0 + i) << (by_count ? 32 + name_bits : name_bits);
+    // pass 2: tiles of 256 slots in order
+    for (uint64_t x0 = lo; x0 < hi; x0 += 256) {
+        const uint64_t x = x0 + threadIdx.x;
+        const unsigned long long w = x < hi ? s[x] : 0ull;
         const unsigned om = __ballot_sync(kBFull, w != 0);
-        if (!om) continue;
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&fill[i], (unsigned long long)__popc(om));
-        base = __shfl_sync(kBFull, base, 0);
-        if (w) {
-            const uint64_t pos = seg_off[i] + base + __popc(om & ((1u << lane) - 1u));
-            out_key[pos] = ((unsigned long long)(t_index0 + i) << name_bits) | int2name[(uint32_t)(w >> 32) - 1];
-            out_cnt[pos] = (uint32_t)(w & 0xFFFFFFFFull);
+        __syncthreads();  // previous tile's readers of warp_n are done
+        if (lane == 0) warp_n[warp] = __popc(om);
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t v = warp_n[k];
+            before += k < (int)warp ? v : 0u;
+            total += v;
         }
+        if (w) {
+            const unsigned long long p = pos0 + before + __popc(om & ((1u << lane) - 1u));
+            const uint32_t cnt = (uint32_t)(w & 0xFFFFFFFFull);
+            const unsigned long long inv = by_count ? (unsigned long long)(0xFFFFFFFFu - cnt) << name_bits : 0ull;
+            out_key[p] = tagged | inv | int2name[(uint32_t)(w >> 32) - 1];
+            out_cnt[p] = cnt;
+        }
+        pos0 += total;
     }
 }
 
@@ -240,6 +276,56 @@ __global__ void k_key_names(const unsigned long long *key, uint64_t n, unsigned 
 {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
         name[i] = (uint32_t)(key[i] & mask);
+}
+
+// Top-k, step 1: key (table << 32 | ~count) with the name as value, from the
+// (table << name_bits | name) keys and counts of the name-ordered lists.
+__global__ void k_count_keys(const unsigned long long *key, const uint32_t *cnt, uint64_t n, int name_bits,
+                             unsigned long long *ckey, uint32_t *name)
+{
+    const unsigned long long mask = (1ull << name_bits) - 1;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long k = key[i];
+        ckey[i] = ((k >> name_bits) << 32) | (unsigned long long)(0xFFFFFFFFu - cnt[i]);
+        name[i] = (uint32_t)(k & mask);
+    }
+}
+
+// Top-k, step 2: entry i of the count-ordered lists is rank i - seg[t] of its
+// table t; ranks below k go to position kseg[t] + rank of the output.
+__global__ void k_topk_copy(const unsigned long long *ckey, const uint32_t *name, uint64_t n,
+                            const unsigned long long *seg, const unsigned long long *kseg, uint32_t k,
+                            uint32_t *out_name, uint32_t *out_cnt)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long c = ckey[i];
+        const uint32_t t = (uint32_t)(c >> 32);
+        const uint64_t r = i - seg[t];
+        if (r < k) {
+            const uint64_t p = kseg[t] + r;
+            out_name[p] = name[i];
+            out_cnt[p] = 0xFFFFFFFFu - (uint32_t)(c & 0xFFFFFFFFull);
+        }
+    }
+}
+
+// Top-k from (table, ~count, name) keys sorted in one pass: entry i is rank
+// i - seg[t] of its table t; ranks below k go to kseg[t] + rank.
+__global__ void k_topk_copy_packed(const unsigned long long *key, uint64_t n, int name_bits,
+                                   const unsigned long long *seg, const unsigned long long *kseg, uint32_t k,
+                                   uint32_t *out_name, uint32_t *out_cnt)
+{
+    const unsigned long long nmask = (1ull << name_bits) - 1;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long c = key[i];
+        const uint32_t t = (uint32_t)(c >> (32 + name_bits));
+        const uint64_t r = i - seg[t];
+        if (r < k) {
+            const uint64_t p = kseg[t] + r;
+            out_name[p] = (uint32_t)(c & nmask);
+            out_cnt[p] = 0xFFFFFFFFu - (uint32_t)((c >> name_bits) & 0xFFFFFFFFull);
+        }
+    }
 }
 
 }  // namespace

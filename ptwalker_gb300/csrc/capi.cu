@@ -13,6 +13,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <mutex>
 #include <vector>
 
 #include "ptw_internal.cuh"
@@ -32,6 +33,38 @@ int cuda_fail(cudaError_t e, const char *what)
     const int code = (e == cudaErrorMemoryAllocation) ? PTW_ENOMEM : PTW_ECUDA;
     cudaGetLastError();  // clear a sticky-free error so later calls can run
     return fail(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+cudaError_t pooled_alloc_async(void **p, size_t bytes, cudaStream_t st)
+{
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaMallocAsync(p, bytes, st);
+    cudaMemPool_t pool;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!pools[dev]) {
+            cudaMemPoolProps props{};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            cudaMemPool_t np = nullptr;
+            e = cudaMemPoolCreate(&np, &props);
+            if (e != cudaSuccess) return e;
+            uint64_t keep = 1ull << 30;
+            e = cudaMemPoolSetAttribute(np, cudaMemPoolAttrReleaseThreshold, &keep);
+            if (e != cudaSuccess) {
+                cudaMemPoolDestroy(np);
+                return e;
+            }
+            pools[dev] = np;
+        }
+        pool = pools[dev];
+    }
+    return cudaMallocFromPoolAsync(p, bytes, pool, st);
 }
 
 namespace {
@@ -357,6 +390,35 @@ extern "C" int ptw_graph_from_edges(const uint32_t *h_src, const uint32_t *h_dst
                                     int32_t as_undirected, ptw_graph **out)
 {
     return upload_and_build(h_src, h_dst, m, as_undirected != 0, out);
+}
+
+extern "C" int ptw_graph_from_csr(const uint64_t *h_row_ptr, const uint32_t *h_col, uint32_t n,
+                                  const uint32_t *h_names, ptw_graph **out)
+{
+    if (!out) return fail(PTW_EINVAL, "null output handle");
+    *out = nullptr;
+    if (!h_row_ptr || n == 0) return fail(PTW_EINVAL, "CSR needs n >= 1 rows and a row_ptr array");
+    if (h_row_ptr[0] != 0) return fail(PTW_EINVAL, "CSR row_ptr[0] must be 0");
+    for (uint32_t i = 0; i < n; ++i)
+        if (h_row_ptr[i + 1] < h_row_ptr[i])
+            return fail(PTW_EINVAL, "CSR row_ptr decreases at row " + std::to_string(i));
+    const uint64_t m = h_row_ptr[n];
+    if (m == 0) return fail(PTW_EINVAL, "edge list is empty");
+    if (!h_col) return fail(PTW_EINVAL, "null CSR column array");
+    if (m >= (1ull << 32)) return fail(PTW_EINVAL, "graphs with 2^32 or more CSR entries are not supported");
+    ptw_graph *g = new (std::nothrow) ptw_graph();
+    if (!g) return fail(PTW_ENOMEM, "host allocation failed");
+    int rc = graph_init_handle(g);
+    uint32_t *d_src = nullptr, *d_dst = nullptr;
+    if (rc == PTW_OK) rc = csr_to_device_edges(h_row_ptr, h_col, h_names, n, &d_src, &d_dst, g->stream);
+    if (rc == PTW_OK) rc = build_graph_from_device_edges(g, d_src, d_dst, m, false, false, false);
+    if (rc != PTW_OK) {
+        graph_release(g);
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return PTW_OK;
 }
 
 extern "C" int ptw_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,

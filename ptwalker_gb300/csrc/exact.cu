@@ -149,6 +149,7 @@ extern "C" int ptw_batch_l1(ptw_graph *g, const ptw_batch *b, double sp, int32_t
     if (!(sp > 0.0 && sp < 1.0)) return fail(PTW_EINVAL, "sp must be in (0, 1)");
     if (app != PTW_APP_VISITS && app != PTW_APP_ENDPOINT) return fail(PTW_EINVAL, "unknown app");
     if (!(tol > 0.0)) return fail(PTW_EINVAL, "tol must be > 0");
+    if (batch_top_k(b)) return fail(PTW_EINVAL, "the L1 error needs full results (batch run with top_k > 0)");
     PTW_CUDA(cudaSetDevice(g->device));
     uint32_t nq = 0;
     uint64_t ne = 0;

@@ -102,11 +102,24 @@ __global__ void k_to_index(uint32_t *x, uint64_t m, const uint32_t *names, uint3
         x[i] = lower_bound_u32(names, n, x[i]);
 }
 
-__global__ void k_degree(const uint32_t *si, uint64_t m, uint32_t *deg)
+// Row bounds from the sorted source indices, without atomics (a hub of
+// degree d would otherwise serialise d atomics on one counter): the first
+// entry of a run of v records first[v], the last records end[v].
+__global__ void k_row_bounds(const uint32_t *si, uint64_t m, uint32_t *first, uint32_t *end)
 {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
-         i += (uint64_t)gridDim.x * blockDim.x)
-        atomicAdd(&deg[si[i]], 1u);
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = si[i];
+        if (i == 0 || si[i - 1] != v) first[v] = (uint32_t)i;
+        if (i + 1 == m || si[i + 1] != v) end[v] = (uint32_t)(i + 1);
+    }
+}
+
+// deg[v] = end[v] - first[v] in place (both 0 for a vertex without out-edges).
+__global__ void k_degree_from_bounds(uint32_t *end_deg, const uint32_t *first, uint32_t n)
+{
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x)
+        end_deg[v] -= first[v];
 }
 
 __global__ void k_iota(uint32_t *x, uint32_t n)
@@ -228,6 +241,41 @@ __global__ void k_cl_edges(uint64_t m, const double *cdf, uint32_t n, uint32_t k
     }
 }
 
+// CSR -> (src, dst) names, one thread per entry.  The row of entry e is the
+// largest r with row_ptr[r] <= e (row_ptr is validated non-decreasing with
+// row_ptr[0] = 0 and row_ptr[n] = m on the host, so the search invariant
+// row_ptr[lo] <= e < row_ptr[hi] holds from lo = 0, hi = n).  A column index
+// >= n raises *bad and writes name 0 so the arrays stay defined.
+__global__ void k_csr_to_edges(const uint64_t *row_ptr, const uint32_t *col, const uint32_t *names,
+                               uint32_t n, uint64_t m, uint32_t *src, uint32_t *dst, unsigned *bad)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = n;
+        while (hi - lo > 1) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            if (row_ptr[mid] <= e) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t c = col[e];
+        if (c >= n) {
+            atomicOr(bad, 1u);
+            src[e] = dst[e] = 0;
+            continue;
+        }
+        src[e] = names ? names[lo] : lo;
+        dst[e] = names ? names[c] : c;
+    }
+}
+
+// Raises *bad when two neighbours of a sorted array are equal.
+__global__ void k_adjacent_equal(const uint32_t *x, uint32_t n, unsigned *bad)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i + 1 < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        if (x[i] == x[i + 1]) atomicOr(bad, 2u);
+}
+
 // Frees every pointer on scope exit (stream-ordered).
 struct AsyncBufs {
     cudaStream_t st;
@@ -346,6 +394,55 @@ int chung_lu_generate_device(uint32_t n, double gamma, uint64_t m, uint64_t seed
     return PTW_OK;
 }
 
+int csr_to_device_edges(const uint64_t *h_row_ptr, const uint32_t *h_col, const uint32_t *h_names,
+                        uint32_t n, uint32_t **d_src, uint32_t **d_dst, cudaStream_t st)
+{
+    *d_src = *d_dst = nullptr;
+    const uint64_t m = h_row_ptr[n];
+    AsyncBufs tmp(st);
+    uint64_t *row = nullptr;
+    uint32_t *col = nullptr, *names = nullptr, *src = nullptr, *dst = nullptr;
+    unsigned *bad = nullptr;
+    PTW_CUDA(tmp.alloc(&row, (uint64_t)n + 1));
+    PTW_CUDA(tmp.alloc(&col, m));
+    PTW_CUDA(tmp.alloc(&bad, 1));
+    PTW_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned), st));
+    PTW_CUDA(cudaMemcpyAsync(row, h_row_ptr, ((uint64_t)n + 1) * 8, cudaMemcpyHostToDevice, st));
+    PTW_CUDA(cudaMemcpyAsync(col, h_col, m * 4, cudaMemcpyHostToDevice, st));
+    if (h_names) {
+        uint32_t *sorted = nullptr;
+        PTW_CUDA(tmp.alloc(&names, n));
+        PTW_CUDA(tmp.alloc(&sorted, n));
+        PTW_CUDA(cudaMemcpyAsync(names, h_names, (uint64_t)n * 4, cudaMemcpyHostToDevice, st));
+        PTW_CUDA(cub_call([&](void *t, size_t &b) {
+            return cub::DeviceRadixSort::SortKeys(t, b, names, sorted, (int64_t)n, 0, 32, st);
+        }, st));
+        k_adjacent_equal<<<grid_for(n), kThreads, 0, st>>>(sorted, n, bad);
+        tmp.release(sorted);
+    }
+    // The edge arrays are handed to the caller, so they are not in tmp.
+    PTW_CUDA(cudaMallocAsync(&src, std::max<uint64_t>(m, 1) * 4, st));
+    cudaError_t e = cudaMallocAsync(&dst, std::max<uint64_t>(m, 1) * 4, st);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(src, st);
+        return cuda_fail(e, "CSR edge buffers");
+    }
+    k_csr_to_edges<<<grid_for(m), kThreads, 0, st>>>(row, col, names, n, m, src, dst, bad);
+    unsigned h_bad = 0;
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h_bad, bad, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess || h_bad) {
+        cudaFreeAsync(src, st);
+        cudaFreeAsync(dst, st);
+        if (e != cudaSuccess) return cuda_fail(e, "CSR expansion");
+        return fail(PTW_EINVAL, (h_bad & 1) ? "CSR column index >= n" : "CSR vertex names are not distinct");
+    }
+    *d_src = src;
+    *d_dst = dst;
+    return PTW_OK;
+}
+
 int build_graph_from_device_edges(ptw_graph *g, uint32_t *d_src, uint32_t *d_dst, uint64_t m,
                                   bool as_undirected, bool clean, bool compact_names)
 {
@@ -437,7 +534,14 @@ int build_graph_from_device_edges(ptw_graph *g, uint32_t *d_src, uint32_t *d_dst
     PTW_CUDA(tmp.alloc(&deg, n + 1));
     PTW_CUDA(tmp.alloc(&row_ptr, n + 1));
     PTW_CUDA(cudaMemsetAsync(deg, 0, (n + 1) * 4ull, st));
-    k_degree<<<grid_for(mm), kThreads, 0, st>>>(si, mm, deg);
+    {
+        uint32_t *first = nullptr;
+        PTW_CUDA(tmp.alloc(&first, n));
+        PTW_CUDA(cudaMemsetAsync(first, 0, n * 4ull, st));
+        k_row_bounds<<<grid_for(mm), kThreads, 0, st>>>(si, mm, first, deg);
+        k_degree_from_bounds<<<grid_for(n), kThreads, 0, st>>>(deg, first, n);
+        tmp.release(first);
+    }
     PTW_CUDA(cub_call([&](void *t, size_t &b) {
         return cub::DeviceScan::ExclusiveSum(t, b, deg, row_ptr, (int64_t)n + 1, st);
     }, st));

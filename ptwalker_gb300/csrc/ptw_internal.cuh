@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -126,6 +127,11 @@ namespace ptw {
 // (consumes them).  Implemented in graph.cu.
 int build_graph_from_device_edges(ptw_graph *g, uint32_t *d_src, uint32_t *d_dst, uint64_t m,
                                   bool as_undirected, bool clean, bool compact_names);
+// Expands a validated host CSR (row_ptr[n+1], col[row_ptr[n]], optional
+// names[n]) into device (src, dst) name arrays allocated on st; rejects a
+// column index >= n and repeated names.  Implemented in graph.cu.
+int csr_to_device_edges(const uint64_t *h_row_ptr, const uint32_t *h_col, const uint32_t *h_names,
+                        uint32_t n, uint32_t **d_src, uint32_t **d_dst, cudaStream_t st);
 int rmat_generate_device(uint32_t scale, uint64_t m, uint32_t ta, uint32_t tab, uint32_t tabc,
                          uint64_t seed, uint32_t *d_src, uint32_t *d_dst, cudaStream_t st);
 int chung_lu_generate_device(uint32_t n, double gamma, uint64_t m, uint64_t seed, uint32_t *d_src,
@@ -147,18 +153,33 @@ struct WalkLaunch {
 int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t);
 int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
                  int start_mode, uint32_t n_sources, int32_t *paths);
+// Stream-ordered device allocation from a per-device pool that keeps up to
+// 1 GiB cached across synchronisations (the default pool hands memory back at
+// each one), for the short-lived buffers of every result compaction.  Freed
+// with cudaFreeAsync.
+cudaError_t pooled_alloc_async(void **p, size_t bytes, cudaStream_t st);
+
 int launch_counts_by_name(ptw_graph *g, uint32_t *d_out);
 int check_tune(const ptw_tune &t);
 
 // The query table a batch was run with (batch.cu).
 const ptw_query *batch_queries(const ptw_batch *b);
+uint32_t batch_top_k(const ptw_batch *b);
 
 // (name, count) lists of nt tables in host memory: table i owns entries
-// [seg[i], seg[i+1]), sorted by name.
+// [seg[i], seg[i+1]), sorted by name.  Without a sink the lists land in the
+// owned arrays names / counts; with one, sink(n) returns 2n words of caller
+// memory (names in the first n, counts in the next n; nullptr = no memory).
+// h_names / h_counts point at wherever they landed.  top_k > 0 keeps the
+// top_k largest counts of every table instead, ordered by count descending
+// and then by name (seg then delimits the kept entries).
 struct Compacted {
+    uint32_t top_k = 0;
     uint64_t n = 0;
     std::vector<uint64_t> seg;
     std::unique_ptr<uint32_t[]> names, counts;
+    std::function<uint32_t *(uint64_t)> sink;
+    uint32_t *h_names = nullptr, *h_counts = nullptr;
 };
 // Compacts nt count tables (slots [h_base[i], h_base[i] + h_cap[i]) of
 // d_slots) into *out (batch.cu).

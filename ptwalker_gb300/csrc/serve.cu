@@ -93,9 +93,21 @@ struct Active {
     double admit_s;
 };
 
+// Pinned host memory that completed results are copied into by the device;
+// a block is reused once no pending result refers to it.
+struct PinnedBlock {
+    uint32_t *p = nullptr;
+    uint64_t words = 0;
+    ~PinnedBlock()
+    {
+        if (p) cudaFreeHost(p);
+    }
+};
+
 struct Done {
     ptw_serve_result r;
-    std::vector<uint32_t> names, counts;
+    std::shared_ptr<PinnedBlock> blk;  // keeps names / counts alive
+    const uint32_t *names = nullptr, *counts = nullptr;
 };
 
 }  // namespace
@@ -122,7 +134,9 @@ struct ptw_server {
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t knode = nullptr;
     cudaKernelNodeParams kparams{};
-    uint64_t ticks = 0, moves = 0;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    std::vector<std::shared_ptr<ptw::PinnedBlock>> pinned;  // result staging pool
+    ptw_serve_stats st{};
 };
 
 namespace ptw {
@@ -200,6 +214,29 @@ int build_tick_graph(ptw_server *s)
     return PTW_OK;
 }
 
+// A free pinned block of at least `words` words: reuses one that no pending
+// result refers to, else allocates (blocks grow geometrically).
+std::shared_ptr<PinnedBlock> pinned_block(ptw_server *s, uint64_t words)
+{
+    std::shared_ptr<PinnedBlock> *spare = nullptr;
+    for (auto &b : s->pinned) {
+        if (b.use_count() != 1) continue;
+        if (b->words >= words) return b;
+        spare = &b;  // free but too small: replace it
+    }
+    auto nb = std::make_shared<PinnedBlock>();
+    uint64_t w = std::max<uint64_t>(words, 1ull << 23);
+    if (spare) w = std::max(w, 2 * (*spare)->words);
+    if (cudaMallocHost(&nb->p, w * 4) != cudaSuccess) {
+        nb->p = nullptr;
+        return nullptr;
+    }
+    nb->words = w;
+    if (spare) *spare = nb;
+    else s->pinned.push_back(nb);
+    return nb;
+}
+
 // Turns the tables of finished queries (indices into s->active) into results
 // and releases the tables; the caller removes them from s->active.
 int collect(ptw_server *s, const std::vector<size_t> &fin)
@@ -213,19 +250,27 @@ int collect(ptw_server *s, const std::vector<size_t> &fin)
         cap[i] = (uint32_t)s->active[fin[i]].cap;
     }
     Compacted c;
+    c.top_k = s->cfg.top_k;
+    std::shared_ptr<PinnedBlock> blk;
+    c.sink = [&](uint64_t n) -> uint32_t * {
+        blk = pinned_block(s, 2 * n);
+        return blk ? blk->p : nullptr;
+    };
     int rc = compact_tables(s->g, s->arena, base.data(), cap.data(), (uint32_t)fin.size(), &c);
     if (rc) return rc;
     for (size_t i = 0; i < fin.size(); ++i) {
-        out[i].names.assign(c.names.get() + c.seg[i], c.names.get() + c.seg[i + 1]);
-        out[i].counts.assign(c.counts.get() + c.seg[i], c.counts.get() + c.seg[i + 1]);
+        out[i].blk = blk;
+        out[i].names = c.h_names + c.seg[i];
+        out[i].counts = c.h_counts + c.seg[i];
     }
+    s->st.entries += c.n;
     const double t = now_s(s);
     for (size_t i = 0; i < fin.size(); ++i) {
         const Active &a = s->active[fin[i]];
         out[i].r.query_id = a.p.q.query_id;
         out[i].r.source = a.p.q.source;
         out[i].r.budget = a.p.q.budget;
-        out[i].r.n_entries = out[i].names.size();
+        out[i].r.n_entries = c.seg[i + 1] - c.seg[i];
         out[i].r.submit_s = a.p.submit_s;
         out[i].r.admit_s = a.admit_s;
         out[i].r.done_s = t;
@@ -305,7 +350,14 @@ extern "C" int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, 256, 0);
         if (e != cudaSuccess) rc = cuda_fail(e, "occupancy");
         s->grid = (unsigned)std::max(1, g->num_sms * std::max(per_sm, 1));
+        if (rc == PTW_OK) {
+            e = cudaEventCreate(&s->ev[0]);
+            if (e == cudaSuccess) e = cudaEventCreate(&s->ev[1]);
+            if (e != cudaSuccess) rc = cuda_fail(e, "server events");
+        }
         if (rc == PTW_OK && cfg->use_graph) rc = build_tick_graph(s);
+        // one staging block up front, so the first results do not wait for it
+        if (rc == PTW_OK && !pinned_block(s, 1)) rc = fail(PTW_ENOMEM, "pinned result staging");
     }
     if (rc != PTW_OK) {
         ptw_serve_close(s);
@@ -336,6 +388,7 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
 {
     if (!s) return fail(PTW_EINVAL, "null server");
     PTW_CUDA(cudaSetDevice(s->g->device));
+    const double t_enter = now_s(s);
     cudaStream_t st = s->g->stream;
     const uint32_t n = s->g->dg.n;
     const size_t done_before = s->done.size();
@@ -396,6 +449,7 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
         hv.ctrl[0] = hv.ctrl[1] = 0;
         s->args.ndesc = (uint32_t)desc.size();
         // 3. the tick
+        PTW_CUDA(cudaEventRecord(s->ev[0], st));
         if (s->exec) {
             void *kp[] = {&s->args};
             cudaKernelNodeParams p = s->kparams;
@@ -409,9 +463,13 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
             PTW_CUDA(cudaMemcpyAsync((char *)s->h_plan + s->ret_off, (char *)s->d_plan + s->ret_off,
                                      s->ret_bytes, cudaMemcpyDeviceToHost, st));
         }
+        PTW_CUDA(cudaEventRecord(s->ev[1], st));
         PTW_CUDA(cudaStreamSynchronize(st));
-        ++s->ticks;
-        s->moves += hv.ctrl[1];
+        float dev_ms = 0;
+        PTW_CUDA(cudaEventElapsedTime(&dev_ms, s->ev[0], s->ev[1]));
+        s->st.device_ms += dev_ms;
+        ++s->st.ticks;
+        s->st.moves += hv.ctrl[1];
         // 4. progress; completed queries become results; a query whose table
         //    filled is queued again (first) with a table that cannot fill
         std::vector<size_t> fin;
@@ -420,6 +478,7 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
         for (uint32_t i = 0; i < na; ++i) {
             Active &a = s->active[i];
             if (hv.flag[i]) {
+                ++s->st.retries;
                 retry.push_back(a.p);
                 retry.back().full = true;
                 s->buddy.release(a.off);
@@ -427,13 +486,17 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
                 continue;
             }
             a.started += s->take[i];
+            s->st.walkers += s->take[i];
             if (a.started == a.p.q.budget) {
                 fin.push_back(i);
                 drop[i] = 1;
             }
         }
+        const double t_collect = now_s(s);
         int rc = collect(s, fin);
         if (rc) return rc;
+        s->st.collect_ms += 1e3 * (now_s(s) - t_collect);
+        s->st.completed += fin.size();
         std::vector<Active> keep;
         for (uint32_t i = 0; i < na; ++i)
             if (!drop[i]) keep.push_back(s->active[i]);
@@ -441,6 +504,7 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
         for (auto it = retry.rbegin(); it != retry.rend(); ++it) s->pending.push_front(*it);
         nd = (uint32_t)(s->done.size() - done_before);
     }
+    s->st.step_ms += 1e3 * (now_s(s) - t_enter);
     if (n_done) *n_done = nd;
     if (n_active) *n_active = (uint32_t)s->active.size();
     if (n_pending) *n_pending = (uint32_t)s->pending.size();
@@ -460,9 +524,30 @@ extern "C" int ptw_serve_take(ptw_server *s, uint32_t *h_names, uint32_t *h_coun
     if (!s) return fail(PTW_EINVAL, "null server");
     if (s->done.empty()) return fail(PTW_EINVAL, "no completed result");
     Done &d = s->done.front();
-    if (h_names && !d.names.empty()) std::memcpy(h_names, d.names.data(), d.names.size() * 4);
-    if (h_counts && !d.counts.empty()) std::memcpy(h_counts, d.counts.data(), d.counts.size() * 4);
+    const size_t ne = d.r.n_entries;
+    if (h_names && ne) std::memcpy(h_names, d.names, ne * 4);
+    if (h_counts && ne) std::memcpy(h_counts, d.counts, ne * 4);
     s->done.pop_front();
+    return PTW_OK;
+}
+
+extern "C" int ptw_serve_view(const ptw_server *s, const uint32_t **names, const uint32_t **counts)
+{
+    if (!s || !names || !counts) return fail(PTW_EINVAL, "null argument");
+    if (s->done.empty()) return fail(PTW_EINVAL, "no completed result");
+    *names = s->done.front().names;
+    *counts = s->done.front().counts;
+    return PTW_OK;
+}
+
+extern "C" int ptw_serve_get_stats(const ptw_server *s, ptw_serve_stats *out)
+{
+    if (!s || !out) return fail(PTW_EINVAL, "null argument");
+    *out = s->st;
+    out->active = (uint32_t)s->active.size();
+    out->pending = (uint32_t)s->pending.size();
+    out->pinned_bytes = 0;
+    for (const auto &b : s->pinned) out->pinned_bytes += b->words * 4;
     return PTW_OK;
 }
 
@@ -473,6 +558,10 @@ extern "C" void ptw_serve_close(ptw_server *s)
     if (!s) return;
     cudaSetDevice(s->g->device);
     cudaStreamSynchronize(s->g->stream);
+    s->done.clear();
+    s->pinned.clear();
+    for (cudaEvent_t e : s->ev)
+        if (e) cudaEventDestroy(e);
     if (s->exec) cudaGraphExecDestroy(s->exec);
     if (s->graph) cudaGraphDestroy(s->graph);
     cudaFree(s->arena);

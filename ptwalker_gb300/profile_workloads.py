@@ -6,6 +6,7 @@
     python -m ptwalker_gb300.profile_workloads exact --scale 18
     python -m ptwalker_gb300.profile_workloads mlp
     python -m ptwalker_gb300.profile_workloads build --scale 22
+    python -m ptwalker_gb300.profile_workloads serve --n 8400000 --queries 600 --top-k 1000
 
 Each runs a warm-up call and `--reps` measured calls and prints one JSON line
 with CUDA-event timings.  Sizes default to cases that fit a full ncu capture
@@ -20,12 +21,14 @@ import numpy as np
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("what", choices=["pagerank", "deepwalk", "batch", "exact", "mlp", "build"])
+    p.add_argument("what", choices=["pagerank", "deepwalk", "batch", "exact", "mlp", "build", "serve"])
     p.add_argument("--scale", type=int, default=22)
     p.add_argument("--walk-len", type=int, default=80)
     p.add_argument("--queries", type=int, default=512)
     p.add_argument("--reps", type=int, default=3)
     p.add_argument("--sp", type=float, default=0.15)
+    p.add_argument("--n", type=int, default=8_400_000, help="Chung-Lu vertices (serve)")
+    p.add_argument("--top-k", type=int, default=1000)
     a = p.parse_args(argv)
 
     import torch
@@ -49,6 +52,25 @@ def main(argv=None):
         m = learned.MLP(seed=1)
         curve = m.train(x, t, epochs=a.reps, batch=4096, lr=1e-3)
         out.update(loss=[float(curve[0]), float(curve[-1])])
+        print(json.dumps(out))
+        return
+    if a.what == "serve":
+        # closed loop: every query queued at once, served to completion
+        G = ptw.Graph.chung_lu(a.n, 2.1, 32.0, seed=1)
+        rng = np.random.default_rng(4)
+        src = rng.integers(0, G.n, a.queries)
+        bud = np.exp(rng.uniform(np.log(1e3), np.log(1e6), a.queries)).astype(np.int64)
+        with ptw.Server(G, sp=0.2, seed=3, tick_walkers=1 << 21, top_k=a.top_k) as srv:
+            srv.submit(int(src[0]), 1000, 1 << 30)
+            srv.drain()
+            t1 = time.perf_counter()
+            for q in range(a.queries):
+                srv.submit(int(src[q]), int(bud[q]), q)
+            res = srv.drain()
+            wall = time.perf_counter() - t1
+            out.update(vertices=G.n, edges=G.m, queries=len(res), seconds=wall, qps=len(res) / wall,
+                       stats=srv.stats())
+        G.close()
         print(json.dumps(out))
         return
     G = ptw.Graph.rmat(a.scale, 16, seed=1, clean=True)

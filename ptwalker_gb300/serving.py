@@ -17,12 +17,12 @@ from .batch import APPS
 
 class Server:
     def __init__(self, graph, sp=0.2, seed=0, app="visits", max_moves=0, table_bytes=0,
-                 tick_walkers=0, max_active=0, use_graph=True, table_factor=0.0):
+                 tick_walkers=0, max_active=0, use_graph=True, table_factor=0.0, top_k=0):
         self._lib = C.load()
         self.graph = graph
         cfg = C.ServeCfg(float(sp), int(seed) & 0xFFFFFFFFFFFFFFFF, APPS[app], int(max_moves),
                          int(table_bytes), int(tick_walkers), int(max_active), int(bool(use_graph)),
-                         float(table_factor))
+                         float(table_factor), int(top_k))
         h = ctypes.c_void_p()
         C.check(self._lib.ptw_serve_open(graph.handle, ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
@@ -36,25 +36,42 @@ class Server:
         q = C.Query(int(source), int(query_id), int(budget))
         C.check(self._lib.ptw_serve_submit(self._h, ctypes.byref(q)))
 
-    def step(self):
+    def step(self, take=True):
         """One admission + tick; returns the list of completed results as
         dicts with keys query_id, source, budget, names, counts, submit_s,
-        admit_s, done_s."""
+        admit_s, done_s.  take=False leaves them on the server for a later
+        results() call."""
         nd, na, npd = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
         C.check(self._lib.ptw_serve_step(self._h, ctypes.byref(nd), ctypes.byref(na), ctypes.byref(npd)))
         self.n_active, self.n_pending = int(na.value), int(npd.value)
+        return self.results() if take else []
+
+    def results(self):
+        """Takes every completed result the server holds."""
         out = []
         r = C.ServeResult()
+        pn, pc = ctypes.POINTER(ctypes.c_uint32)(), ctypes.POINTER(ctypes.c_uint32)()
         while self._lib.ptw_serve_poll(self._h, ctypes.byref(r)) == 1:
             ne = int(r.n_entries)
-            names = np.empty(ne, dtype=np.uint32)
-            counts = np.empty(ne, dtype=np.uint32)
-            C.check(self._lib.ptw_serve_take(self._h, names.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
-                                             counts.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
+            if ne:
+                # one copy out of the pinned block the device wrote the entries to
+                C.check(self._lib.ptw_serve_view(self._h, ctypes.byref(pn), ctypes.byref(pc)))
+                names = np.ctypeslib.as_array(pn, shape=(ne,)).copy()
+                counts = np.ctypeslib.as_array(pc, shape=(ne,)).copy()
+            else:
+                names = np.empty(0, dtype=np.uint32)
+                counts = np.empty(0, dtype=np.uint32)
+            C.check(self._lib.ptw_serve_take(self._h, None, None))
             out.append(dict(query_id=int(r.query_id), source=int(r.source), budget=int(r.budget),
                             names=names, counts=counts, submit_s=float(r.submit_s),
                             admit_s=float(r.admit_s), done_s=float(r.done_s)))
         return out
+
+    def stats(self):
+        """Counters since open (ptw_serve_stats) as a dict."""
+        st = C.ServeStats()
+        C.check(self._lib.ptw_serve_get_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in st._fields_}
 
     def drain(self):
         out = []
@@ -113,7 +130,7 @@ def open_loop(server, sources, budgets, rate, seed=0, query_id0=0, keep_results=
             n_done += 1
             if keep_results:
                 results[i] = r
-    span =done_at.max() - arrive.min()
+    span = done_at.max() - arrive.min()
     out = dict(n=n, rate=rate, qps=n / span, p50_ms=1000 * float(np.percentile(lat, 50)),
                p99_ms=1000 * float(np.percentile(lat, 99)), mean_ms=1000 * float(lat.mean()),
                span_s=float(span))

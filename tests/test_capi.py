@@ -39,7 +39,8 @@ def test_struct_layouts(tmp_path):
     structs = {"ptw_graph_info": _capi.GraphInfo, "ptw_walk_cfg": _capi.WalkCfg,
                "ptw_walk_stats": _capi.WalkStats, "ptw_tune": _capi.Tune,
                "ptw_query": _capi.Query, "ptw_batch_cfg": _capi.BatchCfg,
-               "ptw_serve_cfg": _capi.ServeCfg, "ptw_serve_result": _capi.ServeResult}
+               "ptw_serve_cfg": _capi.ServeCfg, "ptw_serve_result": _capi.ServeResult,
+               "ptw_serve_stats": _capi.ServeStats}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ptw.h"', "int main(void){"]
     for cname, py in structs.items():
         lines.append('printf("%%zu\\n", sizeof(%s));' % cname)
@@ -66,6 +67,15 @@ def test_version_and_errors_without_gpu():
     rc = lib.ptw_graph_from_edges(None, None, 0, 0, ctypes.byref(ctypes.c_void_p()))
     assert rc == _capi.PTW_EINVAL
     assert b"empty" in lib.ptw_last_error()
+    row = (ctypes.c_uint64 * 3)(0, 2, 1)
+    col = (ctypes.c_uint32 * 2)(1, 0)
+    rc = lib.ptw_graph_from_csr(row, col, 2, None, ctypes.byref(ctypes.c_void_p()))
+    assert rc == _capi.PTW_EINVAL and b"decreases at row 1" in lib.ptw_last_error()
+    rc = lib.ptw_graph_from_csr(None, col, 0, None, ctypes.byref(ctypes.c_void_p()))
+    assert rc == _capi.PTW_EINVAL
+    out = ctypes.c_double()
+    assert lib.ptw_probe_gather(1 << 30, 3, ctypes.byref(out)) == _capi.PTW_EINVAL
+    assert lib.ptw_probe_gather(16 << 30, 8, ctypes.byref(out)) == _capi.PTW_EINVAL
     rc = lib.ptw_graph_load(b"/nonexistent/file", _capi.PTW_FMT_TEXT, 0, ctypes.byref(ctypes.c_void_p()))
     assert rc == _capi.PTW_EIO
     rc = lib.ptw_graph_load(b"x", 7, 0, ctypes.byref(ctypes.c_void_p()))

@@ -117,3 +117,47 @@ def test_device_fp64_l1_matches_cpu_oracle(gpu, G16, s16_canon, app):
         l1_cpu = np.abs(c / c.sum() - exp / exp.sum()).sum()
         assert abs(l1_dev[i] - l1_cpu) < 1e-8, (i, l1_dev[i], l1_cpu)
         assert 0.0 < l1_dev[i] < 2.0
+
+
+def top_k_of(dense, k):
+    """Oracle top-k: nonzero entries by count descending, then name ascending."""
+    nz = np.nonzero(dense)[0]
+    order = np.lexsort((nz, -dense[nz].astype(np.int64)))
+    keep = nz[order][:k]
+    return keep.astype(np.uint32), dense[keep]
+
+
+@pytest.mark.parametrize("k", [1, 37, 1 << 30])
+def test_batch_top_k_selection(gpu, G16, s16_canon, k):
+    rng = np.random.default_rng(17)
+    nq = 40
+    src = rng.integers(0, G16.n, nq).astype(np.uint32)
+    bud = rng.integers(1, 30000, nq)
+    bud[0] = 1                                   # a single walker: few entries
+    res = gpu.ppr_batch(G16, src, bud, sp=0.2, seed=12, top_k=k)
+    for i in range(nq):
+        want_n, want_c = top_k_of(replay_query(s16_canon, int(src[i]), i, int(bud[i]), 0.2, 12, "visits"), k)
+        names, counts = res.query(i)
+        assert np.array_equal(names, want_n) and np.array_equal(counts, want_c), i
+    with pytest.raises(gpu.PTWError):
+        res.l1()                                 # truncated lists have no L1 against the oracle
+    res.close()
+
+
+def test_top_k_with_wide_names_takes_the_two_sort_path(gpu, s16_canon):
+    """Names near 2^31 leave no room for (query, count, name) in one 64-bit key,
+    so compaction sorts by name and then by count; results must not change."""
+    c = s16_canon
+    rng = np.random.default_rng(23)
+    big = np.sort(rng.choice(np.arange(1 << 30, (1 << 31) - 1, dtype=np.int64), c.n, replace=False)).astype(np.uint32)
+    k, nq = 9, 40
+    with gpu.Graph.from_csr(c.row_ptr, c.col, big) as G:
+        src_idx = rng.integers(0, c.n, nq)
+        bud = rng.integers(1, 20000, nq)
+        res = gpu.ppr_batch(G, big[src_idx], bud, sp=0.2, seed=3, top_k=k)
+        for i in range(nq):
+            dense = replay_query(c, int(src_idx[i]), i, int(bud[i]), 0.2, 3, "visits")
+            want_idx, want_c = top_k_of(dense, k)
+            names, counts = res.query(i)
+            assert np.array_equal(names, big[want_idx]) and np.array_equal(counts, want_c), i
+        res.close()

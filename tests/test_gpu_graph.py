@@ -68,3 +68,53 @@ def test_single_edge_and_errors(gpu):
         assert list(names) == [7, 9] and list(row_ptr) == [0, 1, 1] and list(col) == [1]
     with pytest.raises(gpu.PTWError):
         gpu.Graph.from_edges([], [])
+
+
+def test_from_csr_round_trip_and_unsorted_rows(gpu, s16_canon):
+    c = s16_canon
+    with gpu.Graph.from_csr(c.row_ptr, c.col, c.names) as G:
+        assert_same_graph(G, c)
+    # rows in any order, duplicates and self-loops kept, names default to row indices
+    rng = np.random.default_rng(5)
+    n = 200
+    deg = rng.integers(0, 12, n)
+    deg[-1] = 0                                        # a row no one points to and with no entries
+    row_ptr = np.concatenate([[0], np.cumsum(deg)]).astype(np.uint64)
+    col = rng.integers(0, n - 1, int(row_ptr[-1])).astype(np.uint32)
+    col[:5] = 3                                        # duplicates
+    src = np.repeat(np.arange(n, dtype=np.uint32), deg)
+    col[src == 7] = 7                                  # self-loops
+    with gpu.Graph.from_csr(row_ptr, col) as G:
+        assert_same_graph(G, oracle.canonical_from_edges(src, col))
+        assert n - 1 not in G.export_csr()[0]
+    names = rng.choice(1 << 30, size=n, replace=False).astype(np.uint32)
+    with gpu.Graph.from_csr(row_ptr, col, names) as G:
+        assert_same_graph(G, oracle.canonical_from_edges(names[src], names[col]))
+
+
+def test_from_csr_errors(gpu):
+    ok_row = np.array([0, 2, 3], np.uint64)
+    ok_col = np.array([1, 0, 0], np.uint32)
+    with gpu.Graph.from_csr(ok_row, ok_col) as G:
+        assert G.n == 2 and G.m == 3
+    bad = [
+        (np.array([1, 2, 3], np.uint64), ok_col, None),                    # row_ptr[0] != 0
+        (np.array([0, 2, 1, 3], np.uint64), ok_col, None),                 # decreasing
+        (ok_row, np.array([1, 2, 0], np.uint32), None),                    # column index >= n
+        (ok_row, ok_col, np.array([5, 5], np.uint32)),                     # repeated names
+        (np.array([0, 0, 0], np.uint64), np.zeros(0, np.uint32), None),    # no entries
+    ]
+    for r, c, nm in bad:
+        with pytest.raises(gpu.PTWError) as e:
+            gpu.Graph.from_csr(r, c, nm)
+        assert e.value.code == -1
+    # the library stays usable after each refusal
+    with gpu.Graph.from_csr(ok_row, ok_col, np.array([10, 4], np.uint32)) as G:
+        names, row_ptr, col = G.export_csr()
+        assert list(names) == [4, 10] and list(row_ptr) == [0, 1, 3] and list(col) == [1, 0, 1]
+
+
+def test_gather_probe_reports_a_rate(gpu):
+    small = gpu.probe_gather(1 << 20, 4)        # L2-resident
+    large = gpu.probe_gather(1 << 30, 4)        # far above L2
+    assert small > large > 1e9

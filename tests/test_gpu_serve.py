@@ -128,3 +128,45 @@ def test_chung_lu_graph(gpu):
         assert np.array_equal(fwd, rev) and np.all(s != d)  # symmetric, no loops
         with gpu.Graph.chung_lu(20000, 2.1, 16.0, seed=3) as G2:
             assert np.array_equal(G2.export_csr()[2], col)  # deterministic
+
+
+def test_untaken_results_survive_later_ticks_and_stats(gpu, G16, s16_canon):
+    """Results wait in pinned staging blocks; later ticks must not overwrite a
+    block that an untaken result still refers to."""
+    sp, seed = 0.2, 77
+    rng = np.random.default_rng(9)
+    budgets = rng.integers(200, 20000, 30)
+    with gpu.Server(G16, sp=sp, seed=seed, tick_walkers=8192) as srv:
+        for k in range(30):
+            srv.submit(int(rng.integers(0, G16.n)), int(budgets[k]), k)
+            srv.step(take=False)
+        while srv.n_active or srv.n_pending:
+            srv.step(take=False)
+        st = srv.stats()
+        res = srv.results()
+        assert srv.results() == []
+    assert len(res) == 30
+    for r in res:
+        check(r, s16_canon, sp, seed)
+    assert st["completed"] == 30 and st["walkers"] == int(budgets.sum())
+    assert st["entries"] == sum(len(r["names"]) for r in res)
+    assert st["moves"] > 0 and st["ticks"] >= 30 and st["retries"] == 0
+    assert st["device_ms"] > 0 and st["step_ms"] >= st["collect_ms"] > 0
+    assert st["active"] == 0 and st["pending"] == 0 and st["pinned_bytes"] >= 8 << 20
+
+
+def test_serving_top_k(gpu, G16, s16_canon):
+    sp, seed, k = 0.2, 13, 25
+    rng = np.random.default_rng(4)
+    with gpu.Server(G16, sp=sp, seed=seed, tick_walkers=8192, top_k=k) as srv:
+        for q in range(12):
+            srv.submit(int(rng.integers(0, G16.n)), int(rng.integers(1, 20000)), q)
+        res = srv.drain()
+    assert len(res) == 12
+    for r in res:
+        dense = replay(s16_canon, r["source"], r["query_id"], r["budget"], sp, seed)
+        nz = np.nonzero(dense)[0]
+        order = np.lexsort((nz, -dense[nz].astype(np.int64)))
+        keep = nz[order][:k]
+        assert np.array_equal(r["names"], keep.astype(np.uint32)), r["query_id"]
+        assert np.array_equal(r["counts"], dense[keep]), r["query_id"]
