@@ -51,7 +51,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--tune", default=None,
-                   help="block,ilp,chunk,hot_k[,min_blocks[,paths_ilp]]: fixed launch parameters "
+                   help="block,ilp,chunk,hot_k[,min_blocks[,paths_ilp[,cache_hints[,paths_named[,ext_columns]]]]]: "
+                        "fixed launch parameters "
                         "(skips the autotuner)")
     p.add_argument("--no-batch", action="store_true", help="skip the batched-PPR side line")
     p.add_argument("--no-serve", action="store_true", help="skip the serving side line")
@@ -319,7 +320,8 @@ def get_tune(G, ptw, args, dev_name):
                                                G.n, G.m, args.sp)
     if args.tune:
         v = [int(x) for x in args.tune.split(",")]
-        names = ["block", "ilp", "chunk", "hot_k", "min_blocks", "paths_ilp"]
+        names = ["block", "ilp", "chunk", "hot_k", "min_blocks", "paths_ilp", "cache_hints", "paths_named",
+                 "ext_columns"]
         G.tune = ptw.Tune(**dict(zip(names, v)))
         return G.tune, "fixed"
     path = tune_cache_path()

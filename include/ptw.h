@@ -102,7 +102,11 @@ typedef struct ptw_tune {
     int32_t paths_named;   /* DeepWalk: 1 = keep a {neighbour, name} column copy (8 bytes per
                               CSR entry, built on the first path walk) so a move needs no
                               separate name lookup; 0 = look names up per move */
-    int32_t reserved;
+    int32_t ext_columns;   /* bit 0: count / endpoint walks, bit 1: DeepWalk paths read a
+                              {neighbour, its first column, its degree, its name} column copy
+                              (16 bytes per CSR entry, built on first use), so a move is one
+                              16-byte gather with no row-record load; 0 = off.  Falls back to
+                              off when the copy does not fit. */
 } ptw_tune;
 
 const char *ptw_last_error(void);

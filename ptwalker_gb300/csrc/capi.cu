@@ -510,6 +510,7 @@ extern "C" int ptw_graph_set_tune(ptw_graph *g, const ptw_tune *t)
     int rc = check_tune(*t);
     if (rc) return rc;
     g->tune = *t;
+    drop_unused_columns(g);
     return PTW_OK;
 }
 
@@ -650,13 +651,15 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
     const ptw_tune saved = g->tune;
     ptw_tune bt = saved;
     float bms = 1e30f;
-    const int blocks[] = {256, 512};
+    const int blocks[] = {256, 512, 1024};
     const int ilps[] = {2, 4};
     const int chunks[] = {64, 256};
     const int hots[] = {0, 8192};
     const int minbs[] = {0, 2};
     const int hintss[] = {0, 1};
+    const int exts[] = {0, 1};
     WalkLaunch wl = make_launch(&cfg);
+    for (int ex : exts)
     for (int hn : hintss)
     for (int mb : minbs)
     for (int hk : hots)
@@ -672,6 +675,7 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
                     t.min_blocks = mb;
                     t.cache_hints = hn;
                     t.paths_ilp = 2;
+                    t.ext_columns = ex;  // walks only; the paths sweep sets bit 1
                     float tot = 0;
                     bool ok = true;
                     for (int rep = 0; rep < 3 && ok; ++rep) {
@@ -689,7 +693,8 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
                         bt = t;
                     }
                 }
-    // DeepWalk groups per warp: time a short fixed-length walk for each.
+    // DeepWalk: groups per warp x column layout (extended / name-paired /
+    // plain), timed on a short fixed-length walk each.
     {
         const uint64_t W = std::min<uint64_t>(g->dg.n, 1u << 20);
         const uint32_t L = 16;
@@ -697,14 +702,18 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
         int rc = stage_bytes(g, W * L * 4, &buf);
         if (rc) return rc;
         float best_ms = 1e30f;
+        const int walk_ext = bt.ext_columns & 1;
         bt.paths_ilp = 2;
         bt.paths_named = saved.paths_named;
-        for (int cfg_i = 0; cfg_i < 6; ++cfg_i) {
+        for (int cfg_i = 0; cfg_i < 9; ++cfg_i) {
             const int G = cfg_i % 3 == 0 ? 1 : cfg_i % 3 == 1 ? 2 : 4;
-            const int named = cfg_i < 3 ? 1 : 0;
+            const int layout = cfg_i / 3;  // 0 extended, 1 name-paired, 2 plain
+            const int named = layout == 1 ? 1 : 0;
+            const int ext = walk_ext | (layout == 0 ? 2 : 0);
             g->tune = bt;
             g->tune.paths_ilp = G;
             g->tune.paths_named = named;
+            g->tune.ext_columns = ext;
             float tot = 0;
             for (int rep = 0; rep < 3; ++rep) {
                 PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
@@ -720,10 +729,12 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
                 best_ms = tot;
                 bt.paths_ilp = G;
                 bt.paths_named = named;
+                bt.ext_columns = ext;
             }
         }
     }
     g->tune = bt;
+    drop_unused_columns(g);
     if (best) *best = bt;
     return PTW_OK;
 }

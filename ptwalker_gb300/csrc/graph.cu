@@ -355,6 +355,7 @@ void graph_release(ptw_graph *g)
     cudaFree(g->dg.idx2int);
     cudaFree(g->dg.int2idx);
     cudaFree(g->dg.col_named);
+    cudaFree(g->dg.col_ext);
     cudaFree(g->sc.counts);
     cudaFree(g->sc.ctrl);
     cudaFree(g->sc.sources);

@@ -66,6 +66,15 @@ __device__ __forceinline__ uint2 ld_hint_u2(const uint2 *p, uint64_t pol)
     return r;
 }
 
+__device__ __forceinline__ uint4 ld_hint_u4(const uint4 *p, uint64_t pol)
+{
+    uint4 r;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+        : "l"(p), "l"(pol));
+    return r;
+}
+
 __device__ __forceinline__ uint32_t ld_hint_u32(const uint32_t *p, uint64_t pol)
 {
     uint32_t r;
@@ -92,6 +101,8 @@ struct DeviceGraph {
     uint32_t *idx2int = nullptr;  // [n] canonical index (name rank) -> internal
     uint32_t *int2idx = nullptr;  // [n] internal -> canonical index
     uint2 *col_named = nullptr;   // [m] {neighbour internal id, its name}; built on first path walk
+    uint4 *col_ext = nullptr;     // [m] {neighbour id, its first column, its degree, its name};
+                                  // built on the first walk with tune.ext_columns
 };
 
 // Scratch owned by a graph handle and reused by every call.
@@ -161,6 +172,8 @@ cudaError_t pooled_alloc_async(void **p, size_t bytes, cudaStream_t st);
 
 int launch_counts_by_name(ptw_graph *g, uint32_t *d_out);
 int check_tune(const ptw_tune &t);
+// Frees the column copies the graph's tune no longer reads.
+void drop_unused_columns(ptw_graph *g);
 
 // The query table a batch was run with (batch.cu).
 const ptw_query *batch_queries(const ptw_batch *b);

@@ -16,6 +16,10 @@
 //   v = col[off + mulhi(u.x, deg)]           one 4-byte random load
 //   counts[v] += 1                           one fire-and-forget reduction
 //   stop iff u.y < floor(sp * 2^32)
+// With the extended column copy (EXT) the column entry also carries the
+// neighbour's {off, deg} (and name), so a move is one dependent 16-byte
+// gather: the walker keeps {off, deg} of its vertex in registers and loads a
+// row record only at its start vertex.
 //
 // K3 k_paths: DeepWalk (src/core/deepwalk.cpp:25-28).  One walker per lane,
 // all walks the same length, so a warp stays converged.  Each warp stages the
@@ -36,6 +40,7 @@ __device__ __forceinline__ uint64_t umin64(uint64_t x, uint64_t y) { return x < 
 struct WalkArgs {
     const uint2 *__restrict__ adj;
     const uint32_t *__restrict__ col;
+    const uint4 *__restrict__ col_ext;       // EXT: {id, first column, degree, name} per entry
     const uint32_t *__restrict__ start_map;  // canonical index -> internal
     const uint32_t *__restrict__ sources;    // internal ids
     const uint32_t *__restrict__ int2name;
@@ -75,7 +80,7 @@ __device__ __forceinline__ void count_visit(const WalkArgs &a, uint32_t *s_hot, 
     else red_add_hint(&a.counts[v], 1u, pol);
 }
 
-template <bool ENDPOINT, int ILP, bool HOT>
+template <bool ENDPOINT, int ILP, bool HOT, bool EXT>
 __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
 {
     if (HOT) {
@@ -89,12 +94,14 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
 
     uint64_t wid[ILP];
     uint32_t v[ILP], step[ILP], s0[ILP];
-    bool act[ILP];
+    bool act[ILP], have[ILP];
+    uint2 rec[ILP];  // {first column, degree} of v (kept across moves with EXT)
 #pragma unroll
     for (int k = 0; k < ILP; ++k) {
-        act[k] = false;
+        act[k] = have[k] = false;
         wid[k] = 0;
         v[k] = step[k] = s0[k] = 0;
+        rec[k] = make_uint2(0u, 0u);
     }
     // Warp-uniform walker-id range [next, end) relative to w_begin.
     uint64_t next = 0, end = 0;
@@ -135,6 +142,7 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
                 s0[k] = v[k];
                 step[k] = 0;
                 act[k] = true;
+                have[k] = false;
                 if (!ENDPOINT) count_visit<HOT>(a, s_hot, v[k], pol_keep);
             }
         }
@@ -144,10 +152,9 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
         if (!__any_sync(kFull, any)) break;
 
         // ---- one move for every active slot --------------------------------
-        uint2 rec[ILP];
 #pragma unroll
         for (int k = 0; k < ILP; ++k)
-            if (act[k]) rec[k] = ld_hint_u2(&a.adj[v[k]], pol_keep);
+            if (act[k] && !(EXT && have[k])) rec[k] = ld_hint_u2(&a.adj[v[k]], pol_keep);
         uint4 r[ILP];
 #pragma unroll
         for (int k = 0; k < ILP; ++k)
@@ -155,10 +162,20 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
                 r[k] = philox(make_uint4((uint32_t)wid[k], (uint32_t)(wid[k] >> 32), step[k], PTW_TAG_WALK),
                               a.key0, a.key1);
         uint32_t nb[ILP];
+        uint2 nrec[ILP];
 #pragma unroll
-        for (int k = 0; k < ILP; ++k)
-            if (act[k] && rec[k].y != 0)
-                nb[k] = ld_hint_u32(&a.col[rec[k].x + __umulhi(r[k].x, rec[k].y)], pol_stream);
+        for (int k = 0; k < ILP; ++k) {
+            if (act[k] && rec[k].y != 0) {
+                const uint32_t e = rec[k].x + __umulhi(r[k].x, rec[k].y);
+                if (EXT) {
+                    const uint4 x = ld_hint_u4(&a.col_ext[e], pol_stream);
+                    nb[k] = x.x;
+                    nrec[k] = make_uint2(x.y, x.z);
+                } else {
+                    nb[k] = ld_hint_u32(&a.col[e], pol_stream);
+                }
+            }
+        }
 #pragma unroll
         for (int k = 0; k < ILP; ++k) {
             if (!act[k]) continue;
@@ -167,6 +184,10 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
                 done = true;  // no out-edge: the walk ends here
             } else {
                 v[k] = nb[k];
+                if (EXT) {
+                    rec[k] = nrec[k];
+                    have[k] = true;
+                }
                 ++step[k];
                 ++moves;
                 if (!ENDPOINT) count_visit<HOT>(a, s_hot, v[k], pol_keep);
@@ -196,26 +217,27 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
 
 // Register budget chosen by the compiler (ILP=4: 72 registers, one
 // 512-thread block per SM).
-template <bool ENDPOINT, int ILP, bool HOT>
+template <bool ENDPOINT, int ILP, bool HOT, bool EXT>
 __global__ void k_walk(const WalkArgs a)
 {
     extern __shared__ uint32_t s_hot[];
-    walk_body<ENDPOINT, ILP, HOT>(a, s_hot);
+    walk_body<ENDPOINT, ILP, HOT, EXT>(a, s_hot);
 }
 
 // At most 64 registers so two 512-thread blocks fit on an SM: twice the
 // walkers in flight for the latency-bound gathers.
-template <bool ENDPOINT, int ILP, bool HOT>
+template <bool ENDPOINT, int ILP, bool HOT, bool EXT>
 __global__ void __launch_bounds__(512, 2) k_walk_b2(const WalkArgs a)
 {
     extern __shared__ uint32_t s_hot[];
-    walk_body<ENDPOINT, ILP, HOT>(a, s_hot);
+    walk_body<ENDPOINT, ILP, HOT, EXT>(a, s_hot);
 }
 
 struct PathArgs {
     const uint2 *__restrict__ adj;
     const uint32_t *__restrict__ col;
     const uint2 *__restrict__ col_named;  // {internal id, name} per column entry
+    const uint4 *__restrict__ col_ext;    // {internal id, first column, degree, name} per entry
     const uint32_t *__restrict__ start_map;
     const uint32_t *__restrict__ sources;
     const uint32_t *__restrict__ int2name;
@@ -231,10 +253,12 @@ struct PathArgs {
 constexpr int kPathWarps = 4;  // warps per block
 
 // G groups of 32 consecutive walkers per warp (one walker of each group per
-// lane), stepped together so a lane has G gathers in flight.  NAMED reads
-// {internal id, name} pairs from col_named, so a move costs two random reads
-// (row record, column pair) instead of three (plus the name lookup).
-template <int G, bool NAMED>
+// lane), stepped together so a lane has G gathers in flight.  MODE 0 reads
+// the row record, the column entry and the neighbour's name (three random
+// reads per move); MODE 1 reads {internal id, name} pairs from col_named (two:
+// row record, pair); MODE 2 reads {id, first column, degree, name} from
+// col_ext and keeps the row record in registers (one).
+template <int G, int MODE>
 __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
 {
     // C path positions are staged per walker before a flush; rows are padded
@@ -261,6 +285,7 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
         uint64_t wid[G];
         uint32_t v[G], rows[G];
         bool dead[G];
+        uint2 rec[G];
 #pragma unroll
         for (int g = 0; g < G; ++g) {
             const uint64_t grp = g0 + g;
@@ -270,6 +295,7 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
             rows[g] = grp < n_groups ? (uint32_t)umin64(32, a.n_walk - grp * 32) : 0;
             v[g] = valid ? start_vertex(sa, wid[g]) : 0;
             dead[g] = !valid;
+            if (MODE == 2) rec[g] = valid ? ld_hint_u2(&a.adj[v[g]], pol_keep) : make_uint2(0u, 0u);
             stage[wib][g][lane][0] = valid ? (int32_t)a.int2name[v[g]] : -1;
         }
         uint32_t c0 = 0;  // path position of stage column 0
@@ -289,10 +315,11 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
                 c0 = p;
                 if (p == a.L) break;
             }
-            uint2 rec[G];
+            if (MODE != 2) {
 #pragma unroll
-            for (int g = 0; g < G; ++g)
-                if (!dead[g]) rec[g] = ld_hint_u2(&a.adj[v[g]], pol_keep);
+                for (int g = 0; g < G; ++g)
+                    if (!dead[g]) rec[g] = ld_hint_u2(&a.adj[v[g]], pol_keep);
+            }
             uint4 r[G];
 #pragma unroll
             for (int g = 0; g < G; ++g)
@@ -305,7 +332,12 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
                 if (!dead[g]) {
                     if (rec[g].y == 0) {
                         dead[g] = true;
-                    } else if (NAMED) {
+                    } else if (MODE == 2) {
+                        const uint4 cx = ld_hint_u4(&a.col_ext[rec[g].x + __umulhi(r[g].x, rec[g].y)], pol_stream);
+                        v[g] = cx.x;
+                        rec[g] = make_uint2(cx.y, cx.z);
+                        nm[g] = cx.w;
+                    } else if (MODE == 1) {
                         const uint2 cn = ld_hint_u2(&a.col_named[rec[g].x + __umulhi(r[g].x, rec[g].y)], pol_stream);
                         v[g] = cn.x;
                         nm[g] = cn.y;
@@ -317,7 +349,7 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
 #pragma unroll
             for (int g = 0; g < G; ++g) {
                 int32_t out = -1;
-                if (!dead[g]) out = NAMED ? (int32_t)nm[g] : (int32_t)ld_hint_u32(&a.int2name[v[g]], pol_keep);
+                if (!dead[g]) out = MODE != 0 ? (int32_t)nm[g] : (int32_t)ld_hint_u32(&a.int2name[v[g]], pol_keep);
                 stage[wib][g][lane][p - c0] = out;
             }
         }
@@ -332,6 +364,17 @@ __global__ void k_name_columns(const uint32_t *col, const uint32_t *int2name, ui
     }
 }
 
+// {neighbour id, its first column, its degree, its name} for every entry.
+__global__ void k_ext_columns(const uint32_t *col, const uint2 *adj, const uint32_t *int2name, uint64_t m,
+                              uint4 *col_ext)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = col[e];
+        const uint2 r = adj[c];
+        col_ext[e] = make_uint4(c, r.x, r.y, int2name[c]);
+    }
+}
+
 __global__ void k_counts_by_name(const uint32_t *counts, const uint32_t *int2name, uint32_t n,
                                  uint32_t *out)
 {
@@ -339,57 +382,73 @@ __global__ void k_counts_by_name(const uint32_t *counts, const uint32_t *int2nam
         out[int2name[i]] = counts[i];
 }
 
-template <bool E, int ILP, bool H> void *walk_fn() { return (void *)k_walk<E, ILP, H>; }
-template <bool E, int ILP, bool H> void *walk_fn_b2() { return (void *)k_walk_b2<E, ILP, H>; }
-
-void *pick_walk_b2(bool endpoint, int ilp, bool hot)
+template <bool E, int ILP, bool H, bool X> void *walk_fn(bool b2)
 {
-    if (endpoint) {
-        switch (ilp) {
-        case 1: return walk_fn_b2<true, 1, false>();
-        case 4: return walk_fn_b2<true, 4, false>();
-        default: return walk_fn_b2<true, 2, false>();
-        }
-    }
-    if (hot) {
-        switch (ilp) {
-        case 1: return walk_fn_b2<false, 1, true>();
-        case 4: return walk_fn_b2<false, 4, true>();
-        default: return walk_fn_b2<false, 2, true>();
-        }
-    }
+    return b2 ? (void *)k_walk_b2<E, ILP, H, X> : (void *)k_walk<E, ILP, H, X>;
+}
+
+template <bool E, bool H, bool X> void *walk_fn_ilp(int ilp, bool b2)
+{
     switch (ilp) {
-    case 1: return walk_fn_b2<false, 1, false>();
-    case 4: return walk_fn_b2<false, 4, false>();
-    default: return walk_fn_b2<false, 2, false>();
+    case 1: return walk_fn<E, 1, H, X>(b2);
+    case 4: return walk_fn<E, 4, H, X>(b2);
+    default: return walk_fn<E, 2, H, X>(b2);
     }
 }
 
-void *pick_walk(bool endpoint, int ilp, bool hot, int min_blocks)
+template <bool X> void *pick_walk_x(bool endpoint, int ilp, bool hot, bool b2)
 {
-    if (min_blocks == 2) return pick_walk_b2(endpoint, ilp, hot);
-    if (endpoint) {
-        switch (ilp) {
-        case 1: return walk_fn<true, 1, false>();
-        case 4: return walk_fn<true, 4, false>();
-        default: return walk_fn<true, 2, false>();
-        }
+    if (endpoint) return walk_fn_ilp<true, false, X>(ilp, b2);
+    if (hot) return walk_fn_ilp<false, true, X>(ilp, b2);
+    return walk_fn_ilp<false, false, X>(ilp, b2);
+}
+
+void *pick_walk(bool endpoint, int ilp, bool hot, int min_blocks, bool ext)
+{
+    const bool b2 = min_blocks == 2;
+    return ext ? pick_walk_x<true>(endpoint, ilp, hot, b2) : pick_walk_x<false>(endpoint, ilp, hot, b2);
+}
+
+// Builds the extended column copy on first use; false (and no error) when
+// it does not fit in device memory, so the caller walks without it.
+bool ensure_ext_columns(ptw_graph *g)
+{
+    if (g->dg.col_ext) return true;
+    const DeviceGraph &dg = g->dg;
+    uint4 *cx = nullptr;
+    if (cudaMalloc(&cx, std::max<uint64_t>(dg.m, 1) * sizeof(uint4)) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
     }
-    if (hot) {
-        switch (ilp) {
-        case 1: return walk_fn<false, 1, true>();
-        case 4: return walk_fn<false, 4, true>();
-        default: return walk_fn<false, 2, true>();
-        }
+    const unsigned grid = (unsigned)std::min<uint64_t>((dg.m + 255) / 256, (uint64_t)g->num_sms * 64);
+    k_ext_columns<<<std::max(grid, 1u), 256, 0, g->stream>>>(dg.col, dg.adj, dg.int2name, dg.m, cx);
+    if (cudaGetLastError() != cudaSuccess) {
+        cudaFree(cx);
+        return false;
     }
-    switch (ilp) {
-    case 1: return walk_fn<false, 1, false>();
-    case 4: return walk_fn<false, 4, false>();
-    default: return walk_fn<false, 2, false>();
-    }
+    g->dg.col_ext = cx;
+    g->device_bytes += dg.m * sizeof(uint4);
+    return true;
 }
 
 }  // namespace
+
+void drop_unused_columns(ptw_graph *g)
+{
+    DeviceGraph &dg = g->dg;
+    if (dg.col_ext && !g->tune.ext_columns) {
+        cudaStreamSynchronize(g->stream);
+        cudaFree(dg.col_ext);
+        dg.col_ext = nullptr;
+        g->device_bytes -= dg.m * sizeof(uint4);
+    }
+    if (dg.col_named && ((g->tune.ext_columns & 2) || !g->tune.paths_named)) {
+        cudaStreamSynchronize(g->stream);
+        cudaFree(dg.col_named);
+        dg.col_named = nullptr;
+        g->device_bytes -= dg.m * sizeof(uint2);
+    }
+}
 
 int check_tune(const ptw_tune &t)
 {
@@ -408,6 +467,7 @@ int check_tune(const ptw_tune &t)
         return fail(PTW_EINVAL, "tune.paths_ilp must be 1, 2 or 4 (0 = default)");
     if (t.cache_hints != 0 && t.cache_hints != 1) return fail(PTW_EINVAL, "tune.cache_hints must be 0 or 1");
     if (t.paths_named != 0 && t.paths_named != 1) return fail(PTW_EINVAL, "tune.paths_named must be 0 or 1");
+    if (t.ext_columns < 0 || t.ext_columns > 3) return fail(PTW_EINVAL, "tune.ext_columns must be in [0, 3]");
     return PTW_OK;
 }
 
@@ -439,7 +499,9 @@ int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t)
     a.start_mode = wl.start_mode;
     a.hints = t.cache_hints;
 
-    void *fn = pick_walk(wl.endpoint, t.ilp, hot, t.min_blocks);
+    const bool ext = (t.ext_columns & 1) && ensure_ext_columns(g);
+    a.col_ext = g->dg.col_ext;
+    void *fn = pick_walk(wl.endpoint, t.ilp, hot, t.min_blocks, ext);
     const size_t smem = hot ? (size_t)a.hot_k * 4 : 0;
     if (smem > 48 * 1024)
         PTW_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -479,9 +541,12 @@ int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uin
     a.n_sources = n_sources;
     a.start_mode = start_mode;
     a.hints = g->tune.cache_hints;
-    // Name-paired columns: built once on the first path walk (8 bytes per
-    // CSR entry); without them the kernel looks names up per move.
-    bool named = g->tune.paths_named != 0;
+    // Extended columns (16 bytes per CSR entry) take precedence; then
+    // name-paired columns, built once on the first path walk (8 bytes per
+    // CSR entry); without either the kernel looks names up per move.
+    const bool ext = (g->tune.ext_columns & 2) && ensure_ext_columns(g);
+    a.col_ext = g->dg.col_ext;
+    bool named = !ext && g->tune.paths_named != 0;
     if (named && !g->dg.col_named) {
         uint2 *cn = nullptr;
         if (cudaMalloc(&cn, std::max<uint64_t>(dg.m, 1) * sizeof(uint2)) == cudaSuccess) {
@@ -498,12 +563,12 @@ int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uin
     a.col_named = g->dg.col_named;
     const int G = g->tune.paths_ilp == 1 || g->tune.paths_ilp == 4 ? g->tune.paths_ilp : 2;
     const void *fn;
-    if (named)
-        fn = G == 1 ? (const void *)k_paths<1, true> : G == 4 ? (const void *)k_paths<4, true>
-                                                              : (const void *)k_paths<2, true>;
+    if (ext)
+        fn = G == 1 ? (const void *)k_paths<1, 2> : G == 4 ? (const void *)k_paths<4, 2> : (const void *)k_paths<2, 2>;
+    else if (named)
+        fn = G == 1 ? (const void *)k_paths<1, 1> : G == 4 ? (const void *)k_paths<4, 1> : (const void *)k_paths<2, 1>;
     else
-        fn = G == 1 ? (const void *)k_paths<1, false> : G == 4 ? (const void *)k_paths<4, false>
-                                                               : (const void *)k_paths<2, false>;
+        fn = G == 1 ? (const void *)k_paths<1, 0> : G == 4 ? (const void *)k_paths<4, 0> : (const void *)k_paths<2, 0>;
     int per_sm = 0;
     PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPathWarps * 32, 0));
     per_sm = std::max(per_sm, 1);

@@ -71,6 +71,10 @@ def test_ppr_sources_and_query_ids(gpu, G16, s16_canon, sources, W, qid):
     dict(block=128, ilp=2, chunk=7, hot_k=100, min_blocks=2),
     dict(block=512, ilp=4, chunk=256, hot_k=8192, cache_hints=1),
     dict(block=256, ilp=2, chunk=64, hot_k=0, min_blocks=2, cache_hints=1),
+    dict(block=512, ilp=4, chunk=256, hot_k=8192, cache_hints=1, ext_columns=1),
+    dict(block=256, ilp=1, chunk=5, hot_k=0, cache_hints=0, ext_columns=1),
+    dict(block=128, ilp=2, chunk=64, hot_k=300, min_blocks=2, ext_columns=1),
+    dict(block=512, ilp=4, chunk=64, hot_k=0, min_blocks=2, ext_columns=1),
 ])
 def test_launch_parameters_do_not_change_results(gpu, G16, s16_canon, tune):
     saved = G16.tune
@@ -110,15 +114,17 @@ def test_deepwalk_paths_bit_exact(gpu, G16, s16_canon, L, W, start):
     assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("paths_ilp,hints,named", [(1, 0, 0), (2, 0, 0), (4, 0, 1), (2, 1, 1), (4, 1, 0),
-                                                   (1, 1, 1)])
-def test_deepwalk_groups_per_warp(gpu, G16, s16_canon, paths_ilp, hints, named):
+@pytest.mark.parametrize("paths_ilp,hints,named,ext", [(1, 0, 0, 0), (2, 0, 0, 0), (4, 0, 1, 0), (2, 1, 1, 0),
+                                                       (4, 1, 0, 0), (1, 1, 1, 0), (1, 1, 0, 2), (2, 1, 1, 3),
+                                                       (4, 0, 0, 2), (2, 0, 1, 1)])
+def test_deepwalk_groups_per_warp(gpu, G16, s16_canon, paths_ilp, hints, named, ext):
     saved = G16.tune
     try:
         t = G16.tune
         t.paths_ilp = paths_ilp
         t.cache_hints = hints
         t.paths_named = named
+        t.ext_columns = ext
         G16.tune = t
         for W, L in ((G16.n, 40), (4096 + 33, 7), (65, 33)):
             got = gpu.deepwalk(G16, W, L, 17)
@@ -243,3 +249,20 @@ def test_pagerank_vs_fp64_oracle(gpu, G16, s16_canon):
     assert l1 <= 1.5 * max(ref_l1), (l1, ref_l1)
     zz = (got - exp) / np.sqrt(exp)
     assert abs(zz.mean()) < 0.05 and zz.std() < 1.5
+
+
+def test_rwr_and_ppr_with_extended_columns(gpu, G16, s16_canon):
+    saved = G16.tune
+    try:
+        G16.tune = gpu.Tune(block=256, ilp=4, chunk=64, hot_k=0, ext_columns=3)
+        got = gpu.rwr(G16, 3 * G16.n, 0.3, 29, "uniform")
+        want, _ = oracle.replay_pairs(s16_canon, 0, 3 * G16.n, 0.3, 29, START_UNIFORM)
+        assert np.array_equal(got, want)
+        got = gpu.ppr(G16, 77, 50000, 0.2, 5, query_id=9)
+        want, _ = oracle.replay_counts(s16_canon, 9 << 32, (9 << 32) + 50000, 0.2, 5, START_SOURCES, [77])
+        assert np.array_equal(got, want)
+        with_ext = G16.device_bytes
+    finally:
+        G16.tune = saved
+    # turning the copy off releases its 16 bytes per CSR entry
+    assert with_ext - G16.device_bytes == 16 * G16.m
