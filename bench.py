@@ -11,9 +11,14 @@ removed (synthetic, built on the device).  Each step uses a new seed.
   e2e       the same through the host-facing C ABI call ptw_pagerank,
             counts read back into pinned host memory every step
   roofline  random-gather bound: 64 B per move (row record + column
-            sector) + 32 B per counted visit, against the measured HBM peak
+            sector) + 32 B per counted visit, against the measured HBM peak;
+            traffic = the ncu DRAM bytes per move of the committed scale-24
+            capture times this run's moves per launch; gather_peak = random
+            4-byte loads/s this GPU serves from a 2 GB array, measured here
   cpu_baseline  the oracle port (C, all host threads) on a bounded sample of
             the same workload
+  graph_replay  the same timed steps captured in one CUDA graph and
+            replayed once (no host launch gaps)
 
 --impl reference times the reference's walker semantics on the host CPU
 (the oracle port; the reference's own sources do not exist on the GPU host)
@@ -76,7 +81,16 @@ def config(args, world):
                         % (args.scale, args.edge_factor, args.seed, args.sp),
             "graph": "rmat-s%d-ef%d" % (args.scale, args.edge_factor),
             "walkers_per_gpu": "|V|", "sp": args.sp, "parallelism": "walker-shard x%d" % world,
-            "l2": "inputs exceed L2 (CSR column array > 2 GB, L2 129 MB); no flush"}
+            "l2": l2_note(args)}
+
+
+def l2_note(args):
+    """R-MAT with edge factor ef keeps about 1.9 * ef * 2^scale CSR entries after
+    symmetrising and de-duplication at these quadrant probabilities."""
+    col_bytes = 4 * 1.9 * args.edge_factor * (1 << args.scale)
+    if col_bytes > 2 * 129e6:
+        return "inputs exceed L2 (CSR column array about %.1f GB, L2 129 MB); no flush" % (col_bytes / 1e9)
+    return "small graph: CSR column array about %.0f MB may sit in the 129 MB L2; no flush" % (col_bytes / 1e6)
 
 
 # ---- clocks ---------------------------------------------------------------
@@ -347,6 +361,38 @@ def get_tune(G, ptw, args, dev_name):
     return t, "autotune"
 
 
+def graph_replay(G, ptw, torch, stream, args, seeds, d_counts, first, total_moves):
+    """The timed steps again, captured into one CUDA graph and replayed once
+    (same seeds, so the same moves): the step loop without host launch gaps."""
+    try:
+        cg = torch.cuda.CUDAGraph()
+        torch.cuda.synchronize()
+        with torch.cuda.graph(cg, stream=stream):
+            for k in range(args.steps):
+                ptw.pagerank(G, G.n, args.sp, seeds[k], "per_vertex", out=d_counts, first_walker=first)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):  # replay where the events are recorded
+            cg.replay()  # warm-up replay
+            torch.cuda.synchronize()
+            e0.record(stream)
+            cg.replay()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        del cg
+        # the replay's last step left its counts in d_counts: check them
+        # against the same step run directly
+        direct = torch.empty_like(d_counts)
+        ptw.pagerank(G, G.n, args.sp, seeds[-1], "per_vertex", out=direct, first_walker=first)
+        torch.cuda.synchronize()
+        return {"steps": args.steps, "ms_per_step": ms / args.steps, "value": total_moves / (ms / 1000.0),
+                "unit": UNIT, "last_step_equals_direct_call": bool(torch.equal(direct, d_counts))}
+    except Exception as e:  # report, do not fail the headline
+        torch.cuda.synchronize()
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -515,6 +561,9 @@ def run_ours(args):
         "moves_per_step": sum(moves) / len(moves),
         "deepwalk": deepwalk,
     }
+    if world == 1:
+        line["graph_replay"] = graph_replay(G, ptw, torch, stream, args, seeds, d_counts, first,
+                                            sum(moves))
     G.set_stream(None)
     G.close()
     if rank == 0 and world == 1:

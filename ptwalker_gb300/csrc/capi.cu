@@ -676,18 +676,21 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
                     t.cache_hints = hn;
                     t.paths_ilp = 2;
                     t.ext_columns = ex;  // walks only; the paths sweep sets bit 1
-                    float tot = 0;
+                    // median of four timed launches after one warm-up: the
+                    // candidates differ by a few percent, so one noisy
+                    // launch must not pick the winner
+                    float ms_rep[5] = {0, 0, 0, 0, 0};
                     bool ok = true;
-                    for (int rep = 0; rep < 3 && ok; ++rep) {
+                    for (int rep = 0; rep < 5 && ok; ++rep) {
                         PTW_CUDA(cudaMemsetAsync(g->sc.counts, 0, (uint64_t)g->dg.n * 4, g->stream));
                         PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
                         if (launch_walk(g, wl, t) != PTW_OK) ok = false;
                         PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
                         PTW_CUDA(cudaEventSynchronize(g->ev[1]));
-                        float ms = 0;
-                        PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]));
-                        if (rep) tot += ms;  // first run warms up
+                        PTW_CUDA(cudaEventElapsedTime(&ms_rep[rep], g->ev[0], g->ev[1]));
                     }
+                    std::sort(ms_rep + 1, ms_rep + 5);
+                    const float tot = 0.5f * (ms_rep[2] + ms_rep[3]);
                     if (ok && tot < bms) {
                         bms = tot;
                         bt = t;

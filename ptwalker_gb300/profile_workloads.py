@@ -29,6 +29,8 @@ def main(argv=None):
     p.add_argument("--sp", type=float, default=0.15)
     p.add_argument("--n", type=int, default=8_400_000, help="Chung-Lu vertices (serve)")
     p.add_argument("--top-k", type=int, default=1000)
+    p.add_argument("--tune", default=None,
+                   help="launch parameters as name=value pairs, e.g. block=1024,ilp=2,hot_k=8192")
     a = p.parse_args(argv)
 
     import torch
@@ -75,6 +77,9 @@ def main(argv=None):
         return
     G = ptw.Graph.rmat(a.scale, 16, seed=1, clean=True)
     out.update(vertices=G.n, edges=G.m)
+    if a.tune:
+        G.tune = ptw.Tune(**{k: int(v) for k, v in (kv.split("=") for kv in a.tune.split(","))})
+        out["tune"] = G.tune.as_dict()
     if a.what == "pagerank":
         dev = torch.empty(G.id_bound, dtype=torch.int32, device="cuda")
         ptw.pagerank(G, G.n, a.sp, 1, out=dev)
