@@ -12,13 +12,18 @@
 //   query id and the walker's rank in its query only, so a query's counts are
 //   the same alone or in any batch and wave.
 //
-// Per-query counts are kept sparse in open-addressing tables of 64-bit slots
-// (vertex internal id + 1 in the high half, count in the low half), sized
-// from the query's budget; a query that finds no free slot within the probe
-// limit raises its flag and the host runs it again with a table of 2n slots,
-// which cannot fill.  Waves take queries in order while their tables fit the
-// table budget (admission by device memory).  After a wave the tables are
-// compacted into (name, count) lists sorted by name and copied to the host.
+// Per-query counts of a small query are kept sparse in an open-addressing
+// table of 64-bit slots (vertex internal id + 1 in the high half, count in the
+// low half), sized from the query's budget; a query that finds no free slot
+// within the probe limit raises its flag and the host runs it again with a
+// dense array.  A query whose table would take at least 4n bytes counts into
+// a dense array of n 32-bit counters indexed by canonical vertex index: a
+// visit is one fire-and-forget reduction instead of a probe, and the array
+// is already in name order, so its compaction needs no sort.  Waves take
+// queries in order while their tables fit the table budget (admission by
+// device memory).  After a wave the tables are compacted into (name, count)
+// lists sorted by name (or each query's top k by count) and copied to the
+// host.
 #include <cub/cub.cuh>
 
 #include <algorithm>
@@ -27,7 +32,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
 #include <vector>
+
+#include <unistd.h>
 
 #include "batch_kernels.cuh"
 
@@ -56,6 +64,44 @@ namespace ptw {
 namespace {
 
 constexpr uint64_t kMaxBudget = 1ull << 28;
+
+// Faults in the pages of fresh host buffers from several threads.  A
+// device-to-host copy into pages the process has never touched takes the
+// faults one by one inside the copy (about 6x slower than the copy itself
+// for gigabytes); touching one byte per page first, while the device is
+// still busy, leaves the copy at link speed.
+class Prefault {
+public:
+    void start(std::initializer_list<std::pair<void *, size_t>> bufs)
+    {
+        const long pg = sysconf(_SC_PAGESIZE);
+        const size_t page = pg > 0 ? (size_t)pg : 4096;
+        size_t total = 0;
+        for (auto &b : bufs) total += b.second;
+        if (total < (64u << 20)) return;  // small: the copy absorbs it
+        const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        for (auto &b : bufs) {
+            char *p = (char *)b.first;
+            const size_t len = b.second;
+            for (unsigned t = 0; t < nt; ++t) {
+                const size_t lo = len * t / nt, hi = len * (t + 1) / nt;
+                th_.emplace_back([p, lo, hi, page] {
+                    for (size_t x = lo - lo % page; x < hi; x += page)
+                        if (x >= lo) ((volatile char *)p)[x] = 0;
+                });
+            }
+        }
+    }
+    void join()
+    {
+        for (auto &t : th_) t.join();
+        th_.clear();
+    }
+    ~Prefault() { join(); }
+
+private:
+    std::vector<std::thread> th_;
+};
 
 struct DevBuf {
     cudaStream_t st;
@@ -93,29 +139,46 @@ struct WaveQuery {
     uint32_t src;    // internal id
     uint32_t qid;
     uint64_t budget;
-    uint64_t cap;    // table slots (power of two)
+    uint64_t cap;    // 64-bit slots of its table (a power of two for a hash table)
+    bool dense;      // dense array of n counters instead of a hash table
 };
 
 }  // namespace
 
 // Splits [j0, j0 + count) of every entry into descriptors of at most
-// kDescWalkers ranks, ordered round-robin over the entries.
+// kDescWalkers ranks.  Entries are cut into consecutive groups whose tables
+// add up to about group_bytes (0 = one group); descriptors go round-robin
+// over the entries of a group, and groups follow one another.  Warps take
+// descriptors in order, so the count tables being written at any moment are
+// those of about one group: a few hundred MB stay largely in L2 where the
+// tables of thousands of queries at once would not (1.6x faster walk kernel
+// on 4096 queries at R-MAT scale 22 with 384 MB groups).
 void interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<uint64_t> &count,
+                            const std::vector<uint64_t> &table_bytes, uint64_t group_bytes,
                             std::vector<uint3> &desc)
 {
     desc.clear();
-    std::vector<uint32_t> live;
-    for (uint32_t i = 0; i < count.size(); ++i)
-        if (count[i]) live.push_back(i);
-    for (uint64_t r = 0; !live.empty(); ++r) {
-        size_t keep = 0;
-        for (uint32_t i : live) {
-            const uint64_t off = r * kDescWalkers;
-            const uint64_t c = std::min<uint64_t>(kDescWalkers, count[i] - off);
-            desc.push_back(make_uint3(i, (uint32_t)(j0[i] + off), (uint32_t)c));
-            if (off + c < count[i]) live[keep++] = i;
+    const uint32_t ne = (uint32_t)count.size();
+    for (uint32_t g0 = 0; g0 < ne;) {
+        std::vector<uint32_t> live;
+        uint64_t bytes = 0;
+        uint32_t g1 = g0;
+        while (g1 < ne && (g1 == g0 || group_bytes == 0 || bytes + table_bytes[g1] <= group_bytes)) {
+            bytes += table_bytes[g1];
+            if (count[g1]) live.push_back(g1);
+            ++g1;
         }
-        live.resize(keep);
+        for (uint64_t r = 0; !live.empty(); ++r) {
+            size_t keep = 0;
+            for (uint32_t i : live) {
+                const uint64_t off = r * kDescWalkers;
+                const uint64_t c = std::min<uint64_t>(kDescWalkers, count[i] - off);
+                desc.push_back(make_uint3(i, (uint32_t)(j0[i] + off), (uint32_t)c));
+                if (off + c < count[i]) live[keep++] = i;
+            }
+            live.resize(keep);
+        }
+        g0 = g1;
     }
 }
 
@@ -130,17 +193,21 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     const uint32_t nq = (uint32_t)wq.size();
     std::vector<unsigned long long> h_tab(nq + 1);
     std::vector<uint32_t> h_src(nq), h_qid(nq), h_mask(nq), h_cap(nq);
+    std::vector<uint8_t> h_dense(nq);
     std::vector<uint64_t> j0(nq, 0), cnt(nq);
     for (uint32_t i = 0; i < nq; ++i) {
         h_tab[i + 1] = h_tab[i] + wq[i].cap;
         h_src[i] = wq[i].src;
         h_qid[i] = wq[i].qid;
-        h_mask[i] = (uint32_t)(wq[i].cap - 1);
-        h_cap[i] = (uint32_t)wq[i].cap;
+        h_dense[i] = wq[i].dense ? 1 : 0;
+        h_mask[i] = wq[i].dense ? kDenseMask : (uint32_t)(wq[i].cap - 1);
+        h_cap[i] = wq[i].dense ? g->dg.n : (uint32_t)wq[i].cap;
         cnt[i] = wq[i].budget;
     }
     std::vector<uint3> h_desc;
-    interleave_descriptors(j0, cnt, h_desc);
+    std::vector<uint64_t> tbytes(nq);
+    for (uint32_t i = 0; i < nq; ++i) tbytes[i] = wq[i].cap * 8;
+    interleave_descriptors(j0, cnt, tbytes, kGroupBytes, h_desc);
     const uint64_t n_slots = h_tab[nq], nd = h_desc.size();
     DevBuf db(st);
     unsigned long long *d_tab, *d_slots, *d_ctrl;
@@ -166,6 +233,7 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     BatchArgs a;
     a.adj = g->dg.adj;
     a.col = g->dg.col;
+    a.int2idx = g->dg.int2idx;
     a.desc = d_desc;
     a.q_src = d_src;
     a.q_qid = d_qid;
@@ -195,7 +263,7 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     PTW_CUDA(cudaMemcpyAsync(&h_moves, d_ctrl + 1, 8, cudaMemcpyDeviceToHost, st));
     WaveResult wr;
     wr.c.top_k = cfg->top_k;
-    int rc = compact_tables(g, d_slots, h_tab.data(), h_cap.data(), nq, &wr.c);
+    int rc = compact_tables(g, d_slots, h_tab.data(), h_cap.data(), h_dense.data(), nq, &wr.c);
     if (rc) return rc;
     float ms = 0;
     PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]));
@@ -272,7 +340,7 @@ const ptw_query *batch_queries(const ptw_batch *b) { return b->queries.data(); }
 uint32_t batch_top_k(const ptw_batch *b) { return b->top_k; }
 
 int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned long long *h_base,
-                   const uint32_t *h_cap, uint32_t nt, Compacted *out)
+                   const uint32_t *h_cap, const uint8_t *h_dense, uint32_t nt, Compacted *out)
 {
     out->n = 0;
     out->seg.assign(nt + 1, 0);
@@ -285,16 +353,25 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     auto clk = [] { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
     const double t0 = timing ? (cudaStreamSynchronize(st), clk()) : 0.0;
     double t1 = 0, t2 = 0;
+    Prefault prefault;  // joined before the copies (and on any early return)
+    std::vector<uint8_t> dense_flags(nt, 0);
+    if (h_dense) dense_flags.assign(h_dense, h_dense + nt);
+    std::vector<uint32_t> dl;  // dense tables, in table order
+    for (uint32_t i = 0; i < nt; ++i)
+        if (dense_flags[i]) dl.push_back(i);
     DevBuf db(st);
     unsigned long long *d_base, *d_cnt, *d_seg, *d_fill;
     uint32_t *d_cap;
+    uint8_t *d_dense;
     PTW_CUDA(db.alloc(&d_base, nt));
     PTW_CUDA(db.alloc(&d_cap, nt));
+    PTW_CUDA(db.alloc(&d_dense, nt));
     PTW_CUDA(db.alloc(&d_cnt, nt));
     PTW_CUDA(db.alloc(&d_seg, nt + 1));
     PTW_CUDA(db.alloc(&d_fill, nt));
     PTW_CUDA(cudaMemcpyAsync(d_base, h_base, nt * 8ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_cap, h_cap, nt * 4ull, cudaMemcpyHostToDevice, st));
+    PTW_CUDA(cudaMemcpyAsync(d_dense, dense_flags.data(), nt, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemsetAsync(d_cnt, 0, nt * 8ull, st));
     PTW_CUDA(cudaMemsetAsync(d_fill, 0, nt * 8ull, st));
     PTW_CUDA(cudaMemsetAsync(d_seg, 0, 8, st));
@@ -303,7 +380,8 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     const unsigned gx = (unsigned)std::min<uint64_t>(256, (max_cap + 2047) / 2048);
     for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
         const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
-        k_tabs_count<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(d_slots, d_base + t0, d_cap + t0, d_cnt + t0);
+        k_tabs_count<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(d_slots, d_base + t0, d_cap + t0, d_dense + t0,
+                                                                d_cnt + t0);
     }
     PTW_CUDA(cudaGetLastError());
     PTW_CUDA(cub_call([&](void *t, size_t &b) {
@@ -335,73 +413,123 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             if (!out->names || !out->counts) return fail(PTW_ENOMEM, "host allocation of batch results failed");
             out->h_names = out->names.get();
             out->h_counts = out->counts.get();
+            prefault.start({{out->h_names, n_out * 4}, {out->h_counts, n_out * 4}});
         }
         int name_bits = 1, q_bits = 1;
         while (name_bits < 32 && (1ull << name_bits) < g->dg.id_bound) ++name_bits;
         while ((1ull << q_bits) < nt) ++q_bits;
-        unsigned long long *e_key, *s_key;
-        uint32_t *e_cnt, *s_cnt, *s_name;
-        PTW_CUDA(db.alloc(&e_key, n_ent));
-        PTW_CUDA(db.alloc(&s_key, n_ent));
-        PTW_CUDA(db.alloc(&e_cnt, n_ent));
-        PTW_CUDA(db.alloc(&s_cnt, n_ent));
-        // top-k with (table, ~count, name) in 64 bits: one sort, keys only
-        const bool packed = k && q_bits + 32 + name_bits <= 64;
-        for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
-            const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
-            k_tabs_emit<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(d_slots, d_base + t0, d_cap + t0, d_seg + t0,
-                                                                   d_fill + t0, g->dg.int2name, t0, name_bits,
-                                                                   packed, e_key, e_cnt);
-        }
-        PTW_CUDA(cudaGetLastError());
         const unsigned kg = (unsigned)std::min<uint64_t>((n_ent + 255) / 256, (uint64_t)g->num_sms * 32);
         uint32_t *o_name = nullptr, *o_cnt = nullptr;
-        if (packed) {
-            PTW_CUDA(cub_call([&](void *t, size_t &b) {
-                return cub::DeviceRadixSort::SortKeys(t, b, e_key, s_key, (int64_t)n_ent, 0,
-                                                      q_bits + 32 + name_bits, st);
-            }, st));
-        } else {
-            // one radix sort over (table, name): tables stay in their segments
-            PTW_CUDA(cub_call([&](void *t, size_t &b) {
-                return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_ent, 0,
-                                                       name_bits + q_bits, st);
-            }, st));
-        }
-        if (packed) {
+        if (k) {
+            // Top-k: every table (hash or dense) emits its entries as keys; a
+            // radix sort orders each table by count, the first k are kept.
+            unsigned long long *e_key, *s_key;
+            uint32_t *e_cnt, *s_cnt;
+            PTW_CUDA(db.alloc(&e_key, n_ent));
+            PTW_CUDA(db.alloc(&s_key, n_ent));
+            PTW_CUDA(db.alloc(&e_cnt, n_ent));
+            PTW_CUDA(db.alloc(&s_cnt, n_ent));
+            // (table, ~count, name) in 64 bits: one sort, keys only
+            const bool packed = q_bits + 32 + name_bits <= 64;
+            for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
+                const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
+                k_tabs_emit<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(
+                    d_slots, d_base + t0, d_cap + t0, d_dense + t0, false, d_seg + t0, d_fill + t0, g->dg.int2name,
+                    g->dg.names, t0, name_bits, packed, e_key, e_cnt);
+            }
+            PTW_CUDA(cudaGetLastError());
             unsigned long long *d_kseg;
             PTW_CUDA(db.alloc(&d_kseg, nt + 1));
             PTW_CUDA(db.alloc(&o_name, n_out));
             PTW_CUDA(db.alloc(&o_cnt, n_out));
             PTW_CUDA(cudaMemcpyAsync(d_kseg, kseg.data(), (nt + 1) * 8ull, cudaMemcpyHostToDevice, st));
-            k_topk_copy_packed<<<std::max(kg, 1u), 256, 0, st>>>(s_key, n_ent, name_bits, d_seg, d_kseg, k, o_name,
-                                                                 o_cnt);
-            PTW_CUDA(cudaGetLastError());
-            out->seg = kseg;
-        } else if (k) {
-            // re-key by (table, count descending) with the name as value; the
-            // radix sort is stable, so equal counts stay in name order
-            k_count_keys<<<std::max(kg, 1u), 256, 0, st>>>(s_key, s_cnt, n_ent, name_bits, e_key, e_cnt);
-            PTW_CUDA(cudaGetLastError());
-            PTW_CUDA(cub_call([&](void *t, size_t &b) {
-                return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_ent, 0,
-                                                       32 + q_bits, st);
-            }, st));
-            unsigned long long *d_kseg;
-            PTW_CUDA(db.alloc(&d_kseg, nt + 1));
-            PTW_CUDA(db.alloc(&o_name, n_out));
-            PTW_CUDA(db.alloc(&o_cnt, n_out));
-            PTW_CUDA(cudaMemcpyAsync(d_kseg, kseg.data(), (nt + 1) * 8ull, cudaMemcpyHostToDevice, st));
-            k_topk_copy<<<std::max(kg, 1u), 256, 0, st>>>(s_key, s_cnt, n_ent, d_seg, d_kseg, k, o_name, o_cnt);
+            if (packed) {
+                PTW_CUDA(cub_call([&](void *t, size_t &b) {
+                    return cub::DeviceRadixSort::SortKeys(t, b, e_key, s_key, (int64_t)n_ent, 0,
+                                                          q_bits + 32 + name_bits, st);
+                }, st));
+                k_topk_copy_packed<<<std::max(kg, 1u), 256, 0, st>>>(s_key, n_ent, name_bits, d_seg, d_kseg, k,
+                                                                     o_name, o_cnt);
+            } else {
+                // sort by (table, name), then stably by (table, ~count): equal
+                // counts stay in name order
+                PTW_CUDA(cub_call([&](void *t, size_t &b) {
+                    return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_ent, 0,
+                                                           name_bits + q_bits, st);
+                }, st));
+                k_count_keys<<<std::max(kg, 1u), 256, 0, st>>>(s_key, s_cnt, n_ent, name_bits, e_key, e_cnt);
+                PTW_CUDA(cudaGetLastError());
+                PTW_CUDA(cub_call([&](void *t, size_t &b) {
+                    return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_ent, 0,
+                                                           32 + q_bits, st);
+                }, st));
+                k_topk_copy<<<std::max(kg, 1u), 256, 0, st>>>(s_key, s_cnt, n_ent, d_seg, d_kseg, k, o_name, o_cnt);
+            }
             PTW_CUDA(cudaGetLastError());
             out->seg = kseg;
         } else {
-            s_name = (uint32_t *)e_key;  // reuse the unsorted-key buffer
-            k_key_names<<<std::max(kg, 1u), 256, 0, st>>>(s_key, n_ent, (1ull << name_bits) - 1, s_name);
-            PTW_CUDA(cudaGetLastError());
-            o_name = s_name;
-            o_cnt = s_cnt;
+            // Full lists by name.  Dense tables are already in name order:
+            // their nonzero counters are compacted in place of a sort.  Hash
+            // tables emit (table, name) keys into a separate range, one radix
+            // sort orders them, and they are placed into their segments.
+            PTW_CUDA(db.alloc(&o_name, n_ent));
+            PTW_CUDA(db.alloc(&o_cnt, n_ent));
+            std::vector<uint64_t> hseg(nt + 1, 0);
+            for (uint32_t i = 0; i < nt; ++i)
+                hseg[i + 1] = hseg[i] + (dense_flags[i] ? 0 : out->seg[i + 1] - out->seg[i]);
+            const uint64_t n_hash = hseg[nt];
+            if (n_hash) {
+                unsigned long long *e_key, *s_key, *d_hseg;
+                uint32_t *e_cnt, *s_cnt;
+                PTW_CUDA(db.alloc(&e_key, n_hash));
+                PTW_CUDA(db.alloc(&s_key, n_hash));
+                PTW_CUDA(db.alloc(&e_cnt, n_hash));
+                PTW_CUDA(db.alloc(&s_cnt, n_hash));
+                PTW_CUDA(db.alloc(&d_hseg, nt + 1));
+                PTW_CUDA(cudaMemcpyAsync(d_hseg, hseg.data(), (nt + 1) * 8ull, cudaMemcpyHostToDevice, st));
+                for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
+                    const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
+                    k_tabs_emit<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(
+                        d_slots, d_base + t0, d_cap + t0, d_dense + t0, true, d_hseg + t0, d_fill + t0,
+                        g->dg.int2name, g->dg.names, t0, name_bits, false, e_key, e_cnt);
+                }
+                PTW_CUDA(cudaGetLastError());
+                PTW_CUDA(cub_call([&](void *t, size_t &b) {
+                    return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_hash, 0,
+                                                           name_bits + q_bits, st);
+                }, st));
+                const unsigned hg = (unsigned)std::min<uint64_t>((n_hash + 255) / 256, (uint64_t)g->num_sms * 32);
+                k_place_hash<<<std::max(hg, 1u), 256, 0, st>>>(s_key, s_cnt, n_hash, name_bits, d_seg, d_hseg,
+                                                              o_name, o_cnt);
+                PTW_CUDA(cudaGetLastError());
+            }
+            if (!dl.empty()) {
+                const uint32_t n = g->dg.n;
+                const uint32_t chunks = (n + kDenseChunk - 1) / kDenseChunk;
+                const uint64_t ncc = (uint64_t)dl.size() * chunks;
+                uint32_t *d_dl;
+                unsigned long long *d_cc, *d_cpos;
+                PTW_CUDA(db.alloc(&d_dl, dl.size()));
+                PTW_CUDA(db.alloc(&d_cc, ncc));
+                PTW_CUDA(db.alloc(&d_cpos, ncc));
+                PTW_CUDA(cudaMemcpyAsync(d_dl, dl.data(), dl.size() * 4ull, cudaMemcpyHostToDevice, st));
+                for (uint32_t y0 = 0; y0 < dl.size(); y0 += 65535) {
+                    const uint32_t ny = std::min<uint32_t>(65535, (uint32_t)dl.size() - y0);
+                    k_dense_chunks<<<dim3(chunks, ny), 256, 0, st>>>(d_slots, d_base, d_dl, y0, n, chunks, d_cc);
+                }
+                PTW_CUDA(cudaGetLastError());
+                PTW_CUDA(cub_call([&](void *t, size_t &b) {
+                    return cub::DeviceScan::ExclusiveSum(t, b, d_cc, d_cpos, (int64_t)ncc, st);
+                }, st));
+                for (uint32_t y0 = 0; y0 < dl.size(); y0 += 65535) {
+                    const uint32_t ny = std::min<uint32_t>(65535, (uint32_t)dl.size() - y0);
+                    k_dense_place<<<dim3(chunks, ny), 256, 0, st>>>(d_slots, d_base, d_dl, y0, n, chunks, d_cpos,
+                                                                    d_seg, g->dg.names, o_name, o_cnt);
+                }
+                PTW_CUDA(cudaGetLastError());
+            }
         }
+        prefault.join();
         if (timing) {
             PTW_CUDA(cudaStreamSynchronize(st));
             t1 = clk();
@@ -412,9 +540,21 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
         if (timing) t2 = clk();
     }
     if (timing)
-        std::fprintf(stderr, "[ptw] compact %u tables, %llu entries: device %.1f ms, d2h %.1f ms\n", nt,
-                     (unsigned long long)n_ent, 1e3 * (t1 - t0), 1e3 * (t2 - t1));
+        std::fprintf(stderr, "[ptw] compact %u tables (%zu dense), %llu entries: device %.1f ms, d2h %.1f ms\n", nt,
+                     dl.size(), (unsigned long long)n_ent, 1e3 * (t1 - t0), 1e3 * (t2 - t1));
     return PTW_OK;
+}
+
+uint64_t table_slots(double sp, uint32_t max_moves, int32_t app, double factor, uint64_t budget, uint32_t n);
+
+TableSize dense_table(uint32_t n) { return TableSize{((uint64_t)n + 1) / 2, true}; }
+
+TableSize count_table(double sp, uint32_t max_moves, int32_t app, double factor, uint64_t budget, uint32_t n)
+{
+    const uint64_t hash = table_slots(sp, max_moves, app, factor, budget, n);
+    const TableSize d = dense_table(n);
+    if (d.slots <= hash) return d;
+    return TableSize{hash, false};
 }
 
 uint64_t table_slots(double sp, uint32_t max_moves, int32_t app, double factor, uint64_t budget, uint32_t n)
@@ -428,7 +568,6 @@ uint64_t table_slots(double sp, uint32_t max_moves, int32_t app, double factor, 
     return std::min(full_cap, std::max<uint64_t>(256, next_pow2((uint64_t)std::min(expect, 4e18))));
 }
 
-uint64_t full_table_slots(uint32_t n) { return next_pow2(2ull * n); }
 
 }  // namespace ptw
 
@@ -459,7 +598,9 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
         all[i].src = g->h_idx2int[p - g->h_names];
         all[i].qid = q.query_id;
         all[i].budget = q.budget;
-        all[i].cap = table_slots(cfg->sp, cfg->max_moves, cfg->app, cfg->table_factor, q.budget, n);
+        const TableSize ts = count_table(cfg->sp, cfg->max_moves, cfg->app, cfg->table_factor, q.budget, n);
+        all[i].cap = ts.slots;
+        all[i].dense = ts.dense;
     }
     uint64_t budget_bytes = cfg->table_bytes;
     if (budget_bytes == 0) {
@@ -488,15 +629,18 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
         }
         rc = run_wave(g, wave, cfg, thr, waves, overflow, &moves, &walk_ms);
     }
-    // Queries whose table filled run again with 2n slots (they cannot fill).
+    // Queries whose hash table filled run again with a dense array (which
+    // cannot fill).
     std::vector<uint32_t> again;
     again.swap(overflow);
     for (size_t k = 0; k < again.size() && rc == PTW_OK; ++k) {
         WaveQuery w = all[again[k]];
-        w.cap = full_table_slots(n);
+        const TableSize d = dense_table(n);
+        w.cap = d.slots;
+        w.dense = true;
         uint64_t m2 = 0;
         rc = run_wave(g, {w}, cfg, thr, waves, overflow, &m2, &walk_ms);
-        if (rc == PTW_OK && !overflow.empty()) rc = fail(PTW_EFULL, "count table overflow at 2n slots");
+        if (rc == PTW_OK && !overflow.empty()) rc = fail(PTW_EFULL, "count table overflow in a dense array");
     }
     if (rc == PTW_OK) rc = assemble(b, waves);
     if (rc != PTW_OK) {

@@ -9,6 +9,9 @@ namespace {
 
 constexpr unsigned kBFull = 0xffffffffu;
 constexpr uint32_t kProbeLimit = 256;
+// q_mask value of a query whose counts are a dense array of n 32-bit
+// counters indexed by canonical vertex index (instead of a hash table).
+constexpr uint32_t kDenseMask = 0xFFFFFFFFu;
 
 __device__ __forceinline__ uint32_t mix32(uint32_t x)
 {
@@ -49,16 +52,28 @@ __device__ __forceinline__ void tab_add(unsigned long long *slots, uint32_t mask
     atomicOr(flag, 1u);
 }
 
+// Adds inc to the count of internal vertex v: in a dense array (mask ==
+// kDenseMask) one fire-and-forget reduction at its canonical index, else a
+// hash-table insert.
+__device__ __forceinline__ void count_add(unsigned long long *tab, uint32_t mask, uint32_t v, uint32_t inc,
+                                          uint32_t *flag, const uint32_t *__restrict__ int2idx)
+{
+    if (mask == kDenseMask) atomicAdd(reinterpret_cast<uint32_t *>(tab) + __ldg(&int2idx[v]), inc);
+    else tab_add(tab, mask, v, inc, flag);
+}
+
 // Work of one launch: descriptor d runs walker ranks desc[d].y ..
 // desc[d].y + desc[d].z - 1 of query entry q = desc[d].x, whose walker ids
 // are (q_qid[q] << 32) + rank, source q_src[q], count table at slots +
-// q_tab[q] (q_mask[q] + 1 slots).  Descriptors are ordered round-robin over
+// q_tab[q] (q_mask[q] + 1 slots, or a dense array when q_mask[q] ==
+// kDenseMask).  Descriptors are ordered round-robin over
 // the queries (the host builds them so), and a warp takes one descriptor at
 // a time, so the walkers in flight belong to many queries at once and no
 // single query's hot slots serialise the whole GPU.
 struct BatchArgs {
     const uint2 *__restrict__ adj;
     const uint32_t *__restrict__ col;
+    const uint32_t *__restrict__ int2idx;  // internal id -> canonical index (dense tables)
     const uint3 *__restrict__ desc;  // [ndesc] {entry, first rank, count}
     const uint32_t *__restrict__ q_src;
     const uint32_t *__restrict__ q_qid;
@@ -81,13 +96,14 @@ constexpr int kBatchIlp = 2;
 // Counts one visit of key v in query entry q's table, aggregated over the
 // lanes of the warp that visit the same (query, vertex) now.
 __device__ __forceinline__ void visit_agg(unsigned mask_active, bool on, uint32_t q, uint32_t v,
-                                          unsigned long long *tab, uint32_t tmask, uint32_t *flag, uint32_t lane)
+                                          unsigned long long *tab, uint32_t tmask, uint32_t *flag, uint32_t lane,
+                                          const uint32_t *__restrict__ int2idx)
 {
     const unsigned m = __ballot_sync(mask_active, on);
     if (!on) return;
     const unsigned long long key = ((unsigned long long)q << 32) | v;
     const unsigned grp = __match_any_sync(m, key);
-    if ((grp & ((1u << lane) - 1u)) == 0) tab_add(tab, tmask, v, __popc(grp), flag);
+    if ((grp & ((1u << lane) - 1u)) == 0) count_add(tab, tmask, v, __popc(grp), flag, int2idx);
 }
 
 __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
@@ -152,7 +168,7 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
             }
             if (a.app == PTW_APP_VISITS) {
                 // Start visits: one table update per (warp, query) group.
-                visit_agg(kBFull, got, q[k], v[k], tab[k], mask[k], &a.q_flag[q[k]], lane);
+                visit_agg(kBFull, got, q[k], v[k], tab[k], mask[k], &a.q_flag[q[k]], lane, a.int2idx);
             }
         }
         bool any = false;
@@ -181,9 +197,11 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
                 ++step[k];
                 ++moves;
             }
-            if (a.app == PTW_APP_VISITS) visit_agg(kBFull, moved, q[k], v[k], tab[k], mask[k], &a.q_flag[q[k]], lane);
+            if (a.app == PTW_APP_VISITS)
+                visit_agg(kBFull, moved, q[k], v[k], tab[k], mask[k], &a.q_flag[q[k]], lane, a.int2idx);
             const bool done = act[k] && (!moved || (uint64_t)r[k].y < a.thr || (a.max_moves && step[k] >= a.max_moves));
-            if (a.app == PTW_APP_ENDPOINT) visit_agg(kBFull, done, q[k], v[k], tab[k], mask[k], &a.q_flag[q[k]], lane);
+            if (a.app == PTW_APP_ENDPOINT)
+                visit_agg(kBFull, done, q[k], v[k], tab[k], mask[k], &a.q_flag[q[k]], lane, a.int2idx);
             if (done) act[k] = false;
         }
     }
@@ -194,15 +212,24 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
 
 // ---- compaction of count tables into (name, count) lists ------------------
 
-// Table i occupies slots[t_base[i] .. t_base[i] + t_cap[i]).  blockIdx.y = i.
+// Entry x of table i: a 64-bit hash slot, or a 32-bit dense counter.
+__device__ __forceinline__ unsigned long long table_word(const unsigned long long *s, bool dense, uint64_t x)
+{
+    return dense ? (unsigned long long)reinterpret_cast<const uint32_t *>(s)[x] : s[x];
+}
+
+// Table i starts at slots + t_base[i] and has t_cap[i] entries (64-bit
+// slots, or 32-bit counters when t_dense[i]).  blockIdx.y = i.
 __global__ void k_tabs_count(const unsigned long long *slots, const unsigned long long *t_base,
-                             const uint32_t *t_cap, unsigned long long *cnt)
+                             const uint32_t *t_cap, const uint8_t *t_dense, unsigned long long *cnt)
 {
     const uint32_t i = blockIdx.y;
     const unsigned long long *s = slots + t_base[i];
     const uint32_t cap = t_cap[i];
+    const bool dense = t_dense[i] != 0;
     uint32_t c = 0;
-    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < cap; x += gridDim.x * blockDim.x) c += s[x] != 0;
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < cap; x += gridDim.x * blockDim.x)
+        c += table_word(s, dense, x) != 0;
     for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kBFull, c, o);
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(&cnt[i], (unsigned long long)c);
 }
@@ -215,14 +242,19 @@ __global__ void k_tabs_count(const unsigned long long *slots, const unsigned lon
 // table's fill cursor, then writes them (warp offsets through shared
 // memory).  One atomic per block instead of one per 32 slots keeps warps from
 // queueing on the cursor of a large table.  Launch with 256 threads.
+// Dense tables (t_dense[i]) are emitted the same way (entry x = canonical
+// index x, name idx_names[x]) unless skip_dense is set.
 __global__ void __launch_bounds__(256) k_tabs_emit(const unsigned long long *slots, const unsigned long long *t_base,
-                            const uint32_t *t_cap, const unsigned long long *seg_off, unsigned long long *fill,
-                            const uint32_t *int2name, uint32_t t_index0, int name_bits, bool by_count,
-                            unsigned long long *out_key, uint32_t *out_cnt)
+                            const uint32_t *t_cap, const uint8_t *t_dense, bool skip_dense,
+                            const unsigned long long *seg_off, unsigned long long *fill,
+                            const uint32_t *int2name, const uint32_t *idx_names, uint32_t t_index0, int name_bits,
+                            bool by_count, unsigned long long *out_key, uint32_t *out_cnt)
 {
     __shared__ uint32_t warp_n[8];
     __shared__ unsigned long long base_s;
     const uint32_t i = blockIdx.y;
+    const bool dense = t_dense[i] != 0;
+    if (dense && skip_dense) return;
     const unsigned long long *s = slots + t_base[i];
     const uint32_t cap = t_cap[i];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -233,7 +265,7 @@ __global__ void __launch_bounds__(256) k_tabs_emit(const unsigned long long *slo
     if (lo >= hi) return;  // whole block leaves together
     // pass 1: occupied slots of the chunk
     uint32_t c = 0;
-    for (uint64_t x = lo + threadIdx.x; x < hi; x += 256) c += s[x] != 0;
+    for (uint64_t x = lo + threadIdx.x; x < hi; x += 256) c += table_word(s, dense, x) != 0;
     for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kBFull, c, o);
     if (lane == 0) warp_n[warp] = c;
     __syncthreads();
@@ -250,7 +282,7 @@ __global__ void __launch_bounds__(256) k_tabs_emit(const unsigned long long *slo
     // pass 2: tiles of 256 slots in order
     for (uint64_t x0 = lo; x0 < hi; x0 += 256) {
         const uint64_t x = x0 + threadIdx.x;
-        const unsigned long long w = x < hi ? s[x] : 0ull;
+        const unsigned long long w = x < hi ? table_word(s, dense, x) : 0ull;
         const unsigned om = __ballot_sync(kBFull, w != 0);
         __syncthreads();  // previous tile's readers of warp_n are done
         if (lane == 0) warp_n[warp] = __popc(om);
@@ -265,10 +297,92 @@ __global__ void __launch_bounds__(256) k_tabs_emit(const unsigned long long *slo
             const unsigned long long p = pos0 + before + __popc(om & ((1u << lane) - 1u));
             const uint32_t cnt = (uint32_t)(w & 0xFFFFFFFFull);
             const unsigned long long inv = by_count ? (unsigned long long)(0xFFFFFFFFu - cnt) << name_bits : 0ull;
-            out_key[p] = tagged | inv | int2name[(uint32_t)(w >> 32) - 1];
+            const uint32_t name = dense ? idx_names[x] : int2name[(uint32_t)(w >> 32) - 1];
+            out_key[p] = tagged | inv | name;
             out_cnt[p] = cnt;
         }
         pos0 += total;
+    }
+}
+
+// Sorted hash entries j (keys table << name_bits | name, counts) go to
+// position seg[t] + (j - hseg[t]) of their table t's output segment.
+__global__ void k_place_hash(const unsigned long long *key, const uint32_t *cnt, uint64_t n, int name_bits,
+                             const unsigned long long *seg, const unsigned long long *hseg, uint32_t *out_name,
+                             uint32_t *out_cnt)
+{
+    const unsigned long long nmask = (1ull << name_bits) - 1;
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long k = key[j];
+        const uint32_t t = (uint32_t)(k >> name_bits);
+        const uint64_t p = seg[t] + (j - hseg[t]);
+        out_name[p] = (uint32_t)(k & nmask);
+        out_cnt[p] = cnt[j];
+    }
+}
+
+// Dense tables, pass 1: nonzero counters of chunk blockIdx.x (kDenseChunk
+// counters) of dense table dl[y0 + blockIdx.y] -> cc[(y0 + blockIdx.y) *
+// chunks + blockIdx.x].  Launch with 256 threads.
+constexpr uint32_t kDenseChunk = 4096;
+__global__ void __launch_bounds__(256) k_dense_chunks(const unsigned long long *slots,
+                                                      const unsigned long long *t_base, const uint32_t *dl,
+                                                      uint32_t y0, uint32_t n, uint32_t chunks,
+                                                      unsigned long long *cc)
+{
+    __shared__ uint32_t warp_n[8];
+    const uint32_t y = y0 + blockIdx.y;
+    const uint32_t *c = reinterpret_cast<const uint32_t *>(slots + t_base[dl[y]]);
+    const uint64_t lo = (uint64_t)blockIdx.x * kDenseChunk;
+    const uint64_t hi = lo + kDenseChunk < n ? lo + kDenseChunk : n;
+    uint32_t k = 0;
+    for (uint64_t x = lo + threadIdx.x; x < hi; x += 256) k += c[x] != 0;
+    for (int o = 16; o; o >>= 1) k += __shfl_xor_sync(kBFull, k, o);
+    if ((threadIdx.x & 31) == 0) warp_n[threadIdx.x >> 5] = k;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < 8; ++w) t += warp_n[w];
+        cc[(uint64_t)y * chunks + blockIdx.x] = (unsigned long long)t;
+    }
+}
+
+// Dense tables, pass 2: writes the nonzero counters of the chunk, in index
+// (= name) order, at seg[t] + cpos[chunk] - cpos[table's first chunk] +
+// rank within the chunk, where cpos is the exclusive scan of pass 1.
+__global__ void __launch_bounds__(256) k_dense_place(const unsigned long long *slots,
+                                                     const unsigned long long *t_base, const uint32_t *dl,
+                                                     uint32_t y0, uint32_t n, uint32_t chunks,
+                                                     const unsigned long long *cpos, const unsigned long long *seg,
+                                                     const uint32_t *idx_names, uint32_t *out_name, uint32_t *out_cnt)
+{
+    __shared__ uint32_t warp_n[8];
+    const uint32_t y = y0 + blockIdx.y;
+    const uint32_t t = dl[y];
+    const uint32_t *c = reinterpret_cast<const uint32_t *>(slots + t_base[t]);
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t lo = (uint64_t)blockIdx.x * kDenseChunk;
+    const uint64_t hi = lo + kDenseChunk < n ? lo + kDenseChunk : n;
+    unsigned long long pos = seg[t] + cpos[(uint64_t)y * chunks + blockIdx.x] - cpos[(uint64_t)y * chunks];
+    for (uint64_t x0 = lo; x0 < hi; x0 += 256) {
+        const uint64_t x = x0 + threadIdx.x;
+        const uint32_t v = x < hi ? c[x] : 0u;
+        const unsigned om = __ballot_sync(kBFull, v != 0);
+        __syncthreads();
+        if (lane == 0) warp_n[warp] = __popc(om);
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t w = warp_n[k];
+            before += k < (int)warp ? w : 0u;
+            total += w;
+        }
+        if (v) {
+            const unsigned long long p = pos + before + __popc(om & ((1u << lane) - 1u));
+            out_name[p] = idx_names[x];
+            out_cnt[p] = v;
+        }
+        pos += total;
     }
 }
 

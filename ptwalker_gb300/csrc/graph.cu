@@ -354,6 +354,7 @@ void graph_release(ptw_graph *g)
     cudaFree(g->dg.int2name);
     cudaFree(g->dg.idx2int);
     cudaFree(g->dg.int2idx);
+    cudaFree(g->dg.names);
     cudaFree(g->dg.col_named);
     cudaFree(g->dg.col_ext);
     cudaFree(g->sc.counts);
@@ -571,6 +572,8 @@ int build_graph_from_device_edges(ptw_graph *g, uint32_t *d_src, uint32_t *d_dst
     PTW_CUDA(cudaMalloc(&dg.idx2int, (uint64_t)n * 4));
     PTW_CUDA(cudaMalloc(&dg.int2idx, (uint64_t)n * 4));
     PTW_CUDA(cudaMemcpyAsync(dg.int2idx, order, (uint64_t)n * 4, cudaMemcpyDeviceToDevice, st));
+    PTW_CUDA(cudaMalloc(&dg.names, (uint64_t)n * 4));
+    PTW_CUDA(cudaMemcpyAsync(dg.names, names, (uint64_t)n * 4, cudaMemcpyDeviceToDevice, st));
     uint32_t *int_deg = iota;  // reuse
     k_relabel<<<grid_for(n), kThreads, 0, st>>>(order, deg, names, n, dg.idx2int, int_deg,
                                                 dg.int2name);
@@ -595,7 +598,7 @@ int build_graph_from_device_edges(ptw_graph *g, uint32_t *d_src, uint32_t *d_dst
     PTW_CUDA(cudaMalloc(&g->sc.ctrl, 8 * sizeof(unsigned long long)));
     PTW_CUDA(cudaStreamSynchronize(st));
     dg.max_degree = h_maxdeg;
-    g->device_bytes = (uint64_t)n * (8 + 4 * 3 + 4) + mm * 4 + 64;
+    g->device_bytes = (uint64_t)n * (8 + 4 * 4 + 4) + mm * 4 + 64;
     return PTW_OK;
 }
 

@@ -100,6 +100,7 @@ struct DeviceGraph {
     uint32_t *int2name = nullptr; // [n]
     uint32_t *idx2int = nullptr;  // [n] canonical index (name rank) -> internal
     uint32_t *int2idx = nullptr;  // [n] internal -> canonical index
+    uint32_t *names = nullptr;    // [n] canonical index -> name (ascending)
     uint2 *col_named = nullptr;   // [m] {neighbour internal id, its name}; built on first path walk
     uint4 *col_ext = nullptr;     // [m] {neighbour id, its first column, its degree, its name};
                                   // built on the first walk with tune.ext_columns
@@ -194,16 +195,29 @@ struct Compacted {
     std::function<uint32_t *(uint64_t)> sink;
     uint32_t *h_names = nullptr, *h_counts = nullptr;
 };
-// Compacts nt count tables (slots [h_base[i], h_base[i] + h_cap[i]) of
-// d_slots) into *out (batch.cu).
+// Compacts nt count tables into *out (batch.cu).  Table i starts at slot
+// h_base[i] of d_slots; a hash table (h_dense[i] == 0, or h_dense NULL) has
+// h_cap[i] 64-bit slots, a dense table h_cap[i] = n 32-bit counters indexed
+// by canonical vertex index.
 int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned long long *h_base,
-                   const uint32_t *h_cap, uint32_t nt, Compacted *out);
-// Count-table size for a query of `budget` walkers, and the size that cannot fill.
-uint64_t table_slots(double sp, uint32_t max_moves, int32_t app, double factor, uint64_t budget, uint32_t n);
-uint64_t full_table_slots(uint32_t n);
+                   const uint32_t *h_cap, const uint8_t *h_dense, uint32_t nt, Compacted *out);
+// The count table of a query: an open-addressing hash table sized from its
+// budget, or, when that would take at least as many bytes, a dense array of
+// n 32-bit counters (which cannot fill).  slots = 64-bit slots it occupies.
+struct TableSize {
+    uint64_t slots;
+    bool dense;
+};
+TableSize count_table(double sp, uint32_t max_moves, int32_t app, double factor, uint64_t budget, uint32_t n);
+TableSize dense_table(uint32_t n);
 // Splits [j0[i], j0[i] + count[i]) of every query entry i into walker
-// descriptors {entry, first rank, count}, ordered round-robin over entries.
+// descriptors {entry, first rank, count}, ordered round-robin within groups
+// of consecutive entries whose tables add up to about group_bytes (0 = one
+// group), group after group (batch.cu).
 void interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<uint64_t> &count,
+                            const std::vector<uint64_t> &table_bytes, uint64_t group_bytes,
                             std::vector<uint3> &desc);
+// Count-table bytes per descriptor group: about 3x the 129 MB L2.
+constexpr uint64_t kGroupBytes = 384ull << 20;
 
 }  // namespace ptw

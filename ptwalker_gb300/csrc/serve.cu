@@ -89,6 +89,7 @@ struct Pending {
 struct Active {
     Pending p;
     uint64_t cap, off;  // table slots, arena offset
+    bool dense;         // dense array of n counters instead of a hash table
     uint64_t started;   // ranks run so far
     double admit_s;
 };
@@ -244,10 +245,12 @@ int collect(ptw_server *s, const std::vector<size_t> &fin)
     if (fin.empty()) return PTW_OK;
     std::vector<unsigned long long> base(fin.size());
     std::vector<uint32_t> cap(fin.size());
+    std::vector<uint8_t> dense(fin.size());
     std::vector<Done> out(fin.size());
     for (size_t i = 0; i < fin.size(); ++i) {
         base[i] = s->active[fin[i]].off;
-        cap[i] = (uint32_t)s->active[fin[i]].cap;
+        dense[i] = s->active[fin[i]].dense ? 1 : 0;
+        cap[i] = dense[i] ? s->g->dg.n : (uint32_t)s->active[fin[i]].cap;
     }
     Compacted c;
     c.top_k = s->cfg.top_k;
@@ -256,7 +259,7 @@ int collect(ptw_server *s, const std::vector<size_t> &fin)
         blk = pinned_block(s, 2 * n);
         return blk ? blk->p : nullptr;
     };
-    int rc = compact_tables(s->g, s->arena, base.data(), cap.data(), (uint32_t)fin.size(), &c);
+    int rc = compact_tables(s->g, s->arena, base.data(), cap.data(), dense.data(), (uint32_t)fin.size(), &c);
     if (rc) return rc;
     for (size_t i = 0; i < fin.size(); ++i) {
         out[i].blk = blk;
@@ -332,6 +335,7 @@ extern "C" int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server
         BatchArgs &a = s->args;
         a.adj = g->dg.adj;
         a.col = g->dg.col;
+        a.int2idx = g->dg.int2idx;
         a.desc = dv.desc;
         a.q_src = dv.src;
         a.q_qid = dv.qid;
@@ -395,9 +399,10 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
     // 1. admission: FIFO while a slot and a table fit
     while (!s->pending.empty() && s->active.size() < s->S) {
         Pending &pd = s->pending.front();
-        const uint64_t cap = pd.full ? full_table_slots(n)
-                                     : table_slots(s->cfg.sp, s->cfg.max_moves, s->cfg.app,
-                                                   s->cfg.table_factor, pd.q.budget, n);
+        const TableSize ts = pd.full ? dense_table(n)
+                                     : count_table(s->cfg.sp, s->cfg.max_moves, s->cfg.app, s->cfg.table_factor,
+                                                   pd.q.budget, n);
+        const uint64_t cap = ts.slots;
         uint64_t off = 0;
         if (!s->buddy.alloc(cap, &off)) {
             if (s->active.empty() && cap > s->buddy.capacity())
@@ -408,6 +413,7 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
         Active a;
         a.p = pd;
         a.cap = cap;
+        a.dense = ts.dense;
         a.off = off;
         a.started = 0;
         a.admit_s = now_s(s);
@@ -432,11 +438,13 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
             hv.tab[i] = a.off;
             hv.src[i] = a.p.src;
             hv.qid[i] = a.p.q.query_id;
-            hv.mask[i] = (uint32_t)(a.cap - 1);
+            hv.mask[i] = a.dense ? kDenseMask : (uint32_t)(a.cap - 1);
             hv.flag[i] = 0;
         }
         std::vector<uint3> desc;
-        interleave_descriptors(j0, s->take, desc);
+        std::vector<uint64_t> tbytes(na);
+        for (uint32_t i = 0; i < na; ++i) tbytes[i] = s->active[i].cap * 8;
+        interleave_descriptors(j0, s->take, tbytes, kGroupBytes, desc);
         if (desc.size() > s->D) {
             // more active queries than the plan holds descriptors for: keep
             // the first D (whole queries stay consistent: trim their takes)

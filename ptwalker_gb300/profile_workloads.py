@@ -29,6 +29,7 @@ def main(argv=None):
     p.add_argument("--sp", type=float, default=0.15)
     p.add_argument("--n", type=int, default=8_400_000, help="Chung-Lu vertices (serve)")
     p.add_argument("--top-k", type=int, default=1000)
+    p.add_argument("--budget-max", type=float, default=1e5, help="batch: budgets log-uniform in [1e3, this]")
     p.add_argument("--tune", default=None,
                    help="launch parameters as name=value pairs, e.g. block=1024,ilp=2,hot_k=8192")
     a = p.parse_args(argv)
@@ -100,7 +101,7 @@ def main(argv=None):
         names, row_ptr, col = G.export_csr()
         rng = np.random.default_rng(2)
         src = names[col[rng.integers(0, G.m, a.queries)]]
-        bud = np.exp(rng.uniform(np.log(1e3), np.log(1e5), a.queries)).astype(np.int64)
+        bud = np.exp(rng.uniform(np.log(1e3), np.log(a.budget_max), a.queries)).astype(np.int64)
         ptw.ppr_batch(G, src, bud, sp=0.2, seed=1).close()
         res = [ptw.ppr_batch(G, src, bud, sp=0.2, seed=2 + k) for k in range(a.reps)]
         out.update(kernel_ms=[r.kernel_ms for r in res], total_ms=[r.ms for r in res], moves=res[-1].moves)

@@ -72,21 +72,28 @@ def test_alone_and_in_the_mix(gpu, G16, s16_canon, use_graph):
 
 def test_admission_waits_for_table_memory(gpu, G16, s16_canon):
     sp, seed = 0.25, 5
-    # arena of 2^17 slots: one 20000-walker query (table 2^18 > arena? no: 2^17)
-    with gpu.Server(G16, sp=sp, seed=seed, tick_walkers=8192, table_bytes=8 << 17) as srv:
-        for k in range(8):
-            srv.submit(100 + k, 5000, k)  # table 2^16 slots each: two fit at once
-        seen_active = []
-        res = []
-        while True:
-            res += srv.step()
-            seen_active.append(srv.n_active)
-            if srv.n_active == 0 and srv.n_pending == 0:
-                break
-    assert max(seen_active) <= 2
-    assert len(res) == 8
-    for r in res:
-        check(r, s16_canon, sp, seed)
+    n = G16.n
+    # Arena of 2^17 64-bit slots.  A 5000-walker query would need a 2^16-slot
+    # hash table, so it counts into a dense array of n 32-bit counters instead
+    # ((n + 1) / 2 slots, a 2^15 buddy block): four fit at once.  A 1500-walker
+    # query keeps a 2^14-slot hash table: eight fit at once.
+    assert 2 ** 14 < (n + 1) // 2 <= 2 ** 15
+    for budget, fit, nq in ((5000, 4, 8), (1500, 8, 16)):
+        with gpu.Server(G16, sp=sp, seed=seed, tick_walkers=8192, table_bytes=8 << 17) as srv:
+            for k in range(nq):
+                srv.submit(100 + k, budget, k)
+            seen_active, seen_pending = [], []
+            res = []
+            while True:
+                res += srv.step()
+                seen_active.append(srv.n_active)
+                seen_pending.append(srv.n_pending)
+                if srv.n_active == 0 and srv.n_pending == 0:
+                    break
+        assert max(seen_active) == fit and max(seen_pending) > 0
+        assert len(res) == nq
+        for r in res:
+            check(r, s16_canon, sp, seed)
 
 
 def test_overflow_and_endpoint_app(gpu, G16, s16_canon):
