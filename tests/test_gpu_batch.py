@@ -94,6 +94,8 @@ def test_batch_max_moves_and_errors(gpu, G16, s16_canon):
     with pytest.raises(gpu.PTWError):
         gpu.ppr_batch(G16, [1], [0])
     with pytest.raises(gpu.PTWError):
+        gpu.ppr_batch(G16, [1], [(1 << 28) + 1])   # above the largest budget
+    with pytest.raises(gpu.PTWError):
         gpu.ppr_batch(G16, [1], [10], sp=0.0)
     empty = gpu.ppr_batch(G16, [], [])
     assert empty.nq == 0 and empty.entries == 0

@@ -118,6 +118,8 @@ def test_submit_errors_and_open_loop(gpu, G16):
             srv.submit(10 ** 8, 10, 0)
         with pytest.raises(gpu.PTWError):
             srv.submit(1, 0, 0)
+        with pytest.raises(gpu.PTWError):
+            srv.submit(1, (1 << 28) + 1, 0)
         rng = np.random.default_rng(0)
         out = gpu.open_loop(srv, rng.integers(0, G16.n, 200), rng.integers(1000, 5000, 200), rate=2000.0)
     assert out["n"] == 200 and out["p99_ms"] >= out["p50_ms"] > 0 and out["qps"] > 0
