@@ -421,21 +421,48 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
         const unsigned kg = (unsigned)std::min<uint64_t>((n_ent + 255) / 256, (uint64_t)g->num_sms * 32);
         uint32_t *o_name = nullptr, *o_cnt = nullptr;
         if (k) {
-            // Top-k: every table (hash or dense) emits its entries as keys; a
-            // radix sort orders each table by count, the first k are kept.
+            // Top-k.  A histogram of each large table's counts (exact below
+            // 256, 16 bins per octave above) gives the lowest bin that still
+            // holds k entries; only entries in that bin or above are emitted
+            // as keys, so the radix sort sees about k entries per table
+            // instead of all of them.  The sort orders each table by count
+            // (ties by name) and the first k are kept.
+            uint32_t *d_hist, *d_thr;
+            unsigned long long *d_sel, *d_sseg;
+            PTW_CUDA(db.alloc(&d_hist, (uint64_t)nt * kCountBins));
+            PTW_CUDA(db.alloc(&d_thr, nt));
+            PTW_CUDA(db.alloc(&d_sel, nt));
+            PTW_CUDA(db.alloc(&d_sseg, nt + 1));
+            PTW_CUDA(cudaMemsetAsync(d_hist, 0, (uint64_t)nt * kCountBins * 4, st));
+            PTW_CUDA(cudaMemsetAsync(d_sseg, 0, 8, st));
+            PTW_CUDA(cudaMemsetAsync(d_fill, 0, nt * 8ull, st));
+            for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
+                const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
+                k_tabs_hist<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(d_slots, d_base + t0, d_cap + t0,
+                                                                       d_dense + t0, d_cnt + t0, k,
+                                                                       d_hist + (uint64_t)t0 * kCountBins);
+            }
+            k_tabs_thresh<<<(nt + 7) / 8, 256, 0, st>>>(d_cnt, d_hist, nt, k, d_thr, d_sel);
+            PTW_CUDA(cudaGetLastError());
+            PTW_CUDA(cub_call([&](void *t, size_t &b) {
+                return cub::DeviceScan::InclusiveSum(t, b, d_sel, d_sseg + 1, (int64_t)nt, st);
+            }, st));
+            unsigned long long n_sel = 0;
+            PTW_CUDA(cudaMemcpyAsync(&n_sel, d_sseg + nt, 8, cudaMemcpyDeviceToHost, st));
+            PTW_CUDA(cudaStreamSynchronize(st));
             unsigned long long *e_key, *s_key;
             uint32_t *e_cnt, *s_cnt;
-            PTW_CUDA(db.alloc(&e_key, n_ent));
-            PTW_CUDA(db.alloc(&s_key, n_ent));
-            PTW_CUDA(db.alloc(&e_cnt, n_ent));
-            PTW_CUDA(db.alloc(&s_cnt, n_ent));
+            PTW_CUDA(db.alloc(&e_key, n_sel));
+            PTW_CUDA(db.alloc(&s_key, n_sel));
+            PTW_CUDA(db.alloc(&e_cnt, n_sel));
+            PTW_CUDA(db.alloc(&s_cnt, n_sel));
             // (table, ~count, name) in 64 bits: one sort, keys only
             const bool packed = q_bits + 32 + name_bits <= 64;
             for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
                 const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
                 k_tabs_emit<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(
-                    d_slots, d_base + t0, d_cap + t0, d_dense + t0, false, d_seg + t0, d_fill + t0, g->dg.int2name,
-                    g->dg.names, t0, name_bits, packed, e_key, e_cnt);
+                    d_slots, d_base + t0, d_cap + t0, d_dense + t0, false, d_sseg + t0, d_fill + t0, g->dg.int2name,
+                    g->dg.names, t0, name_bits, packed, d_thr + t0, e_key, e_cnt);
             }
             PTW_CUDA(cudaGetLastError());
             unsigned long long *d_kseg;
@@ -443,27 +470,29 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             PTW_CUDA(db.alloc(&o_name, n_out));
             PTW_CUDA(db.alloc(&o_cnt, n_out));
             PTW_CUDA(cudaMemcpyAsync(d_kseg, kseg.data(), (nt + 1) * 8ull, cudaMemcpyHostToDevice, st));
+            const unsigned sg = (unsigned)std::min<uint64_t>((n_sel + 255) / 256, (uint64_t)g->num_sms * 32);
             if (packed) {
                 PTW_CUDA(cub_call([&](void *t, size_t &b) {
-                    return cub::DeviceRadixSort::SortKeys(t, b, e_key, s_key, (int64_t)n_ent, 0,
+                    return cub::DeviceRadixSort::SortKeys(t, b, e_key, s_key, (int64_t)n_sel, 0,
                                                           q_bits + 32 + name_bits, st);
                 }, st));
-                k_topk_copy_packed<<<std::max(kg, 1u), 256, 0, st>>>(s_key, n_ent, name_bits, d_seg, d_kseg, k,
+                k_topk_copy_packed<<<std::max(sg, 1u), 256, 0, st>>>(s_key, n_sel, name_bits, d_sseg, d_kseg, k,
                                                                      o_name, o_cnt);
             } else {
                 // sort by (table, name), then stably by (table, ~count): equal
                 // counts stay in name order
                 PTW_CUDA(cub_call([&](void *t, size_t &b) {
-                    return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_ent, 0,
+                    return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_sel, 0,
                                                            name_bits + q_bits, st);
                 }, st));
-                k_count_keys<<<std::max(kg, 1u), 256, 0, st>>>(s_key, s_cnt, n_ent, name_bits, e_key, e_cnt);
+                k_count_keys<<<std::max(sg, 1u), 256, 0, st>>>(s_key, s_cnt, n_sel, name_bits, e_key, e_cnt);
                 PTW_CUDA(cudaGetLastError());
                 PTW_CUDA(cub_call([&](void *t, size_t &b) {
-                    return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_ent, 0,
+                    return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_sel, 0,
                                                            32 + q_bits, st);
                 }, st));
-                k_topk_copy<<<std::max(kg, 1u), 256, 0, st>>>(s_key, s_cnt, n_ent, d_seg, d_kseg, k, o_name, o_cnt);
+                k_topk_copy<<<std::max(sg, 1u), 256, 0, st>>>(s_key, s_cnt, n_sel, d_sseg, d_kseg, k, o_name,
+                                                              o_cnt);
             }
             PTW_CUDA(cudaGetLastError());
             out->seg = kseg;
@@ -491,7 +520,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
                     const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
                     k_tabs_emit<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(
                         d_slots, d_base + t0, d_cap + t0, d_dense + t0, true, d_hseg + t0, d_fill + t0,
-                        g->dg.int2name, g->dg.names, t0, name_bits, false, e_key, e_cnt);
+                        g->dg.int2name, g->dg.names, t0, name_bits, false, nullptr, e_key, e_cnt);
                 }
                 PTW_CUDA(cudaGetLastError());
                 PTW_CUDA(cub_call([&](void *t, size_t &b) {

@@ -212,6 +212,22 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
 
 // ---- compaction of count tables into (name, count) lists ------------------
 
+// Monotone bin of a count: exact below 256, then 16 bins per octave.
+constexpr uint32_t kCountBins = 640;
+__device__ __forceinline__ uint32_t count_bin(uint32_t c)
+{
+    if (c < 256) return c;
+    const uint32_t e = 31 - __clz(c);  // 8 .. 31
+    return 256 + (e - 8) * 16 + ((c >> (e - 4)) & 15u);
+}
+
+// An occupied entry (hash slot with a key, or a nonzero dense counter) whose
+// count falls in bin thr or above.
+__device__ __forceinline__ bool kept(unsigned long long w, uint32_t thr)
+{
+    return w != 0 && (thr == 0 || count_bin((uint32_t)(w & 0xFFFFFFFFull)) >= thr);
+}
+
 // Entry x of table i: a 64-bit hash slot, or a 32-bit dense counter.
 __device__ __forceinline__ unsigned long long table_word(const unsigned long long *s, bool dense, uint64_t x)
 {
@@ -243,12 +259,13 @@ __global__ void k_tabs_count(const unsigned long long *slots, const unsigned lon
 // memory).  One atomic per block instead of one per 32 slots keeps warps from
 // queueing on the cursor of a large table.  Launch with 256 threads.
 // Dense tables (t_dense[i]) are emitted the same way (entry x = canonical
-// index x, name idx_names[x]) unless skip_dense is set.
+// index x, name idx_names[x]) unless skip_dense is set.  With t_thr, only
+// entries whose count bin (count_bin) is at least t_thr[i] are emitted.
 __global__ void __launch_bounds__(256) k_tabs_emit(const unsigned long long *slots, const unsigned long long *t_base,
                             const uint32_t *t_cap, const uint8_t *t_dense, bool skip_dense,
                             const unsigned long long *seg_off, unsigned long long *fill,
                             const uint32_t *int2name, const uint32_t *idx_names, uint32_t t_index0, int name_bits,
-                            bool by_count, unsigned long long *out_key, uint32_t *out_cnt)
+                            bool by_count, const uint32_t *t_thr, unsigned long long *out_key, uint32_t *out_cnt)
 {
     __shared__ uint32_t warp_n[8];
     __shared__ unsigned long long base_s;
@@ -257,6 +274,7 @@ __global__ void __launch_bounds__(256) k_tabs_emit(const unsigned long long *slo
     if (dense && skip_dense) return;
     const unsigned long long *s = slots + t_base[i];
     const uint32_t cap = t_cap[i];
+    const uint32_t thr = t_thr ? t_thr[i] : 0u;  // keep entries whose count bin >= thr
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t per = (cap + gridDim.x - 1) / gridDim.x;
     per = (per + 255u) & ~255u;
@@ -265,7 +283,7 @@ __global__ void __launch_bounds__(256) k_tabs_emit(const unsigned long long *slo
     if (lo >= hi) return;  // whole block leaves together
     // pass 1: occupied slots of the chunk
     uint32_t c = 0;
-    for (uint64_t x = lo + threadIdx.x; x < hi; x += 256) c += table_word(s, dense, x) != 0;
+    for (uint64_t x = lo + threadIdx.x; x < hi; x += 256) c += kept(table_word(s, dense, x), thr);
     for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kBFull, c, o);
     if (lane == 0) warp_n[warp] = c;
     __syncthreads();
@@ -282,7 +300,8 @@ __global__ void __launch_bounds__(256) k_tabs_emit(const unsigned long long *slo
     // pass 2: tiles of 256 slots in order
     for (uint64_t x0 = lo; x0 < hi; x0 += 256) {
         const uint64_t x = x0 + threadIdx.x;
-        const unsigned long long w = x < hi ? table_word(s, dense, x) : 0ull;
+        unsigned long long w = x < hi ? table_word(s, dense, x) : 0ull;
+        if (!kept(w, thr)) w = 0;
         const unsigned om = __ballot_sync(kBFull, w != 0);
         __syncthreads();  // previous tile's readers of warp_n are done
         if (lane == 0) warp_n[warp] = __popc(om);
@@ -303,6 +322,50 @@ __global__ void __launch_bounds__(256) k_tabs_emit(const unsigned long long *slo
         }
         pos0 += total;
     }
+}
+
+// Top-k selection, histogram: counts of the occupied entries of every table
+// with more than k of them, by count_bin, into hist[i * kCountBins + bin].
+__global__ void __launch_bounds__(256) k_tabs_hist(const unsigned long long *slots, const unsigned long long *t_base,
+                                                   const uint32_t *t_cap, const uint8_t *t_dense,
+                                                   const unsigned long long *cnt, uint32_t k, uint32_t *hist)
+{
+    __shared__ uint32_t h[kCountBins];
+    const uint32_t i = blockIdx.y;
+    if (cnt[i] <= k) return;  // every entry is kept
+    for (uint32_t b = threadIdx.x; b < kCountBins; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    const unsigned long long *s = slots + t_base[i];
+    const uint32_t cap = t_cap[i];
+    const bool dense = t_dense[i] != 0;
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < cap; x += gridDim.x * blockDim.x) {
+        const unsigned long long w = table_word(s, dense, x);
+        if (w) atomicAdd(&h[count_bin((uint32_t)(w & 0xFFFFFFFFull))], 1u);
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < kCountBins; b += blockDim.x)
+        if (h[b]) atomicAdd(&hist[(uint64_t)i * kCountBins + b], h[b]);
+}
+
+// Top-k selection, threshold: the lowest bin thr[i] such that the entries in
+// bins >= thr[i] number at least k (0 = keep every entry when there are at
+// most k); sel[i] = how many entries that keeps.  One warp per table.
+__global__ void k_tabs_thresh(const unsigned long long *cnt, const uint32_t *hist, uint32_t nt, uint32_t k,
+                              uint32_t *thr, unsigned long long *sel)
+{
+    const uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= nt || (threadIdx.x & 31) != 0) return;
+    if (cnt[i] <= k) {
+        thr[i] = 0;
+        sel[i] = cnt[i];
+        return;
+    }
+    const uint32_t *h = hist + (uint64_t)i * kCountBins;
+    unsigned long long acc = 0;
+    uint32_t b = kCountBins;
+    while (b > 0 && acc < k) acc += h[--b];
+    thr[i] = b > 0 ? b : 1;  // bin 0 is the empty count and never occupied
+    sel[i] = acc;
 }
 
 // Sorted hash entries j (keys table << name_bits | name, counts) go to
