@@ -68,7 +68,7 @@ def parse():
     p.add_argument("--serve-rates", default="1000,10000,50000")
     p.add_argument("--serve-queries", type=int, default=3000)
     p.add_argument("--serve-budget-max", type=float, default=1e6)
-    p.add_argument("--serve-tick", type=int, default=1 << 21, help="walkers per serving tick")
+    p.add_argument("--serve-tick", type=int, default=1 << 23, help="walkers per serving tick")
     p.add_argument("--serve-top-k", type=int, default=1000,
                    help="entries returned per query (largest counts); 0 = full vectors.  With k > 0 one "
                         "extra run at the second rate returns full vectors")
@@ -194,7 +194,10 @@ def run_reference(args):
     t0 = time.perf_counter()
     canon = oracle.rmat_clean_csr(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed, threads)
     build_s = time.perf_counter() - t0
-    S, _, _ = cpu_port_sample(canon, args.sp, args.seed, threads, target_s=2.0)
+    # each step a bounded sample, sized so that warm-up + timed steps take
+    # about 90 s of walking whatever K and W are (at most 2 s per step)
+    S, _, _ = cpu_port_sample(canon, args.sp, args.seed, threads,
+                              target_s=min(2.0, 90.0 / max(1, args.steps + args.warmup)))
     for k in range(args.warmup):
         cpu_port_run(canon, args.sp, 1000 + k, S, threads)
     tot_moves, tot_s = 0, 0.0

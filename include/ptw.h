@@ -269,7 +269,7 @@ typedef struct ptw_serve_cfg {
     int32_t app;            /* PTW_APP_* */
     uint32_t max_moves;
     uint64_t table_bytes;   /* device arena for count tables; 0 = 1/4 of free memory */
-    uint64_t tick_walkers;  /* walkers started per tick over all active queries; 0 = 2^22 */
+    uint64_t tick_walkers;  /* walkers started per tick over all active queries; 0 = 2^23 */
     uint32_t max_active;    /* query slots; 0 = 4096 */
     uint32_t use_graph;     /* 1 = replay the tick as a CUDA graph */
     double table_factor;    /* as in ptw_batch_cfg */

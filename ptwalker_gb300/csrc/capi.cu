@@ -650,7 +650,6 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
     cfg.start_mode = PTW_START_PER_VERTEX;
     const ptw_tune saved = g->tune;
     ptw_tune bt = saved;
-    float bms = 1e30f;
     const int blocks[] = {256, 512, 1024};
     const int ilps[] = {2, 4};
     const int chunks[] = {64, 256};
@@ -659,6 +658,36 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
     const int hintss[] = {0, 1};
     const int exts[] = {0, 1};
     WalkLaunch wl = make_launch(&cfg);
+    // Median time per launch of `reps` timings after one warm-up (the warm-up
+    // also builds a column copy the candidate asks for); each timing runs
+    // three launches back to back, as a caller's loop of walks does, so the
+    // launch tails and gaps count the way they do there.  A negative time
+    // marks a candidate that does not launch.
+    auto time_walk = [&](const ptw_tune &t, int reps, float *med) -> int {
+        std::vector<float> ms(reps);
+        for (int rep = -1; rep < reps; ++rep) {
+            PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
+            for (int l = 0; l < 3; ++l) {
+                PTW_CUDA(cudaMemsetAsync(g->sc.counts, 0, (uint64_t)g->dg.n * 4, g->stream));
+                if (launch_walk(g, wl, t) != PTW_OK) {
+                    *med = -1.f;
+                    return PTW_OK;
+                }
+            }
+            PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
+            PTW_CUDA(cudaEventSynchronize(g->ev[1]));
+            float x = 0;
+            PTW_CUDA(cudaEventElapsedTime(&x, g->ev[0], g->ev[1]));
+            if (rep >= 0) ms[rep] = x / 3.f;
+        }
+        std::sort(ms.begin(), ms.end());
+        *med = reps % 2 ? ms[reps / 2] : 0.5f * (ms[reps / 2 - 1] + ms[reps / 2]);
+        return PTW_OK;
+    };
+    // Stage 1: every candidate, median of 3.  The candidates differ by a few
+    // percent, about the launch-to-launch noise, so stage 2 re-times the six
+    // fastest in three interleaved rounds of 5 and keeps the lowest median.
+    std::vector<std::pair<float, ptw_tune>> cand;
     for (int ex : exts)
     for (int hn : hintss)
     for (int mb : minbs)
@@ -676,26 +705,23 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
                     t.cache_hints = hn;
                     t.paths_ilp = 2;
                     t.ext_columns = ex;  // walks only; the paths sweep sets bit 1
-                    // median of four timed launches after one warm-up: the
-                    // candidates differ by a few percent, so one noisy
-                    // launch must not pick the winner
-                    float ms_rep[5] = {0, 0, 0, 0, 0};
-                    bool ok = true;
-                    for (int rep = 0; rep < 5 && ok; ++rep) {
-                        PTW_CUDA(cudaMemsetAsync(g->sc.counts, 0, (uint64_t)g->dg.n * 4, g->stream));
-                        PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
-                        if (launch_walk(g, wl, t) != PTW_OK) ok = false;
-                        PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
-                        PTW_CUDA(cudaEventSynchronize(g->ev[1]));
-                        PTW_CUDA(cudaEventElapsedTime(&ms_rep[rep], g->ev[0], g->ev[1]));
-                    }
-                    std::sort(ms_rep + 1, ms_rep + 5);
-                    const float tot = 0.5f * (ms_rep[2] + ms_rep[3]);
-                    if (ok && tot < bms) {
-                        bms = tot;
-                        bt = t;
-                    }
+                    float med = 0;
+                    int rc = time_walk(t, 3, &med);
+                    if (rc) return rc;
+                    if (med > 0) cand.push_back({med, t});
                 }
+    if (cand.empty()) return fail(PTW_EINVAL, "no walk configuration launches on this device");
+    std::sort(cand.begin(), cand.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+    cand.resize(std::min<size_t>(cand.size(), 6));
+    std::vector<float> sum(cand.size(), 0.f);
+    for (int round = 0; round < 3; ++round)
+        for (size_t c = 0; c < cand.size(); ++c) {
+            float med = 0;
+            int rc = time_walk(cand[c].second, 5, &med);
+            if (rc) return rc;
+            sum[c] += med;
+        }
+    bt = cand[std::min_element(sum.begin(), sum.end()) - sum.begin()].second;
     // DeepWalk: groups per warp x column layout (extended / name-paired /
     // plain), timed on a short fixed-length walk each.
     {

@@ -301,7 +301,7 @@ extern "C" int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server
     if (!s) return fail(PTW_ENOMEM, "host allocation failed");
     s->g = g;
     s->cfg = *cfg;
-    if (!s->cfg.tick_walkers) s->cfg.tick_walkers = 1ull << 22;
+    if (!s->cfg.tick_walkers) s->cfg.tick_walkers = 1ull << 23;
     if (!s->cfg.max_active) s->cfg.max_active = 4096;
     s->S = s->cfg.max_active;
     s->thr = cfg->sp >= 1.0 ? (1ull << 32) : (uint64_t)(cfg->sp * 4294967296.0);
