@@ -61,6 +61,7 @@ def parse():
                         "(skips the autotuner)")
     p.add_argument("--no-batch", action="store_true", help="skip the batched-PPR side line")
     p.add_argument("--no-serve", action="store_true", help="skip the serving side line")
+    p.add_argument("--no-ingest", action="store_true", help="skip the edge-list ingest side line")
     p.add_argument("--learned", action="store_true", help="add the learned-budget side line (minutes)")
     p.add_argument("--batch-scale", type=int, default=22)
     p.add_argument("--batch-queries", type=int, default=4096)
@@ -280,6 +281,38 @@ def bench_batch(args, ptw):
     res.close()
     one.close()
     G.close()
+    return out
+
+
+def bench_ingest(args, ptw):
+    """Edge-list ingest (the reference's Graph::load, graph.hpp:277-785, whose
+    text reader is one thread of sscanf, io.hpp:76-90): the R-MAT scale-22
+    graph written by ptw_graph_save as text and as binary Edge[], then timed
+    through ptw_graph_load: parse on all host threads, upload, device CSR
+    build with the degree-sorted relabelling."""
+    import shutil
+    G = ptw.Graph.rmat(args.batch_scale, 16, 0.57, 0.19, 0.19, seed=1, clean=True)
+    tmp = tempfile.mkdtemp(prefix="ptw_ingest_")
+    out = {"graph": "rmat-s%d" % args.batch_scale, "vertices": G.n, "edges": G.m}
+    try:
+        for fmt in ("text", "binary"):
+            path = os.path.join(tmp, "g." + fmt)
+            t0 = time.perf_counter()
+            G.save(path, fmt)
+            save_s = time.perf_counter() - t0
+            size = os.path.getsize(path)
+            ptw.Graph.load(path, fmt).close()  # warm: page cache, CUDA context
+            t0 = time.perf_counter()
+            H = ptw.Graph.load(path, fmt)
+            load_s = time.perf_counter() - t0
+            ok = H.n == G.n and H.m == G.m
+            H.close()
+            out[fmt] = {"file_bytes": size, "save_s": save_s, "load_s": load_s,
+                        "edges_per_s": G.m / load_s, "gb_per_s": size / load_s / 1e9, "same_graph": ok,
+                        "threads": os.cpu_count()}
+    finally:
+        G.close()
+        shutil.rmtree(tmp, ignore_errors=True)
     return out
 
 
@@ -571,6 +604,7 @@ def run_ours(args):
     G.close()
     if rank == 0 and world == 1:
         for key, flag, fn in (("batched_ppr", args.no_batch, bench_batch), ("serving", args.no_serve, bench_serve),
+                              ("ingest", args.no_ingest, bench_ingest),
                               ("learned_budgets", not args.learned, bench_learned)):
             if flag:
                 continue

@@ -152,6 +152,12 @@ int ptw_graph_export_csr(const ptw_graph *g, uint32_t *h_names /*[n]*/,
  * (include/io.hpp:55-74, :92-105). */
 int ptw_graph_export_edges(const ptw_graph *g, uint32_t *h_src, uint32_t *h_dst);
 
+/* Writes the graph's directed edges, sorted by (src, dst) name, in the
+ * reference's text ("%u %u" per line) or binary (Edge{u32, u32}) format:
+ * write_text_graph / write_binary_graph (include/io.hpp:55-74, :92-105),
+ * formatted on all host threads.  PTW_EIO when the file cannot be written. */
+int ptw_graph_save(const ptw_graph *g, const char *path, int32_t fmt);
+
 void ptw_graph_free(ptw_graph *g);
 
 int ptw_graph_set_tune(ptw_graph *g, const ptw_tune *t);

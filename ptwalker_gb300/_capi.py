@@ -106,6 +106,7 @@ SIGNATURES = [
     ("ptw_graph_get_info", ctypes.c_int, [_G, ctypes.POINTER(GraphInfo)]),
     ("ptw_graph_export_csr", ctypes.c_int, [_G, _u32p, _u64p, _u32p]),
     ("ptw_graph_export_edges", ctypes.c_int, [_G, _u32p, _u32p]),
+    ("ptw_graph_save", ctypes.c_int, [_G, ctypes.c_char_p, ctypes.c_int32]),
     ("ptw_graph_free", None, [_G]),
     ("ptw_graph_set_tune", ctypes.c_int, [_G, ctypes.POINTER(Tune)]),
     ("ptw_graph_get_tune", ctypes.c_int, [_G, ctypes.POINTER(Tune)]),

@@ -171,6 +171,12 @@ class Graph:
         C.check(lib.ptw_graph_chung_lu(int(n), float(gamma), float(mean_degree), int(seed), ctypes.byref(h)))
         return cls(h)
 
+    def save(self, path, fmt="text"):
+        """Writes the directed edge list (sorted by source, then destination
+        name) as text (``%u %u`` lines) or binary Edge[] (include/io.hpp)."""
+        f = {"text": C.PTW_FMT_TEXT, "binary": C.PTW_FMT_BINARY}[fmt]
+        C.check(self._lib.ptw_graph_save(self.handle, str(path).encode(), f))
+
     # -- lifetime ----------------------------------------------------------
     def close(self):
         if self._h:

@@ -386,6 +386,75 @@ extern "C" int ptw_graph_load(const char *path, int32_t fmt, int32_t as_undirect
     return upload_and_build(src.data(), dst.data(), src.size(), as_undirected != 0, out);
 }
 
+namespace ptw {
+namespace {
+
+// Decimal digits of x at p; returns the end.
+inline char *put_u32(char *p, uint32_t x)
+{
+    char tmp[10];
+    int k = 0;
+    do {
+        tmp[k++] = (char)('0' + x % 10);
+        x /= 10;
+    } while (x);
+    while (k) *p++ = tmp[--k];
+    return p;
+}
+
+}  // namespace
+}  // namespace ptw
+
+extern "C" int ptw_graph_save(const ptw_graph *g, const char *path, int32_t fmt)
+{
+    if (!g || !path) return fail(PTW_EINVAL, "null argument");
+    if (fmt != PTW_FMT_BINARY && fmt != PTW_FMT_TEXT) return fail(PTW_EINVAL, "unknown graph format");
+    const uint64_t m = g->dg.m;
+    std::vector<uint32_t> src(m), dst(m);
+    int rc = ptw_graph_export_edges(g, src.data(), dst.data());
+    if (rc) return rc;
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return fail(PTW_EIO, std::string("cannot create ") + path);
+    // Rounds of nt chunks: formatted in parallel, written in order.
+    const unsigned nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    const uint64_t chunk = 1u << 22;
+    std::vector<std::string> buf(nt);
+    bool ok = true;
+    for (uint64_t r0 = 0; r0 < m && ok; r0 += chunk * nt) {
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < nt; ++t) {
+            const uint64_t lo = std::min(m, r0 + t * chunk), hi = std::min(m, lo + chunk);
+            th.emplace_back([&, t, lo, hi] {
+                std::string &b = buf[t];
+                if (fmt == PTW_FMT_BINARY) {
+                    b.resize((hi - lo) * 8);
+                    uint32_t *w = reinterpret_cast<uint32_t *>(&b[0]);
+                    for (uint64_t e = lo; e < hi; ++e) {
+                        w[2 * (e - lo)] = src[e];
+                        w[2 * (e - lo) + 1] = dst[e];
+                    }
+                } else {
+                    b.resize((hi - lo) * 22);  // two 10-digit numbers, a space, a newline
+                    char *p = &b[0];
+                    for (uint64_t e = lo; e < hi; ++e) {
+                        p = put_u32(p, src[e]);
+                        *p++ = ' ';
+                        p = put_u32(p, dst[e]);
+                        *p++ = '\n';
+                    }
+                    b.resize(p - &b[0]);
+                }
+            });
+        }
+        for (auto &x : th) x.join();
+        for (unsigned t = 0; t < nt && ok; ++t)
+            if (!buf[t].empty() && std::fwrite(buf[t].data(), 1, buf[t].size(), f) != buf[t].size()) ok = false;
+    }
+    if (std::fclose(f) != 0) ok = false;
+    if (!ok) return fail(PTW_EIO, std::string("write failed: ") + path);
+    return PTW_OK;
+}
+
 extern "C" int ptw_graph_from_edges(const uint32_t *h_src, const uint32_t *h_dst, uint64_t m,
                                     int32_t as_undirected, ptw_graph **out)
 {

@@ -118,3 +118,20 @@ def test_gather_probe_reports_a_rate(gpu):
     small = gpu.probe_gather(1 << 20, 4)        # L2-resident
     large = gpu.probe_gather(1 << 30, 4)        # far above L2
     assert small > large > 1e9
+
+
+def test_save_round_trip_and_text_bytes(gpu, tmp_path, s16_edges, s16_canon):
+    s, d = s16_edges
+    want_txt = tmp_path / "oracle.txt"
+    oracle.write_text_edges(str(want_txt), s, d)
+    with gpu.Graph.rmat(16, 16, 0.57, 0.19, 0.19, seed=1, clean=True) as G:
+        for fmt in ("text", "binary"):
+            p = tmp_path / ("g." + fmt)
+            G.save(p, fmt)
+            with gpu.Graph.load(p, fmt) as H:
+                assert_same_graph(H, s16_canon)
+        assert (tmp_path / "g.text").read_bytes() == want_txt.read_bytes()
+        raw = np.fromfile(tmp_path / "g.binary", dtype=np.uint32).reshape(-1, 2)
+        assert np.array_equal(raw[:, 0], s) and np.array_equal(raw[:, 1], d)
+        with pytest.raises(gpu.PTWError):
+            G.save(tmp_path / "no_such_dir" / "g.txt", "text")
