@@ -199,7 +199,15 @@ def evaluate(graph, train_src, test_src, b_fix, sp=0.2, seed=0, grid_points=7, r
     learned = ppr_batch(graph, test_src, budgets, sp=sp, seed=seed + 1, query_ids=qids)
     l1_f = fixed.l1(tol=l1_tol)
     l1_l = learned.l1(tol=l1_tol)
+    # Ceiling of any budget predictor: a fixed budget meets eps for 90% of
+    # queries when it is the 90th percentile of the needed budgets b*, while
+    # exact per-query budgets spend their mean; p90(b*) / mean(b*) is the
+    # most a predictor can save at equal 90th-percentile error.
+    b_star = np.exp(np.asarray(log_b, np.float64))
+    ideal_gain = float(np.quantile(b_star, 0.9) / b_star.mean())
     return dict(eps_train=eps, fixed_budget=int(b_fix), fixed_moves=int(fixed.moves),
+                ideal_gain_from_labels=ideal_gain,
+                label_budget_quantiles=[float(np.quantile(b_star, q) / b_fix) for q in (0.1, 0.5, 0.9)],
                 learned_moves=int(learned.moves), gain=fixed.moves / max(learned.moves, 1),
                 fixed_l1_p50=float(np.median(l1_f)), fixed_l1_p90=float(np.quantile(l1_f, 0.9)),
                 learned_l1_p50=float(np.median(l1_l)), learned_l1_p90=float(np.quantile(l1_l, 0.9)),
