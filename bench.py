@@ -56,7 +56,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--tune", default=None,
-                   help="block,ilp,chunk,hot_k[,min_blocks[,paths_ilp[,cache_hints[,paths_named[,ext_columns]]]]]: "
+                   help="block,ilp,chunk,hot_k[,min_blocks[,paths_ilp[,cache_hints[,paths_named[,ext_columns"
+                        "[,gather_slots]]]]]]: "
                         "fixed launch parameters "
                         "(skips the autotuner)")
     p.add_argument("--no-batch", action="store_true", help="skip the batched-PPR side line")
@@ -371,7 +372,7 @@ def get_tune(G, ptw, args, dev_name):
     if args.tune:
         v = [int(x) for x in args.tune.split(",")]
         names = ["block", "ilp", "chunk", "hot_k", "min_blocks", "paths_ilp", "cache_hints", "paths_named",
-                 "ext_columns"]
+                 "ext_columns", "gather_slots"]
         G.tune = ptw.Tune(**dict(zip(names, v)))
         return G.tune, "fixed"
     path = tune_cache_path()

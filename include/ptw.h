@@ -95,7 +95,8 @@ typedef struct ptw_tune {
     int32_t chunk;         /* walker ids taken per warp refill */
     int32_t hot_k;         /* vertex ids < hot_k counted in shared memory (0 = off) */
     int32_t blocks_per_sm; /* 0 = as many as fit */
-    int32_t min_blocks;    /* 2 = cap registers so two 512-thread blocks fit per SM; 0 = no cap */
+    int32_t min_blocks;    /* 2 = cap registers so two blocks fit per SM (block <= 512, 768 or
+                              1024: 64, 42 or 32 registers); 0 = no cap */
     int32_t paths_ilp;     /* DeepWalk: groups of 32 walkers per warp, 1, 2 or 4 */
     int32_t cache_hints;   /* 1 = L2 evict_last for row records and counters, evict_first
                               for the column array; 0 = default L2 policy */
@@ -107,6 +108,12 @@ typedef struct ptw_tune {
                               (16 bytes per CSR entry, built on first use), so a move is one
                               16-byte gather with no row-record load; 0 = off.  Falls back to
                               off when the copy does not fit. */
+    int32_t gather_slots;  /* count / endpoint walks: 0 = walkers in registers (ilp per thread);
+                              8 or 16 = walkers in shared memory, this many per thread, each
+                              move an asynchronous 16-byte gather (cp.async) into shared memory,
+                              so a thread keeps that many gathers in flight without registers.
+                              Uses the extended column copy and a 16-byte record per vertex. */
+    int32_t reserved;
 } ptw_tune;
 
 const char *ptw_last_error(void);

@@ -83,7 +83,8 @@ class Tune(ctypes.Structure):
                 ("hot_k", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("min_blocks", ctypes.c_int32), ("paths_ilp", ctypes.c_int32),
                 ("cache_hints", ctypes.c_int32), ("paths_named", ctypes.c_int32),
-                ("ext_columns", ctypes.c_int32)]
+                ("ext_columns", ctypes.c_int32), ("gather_slots", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 # Every symbol include/ptw.h declares: (name, restype, argtypes).

@@ -719,7 +719,7 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
     cfg.start_mode = PTW_START_PER_VERTEX;
     const ptw_tune saved = g->tune;
     ptw_tune bt = saved;
-    const int blocks[] = {256, 512, 1024};
+    const int blocks[] = {256, 512, 768, 1024};
     const int ilps[] = {2, 4};
     const int chunks[] = {64, 256};
     const int hots[] = {0, 8192};
@@ -779,6 +779,25 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
                     if (rc) return rc;
                     if (med > 0) cand.push_back({med, t});
                 }
+    // walkers in shared memory: slots per thread x block x hot counters
+    for (int gs : {8, 16})
+        for (int bl : {128, 256})
+            for (int hk : {0, 8192})
+                for (int hn : {0, 1})
+                    for (int ch : {64, 256}) {
+                        ptw_tune t{};
+                        t.block = bl;
+                        t.ilp = 2;
+                        t.chunk = ch;
+                        t.hot_k = hk;
+                        t.cache_hints = hn;
+                        t.paths_ilp = 2;
+                        t.gather_slots = gs;
+                        float med = 0;
+                        int rc = time_walk(t, 3, &med);
+                        if (rc) return rc;
+                        if (med > 0) cand.push_back({med, t});
+                    }
     if (cand.empty()) return fail(PTW_EINVAL, "no walk configuration launches on this device");
     std::sort(cand.begin(), cand.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
     cand.resize(std::min<size_t>(cand.size(), 6));

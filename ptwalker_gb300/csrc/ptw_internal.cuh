@@ -75,6 +75,20 @@ __device__ __forceinline__ uint4 ld_hint_u4(const uint4 *p, uint64_t pol)
     return r;
 }
 
+// Asynchronous 16-byte global -> shared copy (cp.async, L1 bypassed) with an
+// L2 eviction-priority policy; completes at the next cp_async_wait_all.
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src, uint64_t pol)
+{
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(d), "l"(gmem_src), "l"(pol)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 __device__ __forceinline__ uint32_t ld_hint_u32(const uint32_t *p, uint64_t pol)
 {
     uint32_t r;
@@ -104,6 +118,7 @@ struct DeviceGraph {
     uint2 *col_named = nullptr;   // [m] {neighbour internal id, its name}; built on first path walk
     uint4 *col_ext = nullptr;     // [m] {neighbour id, its first column, its degree, its name};
                                   // built on the first walk with tune.ext_columns
+    uint4 *vtx_ext = nullptr;     // [n] {id, first column, degree, name}, built with col_ext
 };
 
 // Scratch owned by a graph handle and reused by every call.

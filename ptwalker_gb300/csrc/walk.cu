@@ -41,6 +41,7 @@ struct WalkArgs {
     const uint2 *__restrict__ adj;
     const uint32_t *__restrict__ col;
     const uint4 *__restrict__ col_ext;       // EXT: {id, first column, degree, name} per entry
+    const uint4 *__restrict__ vtx_ext;       // {id, first column, degree, name} per vertex
     const uint32_t *__restrict__ start_map;  // canonical index -> internal
     const uint32_t *__restrict__ sources;    // internal ids
     const uint32_t *__restrict__ int2name;
@@ -224,13 +225,180 @@ __global__ void k_walk(const WalkArgs a)
     walk_body<ENDPOINT, ILP, HOT, EXT>(a, s_hot);
 }
 
-// At most 64 registers so two 512-thread blocks fit on an SM: twice the
-// walkers in flight for the latency-bound gathers.
+// Register caps so that two blocks fit on an SM, for more walkers in flight:
+// two 512-thread blocks (64 registers), two 768-thread blocks (42
+// registers; ILP 2 holds 3072 walkers per SM) or two 1024-thread blocks
+// (32 registers; 4096 walkers per SM at ILP 2, with a few spills).
 template <bool ENDPOINT, int ILP, bool HOT, bool EXT>
 __global__ void __launch_bounds__(512, 2) k_walk_b2(const WalkArgs a)
 {
     extern __shared__ uint32_t s_hot[];
     walk_body<ENDPOINT, ILP, HOT, EXT>(a, s_hot);
+}
+
+template <bool ENDPOINT, int ILP, bool HOT, bool EXT>
+__global__ void __launch_bounds__(768, 2) k_walk_b2_768(const WalkArgs a)
+{
+    extern __shared__ uint32_t s_hot[];
+    walk_body<ENDPOINT, ILP, HOT, EXT>(a, s_hot);
+}
+
+template <bool ENDPOINT, int ILP, bool HOT, bool EXT>
+__global__ void __launch_bounds__(1024, 2) k_walk_b2_1024(const WalkArgs a)
+{
+    extern __shared__ uint32_t s_hot[];
+    walk_body<ENDPOINT, ILP, HOT, EXT>(a, s_hot);
+}
+
+// K1/K2 with walkers in shared memory.  Each thread owns S walker slots;
+// a slot holds the walker's id, step, start name, flags and a 16-byte
+// landing buffer with the record {id, first column, degree, name} of the
+// vertex it stands on.  One round: refill empty slots (warp ballot, as in
+// walk_body) and start their record gathers; for every other walker draw the
+// move and start the gather of the chosen column entry; wait for all of the
+// thread's gathers; count the landed vertices and apply the stop decisions.
+// The gathers are cp.async copies into shared memory, so a thread has S of
+// them in flight without holding S destination registers: with 4096
+// walkers per SM in flight the random-gather rate of the GPU is reached,
+// where register-resident walkers stop at about 2048.  Draws and semantics
+// are those of walk_body, so results are identical.
+constexpr uint32_t kSlotActive = 1, kSlotStart = 2, kSlotMoved = 4, kSlotStop = 8;
+
+template <bool ENDPOINT, bool HOT, int S>
+__global__ void __launch_bounds__(256) k_walk_async(const WalkArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t T = blockDim.x;
+    const uint32_t tid = threadIdx.x;
+    uint4 *land = reinterpret_cast<uint4 *>(smem);                              // [S*T]
+    unsigned long long *wid = reinterpret_cast<unsigned long long *>(land + S * T); // [S*T]
+    uint32_t *step = reinterpret_cast<uint32_t *>(wid + S * T);                  // [S*T]
+    uint32_t *s0n = step + S * T;                                                // [S*T] start name
+    uint32_t *flag = s0n + S * T;                                                // [S*T]
+    uint32_t *s_hot = flag + S * T;                                              // [hot_k]
+    if (HOT) {
+        for (uint32_t i = tid; i < a.hot_k; i += T) s_hot[i] = 0;
+    }
+#pragma unroll
+    for (int k = 0; k < S; ++k) flag[k * T + tid] = 0;
+    __syncthreads();
+    const uint64_t pol_keep = l2_policy(a.hints ? 1 : 0);
+    const uint64_t pol_stream = l2_policy(a.hints ? 2 : 0);
+    const uint32_t lane = tid & 31;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    uint64_t next = 0, end = 0;
+    bool exhausted = false;
+    unsigned long long moves = 0;
+
+    for (;;) {
+        // ---- refill empty slots; start their record gathers --------------
+#pragma unroll 1
+        for (int k = 0; k < S; ++k) {
+            const uint32_t i = k * T + tid;
+            const bool empty = (flag[i] & kSlotActive) == 0;
+            const unsigned need = __ballot_sync(kFull, empty);
+            if (need == 0 || exhausted) continue;
+            const uint32_t n_need = __popc(need);
+            const uint32_t rank = __popc(need & lt_mask);
+            uint64_t my = ~0ull;
+            const uint64_t avail = end - next;
+            const uint32_t took = (uint32_t)umin64(n_need, avail);
+            if (empty && rank < took) my = next + rank;
+            next += took;
+            if (took < n_need) {
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd(&a.ctrl[0], (unsigned long long)a.chunk);
+                base = __shfl_sync(kFull, base, 0);
+                if (base >= a.n_walk) {
+                    exhausted = true;
+                    next = end = a.n_walk;
+                } else {
+                    next = base;
+                    end = umin64(base + a.chunk, a.n_walk);
+                    const uint32_t take2 = (uint32_t)umin64(n_need - took, end - next);
+                    if (empty && rank >= took && rank - took < take2) my = next + (rank - took);
+                    next += take2;
+                }
+            }
+            if (my != ~0ull) {
+                const uint64_t w = a.w_begin + my;
+                wid[i] = w;
+                step[i] = 0;
+                flag[i] = kSlotActive | kSlotStart;
+                cp_async16(&land[i], &a.vtx_ext[start_vertex(a, w)], pol_keep);
+            }
+        }
+        bool any = false;
+#pragma unroll 1
+        for (int k = 0; k < S; ++k) any |= (flag[k * T + tid] & kSlotActive) != 0;
+        if (!__any_sync(kFull, any)) break;
+
+        // ---- draw and start one move for every walker standing on a record
+#pragma unroll 1
+        for (int k = 0; k < S; ++k) {
+            const uint32_t i = k * T + tid;
+            const uint32_t f = flag[i];
+            if ((f & kSlotActive) == 0 || (f & kSlotStart)) continue;
+            const uint4 x = land[i];  // {v, first column, degree, name}
+            if (x.z == 0) {           // no out-edge: the walk ends here
+                if (ENDPOINT) {
+                    const uint64_t j = wid[i] - a.w_begin;
+                    *reinterpret_cast<uint2 *>(&a.pairs[2 * j]) = make_uint2(s0n[i], x.w);
+                }
+                flag[i] = 0;
+                continue;
+            }
+            const uint64_t w = wid[i];
+            const uint32_t st = step[i];
+            const uint4 r = philox(make_uint4((uint32_t)w, (uint32_t)(w >> 32), st, PTW_TAG_WALK), a.key0, a.key1);
+            const bool stop = (uint64_t)r.y < a.thr || (a.max_moves && st + 1 >= a.max_moves);
+            flag[i] = kSlotActive | kSlotMoved | (stop ? kSlotStop : 0u);
+            cp_async16(&land[i], &a.col_ext[x.y + __umulhi(r.x, x.z)], pol_stream);
+        }
+        cp_async_wait_all();
+
+        // ---- count the landed vertices, apply the stop decisions -----------
+#pragma unroll 1
+        for (int k = 0; k < S; ++k) {
+            const uint32_t i = k * T + tid;
+            const uint32_t f = flag[i];
+            if ((f & kSlotActive) == 0) continue;
+            const uint4 x = land[i];
+            if (f & kSlotStart) {
+                s0n[i] = x.w;
+                if (!ENDPOINT) count_visit<HOT>(a, s_hot, x.x, pol_keep);
+                flag[i] = kSlotActive;
+            } else if (f & kSlotMoved) {
+                step[i] += 1;
+                ++moves;
+                if (!ENDPOINT) count_visit<HOT>(a, s_hot, x.x, pol_keep);
+                if (f & kSlotStop) {
+                    if (ENDPOINT) {
+                        const uint64_t j = wid[i] - a.w_begin;
+                        *reinterpret_cast<uint2 *>(&a.pairs[2 * j]) = make_uint2(s0n[i], x.w);
+                    }
+                    flag[i] = 0;
+                } else {
+                    flag[i] = kSlotActive;
+                }
+            }
+        }
+    }
+
+#pragma unroll
+    for (int o = 16; o; o >>= 1) moves += __shfl_xor_sync(kFull, moves, o);
+    if (lane == 0 && moves) atomicAdd(&a.ctrl[1], moves);
+    if (HOT) {
+        __syncthreads();
+        for (uint32_t i = tid; i < a.hot_k; i += T)
+            if (s_hot[i]) atomicAdd(&a.counts[i], s_hot[i]);
+    }
+}
+
+// Dynamic shared memory of k_walk_async: 36 bytes per slot + hot counters.
+inline size_t async_smem(int slots, int block, uint32_t hot_k)
+{
+    return (size_t)slots * block * 36 + (size_t)hot_k * 4;
 }
 
 struct PathArgs {
@@ -375,6 +543,14 @@ __global__ void k_ext_columns(const uint32_t *col, const uint2 *adj, const uint3
     }
 }
 
+__global__ void k_vertex_ext(const uint2 *adj, const uint32_t *int2name, uint32_t n, uint4 *vtx_ext)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint2 r = adj[v];
+        vtx_ext[v] = make_uint4(v, r.x, r.y, int2name[v]);
+    }
+}
+
 __global__ void k_counts_by_name(const uint32_t *counts, const uint32_t *int2name, uint32_t n,
                                  uint32_t *out)
 {
@@ -382,31 +558,48 @@ __global__ void k_counts_by_name(const uint32_t *counts, const uint32_t *int2nam
         out[int2name[i]] = counts[i];
 }
 
-template <bool E, int ILP, bool H, bool X> void *walk_fn(bool b2)
+// cap: 0 = no register cap, 512 / 768 / 1024 = two blocks of that size per SM.
+template <bool E, int ILP, bool H, bool X> void *walk_fn(int cap)
 {
-    return b2 ? (void *)k_walk_b2<E, ILP, H, X> : (void *)k_walk<E, ILP, H, X>;
-}
-
-template <bool E, bool H, bool X> void *walk_fn_ilp(int ilp, bool b2)
-{
-    switch (ilp) {
-    case 1: return walk_fn<E, 1, H, X>(b2);
-    case 4: return walk_fn<E, 4, H, X>(b2);
-    default: return walk_fn<E, 2, H, X>(b2);
+    switch (cap) {
+    case 512: return (void *)k_walk_b2<E, ILP, H, X>;
+    case 768: return (void *)k_walk_b2_768<E, ILP, H, X>;
+    case 1024: return (void *)k_walk_b2_1024<E, ILP, H, X>;
+    default: return (void *)k_walk<E, ILP, H, X>;
     }
 }
 
-template <bool X> void *pick_walk_x(bool endpoint, int ilp, bool hot, bool b2)
+template <bool E, bool H, bool X> void *walk_fn_ilp(int ilp, int cap)
 {
-    if (endpoint) return walk_fn_ilp<true, false, X>(ilp, b2);
-    if (hot) return walk_fn_ilp<false, true, X>(ilp, b2);
-    return walk_fn_ilp<false, false, X>(ilp, b2);
+    switch (ilp) {
+    case 1: return walk_fn<E, 1, H, X>(cap);
+    case 4: return walk_fn<E, 4, H, X>(cap);
+    default: return walk_fn<E, 2, H, X>(cap);
+    }
 }
 
-void *pick_walk(bool endpoint, int ilp, bool hot, int min_blocks, bool ext)
+template <bool X> void *pick_walk_x(bool endpoint, int ilp, bool hot, int cap)
 {
-    const bool b2 = min_blocks == 2;
-    return ext ? pick_walk_x<true>(endpoint, ilp, hot, b2) : pick_walk_x<false>(endpoint, ilp, hot, b2);
+    if (endpoint) return walk_fn_ilp<true, false, X>(ilp, cap);
+    if (hot) return walk_fn_ilp<false, true, X>(ilp, cap);
+    return walk_fn_ilp<false, false, X>(ilp, cap);
+}
+
+void *pick_walk_async(bool endpoint, bool hot, int slots)
+{
+    if (slots == 16) {
+        if (endpoint) return (void *)k_walk_async<true, false, 16>;
+        return hot ? (void *)k_walk_async<false, true, 16> : (void *)k_walk_async<false, false, 16>;
+    }
+    if (endpoint) return (void *)k_walk_async<true, false, 8>;
+    return hot ? (void *)k_walk_async<false, true, 8> : (void *)k_walk_async<false, false, 8>;
+}
+
+// min_blocks 2 picks the register cap by block size (checked by check_tune).
+void *pick_walk(bool endpoint, int ilp, bool hot, int min_blocks, int block, bool ext)
+{
+    const int cap = min_blocks != 2 ? 0 : block <= 512 ? 512 : block <= 768 ? 768 : 1024;
+    return ext ? pick_walk_x<true>(endpoint, ilp, hot, cap) : pick_walk_x<false>(endpoint, ilp, hot, cap);
 }
 
 // Builds the extended column copy on first use; false (and no error) when
@@ -426,8 +619,22 @@ bool ensure_ext_columns(ptw_graph *g)
         cudaFree(cx);
         return false;
     }
+    uint4 *vx = nullptr;
+    if (cudaMalloc(&vx, std::max<uint32_t>(dg.n, 1) * sizeof(uint4)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(cx);
+        return false;
+    }
+    const unsigned vgrid = (unsigned)std::min<uint64_t>((dg.n + 255) / 256, (uint64_t)g->num_sms * 64);
+    k_vertex_ext<<<std::max(vgrid, 1u), 256, 0, g->stream>>>(dg.adj, dg.int2name, dg.n, vx);
+    if (cudaGetLastError() != cudaSuccess) {
+        cudaFree(cx);
+        cudaFree(vx);
+        return false;
+    }
     g->dg.col_ext = cx;
-    g->device_bytes += dg.m * sizeof(uint4);
+    g->dg.vtx_ext = vx;
+    g->device_bytes += dg.m * sizeof(uint4) + (uint64_t)dg.n * sizeof(uint4);
     return true;
 }
 
@@ -436,11 +643,13 @@ bool ensure_ext_columns(ptw_graph *g)
 void drop_unused_columns(ptw_graph *g)
 {
     DeviceGraph &dg = g->dg;
-    if (dg.col_ext && !g->tune.ext_columns) {
+    if (dg.col_ext && !g->tune.ext_columns && !g->tune.gather_slots) {
         cudaStreamSynchronize(g->stream);
         cudaFree(dg.col_ext);
+        cudaFree(dg.vtx_ext);
         dg.col_ext = nullptr;
-        g->device_bytes -= dg.m * sizeof(uint4);
+        dg.vtx_ext = nullptr;
+        g->device_bytes -= dg.m * sizeof(uint4) + (uint64_t)dg.n * sizeof(uint4);
     }
     if (dg.col_named && ((g->tune.ext_columns & 2) || !g->tune.paths_named)) {
         cudaStreamSynchronize(g->stream);
@@ -461,13 +670,16 @@ int check_tune(const ptw_tune &t)
     if (t.blocks_per_sm < 0 || t.blocks_per_sm > 64) return fail(PTW_EINVAL, "tune.blocks_per_sm out of range");
     if (t.min_blocks != 0 && t.min_blocks != 1 && t.min_blocks != 2)
         return fail(PTW_EINVAL, "tune.min_blocks must be 0, 1 or 2");
-    if (t.min_blocks == 2 && t.block > 512)
-        return fail(PTW_EINVAL, "tune.min_blocks = 2 needs tune.block <= 512");
+    if (t.min_blocks == 2 && t.block > 512 && t.block != 768 && t.block != 1024)
+        return fail(PTW_EINVAL, "tune.min_blocks = 2 needs tune.block <= 512, 768 or 1024");
     if (t.paths_ilp != 0 && t.paths_ilp != 1 && t.paths_ilp != 2 && t.paths_ilp != 4)
         return fail(PTW_EINVAL, "tune.paths_ilp must be 1, 2 or 4 (0 = default)");
     if (t.cache_hints != 0 && t.cache_hints != 1) return fail(PTW_EINVAL, "tune.cache_hints must be 0 or 1");
     if (t.paths_named != 0 && t.paths_named != 1) return fail(PTW_EINVAL, "tune.paths_named must be 0 or 1");
     if (t.ext_columns < 0 || t.ext_columns > 3) return fail(PTW_EINVAL, "tune.ext_columns must be in [0, 3]");
+    if (t.gather_slots != 0 && t.gather_slots != 8 && t.gather_slots != 16)
+        return fail(PTW_EINVAL, "tune.gather_slots must be 0, 8 or 16");
+    if (t.gather_slots && t.block > 256) return fail(PTW_EINVAL, "tune.gather_slots needs tune.block <= 256");
     return PTW_OK;
 }
 
@@ -499,10 +711,14 @@ int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t)
     a.start_mode = wl.start_mode;
     a.hints = t.cache_hints;
 
-    const bool ext = (t.ext_columns & 1) && ensure_ext_columns(g);
+    const bool slots = t.gather_slots != 0 && ensure_ext_columns(g);
+    const bool ext = !slots && (t.ext_columns & 1) && ensure_ext_columns(g);
     a.col_ext = g->dg.col_ext;
-    void *fn = pick_walk(wl.endpoint, t.ilp, hot, t.min_blocks, ext);
-    const size_t smem = hot ? (size_t)a.hot_k * 4 : 0;
+    a.vtx_ext = g->dg.vtx_ext;
+    void *fn = slots ? pick_walk_async(wl.endpoint, hot, t.gather_slots)
+                     : pick_walk(wl.endpoint, t.ilp, hot, t.min_blocks, t.block, ext);
+    const size_t smem = slots ? async_smem(t.gather_slots, t.block, a.hot_k) : hot ? (size_t)a.hot_k * 4 : 0;
+    if (smem > 227 * 1024) return fail(PTW_EINVAL, "tune.gather_slots x tune.block x hot_k need too much shared memory");
     if (smem > 48 * 1024)
         PTW_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;

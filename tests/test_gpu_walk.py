@@ -75,6 +75,10 @@ def test_ppr_sources_and_query_ids(gpu, G16, s16_canon, sources, W, qid):
     dict(block=256, ilp=1, chunk=5, hot_k=0, cache_hints=0, ext_columns=1),
     dict(block=128, ilp=2, chunk=64, hot_k=300, min_blocks=2, ext_columns=1),
     dict(block=512, ilp=4, chunk=64, hot_k=0, min_blocks=2, ext_columns=1),
+    dict(block=256, ilp=2, chunk=64, hot_k=8192, gather_slots=16),
+    dict(block=128, ilp=2, chunk=7, hot_k=0, gather_slots=8),
+    dict(block=64, ilp=1, chunk=256, hot_k=100, gather_slots=8, cache_hints=0),
+    dict(block=256, ilp=4, chunk=4096, hot_k=10000, gather_slots=16),
 ])
 def test_launch_parameters_do_not_change_results(gpu, G16, s16_canon, tune):
     saved = G16.tune
@@ -92,6 +96,18 @@ def test_invalid_tune_rejected(gpu, G16):
         G16.tune = gpu.Tune(block=100)
     with pytest.raises(gpu.PTWError):
         G16.tune = gpu.Tune(ilp=3)
+    with pytest.raises(gpu.PTWError):
+        G16.tune = gpu.Tune(gather_slots=4)
+    with pytest.raises(gpu.PTWError):
+        G16.tune = gpu.Tune(block=512, gather_slots=8)
+    saved = G16.tune
+    try:
+        # 16 slots x 256 threads x 36 B + 40000 hot counters x 4 B > 227 KB of shared memory
+        G16.tune = gpu.Tune(block=256, hot_k=40000, gather_slots=16)
+        with pytest.raises(gpu.PTWError):
+            gpu.pagerank(G16, 1000, 0.15, 1)
+    finally:
+        G16.tune = saved
 
 
 @pytest.mark.parametrize("start,W,qid", [("per_vertex", None, 0), ("uniform", 10001, 3)])
@@ -162,13 +178,17 @@ def test_deepwalk_sources(gpu, G16, s16_canon):
     assert np.array_equal(got, want)
 
 
-def test_dead_ends_and_sparse_names(gpu):
+@pytest.mark.parametrize("tune", [None, dict(block=256, ilp=2, chunk=64, hot_k=64, gather_slots=16),
+                                  dict(block=128, ilp=2, chunk=5, hot_k=0, gather_slots=8, ext_columns=3)])
+def test_dead_ends_and_sparse_names(gpu, tune):
     rng = np.random.default_rng(1)
     names = np.sort(rng.choice(1 << 20, size=500, replace=False)).astype(np.uint32)
     src = names[rng.integers(0, 400, 4000)]  # the last 100 names have no out-edge
     dst = names[rng.integers(0, 500, 4000)]
     canon = oracle.canonical_from_edges(src, dst)
     with gpu.Graph.from_edges(src, dst) as G:
+        if tune:
+            G.tune = gpu.Tune(**tune)
         W = 3 * G.n + 1
         got, st = gpu.pagerank(G, W, 0.1, 5, "per_vertex", stats=True)
         want, moves = oracle.replay_counts(canon, 0, W, 0.1, 5, START_PER_VERTEX)
@@ -251,10 +271,13 @@ def test_pagerank_vs_fp64_oracle(gpu, G16, s16_canon):
     assert abs(zz.mean()) < 0.05 and zz.std() < 1.5
 
 
-def test_rwr_and_ppr_with_extended_columns(gpu, G16, s16_canon):
+@pytest.mark.parametrize("tune", [dict(block=256, ilp=4, chunk=64, hot_k=0, ext_columns=3),
+                                  dict(block=256, ilp=2, chunk=64, hot_k=0, ext_columns=3, gather_slots=16),
+                                  dict(block=128, ilp=2, chunk=33, hot_k=512, ext_columns=3, gather_slots=8)])
+def test_rwr_and_ppr_with_extended_columns(gpu, G16, s16_canon, tune):
     saved = G16.tune
     try:
-        G16.tune = gpu.Tune(block=256, ilp=4, chunk=64, hot_k=0, ext_columns=3)
+        G16.tune = gpu.Tune(**tune)
         got = gpu.rwr(G16, 3 * G16.n, 0.3, 29, "uniform")
         want, _ = oracle.replay_pairs(s16_canon, 0, 3 * G16.n, 0.3, 29, START_UNIFORM)
         assert np.array_equal(got, want)
@@ -264,5 +287,22 @@ def test_rwr_and_ppr_with_extended_columns(gpu, G16, s16_canon):
         with_ext = G16.device_bytes
     finally:
         G16.tune = saved
-    # turning the copy off releases its 16 bytes per CSR entry
-    assert with_ext - G16.device_bytes == 16 * G16.m
+    # turning the copy off releases its 16 bytes per CSR entry and per vertex
+    assert with_ext - G16.device_bytes == 16 * (G16.m + G16.n)
+
+
+@pytest.mark.parametrize("slots", [8, 16])
+def test_async_walkers_with_max_moves_and_offsets(gpu, G16, s16_canon, slots):
+    saved = G16.tune
+    try:
+        G16.tune = gpu.Tune(block=256, ilp=2, chunk=64, hot_k=2048, gather_slots=slots)
+        W = 3 * G16.n + 1
+        got, st = gpu.pagerank(G16, W, 0.001, 3, "uniform", max_moves=7, stats=True)
+        want, moves = oracle.replay_counts(s16_canon, 0, W, 0.001, 3, START_UNIFORM, max_moves=7)
+        assert np.array_equal(got, want) and st.moves == moves
+        got = gpu.rwr(G16, 5000, 0.3, 4, "per_vertex", max_moves=3, first_walker=(5 << 32) + 11)
+        want, _ = oracle.replay_pairs(s16_canon, (5 << 32) + 11, (5 << 32) + 5011, 0.3, 4, START_PER_VERTEX,
+                                      max_moves=3)
+        assert np.array_equal(got, want)
+    finally:
+        G16.tune = saved
