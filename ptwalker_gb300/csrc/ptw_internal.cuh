@@ -209,6 +209,12 @@ struct Compacted {
     std::unique_ptr<uint32_t[]> names, counts;
     std::function<uint32_t *(uint64_t)> sink;
     uint32_t *h_names = nullptr, *h_counts = nullptr;
+    // Optional host buffers of pre_cap entries, allocated before the walk
+    // and faulted in on host threads while it runs (pre_join waits for
+    // that); adopted when the lists fit, the unused tail handed back.
+    std::unique_ptr<uint32_t[]> pre_names, pre_counts;
+    uint64_t pre_cap = 0;
+    std::function<void()> pre_join;
 };
 // Compacts nt count tables into *out (batch.cu).  Table i starts at slot
 // h_base[i] of d_slots; a hash table (h_dense[i] == 0, or h_dense NULL) has
