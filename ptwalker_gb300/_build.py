@@ -29,6 +29,8 @@ def _nvcc():
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     files.append(os.path.join(HERE, "..", "include", "ptw.h"))
+    files.append(os.path.join(HERE, "cli", "ptw_cli.cpp"))
+    files.append(os.path.abspath(__file__))
     return files
 
 
@@ -36,6 +38,8 @@ def up_to_date():
     if not os.path.exists(SO):
         return False
     t = os.path.getmtime(SO)
+    if not all(os.path.lexists(os.path.join(OUT, "bin", a)) for a in APPS):
+        return False
     return all(os.path.getmtime(f) <= t for f in _deps())
 
 
@@ -69,7 +73,7 @@ def build(force=False, verbose=False, extra_flags=()):
 
 CLI_SRC = os.path.join(HERE, "cli", "ptw_cli.cpp")
 BIN_DIR = os.path.join(OUT, "bin")
-APPS = ("pagerank", "ppr", "rwr", "deepwalk")
+APPS = ("pagerank", "ppr", "PPR", "rwr", "RWR", "deepwalk")
 
 
 def build_cli():

@@ -14,6 +14,7 @@
 // --as-undirected.  The app is chosen by the executable name or by the
 // first argument (ptw_cli pagerank ...).  Like the reference apps, each
 // prints "ppr value %u" (here: the count of vertex name 0) on stdout.
+#include <cctype>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -33,15 +34,24 @@ struct Opts {
     bool undirected = false;
 };
 
+const char *kUsage =
+    "usage: {pagerank|ppr|rwr|deepwalk} -f text|binary -g PATH (-w W | -e E) [--sp P] [-l L]\n"
+    "       [--source NAME] [--seed S] [--start per_vertex|uniform] [--out FILE]\n"
+    "       [--paths-out FILE] [--as-undirected] [-t T -s S --mem G --socket-mapping M\n"
+    "       --ws N --db D (accepted, ignored)]\n"
+    "The app is the program name (pagerank, ppr or PPR, rwr or RWR, deepwalk) or the first argument.\n";
+
 int usage(const char *msg)
 {
-    std::fprintf(stderr, "error: %s\n", msg);
-    std::fprintf(stderr,
-                 "usage: {pagerank|ppr|rwr|deepwalk} -f text|binary -g PATH (-w W | -e E) [--sp P] [-l L]\n"
-                 "       [--source NAME] [--seed S] [--start per_vertex|uniform] [--out FILE]\n"
-                 "       [--paths-out FILE] [--as-undirected] [-t T -s S --mem G --socket-mapping M\n"
-                 "       --ws N --db D (accepted, ignored)]\n");
+    std::fprintf(stderr, "error: %s\n%s", msg, kUsage);
     return 1;
+}
+
+// The reference's program names (src/core/*.cpp) in lower case.
+std::string app_name(std::string a)
+{
+    for (char &c : a) c = (char)std::tolower((unsigned char)c);
+    return a;
 }
 
 const char *base_name(const char *p)
@@ -70,11 +80,15 @@ int main(int argc, char **argv)
 {
     Opts o;
     int i = 1;
-    o.app = base_name(argv[0]);
+    o.app = app_name(base_name(argv[0]));
     if (o.app != "pagerank" && o.app != "ppr" && o.app != "rwr" && o.app != "deepwalk") {
         if (argc < 2) return usage("missing app name");
-        o.app = argv[1];
+        o.app = app_name(argv[1]);
         i = 2;
+        if (o.app == "-h" || o.app == "--help") {
+            std::fputs(kUsage, stdout);
+            return 0;
+        }
     }
     for (; i < argc; ++i) {
         std::string a = argv[i];
@@ -103,7 +117,8 @@ int main(int argc, char **argv)
                  a == "--db") {
             // CPU pool / NUMA sizing in the reference: not used on the GPU
         } else if (a == "-h" || a == "--help") {
-            return usage("help");
+            std::fputs(kUsage, stdout);
+            return 0;
         } else {
             return usage(("unknown flag " + a).c_str());
         }

@@ -106,6 +106,9 @@ def test_malformed_text_edge_list_is_an_io_error(tmp_path):
 def test_cli_rejects_bad_flags_without_a_gpu(tmp_path):
     import subprocess
     _build.build()
+    for app in ("pagerank", "PPR", "RWR", "deepwalk"):
+        r = subprocess.run([os.path.join(_build.BIN_DIR, app), "--help"], capture_output=True, text=True)
+        assert r.returncode == 0 and r.stdout.startswith("usage:")
     exe = os.path.join(_build.BIN_DIR, "pagerank")
     r = subprocess.run([exe, "-f", "text", "-g", "x", "-w", "5", "--sp", "0.1", "--bogus", "1"],
                        capture_output=True, text=True)
