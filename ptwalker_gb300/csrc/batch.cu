@@ -413,14 +413,22 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     PTW_CUDA(cudaMemsetAsync(d_cnt, 0, nt * 8ull, st));
     PTW_CUDA(cudaMemsetAsync(d_fill, 0, nt * 8ull, st));
     PTW_CUDA(cudaMemsetAsync(d_seg, 0, 8, st));
-    uint32_t max_cap = 0;
-    for (uint32_t i = 0; i < nt; ++i) max_cap = std::max(max_cap, h_cap[i]);
-    const unsigned gx = (unsigned)std::min<uint64_t>(256, (max_cap + 2047) / 2048);
-    for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
-        const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
-        k_tabs_count<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(d_slots, d_base + t0, d_cap + t0, d_dense + t0,
-                                                                d_cnt + t0);
-    }
+    // Chunk lists: every table cut into kChunk-entry pieces (all tables, and
+    // the hash tables alone for the name-ordered path).
+    std::vector<uint2> h_ch, h_hch;
+    for (uint32_t i = 0; i < nt; ++i)
+        for (uint64_t lo = 0; lo < h_cap[i]; lo += kChunk) {
+            h_ch.push_back(make_uint2(i, (uint32_t)lo));
+            if (!dense_flags[i]) h_hch.push_back(make_uint2(i, (uint32_t)lo));
+        }
+    uint2 *d_ch = nullptr, *d_hch = nullptr;
+    PTW_CUDA(db.alloc(&d_ch, h_ch.size() + h_hch.size()));
+    d_hch = d_ch + h_ch.size();
+    PTW_CUDA(cudaMemcpyAsync(d_ch, h_ch.data(), h_ch.size() * sizeof(uint2), cudaMemcpyHostToDevice, st));
+    if (!h_hch.empty())
+        PTW_CUDA(cudaMemcpyAsync(d_hch, h_hch.data(), h_hch.size() * sizeof(uint2), cudaMemcpyHostToDevice, st));
+    if (!h_ch.empty())
+        k_tabs_count<<<(unsigned)h_ch.size(), 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_ch, d_cnt);
     PTW_CUDA(cudaGetLastError());
     PTW_CUDA(cub_call([&](void *t, size_t &b) {
         return cub::DeviceScan::InclusiveSum(t, b, d_cnt, d_seg + 1, (int64_t)nt, st);
@@ -486,12 +494,8 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             PTW_CUDA(cudaMemsetAsync(d_hist, 0, (uint64_t)nt * kCountBins * 4, st));
             PTW_CUDA(cudaMemsetAsync(d_sseg, 0, 8, st));
             PTW_CUDA(cudaMemsetAsync(d_fill, 0, nt * 8ull, st));
-            for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
-                const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
-                k_tabs_hist<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(d_slots, d_base + t0, d_cap + t0,
-                                                                       d_dense + t0, d_cnt + t0, k,
-                                                                       d_hist + (uint64_t)t0 * kCountBins);
-            }
+            k_tabs_hist<<<(unsigned)h_ch.size(), 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_ch, d_cnt, k,
+                                                              d_hist);
             k_tabs_thresh<<<(nt + 7) / 8, 256, 0, st>>>(d_cnt, d_hist, nt, k, d_thr, d_sel);
             PTW_CUDA(cudaGetLastError());
             PTW_CUDA(cub_call([&](void *t, size_t &b) {
@@ -508,12 +512,9 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             PTW_CUDA(db.alloc(&s_cnt, n_sel));
             // (table, ~count, name) in 64 bits: one sort, keys only
             const bool packed = q_bits + 32 + name_bits <= 64;
-            for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
-                const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
-                k_tabs_emit<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(
-                    d_slots, d_base + t0, d_cap + t0, d_dense + t0, false, d_sseg + t0, d_fill + t0, g->dg.int2name,
-                    g->dg.names, t0, name_bits, packed, d_thr + t0, e_key, e_cnt);
-            }
+            k_tabs_emit<<<(unsigned)h_ch.size(), 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_ch, d_sseg,
+                                                              d_fill, g->dg.int2name, g->dg.names, name_bits,
+                                                              packed, d_thr, e_key, e_cnt);
             PTW_CUDA(cudaGetLastError());
             unsigned long long *d_kseg;
             PTW_CUDA(db.alloc(&d_kseg, nt + 1));
@@ -566,12 +567,9 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
                 PTW_CUDA(db.alloc(&s_cnt, n_hash));
                 PTW_CUDA(db.alloc(&d_hseg, nt + 1));
                 PTW_CUDA(cudaMemcpyAsync(d_hseg, hseg.data(), (nt + 1) * 8ull, cudaMemcpyHostToDevice, st));
-                for (uint32_t t0 = 0; t0 < nt; t0 += 65535) {
-                    const uint32_t ny = std::min<uint32_t>(65535, nt - t0);
-                    k_tabs_emit<<<dim3(std::max(gx, 1u), ny), 256, 0, st>>>(
-                        d_slots, d_base + t0, d_cap + t0, d_dense + t0, true, d_hseg + t0, d_fill + t0,
-                        g->dg.int2name, g->dg.names, t0, name_bits, false, nullptr, e_key, e_cnt);
-                }
+                k_tabs_emit<<<(unsigned)h_hch.size(), 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_hch,
+                                                                    d_hseg, d_fill, g->dg.int2name, g->dg.names,
+                                                                    name_bits, false, nullptr, e_key, e_cnt);
                 PTW_CUDA(cudaGetLastError());
                 PTW_CUDA(cub_call([&](void *t, size_t &b) {
                     return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_hash, 0,
@@ -584,27 +582,23 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             }
             if (!dl.empty()) {
                 const uint32_t n = g->dg.n;
-                const uint32_t chunks = (n + kDenseChunk - 1) / kDenseChunk;
-                const uint64_t ncc = (uint64_t)dl.size() * chunks;
+                const uint32_t chunks = (n + kWarpChunk - 1) / kWarpChunk;
+                const uint64_t nw = (uint64_t)dl.size() * chunks;  // warp chunks
                 uint32_t *d_dl;
                 unsigned long long *d_cc, *d_cpos;
                 PTW_CUDA(db.alloc(&d_dl, dl.size()));
-                PTW_CUDA(db.alloc(&d_cc, ncc));
-                PTW_CUDA(db.alloc(&d_cpos, ncc));
+                PTW_CUDA(db.alloc(&d_cc, nw));
+                PTW_CUDA(db.alloc(&d_cpos, nw));
                 PTW_CUDA(cudaMemcpyAsync(d_dl, dl.data(), dl.size() * 4ull, cudaMemcpyHostToDevice, st));
-                for (uint32_t y0 = 0; y0 < dl.size(); y0 += 65535) {
-                    const uint32_t ny = std::min<uint32_t>(65535, (uint32_t)dl.size() - y0);
-                    k_dense_chunks<<<dim3(chunks, ny), 256, 0, st>>>(d_slots, d_base, d_dl, y0, n, chunks, d_cc);
-                }
+                const unsigned wg = (unsigned)((nw + 7) / 8);  // 8 warps per 256-thread block
+                const unsigned cg = (unsigned)((nw + 8 * kCountChunks - 1) / (8 * kCountChunks));
+                k_dense_chunks<<<cg, 256, 0, st>>>(d_slots, d_base, d_dl, n, chunks, nw, d_cc);
                 PTW_CUDA(cudaGetLastError());
                 PTW_CUDA(cub_call([&](void *t, size_t &b) {
-                    return cub::DeviceScan::ExclusiveSum(t, b, d_cc, d_cpos, (int64_t)ncc, st);
+                    return cub::DeviceScan::ExclusiveSum(t, b, d_cc, d_cpos, (int64_t)nw, st);
                 }, st));
-                for (uint32_t y0 = 0; y0 < dl.size(); y0 += 65535) {
-                    const uint32_t ny = std::min<uint32_t>(65535, (uint32_t)dl.size() - y0);
-                    k_dense_place<<<dim3(chunks, ny), 256, 0, st>>>(d_slots, d_base, d_dl, y0, n, chunks, d_cpos,
-                                                                    d_seg, g->dg.names, o_name, o_cnt);
-                }
+                k_dense_place<<<wg, 256, 0, st>>>(d_slots, d_base, d_dl, n, chunks, nw, d_cpos, d_seg, g->dg.names,
+                                                  o_name, o_cnt);
                 PTW_CUDA(cudaGetLastError());
             }
         }
