@@ -245,6 +245,8 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     BatchArgs a;
     a.adj = g->dg.adj;
     a.col = g->dg.col;
+    const bool ext = (g->tune.ext_columns & 1) && ensure_ext_columns(g);
+    a.col_ext = g->dg.col_ext;
     a.int2idx = g->dg.int2idx;
     a.desc = d_desc;
     a.q_src = d_src;
@@ -262,7 +264,8 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     a.app = cfg->app;
     if (nd >= (1ull << 32)) return fail(PTW_EINVAL, "wave too large");
     int per_sm = 0;
-    PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, 256, 0));
+    const void *kfn = ext ? (const void *)k_batch<true> : (const void *)k_batch<false>;
+    PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 256, 0));
     uint64_t grid = (uint64_t)g->num_sms * std::max(per_sm, 1);
     grid = std::min<uint64_t>(grid, std::max<uint64_t>(1, (nd + 7) / 8));
     // Full lists: host buffers of an estimated size are faulted in on host
@@ -290,7 +293,10 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
         }
     }
     PTW_CUDA(cudaEventRecord(g->ev[0], st));
-    k_batch<<<(unsigned)grid, 256, 0, st>>>(a);
+    {
+        void *kargs[] = {&a};
+        PTW_CUDA(cudaLaunchKernel(kfn, dim3((unsigned)grid), dim3(256), kargs, 0, st));
+    }
     PTW_CUDA(cudaEventRecord(g->ev[1], st));
     PTW_CUDA(cudaGetLastError());
     std::vector<uint32_t> h_flag(nq);

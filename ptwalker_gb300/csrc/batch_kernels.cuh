@@ -73,6 +73,7 @@ __device__ __forceinline__ void count_add(unsigned long long *tab, uint32_t mask
 struct BatchArgs {
     const uint2 *__restrict__ adj;
     const uint32_t *__restrict__ col;
+    const uint4 *__restrict__ col_ext;     // EXT: {id, first column, degree, name} per entry
     const uint32_t *__restrict__ int2idx;  // internal id -> canonical index (dense tables)
     const uint3 *__restrict__ desc;  // [ndesc] {entry, first rank, count}
     const uint32_t *__restrict__ q_src;
@@ -106,18 +107,23 @@ __device__ __forceinline__ void visit_agg(unsigned mask_active, bool on, uint32_
     if ((grp & ((1u << lane) - 1u)) == 0) count_add(tab, tmask, v, __popc(grp), flag, int2idx);
 }
 
+// EXT: moves read the extended column copy and keep the row record of the
+// current vertex in registers (one gather per move instead of two).
+template <bool EXT>
 __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt_mask = (1u << lane) - 1u;
     uint32_t q[kBatchIlp], v[kBatchIlp], step[kBatchIlp], j[kBatchIlp], qid[kBatchIlp], mask[kBatchIlp];
     unsigned long long *tab[kBatchIlp];
-    bool act[kBatchIlp];
+    bool act[kBatchIlp], have[kBatchIlp];
+    uint2 rec[kBatchIlp];
 #pragma unroll
     for (int k = 0; k < kBatchIlp; ++k) {
-        act[k] = false;
+        act[k] = have[k] = false;
         q[k] = v[k] = step[k] = j[k] = qid[k] = mask[k] = 0;
         tab[k] = nullptr;
+        rec[k] = make_uint2(0u, 0u);
     }
     // Warp-uniform current descriptor: entry dq, ranks [dnext, dend).
     uint32_t dq = 0, dnext = 0, dend = 0;
@@ -165,6 +171,7 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
                 mask[k] = a.q_mask[q[k]];
                 step[k] = 0;
                 act[k] = true;
+                have[k] = false;
             }
             if (a.app == PTW_APP_VISITS) {
                 // Start visits: one table update per (warp, query) group.
@@ -176,24 +183,38 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
         for (int k = 0; k < kBatchIlp; ++k) any |= act[k];
         if (!__any_sync(kBFull, any)) break;
 
-        uint2 rec[kBatchIlp];
 #pragma unroll
         for (int k = 0; k < kBatchIlp; ++k)
-            if (act[k]) rec[k] = __ldg(&a.adj[v[k]]);
+            if (act[k] && !(EXT && have[k])) rec[k] = __ldg(&a.adj[v[k]]);
         uint4 r[kBatchIlp];
 #pragma unroll
         for (int k = 0; k < kBatchIlp; ++k)
             if (act[k]) r[k] = philox(make_uint4(j[k], qid[k], step[k], PTW_TAG_WALK), a.key0, a.key1);
         uint32_t nb[kBatchIlp];
+        uint2 nrec[kBatchIlp];
 #pragma unroll
-        for (int k = 0; k < kBatchIlp; ++k)
-            if (act[k] && rec[k].y != 0) nb[k] = __ldg(&a.col[rec[k].x + __umulhi(r[k].x, rec[k].y)]);
+        for (int k = 0; k < kBatchIlp; ++k) {
+            if (act[k] && rec[k].y != 0) {
+                const uint32_t e = rec[k].x + __umulhi(r[k].x, rec[k].y);
+                if (EXT) {
+                    const uint4 x = __ldg(&a.col_ext[e]);
+                    nb[k] = x.x;
+                    nrec[k] = make_uint2(x.y, x.z);
+                } else {
+                    nb[k] = __ldg(&a.col[e]);
+                }
+            }
+        }
 #pragma unroll
         for (int k = 0; k < kBatchIlp; ++k) {
             // every lane runs the aggregation calls (warp-collective)
             const bool moved = act[k] && rec[k].y != 0;
             if (moved) {
                 v[k] = nb[k];
+                if (EXT) {
+                    rec[k] = nrec[k];
+                    have[k] = true;
+                }
                 ++step[k];
                 ++moves;
             }

@@ -146,6 +146,7 @@ struct ptw_graph {
     int num_sms = 0;
     ptw_tune tune{};
     uint64_t device_bytes = 0;
+    int ext_users = 0;  // open servers reading the extended columns (kept while > 0)
 };
 
 namespace ptw {
@@ -190,6 +191,9 @@ int launch_counts_by_name(ptw_graph *g, uint32_t *d_out);
 int check_tune(const ptw_tune &t);
 // Frees the column copies the graph's tune no longer reads.
 void drop_unused_columns(ptw_graph *g);
+// Builds the extended column copy (and the per-vertex records) on first use;
+// false, without an error, when they do not fit in device memory.
+bool ensure_ext_columns(ptw_graph *g);
 
 // The query table a batch was run with (batch.cu).
 const ptw_query *batch_queries(const ptw_batch *b);

@@ -131,6 +131,8 @@ struct ptw_server {
     std::deque<ptw::Done> done;
     ptw::BatchArgs args{};
     unsigned grid = 1;
+    const void *kfn = nullptr;        // k_batch<false> or k_batch<true> (extended columns)
+    bool uses_ext = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t knode = nullptr;
@@ -191,8 +193,8 @@ int build_tick_graph(ptw_server *s)
     cudaStream_t st = s->g->stream;
     PTW_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     cudaError_t e1 = cudaMemcpyAsync(s->d_plan, s->h_plan, s->plan_bytes, cudaMemcpyHostToDevice, st);
-    k_batch<<<s->grid, 256, 0, st>>>(s->args);
-    cudaError_t e2 = cudaGetLastError();
+    void *kargs[] = {&s->args};
+    cudaError_t e2 = cudaLaunchKernel(s->kfn, dim3(s->grid), dim3(256), kargs, 0, st);
     cudaError_t e3 = cudaMemcpyAsync((char *)s->h_plan + s->ret_off, (char *)s->d_plan + s->ret_off,
                                      s->ret_bytes, cudaMemcpyDeviceToHost, st);
     cudaError_t e4 = cudaStreamEndCapture(st, &s->graph);
@@ -351,7 +353,12 @@ extern "C" int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server
         a.max_moves = cfg->max_moves;
         a.app = cfg->app;
         int per_sm = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, 256, 0);
+        const bool ext = (g->tune.ext_columns & 1) && ensure_ext_columns(g);
+        a.col_ext = g->dg.col_ext;
+        s->kfn = ext ? (const void *)k_batch<true> : (const void *)k_batch<false>;
+        s->uses_ext = ext;
+        if (ext) ++g->ext_users;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, s->kfn, 256, 0);
         if (e != cudaSuccess) rc = cuda_fail(e, "occupancy");
         s->grid = (unsigned)std::max(1, g->num_sms * std::max(per_sm, 1));
         if (rc == PTW_OK) {
@@ -466,8 +473,8 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
             PTW_CUDA(cudaGraphLaunch(s->exec, st));
         } else {
             PTW_CUDA(cudaMemcpyAsync(s->d_plan, s->h_plan, s->plan_bytes, cudaMemcpyHostToDevice, st));
-            k_batch<<<s->grid, 256, 0, st>>>(s->args);
-            PTW_CUDA(cudaGetLastError());
+            void *kargs[] = {&s->args};
+            PTW_CUDA(cudaLaunchKernel(s->kfn, dim3(s->grid), dim3(256), kargs, 0, st));
             PTW_CUDA(cudaMemcpyAsync((char *)s->h_plan + s->ret_off, (char *)s->d_plan + s->ret_off,
                                      s->ret_bytes, cudaMemcpyDeviceToHost, st));
         }
@@ -566,6 +573,7 @@ extern "C" void ptw_serve_close(ptw_server *s)
     if (!s) return;
     cudaSetDevice(s->g->device);
     cudaStreamSynchronize(s->g->stream);
+    if (s->uses_ext) --s->g->ext_users;
     s->done.clear();
     s->pinned.clear();
     for (cudaEvent_t e : s->ev)

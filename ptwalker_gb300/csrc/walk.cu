@@ -602,6 +602,8 @@ void *pick_walk(bool endpoint, int ilp, bool hot, int min_blocks, int block, boo
     return ext ? pick_walk_x<true>(endpoint, ilp, hot, cap) : pick_walk_x<false>(endpoint, ilp, hot, cap);
 }
 
+}  // namespace
+
 // Builds the extended column copy on first use; false (and no error) when
 // it does not fit in device memory, so the caller walks without it.
 bool ensure_ext_columns(ptw_graph *g)
@@ -638,12 +640,10 @@ bool ensure_ext_columns(ptw_graph *g)
     return true;
 }
 
-}  // namespace
-
 void drop_unused_columns(ptw_graph *g)
 {
     DeviceGraph &dg = g->dg;
-    if (dg.col_ext && !g->tune.ext_columns && !g->tune.gather_slots) {
+    if (dg.col_ext && !g->tune.ext_columns && !g->tune.gather_slots && g->ext_users == 0) {
         cudaStreamSynchronize(g->stream);
         cudaFree(dg.col_ext);
         cudaFree(dg.vtx_ext);

@@ -63,7 +63,7 @@ def main(argv=None):
         rng = np.random.default_rng(4)
         src = rng.integers(0, G.n, a.queries)
         bud = np.exp(rng.uniform(np.log(1e3), np.log(1e6), a.queries)).astype(np.int64)
-        with ptw.Server(G, sp=0.2, seed=3, tick_walkers=1 << 21, top_k=a.top_k) as srv:
+        with ptw.Server(G, sp=0.2, seed=3, tick_walkers=1 << 23, top_k=a.top_k) as srv:
             srv.submit(int(src[0]), 1000, 1 << 30)
             srv.drain()
             t1 = time.perf_counter()

@@ -163,3 +163,32 @@ def test_top_k_with_wide_names_takes_the_two_sort_path(gpu, s16_canon):
             names, counts = res.query(i)
             assert np.array_equal(names, big[want_idx]) and np.array_equal(counts, want_c), i
         res.close()
+
+
+@pytest.mark.parametrize("app", ["visits", "endpoint"])
+def test_batch_and_serving_with_extended_columns(gpu, G16, s16_canon, app):
+    """The walk kernel's one-gather path (row records carried with the
+    column entries) must not change any query's counts."""
+    saved = G16.tune
+    try:
+        t = G16.tune
+        t.ext_columns = 1
+        G16.tune = t
+        rng = np.random.default_rng(31)
+        nq = 30
+        src = rng.integers(0, G16.n, nq).astype(np.uint32)
+        bud = rng.integers(1, 40000, nq)
+        res = gpu.ppr_batch(G16, src, bud, sp=0.25, seed=4, app=app)
+        for i in range(nq):
+            assert sparse_equal(res, i, replay_query(s16_canon, int(src[i]), i, int(bud[i]), 0.25, 4, app)), i
+        res.close()
+        with gpu.Server(G16, sp=0.25, seed=4, app=app, tick_walkers=8192) as srv:
+            for i in range(8):
+                srv.submit(int(src[i]), int(bud[i]), i)
+            got = {r["query_id"]: r for r in srv.drain()}
+        for i in range(8):
+            want = replay_query(s16_canon, int(src[i]), i, int(bud[i]), 0.25, 4, app)
+            nz = np.nonzero(want)[0].astype(np.uint32)
+            assert np.array_equal(got[i]["names"], nz) and np.array_equal(got[i]["counts"], want[nz]), i
+    finally:
+        G16.tune = saved
