@@ -9,7 +9,10 @@ removed (synthetic, built on the device).  Each step uses a new seed.
 
   value     walker steps/s with the graph resident in HBM (device output)
   e2e       the same through the host-facing C ABI call ptw_pagerank,
-            counts read back into pinned host memory every step
+            counts read back into pinned host memory every step; a step's
+            only input is its walk configuration (passed by value, no copy):
+            the graph stays resident, as in the reference, whose walk timer
+            excludes the graph load
   roofline  random-gather bound: 64 B per move (row record + column
             sector) + 32 B per counted visit, against the measured HBM peak;
             traffic = the ncu DRAM bytes per move of the committed scale-24
