@@ -21,6 +21,7 @@ from .api import (  # noqa: F401
     Solver,
     walk,
     probe_gather,
+    trim_memory,
 )
 
 from .batch import BatchResult, ppr_batch  # noqa: F401,E402

@@ -98,6 +98,7 @@ _GP = ctypes.POINTER(ctypes.c_void_p)
 SIGNATURES = [
     ("ptw_last_error", ctypes.c_char_p, []),
     ("ptw_version", ctypes.c_char_p, []),
+    ("ptw_trim_memory", ctypes.c_int, []),
     ("ptw_graph_load", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, _GP]),
     ("ptw_graph_from_edges", ctypes.c_int, [_u32p, _u32p, ctypes.c_uint64, ctypes.c_int32, _GP]),
     ("ptw_graph_from_csr", ctypes.c_int, [_u64p, _u32p, ctypes.c_uint32, _u32p, _GP]),

@@ -288,6 +288,12 @@ def probe_gather(array_bytes=2 << 30, chains=8):
     return float(out.value)
 
 
+def trim_memory():
+    """Hands the device memory the engine keeps cached between batched and
+    served calls back to the driver (ptw_trim_memory)."""
+    C.check(C.load().ptw_trim_memory())
+
+
 def pagerank(graph, n_walkers=None, sp=0.15, seed=0, start="per_vertex", sources=None,
              max_moves=0, out=None, first_walker=0, stats=False):
     """Visit counts by name (uint32[id_bound]); every position is counted.

@@ -27,6 +27,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -165,33 +166,71 @@ struct WaveQuery {
 // those of about one group: a few hundred MB stay largely in L2 where the
 // tables of thousands of queries at once would not (1.6x faster walk kernel
 // on 4096 queries at R-MAT scale 22 with 384 MB groups).
-void interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<uint64_t> &count,
-                            const std::vector<uint64_t> &table_bytes, uint64_t group_bytes,
-                            std::vector<uint3> &desc)
+uint64_t interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<uint64_t> &count,
+                                const std::vector<uint64_t> &table_bytes, uint64_t group_bytes,
+                                std::unique_ptr<uint3[]> &desc, unsigned threads)
 {
-    desc.clear();
     const uint32_t ne = (uint32_t)count.size();
+    std::vector<uint32_t> gb;  // first entry of each group, then ne
     for (uint32_t g0 = 0; g0 < ne;) {
-        std::vector<uint32_t> live;
         uint64_t bytes = 0;
         uint32_t g1 = g0;
         while (g1 < ne && (g1 == g0 || group_bytes == 0 || bytes + table_bytes[g1] <= group_bytes)) {
             bytes += table_bytes[g1];
-            if (count[g1]) live.push_back(g1);
             ++g1;
         }
+        gb.push_back(g0);
+        g0 = g1;
+    }
+    gb.push_back(ne);
+    const size_t ng = gb.size() - 1;
+    std::vector<uint64_t> goff(ng + 1, 0);  // first descriptor of each group
+    for (size_t k = 0; k < ng; ++k) {
+        uint64_t d = 0;
+        for (uint32_t i = gb[k]; i < gb[k + 1]; ++i) d += (count[i] + kDescWalkers - 1) / kDescWalkers;
+        goff[k + 1] = goff[k] + d;
+    }
+    desc.reset(new uint3[std::max<uint64_t>(goff[ng], 1)]);  // not value-initialised
+    uint3 *out = desc.get();
+    auto fill = [&](size_t k) {
+        std::vector<uint32_t> live;
+        for (uint32_t i = gb[k]; i < gb[k + 1]; ++i)
+            if (count[i]) live.push_back(i);
+        uint3 *o = out + goff[k];
         for (uint64_t r = 0; !live.empty(); ++r) {
             size_t keep = 0;
+            const uint64_t off = r * kDescWalkers;
             for (uint32_t i : live) {
-                const uint64_t off = r * kDescWalkers;
                 const uint64_t c = std::min<uint64_t>(kDescWalkers, count[i] - off);
-                desc.push_back(make_uint3(i, (uint32_t)(j0[i] + off), (uint32_t)c));
+                *o++ = make_uint3(i, (uint32_t)(j0[i] + off), (uint32_t)c);
                 if (off + c < count[i]) live[keep++] = i;
             }
             live.resize(keep);
         }
-        g0 = g1;
+    };
+    // groups are independent: fill them on host threads when there are many descriptors
+    const unsigned nth = goff[ng] >= (1u << 18) ? (unsigned)std::min<size_t>(ng, std::max(1u, threads)) : 1u;
+    if (nth <= 1) {
+        for (size_t k = 0; k < ng; ++k) fill(k);
+    } else {
+        std::atomic<size_t> next{0};
+        std::vector<std::thread> pool;
+        for (unsigned t = 0; t < nth; ++t)
+            pool.emplace_back([&] {
+                for (size_t k; (k = next.fetch_add(1)) < ng;) fill(k);
+            });
+        for (std::thread &t : pool) t.join();
     }
+    return goff[ng];
+}
+
+void interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<uint64_t> &count,
+                            const std::vector<uint64_t> &table_bytes, uint64_t group_bytes,
+                            std::vector<uint3> &desc)
+{
+    std::unique_ptr<uint3[]> buf;
+    const uint64_t n = interleave_descriptors(j0, count, table_bytes, group_bytes, buf, 1);
+    desc.assign(buf.get(), buf.get() + n);
 }
 
 namespace {
@@ -203,12 +242,16 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
 {
     cudaStream_t st = g->stream;
     const uint32_t nq = (uint32_t)wq.size();
+    const bool timing = std::getenv("PTW_TIMING") != nullptr;
+    auto clk = [] { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
+    const double t_enter = timing ? clk() : 0.0;
+    double t_plan = 0, t_setup = 0;
     std::vector<unsigned long long> h_tab(nq + 1);
     std::vector<uint32_t> h_src(nq), h_qid(nq), h_mask(nq), h_cap(nq);
     std::vector<uint8_t> h_dense(nq);
     std::vector<uint64_t> j0(nq, 0), cnt(nq);
     for (uint32_t i = 0; i < nq; ++i) {
-        h_tab[i + 1] = h_tab[i] + wq[i].cap;
+        h_tab[i + 1] = h_tab[i] + ((wq[i].cap + 15) & ~15ull);  // tables start on 128-byte lines
         h_src[i] = wq[i].src;
         h_qid[i] = wq[i].qid;
         h_dense[i] = wq[i].dense ? 1 : 0;
@@ -216,11 +259,13 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
         h_cap[i] = wq[i].dense ? g->dg.n : (uint32_t)wq[i].cap;
         cnt[i] = wq[i].budget;
     }
-    std::vector<uint3> h_desc;
+    std::unique_ptr<uint3[]> h_desc;
     std::vector<uint64_t> tbytes(nq);
     for (uint32_t i = 0; i < nq; ++i) tbytes[i] = wq[i].cap * 8;
-    interleave_descriptors(j0, cnt, tbytes, kGroupBytes, h_desc);
-    const uint64_t n_slots = h_tab[nq], nd = h_desc.size();
+    const uint64_t nd = interleave_descriptors(j0, cnt, tbytes, kGroupBytes, h_desc,
+                                               std::min(16u, std::max(1u, std::thread::hardware_concurrency())));
+    if (timing) t_plan = clk();
+    const uint64_t n_slots = h_tab[nq];
     DevBuf db(st);
     unsigned long long *d_tab, *d_slots, *d_ctrl;
     uint32_t *d_src, *d_qid, *d_mask, *d_flag;
@@ -237,10 +282,14 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     PTW_CUDA(cudaMemcpyAsync(d_src, h_src.data(), nq * 4ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_qid, h_qid.data(), nq * 4ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_mask, h_mask.data(), nq * 4ull, cudaMemcpyHostToDevice, st));
-    PTW_CUDA(cudaMemcpyAsync(d_desc, h_desc.data(), nd * sizeof(uint3), cudaMemcpyHostToDevice, st));
+    PTW_CUDA(cudaMemcpyAsync(d_desc, h_desc.get(), nd * sizeof(uint3), cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemsetAsync(d_flag, 0, nq * 4ull, st));
     PTW_CUDA(cudaMemsetAsync(d_ctrl, 0, 16, st));
     PTW_CUDA(cudaMemsetAsync(d_slots, 0, n_slots * 8, st));
+    if (timing) {
+        PTW_CUDA(cudaStreamSynchronize(st));
+        t_setup = clk();
+    }
 
     BatchArgs a;
     a.adj = g->dg.adj;
@@ -313,9 +362,12 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]));
     *walk_ms += ms;
     *moves_out += h_moves;
-    if (std::getenv("PTW_TIMING"))
-        std::fprintf(stderr, "[ptw] wave of %u queries, %llu descriptors, %llu slots: walk kernel %.1f ms\n", nq,
-                     (unsigned long long)nd, (unsigned long long)n_slots, ms);
+    if (timing)
+        std::fprintf(stderr,
+                     "[ptw] wave of %u queries, %llu descriptors, %llu slots: plan %.1f ms, setup %.1f ms, "
+                     "walk kernel %.1f ms, wave %.1f ms\n",
+                     nq, (unsigned long long)nd, (unsigned long long)n_slots, 1e3 * (t_plan - t_enter),
+                     1e3 * (t_setup - t_plan), ms, 1e3 * (clk() - t_enter));
     wr.idx.resize(nq);
     wr.overflow.assign(nq, 0);
     for (uint32_t i = 0; i < nq; ++i) {
@@ -400,12 +452,21 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     Prefault prefault;  // joined before the copies (and on any early return)
     std::vector<uint8_t> dense_flags(nt, 0);
     if (h_dense) dense_flags.assign(h_dense, h_dense + nt);
-    std::vector<uint32_t> dl;  // dense tables, in table order
-    for (uint32_t i = 0; i < nt; ++i)
-        if (dense_flags[i]) dl.push_back(i);
+    uint64_t n_dense = 0;
+    for (uint32_t i = 0; i < nt; ++i) n_dense += dense_flags[i] ? 1 : 0;
+    const uint32_t k = out->top_k;
+    // Block chunks of kChunkBytes per table, in table order.
+    std::vector<unsigned long long> tch(nt + 1, 0);
+    for (uint32_t i = 0; i < nt; ++i) {
+        if (h_base[i] & 1) return fail(PTW_EINVAL, "count table not 16-byte aligned");
+        const uint64_t bytes = (uint64_t)h_cap[i] * (dense_flags[i] ? 4 : 8);
+        tch[i + 1] = tch[i] + (bytes + kChunkBytes - 1) / kChunkBytes;
+    }
+    const uint64_t nch = tch[nt];
+    if (nch >= (1ull << 31)) return fail(PTW_EINVAL, "count tables too large to compact in one call");
     DevBuf db(st);
-    unsigned long long *d_base, *d_cnt, *d_seg, *d_fill;
-    uint32_t *d_cap;
+    unsigned long long *d_base, *d_cnt, *d_seg, *d_fill, *d_tch, *d_cc, *d_hc, *d_pos = nullptr, *d_hpos = nullptr;
+    uint32_t *d_cap, *d_hist = nullptr;
     uint8_t *d_dense;
     PTW_CUDA(db.alloc(&d_base, nt));
     PTW_CUDA(db.alloc(&d_cap, nt));
@@ -413,37 +474,46 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     PTW_CUDA(db.alloc(&d_cnt, nt));
     PTW_CUDA(db.alloc(&d_seg, nt + 1));
     PTW_CUDA(db.alloc(&d_fill, nt));
+    PTW_CUDA(db.alloc(&d_tch, nt + 1));
+    PTW_CUDA(db.alloc(&d_cc, std::max<uint64_t>(nch, 1)));
+    PTW_CUDA(db.alloc(&d_hc, std::max<uint64_t>(nch, 1)));
     PTW_CUDA(cudaMemcpyAsync(d_base, h_base, nt * 8ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_cap, h_cap, nt * 4ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_dense, dense_flags.data(), nt, cudaMemcpyHostToDevice, st));
+    PTW_CUDA(cudaMemcpyAsync(d_tch, tch.data(), (nt + 1) * 8ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemsetAsync(d_cnt, 0, nt * 8ull, st));
     PTW_CUDA(cudaMemsetAsync(d_fill, 0, nt * 8ull, st));
     PTW_CUDA(cudaMemsetAsync(d_seg, 0, 8, st));
-    // Chunk lists: every table cut into kChunk-entry pieces (all tables, and
-    // the hash tables alone for the name-ordered path).
-    std::vector<uint2> h_ch, h_hch;
-    for (uint32_t i = 0; i < nt; ++i)
-        for (uint64_t lo = 0; lo < h_cap[i]; lo += kChunk) {
-            h_ch.push_back(make_uint2(i, (uint32_t)lo));
-            if (!dense_flags[i]) h_hch.push_back(make_uint2(i, (uint32_t)lo));
-        }
-    uint2 *d_ch = nullptr, *d_hch = nullptr;
-    PTW_CUDA(db.alloc(&d_ch, h_ch.size() + h_hch.size()));
-    d_hch = d_ch + h_ch.size();
-    PTW_CUDA(cudaMemcpyAsync(d_ch, h_ch.data(), h_ch.size() * sizeof(uint2), cudaMemcpyHostToDevice, st));
-    if (!h_hch.empty())
-        PTW_CUDA(cudaMemcpyAsync(d_hch, h_hch.data(), h_hch.size() * sizeof(uint2), cudaMemcpyHostToDevice, st));
-    if (!h_ch.empty())
-        k_tabs_count<<<(unsigned)h_ch.size(), 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_ch, d_cnt);
+    // Pass 1: occupied entries per chunk and per table (+ histograms for top-k).
+    if (k) {
+        PTW_CUDA(db.alloc(&d_hist, (uint64_t)nt * kCountBins));
+        PTW_CUDA(cudaMemsetAsync(d_hist, 0, (uint64_t)nt * kCountBins * 4, st));
+        if (nch)
+            k_tabs_count<true><<<(unsigned)nch, 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_tch, nt, d_cnt, d_cc,
+                                                             d_hc, d_hist);
+    } else if (nch) {
+        k_tabs_count<false><<<(unsigned)nch, 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_tch, nt, d_cnt, d_cc,
+                                                          d_hc, nullptr);
+    }
     PTW_CUDA(cudaGetLastError());
     PTW_CUDA(cub_call([&](void *t, size_t &b) {
         return cub::DeviceScan::InclusiveSum(t, b, d_cnt, d_seg + 1, (int64_t)nt, st);
     }, st));
     PTW_CUDA(cudaMemcpyAsync(out->seg.data(), d_seg, (nt + 1) * 8ull, cudaMemcpyDeviceToHost, st));
+    if (!k && nch) {
+        // output position of every dense chunk, sort-input position of every hash chunk
+        PTW_CUDA(db.alloc(&d_pos, nch));
+        PTW_CUDA(db.alloc(&d_hpos, nch));
+        PTW_CUDA(cub_call([&](void *t, size_t &b) {
+            return cub::DeviceScan::ExclusiveSum(t, b, d_cc, d_pos, (int64_t)nch, st);
+        }, st));
+        PTW_CUDA(cub_call([&](void *t, size_t &b) {
+            return cub::DeviceScan::ExclusiveSum(t, b, d_hc, d_hpos, (int64_t)nch, st);
+        }, st));
+    }
     PTW_CUDA(cudaStreamSynchronize(st));
     const uint64_t n_ent = out->seg[nt];
     // top-k: every table keeps its min(k, entries) largest counts
-    const uint32_t k = out->top_k;
     std::vector<uint64_t> kseg;
     uint64_t n_out = n_ent;
     if (k && n_ent) {
@@ -482,7 +552,6 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
         int name_bits = 1, q_bits = 1;
         while (name_bits < 32 && (1ull << name_bits) < g->dg.id_bound) ++name_bits;
         while ((1ull << q_bits) < nt) ++q_bits;
-        const unsigned kg = (unsigned)std::min<uint64_t>((n_ent + 255) / 256, (uint64_t)g->num_sms * 32);
         uint32_t *o_name = nullptr, *o_cnt = nullptr;
         if (k) {
             // Top-k.  A histogram of each large table's counts (exact below
@@ -491,17 +560,12 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             // as keys, so the radix sort sees about k entries per table
             // instead of all of them.  The sort orders each table by count
             // (ties by name) and the first k are kept.
-            uint32_t *d_hist, *d_thr;
+            uint32_t *d_thr;
             unsigned long long *d_sel, *d_sseg;
-            PTW_CUDA(db.alloc(&d_hist, (uint64_t)nt * kCountBins));
             PTW_CUDA(db.alloc(&d_thr, nt));
             PTW_CUDA(db.alloc(&d_sel, nt));
             PTW_CUDA(db.alloc(&d_sseg, nt + 1));
-            PTW_CUDA(cudaMemsetAsync(d_hist, 0, (uint64_t)nt * kCountBins * 4, st));
             PTW_CUDA(cudaMemsetAsync(d_sseg, 0, 8, st));
-            PTW_CUDA(cudaMemsetAsync(d_fill, 0, nt * 8ull, st));
-            k_tabs_hist<<<(unsigned)h_ch.size(), 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_ch, d_cnt, k,
-                                                              d_hist);
             k_tabs_thresh<<<(nt + 7) / 8, 256, 0, st>>>(d_cnt, d_hist, nt, k, d_thr, d_sel);
             PTW_CUDA(cudaGetLastError());
             PTW_CUDA(cub_call([&](void *t, size_t &b) {
@@ -518,9 +582,10 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             PTW_CUDA(db.alloc(&s_cnt, n_sel));
             // (table, ~count, name) in 64 bits: one sort, keys only
             const bool packed = q_bits + 32 + name_bits <= 64;
-            k_tabs_emit<<<(unsigned)h_ch.size(), 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_ch, d_sseg,
-                                                              d_fill, g->dg.int2name, g->dg.names, name_bits,
-                                                              packed, d_thr, e_key, e_cnt);
+            k_tabs_place<true><<<(unsigned)nch, 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_tch, nt, nullptr,
+                                                             nullptr, d_thr, d_sseg, d_fill, g->dg.int2name,
+                                                             g->dg.names, name_bits, packed, nullptr, nullptr, e_key,
+                                                             e_cnt);
             PTW_CUDA(cudaGetLastError());
             unsigned long long *d_kseg;
             PTW_CUDA(db.alloc(&d_kseg, nt + 1));
@@ -564,19 +629,23 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             for (uint32_t i = 0; i < nt; ++i)
                 hseg[i + 1] = hseg[i] + (dense_flags[i] ? 0 : out->seg[i + 1] - out->seg[i]);
             const uint64_t n_hash = hseg[nt];
+            unsigned long long *e_key = nullptr, *s_key = nullptr, *d_hseg = nullptr;
+            uint32_t *e_cnt = nullptr, *s_cnt = nullptr;
             if (n_hash) {
-                unsigned long long *e_key, *s_key, *d_hseg;
-                uint32_t *e_cnt, *s_cnt;
                 PTW_CUDA(db.alloc(&e_key, n_hash));
                 PTW_CUDA(db.alloc(&s_key, n_hash));
                 PTW_CUDA(db.alloc(&e_cnt, n_hash));
                 PTW_CUDA(db.alloc(&s_cnt, n_hash));
                 PTW_CUDA(db.alloc(&d_hseg, nt + 1));
                 PTW_CUDA(cudaMemcpyAsync(d_hseg, hseg.data(), (nt + 1) * 8ull, cudaMemcpyHostToDevice, st));
-                k_tabs_emit<<<(unsigned)h_hch.size(), 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_hch,
-                                                                    d_hseg, d_fill, g->dg.int2name, g->dg.names,
-                                                                    name_bits, false, nullptr, e_key, e_cnt);
-                PTW_CUDA(cudaGetLastError());
+            }
+            // Pass 2: dense tables straight to the output, hash tables to the sort input.
+            k_tabs_place<false><<<(unsigned)nch, 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_tch, nt, d_pos,
+                                                              d_hpos, nullptr, nullptr, nullptr, g->dg.int2name,
+                                                              g->dg.names, name_bits, false, o_name, o_cnt, e_key,
+                                                              e_cnt);
+            PTW_CUDA(cudaGetLastError());
+            if (n_hash) {
                 PTW_CUDA(cub_call([&](void *t, size_t &b) {
                     return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_hash, 0,
                                                            name_bits + q_bits, st);
@@ -584,27 +653,6 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
                 const unsigned hg = (unsigned)std::min<uint64_t>((n_hash + 255) / 256, (uint64_t)g->num_sms * 32);
                 k_place_hash<<<std::max(hg, 1u), 256, 0, st>>>(s_key, s_cnt, n_hash, name_bits, d_seg, d_hseg,
                                                               o_name, o_cnt);
-                PTW_CUDA(cudaGetLastError());
-            }
-            if (!dl.empty()) {
-                const uint32_t n = g->dg.n;
-                const uint32_t chunks = (n + kWarpChunk - 1) / kWarpChunk;
-                const uint64_t nw = (uint64_t)dl.size() * chunks;  // warp chunks
-                uint32_t *d_dl;
-                unsigned long long *d_cc, *d_cpos;
-                PTW_CUDA(db.alloc(&d_dl, dl.size()));
-                PTW_CUDA(db.alloc(&d_cc, nw));
-                PTW_CUDA(db.alloc(&d_cpos, nw));
-                PTW_CUDA(cudaMemcpyAsync(d_dl, dl.data(), dl.size() * 4ull, cudaMemcpyHostToDevice, st));
-                const unsigned wg = (unsigned)((nw + 7) / 8);  // 8 warps per 256-thread block
-                const unsigned cg = (unsigned)((nw + 8 * kCountChunks - 1) / (8 * kCountChunks));
-                k_dense_chunks<<<cg, 256, 0, st>>>(d_slots, d_base, d_dl, n, chunks, nw, d_cc);
-                PTW_CUDA(cudaGetLastError());
-                PTW_CUDA(cub_call([&](void *t, size_t &b) {
-                    return cub::DeviceScan::ExclusiveSum(t, b, d_cc, d_cpos, (int64_t)nw, st);
-                }, st));
-                k_dense_place<<<wg, 256, 0, st>>>(d_slots, d_base, d_dl, n, chunks, nw, d_cpos, d_seg, g->dg.names,
-                                                  o_name, o_cnt);
                 PTW_CUDA(cudaGetLastError());
             }
         }
@@ -620,7 +668,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     }
     if (timing)
         std::fprintf(stderr, "[ptw] compact %u tables (%zu dense), %llu entries: device %.1f ms, d2h %.1f ms\n", nt,
-                     dl.size(), (unsigned long long)n_ent, 1e3 * (t1 - t0), 1e3 * (t2 - t1));
+                     (size_t)n_dense, (unsigned long long)n_ent, 1e3 * (t1 - t0), 1e3 * (t2 - t1));
     return PTW_OK;
 }
 
@@ -663,6 +711,10 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
         return fail(PTW_EINVAL, "sp = 0 needs max_moves > 0 (walks would never end)");
     if (cfg->app != PTW_APP_VISITS && cfg->app != PTW_APP_ENDPOINT) return fail(PTW_EINVAL, "unknown app");
     PTW_CUDA(cudaSetDevice(g->device));
+    const bool timing = std::getenv("PTW_TIMING") != nullptr;
+    auto clk = [] { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
+    const double t_enter = timing ? clk() : 0.0;
+    double t_waves = 0, t_asm = 0;
     const uint32_t n = g->dg.n;
     std::vector<WaveQuery> all(nq);
     for (uint32_t i = 0; i < nq; ++i) {
@@ -721,7 +773,9 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
         rc = run_wave(g, {w}, cfg, thr, waves, overflow, &m2, &walk_ms);
         if (rc == PTW_OK && !overflow.empty()) rc = fail(PTW_EFULL, "count table overflow in a dense array");
     }
+    if (timing) t_waves = clk();
     if (rc == PTW_OK) rc = assemble(b, waves);
+    if (timing) t_asm = clk();
     if (rc != PTW_OK) {
         delete b;
         return rc;
@@ -738,6 +792,9 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
     PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[3], g->ev[2]));
     b->stats.total_ms = ms;
     b->stats.kernel_ms = walk_ms;  // walker kernels only; total_ms includes compaction and copies
+    if (timing)
+        std::fprintf(stderr, "[ptw] batch of %u queries: %zu waves in %.1f ms, assemble %.1f ms, call %.1f ms\n", nq,
+                     waves.size(), 1e3 * (t_waves - t_enter), 1e3 * (t_asm - t_waves), 1e3 * (clk() - t_enter));
     *out = b;
     return PTW_OK;
 }

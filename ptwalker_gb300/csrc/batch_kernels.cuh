@@ -242,137 +242,248 @@ __device__ __forceinline__ uint32_t count_bin(uint32_t c)
     return 256 + (e - 8) * 16 + ((c >> (e - 4)) & 15u);
 }
 
-// An occupied entry (hash slot with a key, or a nonzero dense counter) whose
-// count falls in bin thr or above.
-__device__ __forceinline__ bool kept(unsigned long long w, uint32_t thr)
+// Compaction reads the count tables in block chunks of 32 KB of one table
+// (8,192 dense counters or 4,096 hash slots): one 256-thread block per
+// chunk, 4 KB per warp, eight 16-byte loads per lane issued together, so
+// enough bytes are in flight to stream the tables at HBM rate.  Table t
+// starts at slots + t_base[t] on a 128-byte boundary and has t_len[t]
+// entries (32-bit counters when t_dense[t], else 64-bit hash slots holding
+// (key + 1) << 32 | count); its chunks are tch[t] .. tch[t + 1] - 1 of the
+// grid.  A lane's last 16-byte word may reach past the table's last entry
+// (still inside its allocation); those entries are masked.
+constexpr uint32_t kChunkBytes = 32768;
+constexpr uint32_t kLaneVecs = kChunkBytes / 16 / 256;  // 16-byte words per lane
+
+// The block's table (the last table whose first chunk is at or below the
+// block index; tables without chunks are skipped over) and chunk.
+struct Chunk {
+    uint32_t t;
+    bool dense;
+    uint64_t first;       // table entry of the chunk's first entry
+    uint32_t n;           // entries in the chunk
+    const uint4 *p;       // the chunk's first 16-byte word
+};
+
+__device__ __forceinline__ Chunk block_chunk(const unsigned long long *slots, const unsigned long long *t_base,
+                                             const uint32_t *t_len, const uint8_t *t_dense,
+                                             const unsigned long long *tch, uint32_t nt, uint32_t *s_t)
 {
-    return w != 0 && (thr == 0 || count_bin((uint32_t)(w & 0xFFFFFFFFull)) >= thr);
+    if (threadIdx.x == 0) {
+        const unsigned long long b = blockIdx.x;
+        uint32_t lo = 0, hi = nt;  // tch[lo] <= b < tch[hi]
+        while (hi - lo > 1) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            if (tch[mid] <= b) lo = mid;
+            else hi = mid;
+        }
+        *s_t = lo;
+    }
+    __syncthreads();
+    Chunk c;
+    c.t = *s_t;
+    c.dense = t_dense[c.t] != 0;
+    const uint32_t per = c.dense ? kChunkBytes / 4 : kChunkBytes / 8;
+    c.first = (uint64_t)(blockIdx.x - tch[c.t]) * per;
+    const uint64_t left = t_len[c.t] - c.first;
+    c.n = (uint32_t)(left < per ? left : per);
+    c.p = reinterpret_cast<const uint4 *>(slots + t_base[c.t]) + (c.dense ? c.first / 4 : c.first / 2);
+    return c;
 }
 
-// Entry x of table i: a 64-bit hash slot, or a 32-bit dense counter.
-__device__ __forceinline__ unsigned long long table_word(const unsigned long long *s, bool dense, uint64_t x)
+// Word j of the lane: chunk word w = warp * 256 + j * 32 + lane (coalesced
+// per j), entries w * EPV .. w * EPV + EPV - 1 of the chunk.
+template <int EPV>
+__device__ __forceinline__ void load_chunk(const Chunk &c, uint4 (&v)[kLaneVecs])
 {
-    return dense ? (unsigned long long)reinterpret_cast<const uint32_t *>(s)[x] : s[x];
+    const uint32_t w0 = (threadIdx.x >> 5) * (32 * kLaneVecs) + (threadIdx.x & 31);
+    const uint32_t words = (c.n + EPV - 1) / EPV;
+#pragma unroll
+    for (uint32_t j = 0; j < kLaneVecs; ++j) {
+        const uint32_t w = w0 + 32 * j;
+        v[j] = w < words ? ld_stream_u4(c.p + w) : make_uint4(0u, 0u, 0u, 0u);
+    }
 }
 
-// Compaction work is cut into chunks of kChunk entries of one table:
-// chunk c covers entries [ch[c].y, min(ch[c].y + kChunk, t_cap[t])) of table
-// t = ch[c].x, so every block gets the same amount of table to read whatever
-// the spread of table sizes.  Table t starts at slots + t_base[t] and has
-// t_cap[t] entries: 64-bit hash slots, or 32-bit counters when t_dense[t].
-constexpr uint32_t kChunk = 8192;
-
-// Occupied entries per table: one atomic per chunk.
-__global__ void __launch_bounds__(256) k_tabs_count(const unsigned long long *slots, const unsigned long long *t_base,
-                                                    const uint32_t *t_cap, const uint8_t *t_dense, const uint2 *ch,
-                                                    unsigned long long *cnt)
+// Entry e of word j: its count and, for a hash slot, key + 1 (0 = empty).
+template <int EPV>
+__device__ __forceinline__ void word_entry(const uint4 &x, int e, uint32_t &count, uint32_t &tag)
 {
-    __shared__ uint32_t warp_n[8];
-    const uint2 c = ch[blockIdx.x];
-    const uint32_t t = c.x;
-    const unsigned long long *s = slots + t_base[t];
-    const bool dense = t_dense[t] != 0;
-    const uint64_t lo = c.y, hi = lo + kChunk < t_cap[t] ? lo + kChunk : t_cap[t];
+    if (EPV == 4) {
+        count = e == 0 ? x.x : e == 1 ? x.y : e == 2 ? x.z : x.w;
+        tag = count;
+    } else {
+        count = e == 0 ? x.x : x.z;
+        tag = e == 0 ? x.y : x.w;
+    }
+}
+
+// Pass 1: occupied entries per chunk (cc, and hc for hash tables only) and
+// per table (cnt); with HIST also each table's histogram of count_bin over
+// its occupied entries (hist[t * kCountBins + bin]), for top-k selection.
+template <int EPV, bool HIST>
+__device__ __forceinline__ uint32_t count_chunk(const Chunk &c, uint32_t *h)
+{
+    uint4 v[kLaneVecs];
+    load_chunk<EPV>(c, v);
+    const uint32_t w0 = (threadIdx.x >> 5) * (32 * kLaneVecs) + (threadIdx.x & 31);
     uint32_t k = 0;
-    for (uint64_t x = lo + threadIdx.x; x < hi; x += 256) k += table_word(s, dense, x) != 0;
+#pragma unroll
+    for (uint32_t j = 0; j < kLaneVecs; ++j)
+#pragma unroll
+        for (int e = 0; e < EPV; ++e) {
+            uint32_t cnt, tag;
+            word_entry<EPV>(v[j], e, cnt, tag);
+            if (tag != 0 && (w0 + 32 * j) * EPV + e < c.n) {
+                ++k;
+                if (HIST) atomicAdd(&h[count_bin(cnt)], 1u);
+            }
+        }
+    return k;
+}
+
+template <bool HIST>
+__global__ void __launch_bounds__(256) k_tabs_count(const unsigned long long *slots, const unsigned long long *t_base,
+                                                    const uint32_t *t_len, const uint8_t *t_dense,
+                                                    const unsigned long long *tch, uint32_t nt,
+                                                    unsigned long long *cnt, unsigned long long *cc,
+                                                    unsigned long long *hc, uint32_t *hist)
+{
+    __shared__ uint32_t s_t;
+    __shared__ uint32_t warp_n[8];
+    __shared__ uint32_t h[HIST ? kCountBins : 1];
+    if (HIST)
+        for (uint32_t b = threadIdx.x; b < kCountBins; b += 256) h[b] = 0;
+    const Chunk c = block_chunk(slots, t_base, t_len, t_dense, tch, nt, &s_t);  // synchronises
+    uint32_t k = c.dense ? count_chunk<4, HIST>(c, h) : count_chunk<2, HIST>(c, h);
     for (int o = 16; o; o >>= 1) k += __shfl_xor_sync(kBFull, k, o);
     if ((threadIdx.x & 31) == 0) warp_n[threadIdx.x >> 5] = k;
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t tot = 0;
         for (int w = 0; w < 8; ++w) tot += warp_n[w];
-        if (tot) atomicAdd(&cnt[t], (unsigned long long)tot);
+        cc[blockIdx.x] = tot;
+        hc[blockIdx.x] = c.dense ? 0u : tot;
+        if (tot) atomicAdd(&cnt[c.t], (unsigned long long)tot);
     }
+    if (HIST)
+        for (uint32_t b = threadIdx.x; b < kCountBins; b += 256)
+            if (h[b]) atomicAdd(&hist[(uint64_t)c.t * kCountBins + b], h[b]);
 }
 
-// Writes each occupied entry of the chunk's table t into the table's
-// segment as key (t << name_bits | name) and count, so one radix sort of the
-// keys orders every table's entries by name in place.  The block counts its
-// chunk's entries, reserves that many positions with a single atomic on the
-// table's fill cursor, then writes them (warp offsets through shared
-// memory).  Dense tables (entry x = canonical index x, name idx_names[x])
-// are emitted the same way.  With t_thr, only entries whose count bin
-// (count_bin) is at least t_thr[t] are emitted; with by_count the key is
-// (t, ~count, name), which orders each table by count descending, then name
-// (the caller checks that it fits 64 bits).  Launch with 256 threads.
-__global__ void __launch_bounds__(256) k_tabs_emit(const unsigned long long *slots, const unsigned long long *t_base,
-                            const uint32_t *t_cap, const uint8_t *t_dense, const uint2 *ch,
-                            const unsigned long long *seg_off, unsigned long long *fill,
-                            const uint32_t *int2name, const uint32_t *idx_names, int name_bits,
-                            bool by_count, const uint32_t *t_thr, unsigned long long *out_key, uint32_t *out_cnt)
+// Pass 2: writes the chunk's kept entries in entry order.
+//  Full lists (TOPK false): a dense chunk's (name, count) pairs go straight
+//  to the output at pos[b] (name order = index order); a hash chunk's
+//  (t << name_bits | name) keys and counts go to the sort input at hpos[b].
+//  Top-k (TOPK true): entries whose count bin is at least thr[t] go to the
+//  sort input as (t, ~count, name) keys (by_count) or (t << name_bits |
+//  name) keys with counts, at sseg[t] + a block reservation on fill[t].
+// pos and hpos are exclusive scans of pass 1's cc and hc over the chunks in
+// table order, so pos[b] is also the output position of a dense chunk.  Ranks come from a
+// warp scan of per-word counts packed one byte per word, then warp totals
+// through shared memory.
+template <int EPV, bool TOPK>
+__device__ __forceinline__ void place_chunk(const Chunk &c, uint32_t thr, uint32_t *warp_n,
+                                            unsigned long long *s_base, unsigned long long *fill,
+                                            unsigned long long base_full, const uint32_t *int2name,
+                                            const uint32_t *idx_names, int name_bits, bool by_count,
+                                            uint32_t *out_name, uint32_t *out_cnt, unsigned long long *key_out,
+                                            uint32_t *cnt_out)
 {
-    __shared__ uint32_t warp_n[8];
-    __shared__ unsigned long long base_s;
-    const uint2 chunk = ch[blockIdx.x];
-    const uint32_t i = chunk.x;
-    const bool dense = t_dense[i] != 0;
-    const unsigned long long *s = slots + t_base[i];
-    const uint32_t thr = t_thr ? t_thr[i] : 0u;  // keep entries whose count bin >= thr
+    uint4 v[kLaneVecs];
+    load_chunk<EPV>(c, v);
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint64_t lo = chunk.y, hi = lo + kChunk < t_cap[i] ? lo + kChunk : t_cap[i];
-    // pass 1: occupied slots of the chunk
-    uint32_t c = 0;
-    for (uint64_t x = lo + threadIdx.x; x < hi; x += 256) c += kept(table_word(s, dense, x), thr);
-    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kBFull, c, o);
-    if (lane == 0) warp_n[warp] = c;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t t = 0;
-        for (int w = 0; w < 8; ++w) t += warp_n[w];
-        base_s = t ? atomicAdd(&fill[i], (unsigned long long)t) : 0ull;
+    const uint32_t w0 = warp * (32 * kLaneVecs) + lane;
+    uint32_t km = 0;  // kept entries, bit j * EPV + e
+    unsigned long long packed = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < kLaneVecs; ++j) {
+        uint32_t n_j = 0;
+#pragma unroll
+        for (int e = 0; e < EPV; ++e) {
+            uint32_t cnt, tag;
+            word_entry<EPV>(v[j], e, cnt, tag);
+            const bool keep = tag != 0 && (w0 + 32 * j) * EPV + e < c.n && (!TOPK || count_bin(cnt) >= thr);
+            km |= (uint32_t)keep << (j * EPV + e);
+            n_j += keep;
+        }
+        packed |= (unsigned long long)n_j << (8 * j);
     }
+    // per-word inclusive scan over the lanes; a byte never exceeds 32 * EPV
+    unsigned long long inc = packed;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(kBFull, inc, o);
+        if (lane >= (uint32_t)o) inc += y;
+    }
+    const unsigned long long tot = __shfl_sync(kBFull, inc, 31);
+    const unsigned long long exc = inc - packed;
+    uint32_t wsum = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < kLaneVecs; ++j) wsum += (uint32_t)(tot >> (8 * j)) & 0xFFu;
+    if (lane == 0) warp_n[warp] = wsum;
     __syncthreads();
-    unsigned long long pos0 = seg_off[i] + base_s;
-    const unsigned long long tagged = (unsigned long long)i << (by_count ? 32 + name_bits : name_bits);
-    // pass 2: tiles of 256 slots in order
-    for (uint64_t x0 = lo; x0 < hi; x0 += 256) {
-        const uint64_t x = x0 + threadIdx.x;
-        unsigned long long w = x < hi ? table_word(s, dense, x) : 0ull;
-        if (!kept(w, thr)) w = 0;
-        const unsigned om = __ballot_sync(kBFull, w != 0);
-        __syncthreads();  // previous tile's readers of warp_n are done
-        if (lane == 0) warp_n[warp] = __popc(om);
+    uint32_t before = 0, all = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < 8; ++w) {
+        const uint32_t x = warp_n[w];
+        before += w < warp ? x : 0u;
+        all += x;
+    }
+    if (TOPK) {
+        if (threadIdx.x == 0) *s_base = all ? atomicAdd(&fill[c.t], (unsigned long long)all) : 0ull;
         __syncthreads();
-        uint32_t before = 0, total = 0;
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t v = warp_n[k];
-            before += k < (int)warp ? v : 0u;
-            total += v;
+        base_full += *s_base;
+    }
+    unsigned long long p = base_full + before;
+    const unsigned long long tagged = (unsigned long long)c.t << (by_count ? 32 + name_bits : name_bits);
+#pragma unroll
+    for (uint32_t j = 0; j < kLaneVecs; ++j) {
+        unsigned long long r = p + ((exc >> (8 * j)) & 0xFFu);
+#pragma unroll
+        for (int e = 0; e < EPV; ++e) {
+            if (!((km >> (j * EPV + e)) & 1u)) continue;
+            uint32_t cnt, tag;
+            word_entry<EPV>(v[j], e, cnt, tag);
+            const uint32_t name = EPV == 4 ? idx_names[c.first + (w0 + 32 * j) * EPV + e] : int2name[tag - 1];
+            if (!TOPK && EPV == 4) {
+                out_name[r] = name;
+                out_cnt[r] = cnt;
+            } else {
+                const unsigned long long inv =
+                    TOPK && by_count ? (unsigned long long)(0xFFFFFFFFu - cnt) << name_bits : 0ull;
+                key_out[r] = tagged | inv | name;
+                cnt_out[r] = cnt;
+            }
+            ++r;
         }
-        if (w) {
-            const unsigned long long p = pos0 + before + __popc(om & ((1u << lane) - 1u));
-            const uint32_t cnt = (uint32_t)(w & 0xFFFFFFFFull);
-            const unsigned long long inv = by_count ? (unsigned long long)(0xFFFFFFFFu - cnt) << name_bits : 0ull;
-            const uint32_t name = dense ? idx_names[x] : int2name[(uint32_t)(w >> 32) - 1];
-            out_key[p] = tagged | inv | name;
-            out_cnt[p] = cnt;
-        }
-        pos0 += total;
+        p += (tot >> (8 * j)) & 0xFFu;
     }
 }
 
-// Top-k selection, histogram: counts of the occupied entries of every table
-// with more than k of them, by count_bin, into hist[t * kCountBins + bin].
-__global__ void __launch_bounds__(256) k_tabs_hist(const unsigned long long *slots, const unsigned long long *t_base,
-                                                   const uint32_t *t_cap, const uint8_t *t_dense, const uint2 *ch,
-                                                   const unsigned long long *cnt, uint32_t k, uint32_t *hist)
+template <bool TOPK>
+__global__ void __launch_bounds__(256, 4) k_tabs_place(const unsigned long long *slots, const unsigned long long *t_base,
+                                                    const uint32_t *t_len, const uint8_t *t_dense,
+                                                    const unsigned long long *tch, uint32_t nt,
+                                                    const unsigned long long *pos, const unsigned long long *hpos,
+                                                    const uint32_t *t_thr, const unsigned long long *sseg,
+                                                    unsigned long long *fill, const uint32_t *int2name,
+                                                    const uint32_t *idx_names, int name_bits, bool by_count,
+                                                    uint32_t *out_name, uint32_t *out_cnt,
+                                                    unsigned long long *key_out, uint32_t *cnt_out)
 {
-    __shared__ uint32_t h[kCountBins];
-    const uint2 c = ch[blockIdx.x];
-    const uint32_t i = c.x;
-    if (cnt[i] <= k) return;  // every entry is kept
-    for (uint32_t b = threadIdx.x; b < kCountBins; b += blockDim.x) h[b] = 0;
-    __syncthreads();
-    const unsigned long long *s = slots + t_base[i];
-    const bool dense = t_dense[i] != 0;
-    const uint64_t lo = c.y, hi = lo + kChunk < t_cap[i] ? lo + kChunk : t_cap[i];
-    for (uint64_t x = lo + threadIdx.x; x < hi; x += blockDim.x) {
-        const unsigned long long w = table_word(s, dense, x);
-        if (w) atomicAdd(&h[count_bin((uint32_t)(w & 0xFFFFFFFFull))], 1u);
-    }
-    __syncthreads();
-    for (uint32_t b = threadIdx.x; b < kCountBins; b += blockDim.x)
-        if (h[b]) atomicAdd(&hist[(uint64_t)i * kCountBins + b], h[b]);
+    __shared__ uint32_t s_t;
+    __shared__ uint32_t warp_n[8];
+    __shared__ unsigned long long s_base;
+    const Chunk c = block_chunk(slots, t_base, t_len, t_dense, tch, nt, &s_t);  // synchronises
+    const uint32_t thr = TOPK ? t_thr[c.t] : 0u;
+    if (TOPK && sseg[c.t + 1] == sseg[c.t]) return;  // nothing kept in this table (block-uniform)
+    const unsigned long long base = TOPK ? sseg[c.t] : c.dense ? pos[blockIdx.x] : hpos[blockIdx.x];
+    if (c.dense)
+        place_chunk<4, TOPK>(c, thr, warp_n, &s_base, fill, base, int2name, idx_names, name_bits, by_count, out_name,
+                             out_cnt, key_out, cnt_out);
+    else
+        place_chunk<2, TOPK>(c, thr, warp_n, &s_base, fill, base, int2name, idx_names, name_bits, by_count, out_name,
+                             out_cnt, key_out, cnt_out);
 }
 
 // Top-k selection, threshold: the lowest bin thr[i] such that the entries in
@@ -409,85 +520,6 @@ __global__ void k_place_hash(const unsigned long long *key, const uint32_t *cnt,
         const uint64_t p = seg[t] + (j - hseg[t]);
         out_name[p] = (uint32_t)(k & nmask);
         out_cnt[p] = cnt[j];
-    }
-}
-
-// Dense tables in name order without a sort.  Work is cut into warp chunks
-// of kWarpChunk counters: warp w of the grid takes chunk c = w % chunks of
-// dense table dl[w / chunks] (chunks per table = ceil(n / kWarpChunk)).
-constexpr uint32_t kWarpChunk = 256;
-constexpr uint32_t kWarpSteps = kWarpChunk / 32;
-
-// Pass 1: nonzero counters per warp chunk -> cc[w], the chunk's loads
-// issued together.  (Four chunks per warp measured slower: 224 against
-// 147 us on 512 queries at R-MAT scale 20, registers limiting residency.)
-constexpr uint32_t kCountChunks = 1;
-__global__ void __launch_bounds__(256) k_dense_chunks(const unsigned long long *slots,
-                                                      const unsigned long long *t_base, const uint32_t *dl,
-                                                      uint32_t n, uint32_t chunks, uint64_t nw,
-                                                      unsigned long long *cc)
-{
-    const uint64_t w0 = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * kCountChunks;
-    if (w0 >= nw) return;  // whole warp leaves together
-    const uint32_t lane = threadIdx.x & 31;
-    uint32_t v[kCountChunks][kWarpSteps];
-#pragma unroll
-    for (uint32_t q = 0; q < kCountChunks; ++q) {
-        const uint64_t w = w0 + q;
-        const uint32_t *c = w < nw ? reinterpret_cast<const uint32_t *>(slots + t_base[dl[w / chunks]]) : nullptr;
-        const uint64_t lo = (w % chunks) * (uint64_t)kWarpChunk;
-        const uint64_t hi = lo + kWarpChunk < n ? lo + kWarpChunk : n;
-#pragma unroll
-        for (uint32_t j = 0; j < kWarpSteps; ++j) {
-            const uint64_t x = lo + j * 32 + lane;
-            v[q][j] = (c && x < hi) ? c[x] : 0u;
-        }
-    }
-#pragma unroll
-    for (uint32_t q = 0; q < kCountChunks; ++q) {
-        uint32_t k = 0;
-#pragma unroll
-        for (uint32_t j = 0; j < kWarpSteps; ++j) k += v[q][j] != 0;
-        for (int o = 16; o; o >>= 1) k += __shfl_xor_sync(kBFull, k, o);
-        if (lane == 0 && w0 + q < nw) cc[w0 + q] = k;
-    }
-}
-
-// Pass 2: each warp writes its chunk's nonzero counters in index (= name)
-// order at seg[t] + cpos[w] - cpos[table's first chunk] + rank, where cpos is
-// the exclusive scan of pass 1; ranks within the chunk come from ballots, so
-// no block-wide synchronisation is needed.
-__global__ void __launch_bounds__(256) k_dense_place(const unsigned long long *slots,
-                                                     const unsigned long long *t_base, const uint32_t *dl,
-                                                     uint32_t n, uint32_t chunks, uint64_t nw,
-                                                     const unsigned long long *cpos, const unsigned long long *seg,
-                                                     const uint32_t *idx_names, uint32_t *out_name, uint32_t *out_cnt)
-{
-    const uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-    if (w >= nw) return;  // whole warp leaves together
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t y = w / chunks;
-    const uint32_t t = dl[y];
-    const uint32_t *c = reinterpret_cast<const uint32_t *>(slots + t_base[t]);
-    const uint64_t lo = (w % chunks) * (uint64_t)kWarpChunk;
-    const uint64_t hi = lo + kWarpChunk < n ? lo + kWarpChunk : n;
-    unsigned long long pos = seg[t] + cpos[w] - cpos[y * chunks];
-    uint32_t v[kWarpSteps];  // the chunk's counters, loaded before any write
-#pragma unroll
-    for (uint32_t j = 0; j < kWarpSteps; ++j) {
-        const uint64_t x = lo + j * 32 + lane;
-        v[j] = x < hi ? c[x] : 0u;
-    }
-#pragma unroll
-    for (uint32_t j = 0; j < kWarpSteps; ++j) {
-        const unsigned om = __ballot_sync(kBFull, v[j] != 0);
-        if (v[j]) {
-            const uint64_t x = lo + j * 32 + lane;
-            const unsigned long long p = pos + __popc(om & ((1u << lane) - 1u));
-            out_name[p] = idx_names[x];
-            out_cnt[p] = v[j];
-        }
-        pos += __popc(om);
     }
 }
 

@@ -35,36 +35,67 @@ int cuda_fail(cudaError_t e, const char *what)
     return fail(code, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+namespace {
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[64] = {};
+}  // namespace
+
 cudaError_t pooled_alloc_async(void **p, size_t bytes, cudaStream_t st)
 {
-    static std::mutex mu;
-    static cudaMemPool_t pools[64] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaMallocAsync(p, bytes, st);
     cudaMemPool_t pool;
     {
-        std::lock_guard<std::mutex> lk(mu);
-        if (!pools[dev]) {
+        std::lock_guard<std::mutex> lk(g_pool_mu);
+        if (!g_pools[dev]) {
             cudaMemPoolProps props{};
             props.allocType = cudaMemAllocationTypePinned;
             props.location.type = cudaMemLocationTypeDevice;
             props.location.id = dev;
+            size_t free_b = 0, total_b = 0;
+            e = cudaMemGetInfo(&free_b, &total_b);
+            if (e != cudaSuccess) return e;
             cudaMemPool_t np = nullptr;
             e = cudaMemPoolCreate(&np, &props);
             if (e != cudaSuccess) return e;
-            uint64_t keep = 1ull << 30;
+            // Memory freed to the pool stays mapped up to this much across
+            // synchronisations: a batch of thousands of queries allocates and
+            // frees tens of GB of count tables per call, and handing them back
+            // to the driver at every synchronisation costs about 1.5 ms per GB
+            // to unmap and as much again to map on the next call.
+            uint64_t keep = std::max<uint64_t>(1ull << 30, (uint64_t)total_b / 4);
             e = cudaMemPoolSetAttribute(np, cudaMemPoolAttrReleaseThreshold, &keep);
             if (e != cudaSuccess) {
                 cudaMemPoolDestroy(np);
                 return e;
             }
-            pools[dev] = np;
+            g_pools[dev] = np;
         }
-        pool = pools[dev];
+        pool = g_pools[dev];
     }
     return cudaMallocFromPoolAsync(p, bytes, pool, st);
+}
+
+void trim_pools()
+{
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (cudaMemPool_t p : g_pools)
+        if (p) cudaMemPoolTrimTo(p, 0);
+}
+
+cudaError_t device_malloc_bytes(void **p, size_t bytes)
+{
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+        // the pool may hold freed memory: wait for pending frees, hand it back, retry once
+        cudaGetLastError();
+        cudaDeviceSynchronize();
+        trim_pools();
+        e = cudaMalloc(p, bytes);
+    }
+    return e;
 }
 
 namespace {
@@ -253,7 +284,7 @@ int upload_sources(ptw_graph *g, const ptw_walk_cfg *cfg)
         cudaFree(g->sc.sources);
         g->sc.sources = nullptr;
         g->sc.sources_cap = 0;
-        PTW_CUDA(cudaMalloc(&g->sc.sources, (uint64_t)cfg->n_sources * 4));
+        PTW_CUDA(device_malloc(&g->sc.sources, (uint64_t)cfg->n_sources * 4));
         g->sc.sources_cap = cfg->n_sources;
     }
     PTW_CUDA(cudaMemcpyAsync(g->sc.sources, ids.data(), (uint64_t)cfg->n_sources * 4,
@@ -269,7 +300,7 @@ int stage_bytes(ptw_graph *g, size_t bytes, void **out)
         cudaFree(g->sc.out_stage);
         g->sc.out_stage = nullptr;
         g->sc.out_stage_bytes = 0;
-        PTW_CUDA(cudaMalloc(&g->sc.out_stage, std::max<size_t>(bytes, 256)));
+        PTW_CUDA(device_malloc(&g->sc.out_stage, std::max<size_t>(bytes, 256)));
         g->sc.out_stage_bytes = std::max<size_t>(bytes, 256);
     }
     *out = g->sc.out_stage;
@@ -373,6 +404,14 @@ int run_paths(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *d_path
 using namespace ptw;
 
 extern "C" const char *ptw_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int ptw_trim_memory(void)
+{
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "synchronise before trimming");
+    trim_pools();
+    return PTW_OK;
+}
 
 extern "C" const char *ptw_version(void) { return "ptwalker_gb300 0.1 (sm_103a)"; }
 
@@ -610,7 +649,7 @@ extern "C" int ptw_pagerank(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_c
     if (rc) return rc;
     if (!h_counts) return fail(PTW_EINVAL, "null counts buffer");
     PTW_CUDA(cudaSetDevice(g->device));
-    if (!g->sc.by_name) PTW_CUDA(cudaMalloc(&g->sc.by_name, (uint64_t)g->dg.id_bound * 4));
+    if (!g->sc.by_name) PTW_CUDA(device_malloc(&g->sc.by_name, (uint64_t)g->dg.id_bound * 4));
     rc = run_count(g, cfg, g->sc.by_name);
     if (rc) return rc;
     PTW_CUDA(cudaMemcpyAsync(h_counts, g->sc.by_name, (uint64_t)g->dg.id_bound * 4,

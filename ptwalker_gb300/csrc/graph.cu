@@ -172,13 +172,6 @@ __global__ void k_export(const uint2 *adj, const uint32_t *col, const uint32_t *
     }
 }
 
-__global__ void k_names_by_index(const uint32_t *int2name, const uint32_t *idx2int, uint32_t n,
-                                 uint32_t *names)
-{
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        names[i] = int2name[idx2int[i]];
-}
-
 __global__ void k_deg_by_index(const uint2 *adj, const uint32_t *idx2int, uint32_t n, uint32_t *deg)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -567,13 +560,13 @@ int build_graph_from_device_edges(ptw_graph *g, uint32_t *d_src, uint32_t *d_dst
     dg.n = n;
     dg.m = mm;
     dg.id_bound = compact_names ? n : (uint32_t)id_bound;
-    PTW_CUDA(cudaMalloc(&dg.adj, (uint64_t)n * sizeof(uint2)));
-    PTW_CUDA(cudaMalloc(&dg.col, mm * 4));
-    PTW_CUDA(cudaMalloc(&dg.int2name, (uint64_t)n * 4));
-    PTW_CUDA(cudaMalloc(&dg.idx2int, (uint64_t)n * 4));
-    PTW_CUDA(cudaMalloc(&dg.int2idx, (uint64_t)n * 4));
+    PTW_CUDA(device_malloc(&dg.adj, (uint64_t)n * sizeof(uint2)));
+    PTW_CUDA(device_malloc(&dg.col, mm * 4));
+    PTW_CUDA(device_malloc(&dg.int2name, (uint64_t)n * 4));
+    PTW_CUDA(device_malloc(&dg.idx2int, (uint64_t)n * 4));
+    PTW_CUDA(device_malloc(&dg.int2idx, (uint64_t)n * 4));
     PTW_CUDA(cudaMemcpyAsync(dg.int2idx, order, (uint64_t)n * 4, cudaMemcpyDeviceToDevice, st));
-    PTW_CUDA(cudaMalloc(&dg.names, (uint64_t)n * 4));
+    PTW_CUDA(device_malloc(&dg.names, (uint64_t)n * 4));
     PTW_CUDA(cudaMemcpyAsync(dg.names, names, (uint64_t)n * 4, cudaMemcpyDeviceToDevice, st));
     uint32_t *int_deg = iota;  // reuse
     k_relabel<<<grid_for(n), kThreads, 0, st>>>(order, deg, names, n, dg.idx2int, int_deg,
@@ -595,8 +588,8 @@ int build_graph_from_device_edges(ptw_graph *g, uint32_t *d_src, uint32_t *d_dst
     PTW_CUDA(cudaMemcpyAsync(g->h_idx2int, dg.idx2int, (uint64_t)n * 4, cudaMemcpyDeviceToHost, st));
 
     // Scratch reused by every walk.
-    PTW_CUDA(cudaMalloc(&g->sc.counts, (uint64_t)n * 4));
-    PTW_CUDA(cudaMalloc(&g->sc.ctrl, 8 * sizeof(unsigned long long)));
+    PTW_CUDA(device_malloc(&g->sc.counts, (uint64_t)n * 4));
+    PTW_CUDA(device_malloc(&g->sc.ctrl, 8 * sizeof(unsigned long long)));
     PTW_CUDA(cudaStreamSynchronize(st));
     dg.max_degree = h_maxdeg;
     g->device_bytes = (uint64_t)n * (8 + 4 * 4 + 4) + mm * 4 + 64;

@@ -314,7 +314,7 @@ extern "C" int ptw_mlp_create(uint64_t seed, ptw_mlp **out)
     cudaError_t e = cudaGetDevice(&m->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
     for (float **p : {&m->params, &m->grad, &m->m, &m->v})
-        if (e == cudaSuccess) e = cudaMalloc((void **)p, PTW_MLP_NPARAMS * 4);
+        if (e == cudaSuccess) e = device_malloc((void **)p, PTW_MLP_NPARAMS * 4);
     if (e != cudaSuccess) {
         rc = cuda_fail(e, "MLP allocation");
     } else {

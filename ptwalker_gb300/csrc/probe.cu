@@ -70,8 +70,8 @@ extern "C" int ptw_probe_gather(uint64_t array_bytes, uint32_t chains, double *l
     uint32_t *a = nullptr, *sink = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     int rc = PTW_OK;
-    cudaError_t e = cudaMalloc(&a, (size_t)n * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&sink, 4);
+    cudaError_t e = device_malloc(&a, (size_t)n * 4);
+    if (e == cudaSuccess) e = device_malloc(&sink, 4);
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     if (e == cudaSuccess) {

@@ -89,6 +89,16 @@ __device__ __forceinline__ void cp_async_wait_all()
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
+// Streaming 16-byte load: read-only path, no L1 allocation.
+__device__ __forceinline__ uint4 ld_stream_u4(const uint4 *p)
+{
+    uint4 r;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+                 : "l"(p));
+    return r;
+}
+
 __device__ __forceinline__ uint32_t ld_hint_u32(const uint32_t *p, uint64_t pol)
 {
     uint32_t r;
@@ -182,10 +192,20 @@ int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t);
 int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
                  int start_mode, uint32_t n_sources, int32_t *paths);
 // Stream-ordered device allocation from a per-device pool that keeps up to
-// 1 GiB cached across synchronisations (the default pool hands memory back at
-// each one), for the short-lived buffers of every result compaction.  Freed
-// with cudaFreeAsync.
+// a quarter of the device memory cached across synchronisations (the default
+// pool hands memory back at each one), for count tables and the short-lived
+// buffers of every result compaction.  Freed with cudaFreeAsync.
 cudaError_t pooled_alloc_async(void **p, size_t bytes, cudaStream_t st);
+// Hands the pools' cached memory back to the driver.
+void trim_pools();
+// cudaMalloc that, when the device is out of memory, trims the pools and
+// retries once.
+cudaError_t device_malloc_bytes(void **p, size_t bytes);
+template <class T>
+inline cudaError_t device_malloc(T **p, size_t bytes)
+{
+    return device_malloc_bytes(reinterpret_cast<void **>(p), bytes);
+}
 
 int launch_counts_by_name(ptw_graph *g, uint32_t *d_out);
 int check_tune(const ptw_tune &t);
@@ -221,9 +241,11 @@ struct Compacted {
     std::function<void()> pre_join;
 };
 // Compacts nt count tables into *out (batch.cu).  Table i starts at slot
-// h_base[i] of d_slots; a hash table (h_dense[i] == 0, or h_dense NULL) has
-// h_cap[i] 64-bit slots, a dense table h_cap[i] = n 32-bit counters indexed
-// by canonical vertex index.
+// h_base[i] of d_slots, an even slot (16-byte aligned; callers use 128-byte
+// lines); a hash table (h_dense[i] == 0, or h_dense NULL) has h_cap[i]
+// 64-bit slots, a dense table h_cap[i] = n 32-bit counters indexed by
+// canonical vertex index.  The table's allocation must extend to the end of
+// the 16-byte word holding its last entry (read, then masked).
 int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned long long *h_base,
                    const uint32_t *h_cap, const uint8_t *h_dense, uint32_t nt, Compacted *out);
 // The count table of a query: an open-addressing hash table sized from its
@@ -242,6 +264,11 @@ TableSize dense_table(uint32_t n);
 void interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<uint64_t> &count,
                             const std::vector<uint64_t> &table_bytes, uint64_t group_bytes,
                             std::vector<uint3> &desc);
+// The same into a new buffer, groups filled on up to `threads` host threads
+// when there are many descriptors; returns the number of descriptors.
+uint64_t interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<uint64_t> &count,
+                                const std::vector<uint64_t> &table_bytes, uint64_t group_bytes,
+                                std::unique_ptr<uint3[]> &desc, unsigned threads);
 // Count-table bytes per descriptor group: about 3x the 129 MB L2.
 constexpr uint64_t kGroupBytes = 384ull << 20;
 

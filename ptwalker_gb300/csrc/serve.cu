@@ -320,11 +320,11 @@ extern "C" int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server
     }
     s->buddy.init(bytes / 8, 8);
     int rc = PTW_OK;
-    cudaError_t e = cudaMalloc(&s->arena, std::max<uint64_t>(s->buddy.capacity(), 1) * 8);
+    cudaError_t e = device_malloc(&s->arena, std::max<uint64_t>(s->buddy.capacity(), 1) * 8);
     // every query's share splits into at most share/kDescWalkers + 1 descriptors
     s->D = (uint32_t)std::min<uint64_t>(0xFFFFFFFFull, s->cfg.tick_walkers / kDescWalkers + 2ull * s->S + 1);
     s->plan_bytes = plan_size(s->S, s->D);
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_plan, s->plan_bytes);
+    if (e == cudaSuccess) e = device_malloc(&s->d_plan, s->plan_bytes);
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_plan, s->plan_bytes);
     if (e != cudaSuccess) {
         rc = cuda_fail(e, "server allocation");

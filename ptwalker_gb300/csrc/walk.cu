@@ -611,7 +611,7 @@ bool ensure_ext_columns(ptw_graph *g)
     if (g->dg.col_ext) return true;
     const DeviceGraph &dg = g->dg;
     uint4 *cx = nullptr;
-    if (cudaMalloc(&cx, std::max<uint64_t>(dg.m, 1) * sizeof(uint4)) != cudaSuccess) {
+    if (device_malloc(&cx, std::max<uint64_t>(dg.m, 1) * sizeof(uint4)) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
@@ -622,7 +622,7 @@ bool ensure_ext_columns(ptw_graph *g)
         return false;
     }
     uint4 *vx = nullptr;
-    if (cudaMalloc(&vx, std::max<uint32_t>(dg.n, 1) * sizeof(uint4)) != cudaSuccess) {
+    if (device_malloc(&vx, std::max<uint32_t>(dg.n, 1) * sizeof(uint4)) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(cx);
         return false;
@@ -765,7 +765,7 @@ int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uin
     bool named = !ext && g->tune.paths_named != 0;
     if (named && !g->dg.col_named) {
         uint2 *cn = nullptr;
-        if (cudaMalloc(&cn, std::max<uint64_t>(dg.m, 1) * sizeof(uint2)) == cudaSuccess) {
+        if (device_malloc(&cn, std::max<uint64_t>(dg.m, 1) * sizeof(uint2)) == cudaSuccess) {
             const unsigned grid = (unsigned)std::min<uint64_t>((dg.m + 255) / 256, (uint64_t)g->num_sms * 64);
             k_name_columns<<<std::max(grid, 1u), 256, 0, g->stream>>>(dg.col, dg.int2name, dg.m, cn);
             PTW_CUDA(cudaGetLastError());
