@@ -584,8 +584,8 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             const bool packed = q_bits + 32 + name_bits <= 64;
             k_tabs_place<true><<<(unsigned)nch, 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_tch, nt, nullptr,
                                                              nullptr, d_thr, d_sseg, d_fill, g->dg.int2name,
-                                                             g->dg.names, name_bits, packed, nullptr, nullptr, e_key,
-                                                             e_cnt);
+                                                             g->dg.names, name_bits, packed, nullptr, nullptr,
+                                                             nullptr, nullptr, e_key, e_cnt);
             PTW_CUDA(cudaGetLastError());
             unsigned long long *d_kseg;
             PTW_CUDA(db.alloc(&d_kseg, nt + 1));
@@ -620,39 +620,57 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             out->seg = kseg;
         } else {
             // Full lists by name.  Dense tables are already in name order:
-            // their nonzero counters are compacted in place of a sort.  Hash
-            // tables emit (table, name) keys into a separate range, one radix
-            // sort orders them, and they are placed into their segments.
+            // their nonzero counters go straight to the output.  Hash tables
+            // put their entries into one range per table, each range is
+            // sorted by name (a segmented sort of 32-bit names), and the
+            // ranges are copied into their output segments.
             PTW_CUDA(db.alloc(&o_name, n_ent));
             PTW_CUDA(db.alloc(&o_cnt, n_ent));
             std::vector<uint64_t> hseg(nt + 1, 0);
             for (uint32_t i = 0; i < nt; ++i)
                 hseg[i + 1] = hseg[i] + (dense_flags[i] ? 0 : out->seg[i + 1] - out->seg[i]);
             const uint64_t n_hash = hseg[nt];
-            unsigned long long *e_key = nullptr, *s_key = nullptr, *d_hseg = nullptr;
-            uint32_t *e_cnt = nullptr, *s_cnt = nullptr;
+            unsigned long long *d_hseg = nullptr;
+            uint32_t *h_name = nullptr, *h_cnt = nullptr, *s_name = nullptr, *s_cnt = nullptr;
             if (n_hash) {
-                PTW_CUDA(db.alloc(&e_key, n_hash));
-                PTW_CUDA(db.alloc(&s_key, n_hash));
-                PTW_CUDA(db.alloc(&e_cnt, n_hash));
+                PTW_CUDA(db.alloc(&h_name, n_hash));
+                PTW_CUDA(db.alloc(&h_cnt, n_hash));
+                PTW_CUDA(db.alloc(&s_name, n_hash));
                 PTW_CUDA(db.alloc(&s_cnt, n_hash));
                 PTW_CUDA(db.alloc(&d_hseg, nt + 1));
                 PTW_CUDA(cudaMemcpyAsync(d_hseg, hseg.data(), (nt + 1) * 8ull, cudaMemcpyHostToDevice, st));
             }
-            // Pass 2: dense tables straight to the output, hash tables to the sort input.
+            // Pass 2: dense tables straight to the output, hash tables to their ranges.
             k_tabs_place<false><<<(unsigned)nch, 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_tch, nt, d_pos,
                                                               d_hpos, nullptr, nullptr, nullptr, g->dg.int2name,
-                                                              g->dg.names, name_bits, false, o_name, o_cnt, e_key,
-                                                              e_cnt);
+                                                              g->dg.names, name_bits, false, o_name, o_cnt, h_name,
+                                                              h_cnt, nullptr, nullptr);
             PTW_CUDA(cudaGetLastError());
             if (n_hash) {
-                PTW_CUDA(cub_call([&](void *t, size_t &b) {
-                    return cub::DeviceRadixSort::SortPairs(t, b, e_key, s_key, e_cnt, s_cnt, (int64_t)n_hash, 0,
-                                                           name_bits + q_bits, st);
-                }, st));
+                // segmented sorts over runs of whole tables of under 2^31 entries each
+                for (uint32_t t0 = 0; t0 < nt;) {
+                    uint32_t t1 = t0 + 1;
+                    while (t1 < nt && hseg[t1 + 1] - hseg[t0] < (1ull << 31)) ++t1;
+                    const uint64_t items = hseg[t1] - hseg[t0];
+                    if (items) {
+                        if (items >= (1ull << 31)) return fail(PTW_EINVAL, "a hash table holds 2^31 entries or more");
+                        std::vector<unsigned long long> rel(t1 - t0 + 1);
+                        for (uint32_t i = t0; i <= t1; ++i) rel[i - t0] = hseg[i] - hseg[t0];
+                        unsigned long long *d_rel;
+                        PTW_CUDA(db.alloc(&d_rel, rel.size()));
+                        PTW_CUDA(cudaMemcpyAsync(d_rel, rel.data(), rel.size() * 8ull, cudaMemcpyHostToDevice, st));
+                        const uint64_t o = hseg[t0];
+                        PTW_CUDA(cub_call([&](void *t, size_t &b) {
+                            return cub::DeviceSegmentedSort::SortPairs(t, b, h_name + o, s_name + o, h_cnt + o,
+                                                                       s_cnt + o, (int)items, (int)(t1 - t0), d_rel,
+                                                                       d_rel + 1, st);
+                        }, st));
+                    }
+                    t0 = t1;
+                }
                 const unsigned hg = (unsigned)std::min<uint64_t>((n_hash + 255) / 256, (uint64_t)g->num_sms * 32);
-                k_place_hash<<<std::max(hg, 1u), 256, 0, st>>>(s_key, s_cnt, n_hash, name_bits, d_seg, d_hseg,
-                                                              o_name, o_cnt);
+                k_place_hash<<<std::max(hg, 1u), 256, 0, st>>>(s_name, s_cnt, n_hash, d_hseg, nt, d_seg, o_name,
+                                                              o_cnt);
                 PTW_CUDA(cudaGetLastError());
             }
         }

@@ -242,16 +242,18 @@ __device__ __forceinline__ uint32_t count_bin(uint32_t c)
     return 256 + (e - 8) * 16 + ((c >> (e - 4)) & 15u);
 }
 
-// Compaction reads the count tables in block chunks of 32 KB of one table
-// (8,192 dense counters or 4,096 hash slots): one 256-thread block per
-// chunk, 4 KB per warp, eight 16-byte loads per lane issued together, so
-// enough bytes are in flight to stream the tables at HBM rate.  Table t
-// starts at slots + t_base[t] on a 128-byte boundary and has t_len[t]
+// Compaction reads the count tables in block chunks of 16 KB of one table
+// (4,096 dense counters or 2,048 hash slots): one 256-thread block per
+// chunk, 2 KB per warp, four 16-byte loads per lane issued together, so
+// that with four or more blocks per SM enough bytes are in flight to stream
+// the tables at HBM rate (the placement pass also keeps every kept entry's
+// name in registers, which bounds the chunk).  Table t starts at slots +
+// t_base[t] on a 16-byte boundary (128 bytes in practice) and has t_len[t]
 // entries (32-bit counters when t_dense[t], else 64-bit hash slots holding
 // (key + 1) << 32 | count); its chunks are tch[t] .. tch[t + 1] - 1 of the
 // grid.  A lane's last 16-byte word may reach past the table's last entry
 // (still inside its allocation); those entries are masked.
-constexpr uint32_t kChunkBytes = 32768;
+constexpr uint32_t kChunkBytes = 16384;
 constexpr uint32_t kLaneVecs = kChunkBytes / 16 / 256;  // 16-byte words per lane
 
 // The block's table (the last table whose first chunk is at or below the
@@ -372,22 +374,28 @@ __global__ void __launch_bounds__(256) k_tabs_count(const unsigned long long *sl
 
 // Pass 2: writes the chunk's kept entries in entry order.
 //  Full lists (TOPK false): a dense chunk's (name, count) pairs go straight
-//  to the output at pos[b] (name order = index order); a hash chunk's
-//  (t << name_bits | name) keys and counts go to the sort input at hpos[b].
+//  to the output at pos[b] (name order = index order); a hash chunk's names
+//  and counts go to the sort input at hpos[b], which keeps each hash table's
+//  entries in one range (sorted by name within it afterwards).
 //  Top-k (TOPK true): entries whose count bin is at least thr[t] go to the
 //  sort input as (t, ~count, name) keys (by_count) or (t << name_bits |
 //  name) keys with counts, at sseg[t] + a block reservation on fill[t].
 // pos and hpos are exclusive scans of pass 1's cc and hc over the chunks in
-// table order, so pos[b] is also the output position of a dense chunk.  Ranks come from a
-// warp scan of per-word counts packed one byte per word, then warp totals
-// through shared memory.
+// table order, so pos[b] is also the output position of a dense chunk.
+// Ranks come from a warp scan of per-word counts packed one byte per word,
+// then warp totals through shared memory; each warp stages its kept entries
+// (name, count) in rank order in shared memory, so the stores to global
+// memory are whole coalesced rows.
+constexpr uint32_t kWarpStage = 32 * kLaneVecs * 4;
+
 template <int EPV, bool TOPK>
 __device__ __forceinline__ void place_chunk(const Chunk &c, uint32_t thr, uint32_t *warp_n,
-                                            unsigned long long *s_base, unsigned long long *fill,
-                                            unsigned long long base_full, const uint32_t *int2name,
-                                            const uint32_t *idx_names, int name_bits, bool by_count,
-                                            uint32_t *out_name, uint32_t *out_cnt, unsigned long long *key_out,
-                                            uint32_t *cnt_out)
+                                            unsigned long long *s_base, uint32_t *s_nm, uint32_t *s_ct,
+                                            unsigned long long *__restrict__ fill, unsigned long long base_full,
+                                            const uint32_t *__restrict__ int2name,
+                                            const uint32_t *__restrict__ idx_names, int name_bits, bool by_count,
+                                            uint32_t *__restrict__ out_name, uint32_t *__restrict__ out_cnt,
+                                            unsigned long long *__restrict__ key_out, uint32_t *__restrict__ cnt_out)
 {
     uint4 v[kLaneVecs];
     load_chunk<EPV>(c, v);
@@ -407,6 +415,35 @@ __device__ __forceinline__ void place_chunk(const Chunk &c, uint32_t thr, uint32
             n_j += keep;
         }
         packed |= (unsigned long long)n_j << (8 * j);
+    }
+    // Names of the kept entries, all loads issued before any is used (they
+    // land while the ranks are scanned): a dense chunk's names are
+    // contiguous (16-byte loads of idx_names where the word lies inside the
+    // table), a hash slot's name is int2name[key].
+    uint32_t nm[kLaneVecs][EPV];
+#pragma unroll
+    for (uint32_t j = 0; j < kLaneVecs; ++j) {
+        const uint32_t wm = (km >> (j * EPV)) & ((1u << EPV) - 1u);
+        const uint64_t x0 = c.first + (uint64_t)(w0 + 32 * j) * EPV;
+        if (EPV == 4) {
+            if (wm != 0 && (w0 + 32 * j) * EPV + 4 <= c.n) {
+                const uint4 q = ld_stream_u4(reinterpret_cast<const uint4 *>(idx_names + x0));
+                nm[j][0] = q.x;
+                nm[j][1] = q.y;
+                nm[j][2 % EPV] = q.z;
+                nm[j][3 % EPV] = q.w;
+            } else {
+#pragma unroll
+                for (int e = 0; e < EPV; ++e) nm[j][e] = (wm >> e) & 1u ? idx_names[x0 + e] : 0u;
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < EPV; ++e) {
+                uint32_t cnt, tag;
+                word_entry<EPV>(v[j], e, cnt, tag);
+                nm[j][e] = (wm >> e) & 1u ? int2name[tag - 1] : 0u;
+            }
+        }
     }
     // per-word inclusive scan over the lanes; a byte never exceeds 32 * EPV
     unsigned long long inc = packed;
@@ -434,56 +471,64 @@ __device__ __forceinline__ void place_chunk(const Chunk &c, uint32_t thr, uint32
         __syncthreads();
         base_full += *s_base;
     }
-    unsigned long long p = base_full + before;
-    const unsigned long long tagged = (unsigned long long)c.t << (by_count ? 32 + name_bits : name_bits);
+    // stage in warp-local rank order, then write whole rows
+    uint32_t *wn = s_nm + warp * kWarpStage, *wc = s_ct + warp * kWarpStage;
+    uint32_t jb = 0;
 #pragma unroll
     for (uint32_t j = 0; j < kLaneVecs; ++j) {
-        unsigned long long r = p + ((exc >> (8 * j)) & 0xFFu);
+        uint32_t r = jb + ((uint32_t)(exc >> (8 * j)) & 0xFFu);
 #pragma unroll
         for (int e = 0; e < EPV; ++e) {
             if (!((km >> (j * EPV + e)) & 1u)) continue;
             uint32_t cnt, tag;
             word_entry<EPV>(v[j], e, cnt, tag);
-            const uint32_t name = EPV == 4 ? idx_names[c.first + (w0 + 32 * j) * EPV + e] : int2name[tag - 1];
-            if (!TOPK && EPV == 4) {
-                out_name[r] = name;
-                out_cnt[r] = cnt;
-            } else {
-                const unsigned long long inv =
-                    TOPK && by_count ? (unsigned long long)(0xFFFFFFFFu - cnt) << name_bits : 0ull;
-                key_out[r] = tagged | inv | name;
-                cnt_out[r] = cnt;
-            }
+            wn[r] = nm[j][e];
+            wc[r] = cnt;
             ++r;
         }
-        p += (tot >> (8 * j)) & 0xFFu;
+        jb += (uint32_t)(tot >> (8 * j)) & 0xFFu;
+    }
+    __syncwarp();
+    const unsigned long long p = base_full + before;
+    const unsigned long long tagged = (unsigned long long)c.t << (by_count ? 32 + name_bits : name_bits);
+    for (uint32_t i = lane; i < wsum; i += 32) {
+        const uint32_t name = wn[i], cnt = wc[i];
+        if (TOPK) {
+            const unsigned long long inv = by_count ? (unsigned long long)(0xFFFFFFFFu - cnt) << name_bits : 0ull;
+            key_out[p + i] = tagged | inv | name;
+        } else {
+            out_name[p + i] = name;
+        }
+        (TOPK ? cnt_out : out_cnt)[p + i] = cnt;
     }
 }
 
 template <bool TOPK>
 __global__ void __launch_bounds__(256, 4) k_tabs_place(const unsigned long long *slots, const unsigned long long *t_base,
-                                                    const uint32_t *t_len, const uint8_t *t_dense,
-                                                    const unsigned long long *tch, uint32_t nt,
-                                                    const unsigned long long *pos, const unsigned long long *hpos,
-                                                    const uint32_t *t_thr, const unsigned long long *sseg,
-                                                    unsigned long long *fill, const uint32_t *int2name,
-                                                    const uint32_t *idx_names, int name_bits, bool by_count,
-                                                    uint32_t *out_name, uint32_t *out_cnt,
-                                                    unsigned long long *key_out, uint32_t *cnt_out)
+                                                       const uint32_t *t_len, const uint8_t *t_dense,
+                                                       const unsigned long long *tch, uint32_t nt,
+                                                       const unsigned long long *pos, const unsigned long long *hpos,
+                                                       const uint32_t *t_thr, const unsigned long long *sseg,
+                                                       unsigned long long *fill, const uint32_t *int2name,
+                                                       const uint32_t *idx_names, int name_bits, bool by_count,
+                                                       uint32_t *out_name, uint32_t *out_cnt, uint32_t *h_name,
+                                                       uint32_t *h_cnt, unsigned long long *key_out,
+                                                       uint32_t *cnt_out)
 {
     __shared__ uint32_t s_t;
     __shared__ uint32_t warp_n[8];
     __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_nm[8 * kWarpStage], s_ct[8 * kWarpStage];
     const Chunk c = block_chunk(slots, t_base, t_len, t_dense, tch, nt, &s_t);  // synchronises
     const uint32_t thr = TOPK ? t_thr[c.t] : 0u;
     if (TOPK && sseg[c.t + 1] == sseg[c.t]) return;  // nothing kept in this table (block-uniform)
     const unsigned long long base = TOPK ? sseg[c.t] : c.dense ? pos[blockIdx.x] : hpos[blockIdx.x];
     if (c.dense)
-        place_chunk<4, TOPK>(c, thr, warp_n, &s_base, fill, base, int2name, idx_names, name_bits, by_count, out_name,
-                             out_cnt, key_out, cnt_out);
+        place_chunk<4, TOPK>(c, thr, warp_n, &s_base, s_nm, s_ct, fill, base, int2name, idx_names, name_bits,
+                             by_count, out_name, out_cnt, key_out, cnt_out);
     else
-        place_chunk<2, TOPK>(c, thr, warp_n, &s_base, fill, base, int2name, idx_names, name_bits, by_count, out_name,
-                             out_cnt, key_out, cnt_out);
+        place_chunk<2, TOPK>(c, thr, warp_n, &s_base, s_nm, s_ct, fill, base, int2name, idx_names, name_bits,
+                             by_count, h_name, h_cnt, key_out, cnt_out);
 }
 
 // Top-k selection, threshold: the lowest bin thr[i] such that the entries in
@@ -507,18 +552,20 @@ __global__ void k_tabs_thresh(const unsigned long long *cnt, const uint32_t *his
     sel[i] = acc;
 }
 
-// Sorted hash entries j (keys table << name_bits | name, counts) go to
-// position seg[t] + (j - hseg[t]) of their table t's output segment.
-__global__ void k_place_hash(const unsigned long long *key, const uint32_t *cnt, uint64_t n, int name_bits,
-                             const unsigned long long *seg, const unsigned long long *hseg, uint32_t *out_name,
-                             uint32_t *out_cnt)
+// Hash entries j, sorted by name within their table t's range [hseg[t],
+// hseg[t + 1]), go to position seg[t] + (j - hseg[t]) of the output.
+__global__ void k_place_hash(const uint32_t *name, const uint32_t *cnt, uint64_t n, const unsigned long long *hseg,
+                             uint32_t nt, const unsigned long long *seg, uint32_t *out_name, uint32_t *out_cnt)
 {
-    const unsigned long long nmask = (1ull << name_bits) - 1;
     for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
-        const unsigned long long k = key[j];
-        const uint32_t t = (uint32_t)(k >> name_bits);
-        const uint64_t p = seg[t] + (j - hseg[t]);
-        out_name[p] = (uint32_t)(k & nmask);
+        uint32_t lo = 0, hi = nt;  // hseg[lo] <= j < hseg[hi]
+        while (hi - lo > 1) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            if (hseg[mid] <= j) lo = mid;
+            else hi = mid;
+        }
+        const uint64_t p = seg[lo] + (j - hseg[lo]);
+        out_name[p] = name[j];
         out_cnt[p] = cnt[j];
     }
 }
