@@ -12,7 +12,10 @@ removed (synthetic, built on the device).  Each step uses a new seed.
             counts read back into pinned host memory every step; a step's
             only input is its walk configuration (passed by value, no copy):
             the graph stays resident, as in the reference, whose walk timer
-            excludes the graph load
+            excludes the graph load.  e2e.pipelined: the same walks through
+            ptw_pagerank_submit / ptw_pagerank_wait with two calls in
+            flight, each step's counts copied to pinned host memory while
+            the next step walks
   roofline  random-gather bound: 64 B per move (row record + column
             sector) + 32 B per counted visit, against the measured HBM peak;
             traffic = the ncu DRAM bytes per move of the committed scale-24
@@ -263,12 +266,19 @@ def loguniform_budgets(n, lo, hi, seed):
 
 def bench_batch(args, ptw):
     """Config: R-MAT scale 22, 4096 degree-proportional sources (seed 2),
-    budgets log-uniform in [1e3, 1e6] (seed 3), sp 0.2, one batch call."""
+    budgets log-uniform in [1e3, 1e6] (seed 3), sp 0.2; one timed batch
+    call after one untimed call of the same size (reported as
+    cold_seconds)."""
     import numpy as np
     G = ptw.Graph.rmat(args.batch_scale, 16, 0.57, 0.19, 0.19, seed=1, clean=True)
     src = degree_sources(G, args.batch_queries, 2)
     bud = loguniform_budgets(args.batch_queries, 1e3, 1e6, 3)
-    ptw.ppr_batch(G, src[:64], bud[:64], sp=0.2, seed=7).close()  # warm-up
+    # The first call of this size maps the device memory of its count tables
+    # and faults in its host result pages (cold_seconds); the timed call is
+    # the next one, as in a job that runs batch after batch.
+    t0 = time.perf_counter()
+    ptw.ppr_batch(G, src, bud, sp=0.2, seed=6).close()
+    cold = time.perf_counter() - t0
     t0 = time.perf_counter()
     res = ptw.ppr_batch(G, src, bud, sp=0.2, seed=7)
     wall = time.perf_counter() - t0
@@ -278,6 +288,7 @@ def bench_batch(args, ptw):
     out = {"graph": "rmat-s%d" % args.batch_scale, "vertices": G.n, "edges": G.m,
            "queries": int(args.batch_queries), "walkers": int(res.walkers), "moves": int(res.moves),
            "entries": int(res.entries), "seconds": wall, "queries_per_s": args.batch_queries / wall,
+           "cold_seconds": cold,
            "steps_per_s": res.moves / wall, "device_ms": res.ms, "walk_kernel_ms": res.kernel_ms,
            "walk_kernel_steps_per_s": res.moves / (res.kernel_ms / 1000.0),
            "fp64_l1_sample": {"queries": int(len(sub)), "p50": float(np.median(l1)),
@@ -527,6 +538,26 @@ def run_ours(args):
         e_ms = e0.elapsed_time(e1)
         e2e = {"value": sum(moves) / (e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": 0,
                "d2h_bytes_per_step": 4 * G.id_bound, "host_wall_value": sum(moves) / wall}
+        # The same walks through the pipelined pair (ptw_pagerank_submit /
+        # ptw_pagerank_wait, two calls in flight): each step's counts still
+        # reach pinned host memory inside the timed region, while the next
+        # step walks.  Host wall clock from the first submit to the last wait.
+        hosts = [host, torch.empty(G.id_bound, dtype=torch.int32, pin_memory=True)]
+        for k in range(2):
+            ptw.pagerank_wait(G, ptw.pagerank_submit(G, hosts[k], n, args.sp, 10 + k, "per_vertex"))
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        pend, p_moves = [], 0
+        for k in range(args.steps):
+            if len(pend) == 2:
+                p_moves += ptw.pagerank_wait(G, pend.pop(0)).moves
+            pend.append(ptw.pagerank_submit(G, hosts[k % 2], n, args.sp, seeds[k], "per_vertex"))
+        for t in pend:
+            p_moves += ptw.pagerank_wait(G, t).moves
+        p_wall = time.perf_counter() - w0
+        e2e["pipelined"] = {"value": p_moves / p_wall, "unit": UNIT, "d2h_bytes_per_step": 4 * G.id_bound,
+                            "api": "ptw_pagerank_submit / ptw_pagerank_wait, two calls in flight",
+                            "same_moves_as_device_loop": p_moves == sum(moves)}
 
     # DeepWalk side line: one walker per vertex, L = walk_len, paths in HBM
     deepwalk = None

@@ -43,6 +43,7 @@ extern "C" {
 #define PTW_ETIMEOUT (-4) /* a bounded device-side wait gave up */
 #define PTW_EIO (-5)      /* file could not be read or parsed */
 #define PTW_EFULL (-6)    /* a device table has no free capacity */
+#define PTW_EBUSY (-7)    /* too many pipelined calls in flight */
 
 #define PTW_FMT_BINARY 0  /* raw Edge{u32 src; u32 dst}[]   include/io.hpp:39-53 */
 #define PTW_FMT_TEXT 1    /* "%u %u" lines, '#' comments    include/io.hpp:76-90 */
@@ -188,6 +189,18 @@ int ptw_graph_get_tune(const ptw_graph *g, ptw_tune *t);
  * into h_counts[id_bound] by name. */
 int ptw_pagerank(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_counts,
                  ptw_walk_stats *stats);
+
+/* Pipelined form of ptw_pagerank for a caller that runs many walks: submit
+ * launches the walk and the copy of its counts into h_counts[id_bound] and
+ * returns at once with a ticket; wait blocks until that call's counts are
+ * in h_counts and fills stats (kernel_ms = walk and scatter by name,
+ * total_ms = until the copy ended).  The copy of one call runs on a second
+ * stream while the next call walks.  Two calls may be in flight per graph
+ * (a third submit returns PTW_EBUSY); h_counts must stay valid until the
+ * wait and should be page-locked (cudaHostAlloc) for the copy to overlap.
+ * Results equal ptw_pagerank's with the same configuration. */
+int ptw_pagerank_submit(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_counts, uint64_t *ticket);
+int ptw_pagerank_wait(ptw_graph *g, uint64_t ticket, ptw_walk_stats *stats);
 
 /* Device variant: d_counts[id_bound] receives the counts by name.  Runs on
  * the graph's stream and does not synchronise unless stats != NULL. */

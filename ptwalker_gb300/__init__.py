@@ -22,6 +22,8 @@ from .api import (  # noqa: F401
     walk,
     probe_gather,
     trim_memory,
+    pagerank_submit,
+    pagerank_wait,
 )
 
 from .batch import BatchResult, ppr_batch  # noqa: F401,E402

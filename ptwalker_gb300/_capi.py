@@ -11,6 +11,7 @@ PTW_ECUDA = -3
 PTW_ETIMEOUT = -4
 PTW_EIO = -5
 PTW_EFULL = -6
+PTW_EBUSY = -7
 
 PTW_FMT_BINARY = 0
 PTW_FMT_TEXT = 1
@@ -20,7 +21,8 @@ PTW_START_UNIFORM = 1
 PTW_START_SOURCES = 2
 
 _ERRNAMES = {PTW_EINVAL: "PTW_EINVAL", PTW_ENOMEM: "PTW_ENOMEM", PTW_ECUDA: "PTW_ECUDA",
-             PTW_ETIMEOUT: "PTW_ETIMEOUT", PTW_EIO: "PTW_EIO", PTW_EFULL: "PTW_EFULL"}
+             PTW_ETIMEOUT: "PTW_ETIMEOUT", PTW_EIO: "PTW_EIO", PTW_EFULL: "PTW_EFULL",
+             PTW_EBUSY: "PTW_EBUSY"}
 
 
 class GraphInfo(ctypes.Structure):
@@ -114,6 +116,8 @@ SIGNATURES = [
     ("ptw_graph_get_tune", ctypes.c_int, [_G, ctypes.POINTER(Tune)]),
     ("ptw_pagerank", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, ctypes.POINTER(WalkStats)]),
     ("ptw_pagerank_dev", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, ctypes.POINTER(WalkStats)]),
+    ("ptw_pagerank_submit", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, ctypes.POINTER(ctypes.c_uint64)]),
+    ("ptw_pagerank_wait", ctypes.c_int, [_G, ctypes.c_uint64, ctypes.POINTER(WalkStats)]),
     ("ptw_rwr", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, ctypes.POINTER(WalkStats)]),
     ("ptw_rwr_dev", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, ctypes.POINTER(WalkStats)]),
     ("ptw_deepwalk", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), ctypes.c_uint32, _vp,

@@ -104,6 +104,7 @@ class Graph:
         self.m = int(info.n_edges)
         self.id_bound = int(info.id_bound)
         self.max_degree = int(info.max_degree)
+        self._inflight = {}  # ticket -> host buffer of a pipelined pagerank call
 
     @property
     def device_bytes(self):
@@ -181,8 +182,9 @@ class Graph:
     # -- lifetime ----------------------------------------------------------
     def close(self):
         if self._h:
-            self._lib.ptw_graph_free(self._h)
+            self._lib.ptw_graph_free(self._h)  # waits for the graph's streams
             self._h = None
+        self._inflight.clear()
 
     def __enter__(self):
         return self
@@ -305,6 +307,36 @@ def pagerank(graph, n_walkers=None, sp=0.15, seed=0, start="per_vertex", sources
     if out is None:
         out = np.empty(graph.id_bound, dtype=np.uint32)
     return _run(graph, "ptw_pagerank", (ctypes.byref(cfg),), out, graph.id_bound, stats)
+
+
+def pagerank_submit(graph, out, n_walkers=None, sp=0.15, seed=0, start="per_vertex", sources=None,
+                    max_moves=0, first_walker=0):
+    """Pipelined pagerank (ptw_pagerank_submit): launches the walk and the
+    copy of its counts into ``out`` (uint32[id_bound], best page-locked, e.g.
+    a pinned CPU tensor) and returns a ticket at once.  Two calls may be in
+    flight per graph; ``pagerank_wait(graph, ticket)`` returns the call's
+    WalkStats once ``out`` holds its counts."""
+    n_walkers = graph.n if n_walkers is None else n_walkers
+    if getattr(out, "is_cuda", False):
+        raise ValueError("pagerank_submit copies to host memory; use pagerank(out=<CUDA tensor>) on the device")
+    itemsize = out.itemsize if isinstance(out, np.ndarray) else out.element_size()
+    if itemsize != 4 or _nelem(out) < graph.id_bound:
+        raise ValueError("output needs at least %d 4-byte elements" % graph.id_bound)
+    cfg, _keep = _cfg(n_walkers, sp, seed, start, sources, max_moves, first_walker)
+    t = ctypes.c_uint64()
+    C.check(graph._lib.ptw_pagerank_submit(graph.handle, ctypes.byref(cfg), _host_ptr(out), ctypes.byref(t)))
+    graph._inflight[int(t.value)] = out  # the buffer stays referenced until the wait
+    return int(t.value)
+
+
+def pagerank_wait(graph, ticket):
+    """Waits for a pagerank_submit call; returns its WalkStats."""
+    st = C.WalkStats()
+    try:
+        C.check(graph._lib.ptw_pagerank_wait(graph.handle, int(ticket), ctypes.byref(st)))
+    finally:
+        graph._inflight.pop(int(ticket), None)
+    return WalkStats(st)
 
 
 def _nelem(out):

@@ -33,6 +33,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -46,6 +47,7 @@ struct ptw_batch {
     std::vector<ptw_query> queries;
     std::vector<uint64_t> offsets;  // [nq + 1]
     std::unique_ptr<uint32_t[]> names, counts;
+    uint64_t buf_cap = 0, buf_touched = 0;  // entries allocated / faulted in
     ptw_walk_stats stats{};
     uint32_t top_k = 0;  // results hold each query's top_k largest counts only
 };
@@ -104,6 +106,43 @@ public:
 private:
     std::vector<std::thread> th_;
 };
+
+std::mutex g_host_mu;
+HostBufs g_host_cache;
+constexpr uint64_t kHostCacheMaxBytes = 32ull << 30;
+
+}  // namespace
+
+bool host_cache_take(uint64_t need, HostBufs &out)
+{
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    if (!g_host_cache.names || g_host_cache.cap < need) return false;
+    out = std::move(g_host_cache);
+    g_host_cache = HostBufs();
+    return true;
+}
+
+void host_cache_put(HostBufs &&b)
+{
+    if (!b.names || !b.counts || b.cap * 8 > kHostCacheMaxBytes) return;
+    HostBufs old;
+    {
+        std::lock_guard<std::mutex> lk(g_host_mu);
+        if (g_host_cache.names && g_host_cache.cap > b.cap) return;  // keep the larger pair
+        old = std::move(g_host_cache);
+        g_host_cache = std::move(b);
+    }
+}  // the replaced pair is freed outside the lock
+
+void trim_host_cache()
+{
+    HostBufs old;
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    old = std::move(g_host_cache);
+    g_host_cache = HostBufs();
+}
+
+namespace {
 
 // Hands the whole pages of [p + used, p + cap) back to the system; the
 // range stays valid (it reads as zeros if touched again).
@@ -214,12 +253,9 @@ uint64_t interleave_descriptors(const std::vector<uint64_t> &j0, const std::vect
         for (size_t k = 0; k < ng; ++k) fill(k);
     } else {
         std::atomic<size_t> next{0};
-        std::vector<std::thread> pool;
-        for (unsigned t = 0; t < nth; ++t)
-            pool.emplace_back([&] {
-                for (size_t k; (k = next.fetch_add(1)) < ng;) fill(k);
-            });
-        for (std::thread &t : pool) t.join();
+        parallel_for_threads(nth, [&](unsigned) {
+            for (size_t k; (k = next.fetch_add(1)) < ng;) fill(k);
+        });
     }
     return goff[ng];
 }
@@ -329,15 +365,29 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
         for (uint32_t i = 0; i < nq; ++i)
             est += std::min<uint64_t>(g->dg.n, (uint64_t)(1.5 * (double)wq[i].budget) + 64);
         if (est * 8 >= (64ull << 20)) {
-            wr.c.pre_names.reset(new (std::nothrow) uint32_t[est]);
-            wr.c.pre_counts.reset(new (std::nothrow) uint32_t[est]);
-            if (wr.c.pre_names && wr.c.pre_counts) {
+            HostBufs hb;
+            if (host_cache_take(est, hb)) {
+                // a freed batch's buffers: only the part never faulted in needs it
+                wr.c.pre_names = std::move(hb.names);
+                wr.c.pre_counts = std::move(hb.counts);
+                wr.c.pre_cap = hb.cap;
+                wr.c.pre_touched = std::min(hb.touched, est);
+            } else {
+                wr.c.pre_names.reset(new (std::nothrow) uint32_t[est]);
+                wr.c.pre_counts.reset(new (std::nothrow) uint32_t[est]);
                 wr.c.pre_cap = est;
-                early.start({{wr.c.pre_names.get(), est * 4}, {wr.c.pre_counts.get(), est * 4}});
+                wr.c.pre_touched = 0;
+            }
+            if (wr.c.pre_names && wr.c.pre_counts) {
+                const uint64_t t0 = wr.c.pre_touched;
+                if (t0 < est)
+                    early.start({{wr.c.pre_names.get() + t0, (est - t0) * 4},
+                                 {wr.c.pre_counts.get() + t0, (est - t0) * 4}});
                 wr.c.pre_join = [&early] { early.join(); };
             } else {
                 wr.c.pre_names.reset();
                 wr.c.pre_counts.reset();
+                wr.c.pre_cap = 0;
             }
         }
     }
@@ -407,12 +457,15 @@ int assemble(ptw_batch *b, std::vector<WaveResult> &waves)
     if (adopt) {
         b->names = std::move(waves[0].c.names);
         b->counts = std::move(waves[0].c.counts);
+        b->buf_cap = waves[0].c.cap;
+        b->buf_touched = waves[0].c.touched;
         return PTW_OK;
     }
     if (!total) return PTW_OK;
     b->names.reset(new (std::nothrow) uint32_t[total]);
     b->counts.reset(new (std::nothrow) uint32_t[total]);
     if (!b->names || !b->counts) return fail(PTW_ENOMEM, "host allocation of batch results failed");
+    b->buf_cap = b->buf_touched = total;  // every entry is written below
     for (uint32_t i = 0; i < nq; ++i) {
         const WaveResult *w = src_w[i];
         if (!w) continue;
@@ -448,7 +501,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     const bool timing = std::getenv("PTW_TIMING") != nullptr;
     auto clk = [] { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
     const double t0 = timing ? (cudaStreamSynchronize(st), clk()) : 0.0;
-    double t1 = 0, t2 = 0;
+    double t1 = 0, t2 = 0, t_join = 0;
     Prefault prefault;  // joined before the copies (and on any early return)
     std::vector<uint8_t> dense_flags(nt, 0);
     if (h_dense) dense_flags.assign(h_dense, h_dense + nt);
@@ -531,13 +584,17 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             out->h_counts = base + n_out;
         } else if (out->pre_names && n_out <= out->pre_cap) {
             // the buffers faulted in during the walk hold the lists
+            const double tj = timing ? clk() : 0.0;
             out->pre_join();
+            if (timing) t_join = clk() - tj;
             out->names = std::move(out->pre_names);
             out->counts = std::move(out->pre_counts);
             out->h_names = out->names.get();
             out->h_counts = out->counts.get();
             release_tail(out->h_names, n_out * 4, out->pre_cap * 4);
             release_tail(out->h_counts, n_out * 4, out->pre_cap * 4);
+            out->cap = out->pre_cap;
+            out->touched = n_out;  // the tail's pages were handed back
         } else {
             if (out->pre_join) out->pre_join();
             out->pre_names.reset();
@@ -547,6 +604,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             if (!out->names || !out->counts) return fail(PTW_ENOMEM, "host allocation of batch results failed");
             out->h_names = out->names.get();
             out->h_counts = out->counts.get();
+            out->cap = out->touched = n_out;
             prefault.start({{out->h_names, n_out * 4}, {out->h_counts, n_out * 4}});
         }
         int name_bits = 1, q_bits = 1;
@@ -674,7 +732,9 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
                 PTW_CUDA(cudaGetLastError());
             }
         }
+        const double tj2 = timing ? clk() : 0.0;
         prefault.join();
+        if (timing) t_join += clk() - tj2;
         if (timing) {
             PTW_CUDA(cudaStreamSynchronize(st));
             t1 = clk();
@@ -685,8 +745,10 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
         if (timing) t2 = clk();
     }
     if (timing)
-        std::fprintf(stderr, "[ptw] compact %u tables (%zu dense), %llu entries: device %.1f ms, d2h %.1f ms\n", nt,
-                     (size_t)n_dense, (unsigned long long)n_ent, 1e3 * (t1 - t0), 1e3 * (t2 - t1));
+        std::fprintf(stderr,
+                     "[ptw] compact %u tables (%zu dense), %llu entries: device %.1f ms (waiting for host pages "
+                     "%.1f ms), d2h %.1f ms\n",
+                     nt, (size_t)n_dense, (unsigned long long)n_ent, 1e3 * (t1 - t0), 1e3 * t_join, 1e3 * (t2 - t1));
     return PTW_OK;
 }
 
@@ -720,7 +782,7 @@ using namespace ptw;
 
 extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t nq, const ptw_batch_cfg *cfg,
                              ptw_batch **out)
-{
+try {
     if (!g || !cfg || !out) return fail(PTW_EINVAL, "null argument");
     *out = nullptr;
     if (nq && !h_queries) return fail(PTW_EINVAL, "null query table");
@@ -815,35 +877,58 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
                      waves.size(), 1e3 * (t_waves - t_enter), 1e3 * (t_asm - t_waves), 1e3 * (clk() - t_enter));
     *out = b;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_batch_info(const ptw_batch *b, uint32_t *nq, uint64_t *entries, ptw_walk_stats *stats)
-{
+try {
     if (!b) return fail(PTW_EINVAL, "null batch");
     if (nq) *nq = b->nq;
     if (entries) *entries = b->offsets.empty() ? 0 : b->offsets.back();
     if (stats) *stats = b->stats;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_batch_export(const ptw_batch *b, uint64_t *h_offsets, uint32_t *h_names, uint32_t *h_counts)
-{
+try {
     if (!b) return fail(PTW_EINVAL, "null batch");
     const uint64_t n = b->offsets.empty() ? 0 : b->offsets.back();
     if (h_offsets) std::memcpy(h_offsets, b->offsets.data(), b->offsets.size() * 8);
     if (h_names && n) std::memcpy(h_names, b->names.get(), n * 4);
     if (h_counts && n) std::memcpy(h_counts, b->counts.get(), n * 4);
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_batch_view(const ptw_batch *b, const uint64_t **offsets, const uint32_t **names,
                               const uint32_t **counts)
-{
+try {
     if (!b) return fail(PTW_EINVAL, "null batch");
     if (offsets) *offsets = b->offsets.data();
     if (names) *names = b->names.get();
     if (counts) *counts = b->counts.get();
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
-extern "C" void ptw_batch_free(ptw_batch *b) { delete b; }
+extern "C" void ptw_batch_free(ptw_batch *b)
+try {
+    if (!b) return;
+    if (b->names && b->buf_cap) {
+        HostBufs hb;
+        hb.names = std::move(b->names);
+        hb.counts = std::move(b->counts);
+        hb.cap = b->buf_cap;
+        hb.touched = b->buf_touched;
+        host_cache_put(std::move(hb));
+    }
+    delete b;
+} catch (...) {
+    delete b;
+    host_exception();
+}

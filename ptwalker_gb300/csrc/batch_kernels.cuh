@@ -533,23 +533,46 @@ __global__ void __launch_bounds__(256, 4) k_tabs_place(const unsigned long long 
 
 // Top-k selection, threshold: the lowest bin thr[i] such that the entries in
 // bins >= thr[i] number at least k (0 = keep every entry when there are at
-// most k); sel[i] = how many entries that keeps.  One warp per table.
+// most k); sel[i] = how many entries that keeps.  One warp per table: lane l
+// sums the strip of 20 bins l-th from the top, a scan over the lanes finds
+// the strip where the running count from the top reaches k, and that lane
+// walks its strip down to the bin.
+constexpr uint32_t kThreshStrip = kCountBins / 32;
+static_assert(kCountBins % 32 == 0, "bins split into 32 strips");
+
 __global__ void k_tabs_thresh(const unsigned long long *cnt, const uint32_t *hist, uint32_t nt, uint32_t k,
                               uint32_t *thr, unsigned long long *sel)
 {
     const uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (i >= nt || (threadIdx.x & 31) != 0) return;
+    const uint32_t lane = threadIdx.x & 31;
+    if (i >= nt) return;  // whole warp leaves together
     if (cnt[i] <= k) {
-        thr[i] = 0;
-        sel[i] = cnt[i];
+        if (lane == 0) {
+            thr[i] = 0;
+            sel[i] = cnt[i];
+        }
         return;
     }
     const uint32_t *h = hist + (uint64_t)i * kCountBins;
-    unsigned long long acc = 0;
-    uint32_t b = kCountBins;
-    while (b > 0 && acc < k) acc += h[--b];
-    thr[i] = b > 0 ? b : 1;  // bin 0 is the empty count and never occupied
-    sel[i] = acc;
+    const uint32_t top = kCountBins - kThreshStrip * lane;  // strip [top - kThreshStrip, top)
+    unsigned long long strip = 0;
+    for (uint32_t b = top - kThreshStrip; b < top; ++b) strip += h[b];
+    unsigned long long inc = strip;  // entries in strips 0 .. lane (from the top)
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(kBFull, inc, o);
+        if (lane >= (uint32_t)o) inc += y;
+    }
+    // cnt[i] > k entries in all bins, so some lane's running count reaches k
+    // (lane 31, the bottom strip, otherwise: it ends at bin 1 with them all)
+    const unsigned reach = __ballot_sync(kBFull, inc >= k);
+    const uint32_t first = reach ? __ffs(reach) - 1 : 31u;
+    if (lane == first) {
+        unsigned long long acc = inc - strip;
+        uint32_t b = top;
+        while (b > top - kThreshStrip && acc < k) acc += h[--b];
+        thr[i] = b > 0 ? b : 1;  // bin 0 is the empty count and never occupied
+        sel[i] = acc;
+    }
 }
 
 // Hash entries j, sorted by name within their table t's range [hseg[t],

@@ -28,6 +28,19 @@ int fail(int code, const std::string &msg)
     return code;
 }
 
+int host_exception()
+{
+    try {
+        throw;
+    } catch (const std::bad_alloc &) {
+        return fail(PTW_ENOMEM, "host allocation failed");
+    } catch (const std::exception &e) {
+        return fail(PTW_EINVAL, std::string("host error: ") + e.what());
+    } catch (...) {
+        return fail(PTW_EINVAL, "unknown host error");
+    }
+}
+
 int cuda_fail(cudaError_t e, const char *what)
 {
     const int code = (e == cudaErrorMemoryAllocation) ? PTW_ENOMEM : PTW_ECUDA;
@@ -190,10 +203,12 @@ int read_edges(const char *path, int fmt, std::vector<uint32_t> &src, std::vecto
             cut[t] = std::max(c, cut[t - 1]);
         }
         std::vector<ParseChunk> parts(nt);
-        std::vector<std::thread> th;
-        for (unsigned t = 0; t < nt; ++t)
-            th.emplace_back(parse_range, data + cut[t], data + cut[t + 1], &parts[t]);
-        for (auto &x : th) x.join();
+        try {
+            parallel_for_threads(nt, [&](unsigned t) { parse_range(data + cut[t], data + cut[t + 1], &parts[t]); });
+        } catch (...) {
+            munmap(map, size);
+            throw;
+        }
         uint64_t line0 = 0, total = 0;
         for (unsigned t = 0; t < nt && rc == PTW_OK; ++t) {
             if (parts[t].bad_line) {
@@ -406,23 +421,28 @@ using namespace ptw;
 extern "C" const char *ptw_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" int ptw_trim_memory(void)
-{
+try {
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(e, "synchronise before trimming");
     trim_pools();
+    trim_host_cache();
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" const char *ptw_version(void) { return "ptwalker_gb300 0.1 (sm_103a)"; }
 
 extern "C" int ptw_graph_load(const char *path, int32_t fmt, int32_t as_undirected, ptw_graph **out)
-{
+try {
     if (!path || !out) return fail(PTW_EINVAL, "null argument");
     if (fmt != PTW_FMT_BINARY && fmt != PTW_FMT_TEXT) return fail(PTW_EINVAL, "unknown graph format");
     std::vector<uint32_t> src, dst;
     int rc = read_edges(path, fmt, src, dst);
     if (rc) return rc;
     return upload_and_build(src.data(), dst.data(), src.size(), as_undirected != 0, out);
+} catch (...) {
+    return host_exception();
 }
 
 namespace ptw {
@@ -445,7 +465,7 @@ inline char *put_u32(char *p, uint32_t x)
 }  // namespace ptw
 
 extern "C" int ptw_graph_save(const ptw_graph *g, const char *path, int32_t fmt)
-{
+try {
     if (!g || !path) return fail(PTW_EINVAL, "null argument");
     if (fmt != PTW_FMT_BINARY && fmt != PTW_FMT_TEXT) return fail(PTW_EINVAL, "unknown graph format");
     const uint64_t m = g->dg.m;
@@ -460,10 +480,9 @@ extern "C" int ptw_graph_save(const ptw_graph *g, const char *path, int32_t fmt)
     std::vector<std::string> buf(nt);
     bool ok = true;
     for (uint64_t r0 = 0; r0 < m && ok; r0 += chunk * nt) {
-        std::vector<std::thread> th;
-        for (unsigned t = 0; t < nt; ++t) {
-            const uint64_t lo = std::min(m, r0 + t * chunk), hi = std::min(m, lo + chunk);
-            th.emplace_back([&, t, lo, hi] {
+        try {
+            parallel_for_threads(nt, [&](unsigned t) {
+                const uint64_t lo = std::min(m, r0 + t * chunk), hi = std::min(m, lo + chunk);
                 std::string &b = buf[t];
                 if (fmt == PTW_FMT_BINARY) {
                     b.resize((hi - lo) * 8);
@@ -484,25 +503,31 @@ extern "C" int ptw_graph_save(const ptw_graph *g, const char *path, int32_t fmt)
                     b.resize(p - &b[0]);
                 }
             });
+        } catch (...) {
+            std::fclose(f);
+            throw;
         }
-        for (auto &x : th) x.join();
         for (unsigned t = 0; t < nt && ok; ++t)
             if (!buf[t].empty() && std::fwrite(buf[t].data(), 1, buf[t].size(), f) != buf[t].size()) ok = false;
     }
     if (std::fclose(f) != 0) ok = false;
     if (!ok) return fail(PTW_EIO, std::string("write failed: ") + path);
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_graph_from_edges(const uint32_t *h_src, const uint32_t *h_dst, uint64_t m,
                                     int32_t as_undirected, ptw_graph **out)
-{
+try {
     return upload_and_build(h_src, h_dst, m, as_undirected != 0, out);
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_graph_from_csr(const uint64_t *h_row_ptr, const uint32_t *h_col, uint32_t n,
                                   const uint32_t *h_names, ptw_graph **out)
-{
+try {
     if (!out) return fail(PTW_EINVAL, "null output handle");
     *out = nullptr;
     if (!h_row_ptr || n == 0) return fail(PTW_EINVAL, "CSR needs n >= 1 rows and a row_ptr array");
@@ -527,11 +552,13 @@ extern "C" int ptw_graph_from_csr(const uint64_t *h_row_ptr, const uint32_t *h_c
     }
     *out = g;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
                               uint64_t seed, int32_t clean, ptw_graph **out)
-{
+try {
     if (!out) return fail(PTW_EINVAL, "null output handle");
     *out = nullptr;
     if (scale < 1 || scale > 31) return fail(PTW_EINVAL, "scale must be in [1, 31]");
@@ -568,10 +595,12 @@ extern "C" int ptw_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, do
     }
     *out = g;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_graph_chung_lu(uint32_t n, double gamma, double mean_degree, uint64_t seed, ptw_graph **out)
-{
+try {
     if (!out) return fail(PTW_EINVAL, "null output handle");
     *out = nullptr;
     if (n < 2) return fail(PTW_EINVAL, "n must be >= 2");
@@ -602,36 +631,44 @@ extern "C" int ptw_graph_chung_lu(uint32_t n, double gamma, double mean_degree, 
     }
     *out = g;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" void ptw_graph_free(ptw_graph *g)
-{
+try {
     if (!g) return;
     cudaSetDevice(g->device);
     graph_release(g);
     delete g;
+} catch (...) {
+    host_exception();
 }
 
 extern "C" int ptw_graph_set_tune(ptw_graph *g, const ptw_tune *t)
-{
+try {
     if (!g || !t) return fail(PTW_EINVAL, "null argument");
     int rc = check_tune(*t);
     if (rc) return rc;
     g->tune = *t;
     drop_unused_columns(g);
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_graph_get_tune(const ptw_graph *g, ptw_tune *t)
-{
+try {
     if (!g || !t) return fail(PTW_EINVAL, "null argument");
     *t = g->tune;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_pagerank_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_counts,
                                 ptw_walk_stats *stats)
-{
+try {
     int rc = check_cfg(g, cfg, true);
     if (rc) return rc;
     if (!d_counts) return fail(PTW_EINVAL, "null counts buffer");
@@ -640,11 +677,13 @@ extern "C" int ptw_pagerank_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t 
     if (rc) return rc;
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
     return finish_stats(g, stats, cfg->n_walkers, true);
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_pagerank(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_counts,
                             ptw_walk_stats *stats)
-{
+try {
     int rc = check_cfg(g, cfg, true);
     if (rc) return rc;
     if (!h_counts) return fail(PTW_EINVAL, "null counts buffer");
@@ -657,11 +696,80 @@ extern "C" int ptw_pagerank(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_c
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
     PTW_CUDA(cudaStreamSynchronize(g->stream));
     return finish_stats(g, stats, cfg->n_walkers, true);
+} catch (...) {
+    return host_exception();
+}
+
+// Pipelined count walk: the walk of one call overlaps the copy of the
+// previous call's counts (copies run on a second stream).  Two calls may be
+// in flight; each has its own device by-name buffer.
+extern "C" int ptw_pagerank_submit(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_counts, uint64_t *ticket)
+try {
+    int rc = check_cfg(g, cfg, true);
+    if (rc) return rc;
+    if (!h_counts || !ticket) return fail(PTW_EINVAL, "null counts buffer or ticket");
+    PTW_CUDA(cudaSetDevice(g->device));
+    AsyncSlot *a = nullptr;
+    for (AsyncSlot &x : g->async)
+        if (x.ticket == 0 && (!a || x.by_name)) a = &x;  // prefer a slot already set up
+    if (!a) return fail(PTW_EBUSY, "two pipelined walks in flight: wait for one first");
+    if (!a->by_name) {
+        if (!g->copy_stream) PTW_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+        PTW_CUDA(device_malloc(&a->by_name, std::max<uint64_t>((uint64_t)g->dg.id_bound * 4, 4)));
+        PTW_CUDA(cudaHostAlloc(&a->h_moves, sizeof(unsigned long long), cudaHostAllocDefault));
+        PTW_CUDA(cudaEventCreate(&a->ev_start));
+        PTW_CUDA(cudaEventCreate(&a->ev_walk));
+        PTW_CUDA(cudaEventCreate(&a->ev_copy));
+    } else {
+        // the slot's previous copy (two calls back) must be done reading by_name
+        PTW_CUDA(cudaStreamWaitEvent(g->stream, a->ev_copy, 0));
+    }
+    PTW_CUDA(cudaEventRecord(a->ev_start, g->stream));
+    rc = run_count(g, cfg, a->by_name);
+    if (rc) return rc;
+    PTW_CUDA(cudaMemcpyAsync(a->h_moves, g->sc.ctrl + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             g->stream));
+    PTW_CUDA(cudaEventRecord(a->ev_walk, g->stream));
+    PTW_CUDA(cudaStreamWaitEvent(g->copy_stream, a->ev_walk, 0));
+    PTW_CUDA(cudaMemcpyAsync(h_counts, a->by_name, (uint64_t)g->dg.id_bound * 4, cudaMemcpyDeviceToHost,
+                             g->copy_stream));
+    PTW_CUDA(cudaEventRecord(a->ev_copy, g->copy_stream));
+    a->walkers = cfg->n_walkers;
+    a->ticket = g->next_ticket++;
+    *ticket = a->ticket;
+    return PTW_OK;
+} catch (...) {
+    return host_exception();
+}
+
+extern "C" int ptw_pagerank_wait(ptw_graph *g, uint64_t ticket, ptw_walk_stats *stats)
+try {
+    if (!g) return fail(PTW_EINVAL, "null graph");
+    AsyncSlot *a = nullptr;
+    for (AsyncSlot &x : g->async)
+        if (ticket != 0 && x.ticket == ticket) a = &x;
+    if (!a) return fail(PTW_EINVAL, "no pipelined walk in flight with ticket " + std::to_string(ticket));
+    PTW_CUDA(cudaSetDevice(g->device));
+    a->ticket = 0;  // the slot is free again whatever happens below
+    PTW_CUDA(cudaEventSynchronize(a->ev_copy));
+    if (stats) {
+        stats->walkers = a->walkers;
+        stats->moves = *a->h_moves;
+        stats->visits = a->walkers + *a->h_moves;
+        float ms = 0;
+        PTW_CUDA(cudaEventElapsedTime(&ms, a->ev_start, a->ev_walk));
+        stats->kernel_ms = ms;
+        PTW_CUDA(cudaEventElapsedTime(&ms, a->ev_start, a->ev_copy));
+        stats->total_ms = ms;
+    }
+    return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_rwr_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_pairs,
                            ptw_walk_stats *stats)
-{
+try {
     int rc = check_cfg(g, cfg, true);
     if (rc) return rc;
     if (!d_pairs && cfg->n_walkers) return fail(PTW_EINVAL, "null pairs buffer");
@@ -671,10 +779,12 @@ extern "C" int ptw_rwr_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_pa
     if (rc) return rc;
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
     return finish_stats(g, stats, cfg->n_walkers, false);
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_rwr(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_pairs, ptw_walk_stats *stats)
-{
+try {
     int rc = check_cfg(g, cfg, true);
     if (rc) return rc;
     if (!h_pairs && cfg->n_walkers) return fail(PTW_EINVAL, "null pairs buffer");
@@ -689,11 +799,13 @@ extern "C" int ptw_rwr(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_pairs,
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
     PTW_CUDA(cudaStreamSynchronize(g->stream));
     return finish_stats(g, stats, cfg->n_walkers, false);
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_deepwalk_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *d_paths,
                                 ptw_walk_stats *stats)
-{
+try {
     int rc = check_cfg(g, cfg, false);
     if (rc) return rc;
     if (!d_paths && cfg->n_walkers && L) return fail(PTW_EINVAL, "null paths buffer");
@@ -714,11 +826,13 @@ extern "C" int ptw_deepwalk_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t 
         stats->total_ms = ms;
     }
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_deepwalk(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *h_paths,
                             ptw_walk_stats *stats)
-{
+try {
     int rc = check_cfg(g, cfg, false);
     if (rc) return rc;
     if (!h_paths && cfg->n_walkers && L) return fail(PTW_EINVAL, "null paths buffer");
@@ -744,10 +858,12 @@ extern "C" int ptw_deepwalk(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, i
         stats->total_ms = ms;
     }
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tune *best)
-{
+try {
     if (!g) return fail(PTW_EINVAL, "null graph");
     if (!(sp > 0.0 && sp <= 1.0)) return fail(PTW_EINVAL, "sp must be in (0, 1]");
     PTW_CUDA(cudaSetDevice(g->device));
@@ -893,4 +1009,6 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
     drop_unused_columns(g);
     if (best) *best = bt;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }

@@ -358,6 +358,14 @@ void graph_release(ptw_graph *g)
     cudaFree(g->sc.out_stage);
     for (auto &e : g->ev)
         if (e) cudaEventDestroy(e);
+    if (g->copy_stream) cudaStreamSynchronize(g->copy_stream);
+    for (ptw::AsyncSlot &a : g->async) {
+        cudaFree(a.by_name);
+        cudaFreeHost(a.h_moves);
+        for (cudaEvent_t e : {a.ev_start, a.ev_walk, a.ev_copy})
+            if (e) cudaEventDestroy(e);
+    }
+    if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
     if (g->own_stream) cudaStreamSynchronize(g->own_stream);
     if (g->own_stream) cudaStreamDestroy(g->own_stream);
     delete[] g->h_names;
@@ -601,7 +609,7 @@ int build_graph_from_device_edges(ptw_graph *g, uint32_t *d_src, uint32_t *d_dst
 using namespace ptw;
 
 extern "C" int ptw_graph_get_info(const ptw_graph *g, ptw_graph_info *info)
-{
+try {
     if (!g || !info) return fail(PTW_EINVAL, "null argument");
     info->n_vertices = g->dg.n;
     info->id_bound = g->dg.id_bound;
@@ -610,11 +618,13 @@ extern "C" int ptw_graph_get_info(const ptw_graph *g, ptw_graph_info *info)
     info->reserved = 0;
     info->device_bytes = g->device_bytes;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_graph_export_csr(const ptw_graph *g, uint32_t *h_names, uint64_t *h_row_ptr,
                                     uint32_t *h_col)
-{
+try {
     if (!g) return fail(PTW_EINVAL, "null graph");
     const DeviceGraph &dg = g->dg;
     cudaStream_t st = g->stream;
@@ -645,10 +655,12 @@ extern "C" int ptw_graph_export_csr(const ptw_graph *g, uint32_t *h_names, uint6
     if (h_names) std::memcpy(h_names, g->h_names, (uint64_t)dg.n * 4);
     PTW_CUDA(cudaStreamSynchronize(st));
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_graph_export_edges(const ptw_graph *g, uint32_t *h_src, uint32_t *h_dst)
-{
+try {
     if (!g || !h_src || !h_dst) return fail(PTW_EINVAL, "null argument");
     const DeviceGraph &dg = g->dg;
     std::vector<uint64_t> rp(dg.n + 1);
@@ -658,17 +670,21 @@ extern "C" int ptw_graph_export_edges(const ptw_graph *g, uint32_t *h_src, uint3
         for (uint64_t e = rp[i]; e < rp[i + 1]; ++e) h_src[e] = g->h_names[i];
     for (uint64_t e = 0; e < dg.m; ++e) h_dst[e] = g->h_names[h_dst[e]];
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_graph_sync(ptw_graph *g)
-{
+try {
     if (!g) return fail(PTW_EINVAL, "null graph");
     PTW_CUDA(cudaStreamSynchronize(g->stream));
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_graph_set_stream(ptw_graph *g, void *cuda_stream)
-{
+try {
     if (!g) return fail(PTW_EINVAL, "null graph");
     cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : g->own_stream;
     if (s != g->stream) {
@@ -677,4 +693,6 @@ extern "C" int ptw_graph_set_stream(ptw_graph *g, void *cuda_stream)
     }
     g->stream = s;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }

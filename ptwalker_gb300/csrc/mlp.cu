@@ -266,7 +266,7 @@ int batch_grad(ptw_mlp *m, MlpScratch &s, uint32_t B, double *loss)
 using namespace ptw;
 
 extern "C" int ptw_source_features(ptw_graph *g, const uint32_t *h_sources, uint32_t ns, float *h_feat)
-{
+try {
     if (!g || (ns && (!h_sources || !h_feat))) return fail(PTW_EINVAL, "null argument");
     if (!ns) return PTW_OK;
     PTW_CUDA(cudaSetDevice(g->device));
@@ -299,10 +299,12 @@ extern "C" int ptw_source_features(ptw_graph *g, const uint32_t *h_sources, uint
     cudaFreeAsync(d_f, st);
     if (e != cudaSuccess) return cuda_fail(e, "source features");
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_mlp_create(uint64_t seed, ptw_mlp **out)
-{
+try {
     if (!out) return fail(PTW_EINVAL, "null argument");
     *out = nullptr;
     ptw_mlp *m = new (std::nothrow) ptw_mlp();
@@ -340,28 +342,34 @@ extern "C" int ptw_mlp_create(uint64_t seed, ptw_mlp **out)
     }
     *out = m;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_mlp_set_params(ptw_mlp *m, const float *h_params, const float *h_norm)
-{
+try {
     if (!m) return fail(PTW_EINVAL, "null model");
     PTW_CUDA(cudaSetDevice(m->device));
     if (h_params) PTW_CUDA(cudaMemcpy(m->params, h_params, PTW_MLP_NPARAMS * 4, cudaMemcpyHostToDevice));
     if (h_norm) std::memcpy(m->norm, h_norm, sizeof(m->norm));
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_mlp_get_params(const ptw_mlp *m, float *h_params, float *h_norm)
-{
+try {
     if (!m) return fail(PTW_EINVAL, "null model");
     PTW_CUDA(cudaSetDevice(m->device));
     if (h_params) PTW_CUDA(cudaMemcpy(h_params, m->params, PTW_MLP_NPARAMS * 4, cudaMemcpyDeviceToHost));
     if (h_norm) std::memcpy(h_norm, m->norm, sizeof(m->norm));
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_mlp_forward(ptw_mlp *m, const float *h_x, uint32_t B, float *h_y)
-{
+try {
     if (!m || (B && (!h_x || !h_y))) return fail(PTW_EINVAL, "null argument");
     if (!B) return PTW_OK;
     PTW_CUDA(cudaSetDevice(m->device));
@@ -376,11 +384,13 @@ extern "C" int ptw_mlp_forward(ptw_mlp *m, const float *h_x, uint32_t B, float *
     PTW_CUDA(cudaStreamSynchronize(m->stream));
     for (uint32_t b = 0; b < B; ++b) h_y[b] = y[b] * nm.tsd + nm.tmu;  // de-normalised prediction
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_mlp_grad(ptw_mlp *m, const float *h_x, const float *h_t, uint32_t B, double *h_loss,
                             float *h_grad)
-{
+try {
     if (!m || !B || !h_x || !h_t) return fail(PTW_EINVAL, "null argument or empty batch");
     PTW_CUDA(cudaSetDevice(m->device));
     MlpScratch s(m->stream);
@@ -392,11 +402,13 @@ extern "C" int ptw_mlp_grad(ptw_mlp *m, const float *h_x, const float *h_t, uint
     if (h_grad) PTW_CUDA(cudaMemcpyAsync(h_grad, m->grad, PTW_MLP_NPARAMS * 4, cudaMemcpyDeviceToHost, m->stream));
     PTW_CUDA(cudaStreamSynchronize(m->stream));
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_mlp_train(ptw_mlp *m, const float *h_x, const float *h_t, uint32_t N, uint32_t batch,
                              uint32_t epochs, float lr, uint64_t seed, float *h_loss_curve)
-{
+try {
     if (!m || !N || !h_x || !h_t || !batch) return fail(PTW_EINVAL, "null argument or empty data");
     PTW_CUDA(cudaSetDevice(m->device));
     // Normalisation from the training data (features and target).
@@ -472,10 +484,12 @@ extern "C" int ptw_mlp_train(ptw_mlp *m, const float *h_x, const float *h_t, uin
     cudaFreeAsync(d_idx, st);
     if (rc == PTW_OK) PTW_CUDA(cudaStreamSynchronize(st));
     return rc;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" void ptw_mlp_free(ptw_mlp *m)
-{
+try {
     if (!m) return;
     cudaSetDevice(m->device);
     if (m->stream) cudaStreamSynchronize(m->stream);
@@ -485,4 +499,6 @@ extern "C" void ptw_mlp_free(ptw_mlp *m)
     cudaFree(m->v);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
+} catch (...) {
+    host_exception();
 }

@@ -131,7 +131,7 @@ using namespace ptw;
 
 extern "C" int ptw_pagerank_noalloc(const ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_counts,
                                     void *cuda_stream)
-{
+try {
     if (!g || !cfg || !d_counts) return fail(PTW_EINVAL, "null argument");
     if (g->dg.n > PTW_NOALLOC_MAX_VERTICES)
         return fail(PTW_EINVAL, "graph has " + std::to_string(g->dg.n) +
@@ -178,4 +178,6 @@ extern "C" int ptw_pagerank_noalloc(const ptw_graph *g, const ptw_walk_cfg *cfg,
     k_scatter_noalloc<<<sgrid ? sgrid : 1, 256, 0, st>>>(s, g->dg.int2name, n, d_counts);
     PTW_CUDA(cudaGetLastError());
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }

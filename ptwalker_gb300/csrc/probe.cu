@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(256) k_probe_gather(const uint32_t *__restrict
 using namespace ptw;
 
 extern "C" int ptw_probe_gather(uint64_t array_bytes, uint32_t chains, double *loads_per_s)
-{
+try {
     if (!loads_per_s) return fail(PTW_EINVAL, "null output");
     *loads_per_s = 0.0;
     if (chains != 1 && chains != 2 && chains != 4 && chains != 8) return fail(PTW_EINVAL, "chains must be 1, 2, 4 or 8");
@@ -106,4 +106,6 @@ extern "C" int ptw_probe_gather(uint64_t array_bytes, uint32_t chains, double *l
     cudaFree(sink);
     cudaStreamDestroy(st);
     return rc;
+} catch (...) {
+    return host_exception();
 }

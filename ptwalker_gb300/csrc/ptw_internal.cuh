@@ -4,9 +4,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <exception>
 #include <functional>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/ptw.h"
@@ -22,6 +25,40 @@ namespace ptw {
 // Records msg as the calling thread's last error and returns code.
 int fail(int code, const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
+// Inside a catch block at the C ABI: records the host exception being
+// handled and returns its status (PTW_ENOMEM for an allocation failure).
+// No C++ exception crosses the ABI.
+int host_exception();
+
+// Runs fn(t) for t in [0, n) on n host threads.  An exception thrown on any
+// of them (or while starting them) is rethrown here after every started
+// thread has joined.
+template <class F>
+void parallel_for_threads(unsigned n, F fn)
+{
+    std::vector<std::thread> th;
+    std::exception_ptr err;
+    std::mutex mu;
+    auto keep = [&] {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!err) err = std::current_exception();
+    };
+    try {
+        th.reserve(n);
+        for (unsigned t = 0; t < n; ++t)
+            th.emplace_back([&, t] {
+                try {
+                    fn(t);
+                } catch (...) {
+                    keep();
+                }
+            });
+    } catch (...) {
+        keep();
+    }
+    for (std::thread &x : th) x.join();
+    if (err) std::rethrow_exception(err);
+}
 
 #define PTW_CUDA(call)                                   \
     do {                                                 \
@@ -142,6 +179,18 @@ struct Scratch {
     size_t out_stage_bytes = 0;
 };
 
+// One in-flight call of the pipelined count walk (ptw_pagerank_submit):
+// its counts by name on the device, its moves in page-locked host memory,
+// and events for the start, the end of the walk (moves copied) and the end
+// of the copy to the caller's buffer.
+struct AsyncSlot {
+    uint32_t *by_name = nullptr;            // [id_bound]
+    unsigned long long *h_moves = nullptr;  // page-locked
+    cudaEvent_t ev_start = nullptr, ev_walk = nullptr, ev_copy = nullptr;
+    uint64_t ticket = 0;                    // 0 = free
+    uint64_t walkers = 0;
+};
+
 }  // namespace ptw
 
 struct ptw_graph {
@@ -157,6 +206,9 @@ struct ptw_graph {
     ptw_tune tune{};
     uint64_t device_bytes = 0;
     int ext_users = 0;  // open servers reading the extended columns (kept while > 0)
+    ptw::AsyncSlot async[2];             // pipelined count walks in flight
+    cudaStream_t copy_stream = nullptr;  // their copies to the host
+    uint64_t next_ticket = 1;
 };
 
 namespace ptw {
@@ -238,8 +290,22 @@ struct Compacted {
     // that); adopted when the lists fit, the unused tail handed back.
     std::unique_ptr<uint32_t[]> pre_names, pre_counts;
     uint64_t pre_cap = 0;
+    uint64_t pre_touched = 0;  // leading entries of pre_* already faulted in before this call
     std::function<void()> pre_join;
+    // Capacity of names / counts in entries, and how many leading entries
+    // are faulted in (a freed batch hands them to the host cache).
+    uint64_t cap = 0, touched = 0;
 };
+// Host result buffers of the last freed batch, kept faulted in so that the
+// next batch's copies land in touched pages (batch.cu).  take() hands them
+// over when they hold at least `need` entries; trim_host_cache() frees them.
+struct HostBufs {
+    std::unique_ptr<uint32_t[]> names, counts;
+    uint64_t cap = 0, touched = 0;
+};
+bool host_cache_take(uint64_t need, HostBufs &out);
+void host_cache_put(HostBufs &&b);
+void trim_host_cache();
 // Compacts nt count tables into *out (batch.cu).  Table i starts at slot
 // h_base[i] of d_slots, an even slot (16-byte aligned; callers use 128-byte
 // lines); a hash table (h_dense[i] == 0, or h_dense NULL) has h_cap[i]

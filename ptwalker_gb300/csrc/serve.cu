@@ -291,7 +291,7 @@ int collect(ptw_server *s, const std::vector<size_t> &fin)
 using namespace ptw;
 
 extern "C" int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server **out)
-{
+try {
     if (!g || !cfg || !out) return fail(PTW_EINVAL, "null argument");
     *out = nullptr;
     if (!(cfg->sp >= 0.0 && cfg->sp <= 1.0)) return fail(PTW_EINVAL, "sp must be in [0, 1]");
@@ -376,10 +376,12 @@ extern "C" int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server
     }
     *out = s;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_serve_submit(ptw_server *s, const ptw_query *q)
-{
+try {
     if (!s || !q) return fail(PTW_EINVAL, "null argument");
     if (q->budget < 1 || q->budget > (1ull << 28)) return fail(PTW_EINVAL, "budget must be in [1, 2^28]");
     const uint32_t n = s->g->dg.n;
@@ -393,10 +395,12 @@ extern "C" int ptw_serve_submit(ptw_server *s, const ptw_query *q)
     pd.full = false;
     s->pending.push_back(pd);
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_active, uint32_t *n_pending)
-{
+try {
     if (!s) return fail(PTW_EINVAL, "null server");
     PTW_CUDA(cudaSetDevice(s->g->device));
     const double t_enter = now_s(s);
@@ -524,18 +528,22 @@ extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_activ
     if (n_active) *n_active = (uint32_t)s->active.size();
     if (n_pending) *n_pending = (uint32_t)s->pending.size();
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_serve_poll(ptw_server *s, ptw_serve_result *r)
-{
+try {
     if (!s || !r) return fail(PTW_EINVAL, "null argument");
     if (s->done.empty()) return 0;
     *r = s->done.front().r;
     return 1;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_serve_take(ptw_server *s, uint32_t *h_names, uint32_t *h_counts)
-{
+try {
     if (!s) return fail(PTW_EINVAL, "null server");
     if (s->done.empty()) return fail(PTW_EINVAL, "no completed result");
     Done &d = s->done.front();
@@ -544,19 +552,23 @@ extern "C" int ptw_serve_take(ptw_server *s, uint32_t *h_names, uint32_t *h_coun
     if (h_counts && ne) std::memcpy(h_counts, d.counts, ne * 4);
     s->done.pop_front();
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_serve_view(const ptw_server *s, const uint32_t **names, const uint32_t **counts)
-{
+try {
     if (!s || !names || !counts) return fail(PTW_EINVAL, "null argument");
     if (s->done.empty()) return fail(PTW_EINVAL, "no completed result");
     *names = s->done.front().names;
     *counts = s->done.front().counts;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" int ptw_serve_get_stats(const ptw_server *s, ptw_serve_stats *out)
-{
+try {
     if (!s || !out) return fail(PTW_EINVAL, "null argument");
     *out = s->st;
     out->active = (uint32_t)s->active.size();
@@ -564,12 +576,14 @@ extern "C" int ptw_serve_get_stats(const ptw_server *s, ptw_serve_stats *out)
     out->pinned_bytes = 0;
     for (const auto &b : s->pinned) out->pinned_bytes += b->words * 4;
     return PTW_OK;
+} catch (...) {
+    return host_exception();
 }
 
 extern "C" double ptw_serve_clock(const ptw_server *s) { return s ? now_s(s) : 0.0; }
 
 extern "C" void ptw_serve_close(ptw_server *s)
-{
+try {
     if (!s) return;
     cudaSetDevice(s->g->device);
     cudaStreamSynchronize(s->g->stream);
@@ -584,4 +598,6 @@ extern "C" void ptw_serve_close(ptw_server *s)
     cudaFree(s->d_plan);
     if (s->h_plan) cudaFreeHost(s->h_plan);
     delete s;
+} catch (...) {
+    host_exception();
 }

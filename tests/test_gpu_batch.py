@@ -55,6 +55,36 @@ def test_batch_bit_exact_per_query(gpu, G16, s16_canon, app):
         assert res.moves == tot_moves
 
 
+def test_reused_host_result_buffers(gpu, G16, s16_canon):
+    """Batches large enough for host result buffers sized before the walk
+    (8 M entries and up): a freed batch's buffers are reused by the next
+    batch, whose lists must still equal the replay, and results still held
+    are not touched by later batches."""
+    rng = np.random.default_rng(17)
+    nq = 200  # about 11 M entries estimated: above the 8 M of the sized-before-the-walk path
+    sources = rng.integers(0, G16.n, nq)
+    budgets = np.full(nq, 60000)
+    first = gpu.ppr_batch(G16, sources, budgets, sp=0.2, seed=3)
+    keep = [first.query(i) for i in (0, 1)]
+    kept = [(a.copy(), b.copy()) for a, b in keep]
+    first.close()                                   # buffers go to the host cache
+    second = gpu.ppr_batch(G16, sources, budgets, sp=0.2, seed=4)   # reuses them
+    held = gpu.ppr_batch(G16, sources[:40], budgets[:40], sp=0.2, seed=5)
+    for i in (0, 57, nq - 1):
+        want = replay_query(s16_canon, int(sources[i]), i, int(budgets[i]), 0.2, 4, "visits")
+        assert sparse_equal(second, i, want), i
+    second.close()
+    third = gpu.ppr_batch(G16, sources, budgets, sp=0.2, seed=3)    # same as the first
+    for i in (0, 1):
+        names, counts = third.query(i)
+        assert np.array_equal(names, kept[i][0]) and np.array_equal(counts, kept[i][1])
+    want = replay_query(s16_canon, int(sources[7]), 7, int(budgets[7]), 0.2, 5, "visits")
+    assert sparse_equal(held, 7, want)
+    third.close()
+    held.close()
+    gpu.trim_memory()
+
+
 def test_query_alone_equals_query_in_batch_and_across_waves(gpu, G16):
     sources = [3, 77, 77, 1024, 46000]
     budgets = [5000, 3000, 3000, 7000, 100]

@@ -223,6 +223,41 @@ def test_device_outputs_equal_host_outputs(gpu, G16):
     assert np.array_equal(paths.cpu().numpy(), gpu.deepwalk(G16, 1000, 40, 8))
 
 
+def test_pipelined_pagerank_equals_synchronous_calls(gpu, G16):
+    """ptw_pagerank_submit / ptw_pagerank_wait with two calls in flight: every
+    call's counts and moves equal ptw_pagerank's for the same configuration,
+    whatever overlaps it; a third call in flight and unknown tickets are
+    refused."""
+    import torch
+    W = G16.n
+    bufs = [torch.empty(G16.id_bound, dtype=torch.int32, pin_memory=True) for _ in range(2)]
+    want = {}
+    for seed in range(5):
+        want[seed] = gpu.pagerank(G16, W, 0.15, 100 + seed, stats=True)
+    pend = []
+    for seed in range(5):
+        if len(pend) == 2:
+            s0, t0 = pend.pop(0)
+            st = gpu.pagerank_wait(G16, t0)
+            assert np.array_equal(bufs[s0 % 2].numpy().view(np.uint32), want[s0][0])
+            assert st.moves == want[s0][1].moves and st.walkers == W
+        pend.append((seed, gpu.pagerank_submit(G16, bufs[seed % 2], W, 0.15, 100 + seed)))
+    extra = np.empty(G16.id_bound, dtype=np.uint32)
+    with pytest.raises(gpu.PTWError, match="PTW_EBUSY"):
+        gpu.pagerank_submit(G16, extra, W, 0.15, 7)
+    for s0, t0 in pend:
+        st = gpu.pagerank_wait(G16, t0)
+        assert np.array_equal(bufs[s0 % 2].numpy().view(np.uint32), want[s0][0])
+        assert st.moves == want[s0][1].moves
+    with pytest.raises(gpu.PTWError, match="PTW_EINVAL"):
+        gpu.pagerank_wait(G16, pend[0][1])  # already waited for
+    # a synchronous call between pipelined ones does not disturb them
+    t = gpu.pagerank_submit(G16, extra, W, 0.15, 100)
+    mid = gpu.pagerank(G16, W, 0.15, 101)
+    gpu.pagerank_wait(G16, t)
+    assert np.array_equal(extra, want[0][0]) and np.array_equal(mid, want[1][0])
+
+
 def test_zero_walkers_and_bad_args(gpu, G16):
     z = gpu.pagerank(G16, 0, 0.15, 1)
     assert z.sum() == 0
