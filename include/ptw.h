@@ -276,6 +276,9 @@ int ptw_batch_export(const ptw_batch *b, uint64_t *h_offsets, uint32_t *h_names,
  * valid until ptw_batch_free. */
 int ptw_batch_view(const ptw_batch *b, const uint64_t **offsets, const uint32_t **names,
                    const uint32_t **counts);
+/* Frees a batch.  Its host result arrays (when large) are kept, already
+ * faulted in, for the next batch's results (one pair, up to 32 GB);
+ * ptw_trim_memory hands them back. */
 void ptw_batch_free(ptw_batch *b);
 
 /* FP64 oracle on the device: for each source name, the exact expected count
