@@ -292,8 +292,8 @@ __device__ __forceinline__ Chunk block_chunk(const unsigned long long *slots, co
     return c;
 }
 
-// Word j of the lane: chunk word w = warp * 256 + j * 32 + lane (coalesced
-// per j), entries w * EPV .. w * EPV + EPV - 1 of the chunk.
+// Word j of the lane: chunk word w = warp * 32 * kLaneVecs + j * 32 + lane
+// (coalesced per j), entries w * EPV .. w * EPV + EPV - 1 of the chunk.
 template <int EPV>
 __device__ __forceinline__ void load_chunk(const Chunk &c, uint4 (&v)[kLaneVecs])
 {
