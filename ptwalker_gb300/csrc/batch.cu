@@ -333,6 +333,7 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     const bool ext = (g->tune.ext_columns & 1) && ensure_ext_columns(g);
     a.col_ext = g->dg.col_ext;
     a.int2idx = g->dg.int2idx;
+    a.ext_idx = g->dg.id_bound == g->dg.n ? 1u : 0u;  // names 0..n-1
     a.desc = d_desc;
     a.q_src = d_src;
     a.q_qid = d_qid;

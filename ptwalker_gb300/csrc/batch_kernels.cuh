@@ -53,12 +53,12 @@ __device__ __forceinline__ void tab_add(unsigned long long *slots, uint32_t mask
 }
 
 // Adds inc to the count of internal vertex v: in a dense array (mask ==
-// kDenseMask) one fire-and-forget reduction at its canonical index, else a
-// hash-table insert.
-__device__ __forceinline__ void count_add(unsigned long long *tab, uint32_t mask, uint32_t v, uint32_t inc,
-                                          uint32_t *flag, const uint32_t *__restrict__ int2idx)
+// kDenseMask) one fire-and-forget reduction at v's canonical index idx,
+// else a hash-table insert of v.
+__device__ __forceinline__ void count_add(unsigned long long *tab, uint32_t mask, uint32_t v, uint32_t idx,
+                                          uint32_t inc, uint32_t *flag)
 {
-    if (mask == kDenseMask) atomicAdd(reinterpret_cast<uint32_t *>(tab) + __ldg(&int2idx[v]), inc);
+    if (mask == kDenseMask) atomicAdd(reinterpret_cast<uint32_t *>(tab) + idx, inc);
     else tab_add(tab, mask, v, inc, flag);
 }
 
@@ -75,6 +75,7 @@ struct BatchArgs {
     const uint32_t *__restrict__ col;
     const uint4 *__restrict__ col_ext;     // EXT: {id, first column, degree, name} per entry
     const uint32_t *__restrict__ int2idx;  // internal id -> canonical index (dense tables)
+    uint32_t ext_idx;  // 1: names are 0..n-1, so an extended column's name is the canonical index
     const uint3 *__restrict__ desc;  // [ndesc] {entry, first rank, count}
     const uint32_t *__restrict__ q_src;
     const uint32_t *__restrict__ q_qid;
@@ -94,17 +95,17 @@ constexpr uint32_t kDescWalkers = 256;
 
 constexpr int kBatchIlp = 2;
 
-// Counts one visit of key v in query entry q's table, aggregated over the
-// lanes of the warp that visit the same (query, vertex) now.
-__device__ __forceinline__ void visit_agg(unsigned mask_active, bool on, uint32_t q, uint32_t v,
-                                          unsigned long long *tab, uint32_t tmask, uint32_t *flag, uint32_t lane,
-                                          const uint32_t *__restrict__ int2idx)
+// Counts one visit of key v (canonical index idx, used by dense tables) in
+// query entry q's table, aggregated over the lanes of the warp that visit
+// the same (query, vertex) now.
+__device__ __forceinline__ void visit_agg(unsigned mask_active, bool on, uint32_t q, uint32_t v, uint32_t idx,
+                                          unsigned long long *tab, uint32_t tmask, uint32_t *flag, uint32_t lane)
 {
     const unsigned m = __ballot_sync(mask_active, on);
     if (!on) return;
     const unsigned long long key = ((unsigned long long)q << 32) | v;
     const unsigned grp = __match_any_sync(m, key);
-    if ((grp & ((1u << lane) - 1u)) == 0) count_add(tab, tmask, v, __popc(grp), flag, int2idx);
+    if ((grp & ((1u << lane) - 1u)) == 0) count_add(tab, tmask, v, idx, __popc(grp), flag);
 }
 
 // EXT: moves read the extended column copy and keep the row record of the
@@ -175,7 +176,8 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
             }
             if (a.app == PTW_APP_VISITS) {
                 // Start visits: one table update per (warp, query) group.
-                visit_agg(kBFull, got, q[k], v[k], tab[k], mask[k], &a.q_flag[q[k]], lane, a.int2idx);
+                const uint32_t sidx = got && mask[k] == kDenseMask ? __ldg(&a.int2idx[v[k]]) : 0u;
+                visit_agg(kBFull, got, q[k], v[k], sidx, tab[k], mask[k], &a.q_flag[q[k]], lane);
             }
         }
         bool any = false;
@@ -190,21 +192,30 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
 #pragma unroll
         for (int k = 0; k < kBatchIlp; ++k)
             if (act[k]) r[k] = philox(make_uint4(j[k], qid[k], step[k], PTW_TAG_WALK), a.key0, a.key1);
-        uint32_t nb[kBatchIlp];
+        uint32_t nb[kBatchIlp], nidx[kBatchIlp];
         uint2 nrec[kBatchIlp];
 #pragma unroll
         for (int k = 0; k < kBatchIlp; ++k) {
+            nidx[k] = 0;
             if (act[k] && rec[k].y != 0) {
                 const uint32_t e = rec[k].x + __umulhi(r[k].x, rec[k].y);
                 if (EXT) {
                     const uint4 x = __ldg(&a.col_ext[e]);
                     nb[k] = x.x;
                     nrec[k] = make_uint2(x.y, x.z);
+                    nidx[k] = x.w;  // the neighbour's name: its canonical index when a.ext_idx
                 } else {
                     nb[k] = __ldg(&a.col[e]);
                 }
             }
         }
+        // Canonical indices of the new vertices for dense tables, every
+        // slot's load issued before any table update waits on one (with
+        // a.ext_idx the gathered column entry already holds it).
+#pragma unroll
+        for (int k = 0; k < kBatchIlp; ++k)
+            if (act[k] && rec[k].y != 0 && mask[k] == kDenseMask && !(EXT && a.ext_idx))
+                nidx[k] = __ldg(&a.int2idx[nb[k]]);
 #pragma unroll
         for (int k = 0; k < kBatchIlp; ++k) {
             // every lane runs the aggregation calls (warp-collective)
@@ -219,10 +230,14 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
                 ++moves;
             }
             if (a.app == PTW_APP_VISITS)
-                visit_agg(kBFull, moved, q[k], v[k], tab[k], mask[k], &a.q_flag[q[k]], lane, a.int2idx);
+                visit_agg(kBFull, moved, q[k], v[k], nidx[k], tab[k], mask[k], &a.q_flag[q[k]], lane);
             const bool done = act[k] && (!moved || (uint64_t)r[k].y < a.thr || (a.max_moves && step[k] >= a.max_moves));
-            if (a.app == PTW_APP_ENDPOINT)
-                visit_agg(kBFull, done, q[k], v[k], tab[k], mask[k], &a.q_flag[q[k]], lane, a.int2idx);
+            if (a.app == PTW_APP_ENDPOINT) {
+                // a walker stuck at its start (no out-edge) ends where it began
+                const uint32_t eidx =
+                    moved ? nidx[k] : done && mask[k] == kDenseMask ? __ldg(&a.int2idx[v[k]]) : 0u;
+                visit_agg(kBFull, done, q[k], v[k], eidx, tab[k], mask[k], &a.q_flag[q[k]], lane);
+            }
             if (done) act[k] = false;
         }
     }

@@ -338,6 +338,7 @@ try {
         a.adj = g->dg.adj;
         a.col = g->dg.col;
         a.int2idx = g->dg.int2idx;
+        a.ext_idx = g->dg.id_bound == g->dg.n ? 1u : 0u;  // names 0..n-1
         a.desc = dv.desc;
         a.q_src = dv.src;
         a.q_qid = dv.qid;
