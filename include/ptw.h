@@ -277,8 +277,10 @@ int ptw_batch_export(const ptw_batch *b, uint64_t *h_offsets, uint32_t *h_names,
 int ptw_batch_view(const ptw_batch *b, const uint64_t **offsets, const uint32_t **names,
                    const uint32_t **counts);
 /* Frees a batch.  Its host result arrays (when large) are kept, already
- * faulted in, for the next batch's results (one pair, up to 32 GB);
- * ptw_trim_memory hands them back. */
+ * faulted in and page-locked, for the next batch's results (one pair, up
+ * to 32 GB); ptw_trim_memory hands them back.  Large result arrays are
+ * page-locked while the device walks (within a quarter of the host memory
+ * for all of them), so their copies from the device run at a steady rate. */
 void ptw_batch_free(ptw_batch *b);
 
 /* FP64 oracle on the device: for each source name, the exact expected count

@@ -33,6 +33,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -46,8 +47,9 @@ struct ptw_batch {
     uint32_t nq = 0;
     std::vector<ptw_query> queries;
     std::vector<uint64_t> offsets;  // [nq + 1]
-    std::unique_ptr<uint32_t[]> names, counts;
+    ptw::HostArray names, counts;
     uint64_t buf_cap = 0, buf_touched = 0;  // entries allocated / faulted in
+    bool buf_pinned = false;                // page-locked
     ptw_walk_stats stats{};
     uint32_t top_k = 0;  // results hold each query's top_k largest counts only
 };
@@ -73,52 +75,137 @@ constexpr uint64_t kMaxBudget = 1ull << 28;
 // device-to-host copy into pages the process has never touched takes the
 // faults one by one inside the copy (about 6x slower than the copy itself
 // for gigabytes); touching one byte per page first, while the device is
-// still busy, leaves the copy at link speed.
+// still busy, leaves the copy at link speed.  With pin, the buffers are
+// then registered with CUDA (page-locked): copies into pageable pages that
+// had been faulted in still took 2-3.6x longer in about one call in three,
+// copies into registered pages did not.  One coordinator thread runs the
+// touching threads and the registration, so both overlap the walk.
 class Prefault {
 public:
-    void start(std::initializer_list<std::pair<void *, size_t>> bufs)
+    void start(std::initializer_list<std::pair<void *, size_t>> bufs, bool pin = false)
     {
-        const long pg = sysconf(_SC_PAGESIZE);
-        const size_t page = pg > 0 ? (size_t)pg : 4096;
         size_t total = 0;
         for (auto &b : bufs) total += b.second;
         if (total < (64u << 20)) return;  // small: the copy absorbs it
-        const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-        for (auto &b : bufs) {
-            char *p = (char *)b.first;
-            const size_t len = b.second;
-            for (unsigned t = 0; t < nt; ++t) {
-                const size_t lo = len * t / nt, hi = len * (t + 1) / nt;
-                th_.emplace_back([p, lo, hi, page] {
+        std::vector<std::pair<void *, size_t>> v(bufs);
+        pinned_.assign(v.size(), false);
+        coord_ = std::thread([this, v, pin] {
+            const long pg = sysconf(_SC_PAGESIZE);
+            const size_t page = pg > 0 ? (size_t)pg : 4096;
+            const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+            try {
+                parallel_for_threads(nt * (unsigned)v.size(), [&](unsigned i) {
+                    char *p = (char *)v[i / nt].first;
+                    const size_t len = v[i / nt].second, t = i % nt;
+                    const size_t lo = len * t / nt, hi = len * (t + 1) / nt;
                     for (size_t x = lo - lo % page; x < hi; x += page)
                         if (x >= lo) ((volatile char *)p)[x] = 0;
                 });
+            } catch (...) {
+                return;  // pages not touched yet fault in during the copy
             }
-        }
+            if (pin)
+                for (size_t b = 0; b < v.size(); ++b) pinned_[b] = host_pin((uint32_t *)v[b].first, v[b].second);
+        });
     }
     void join()
     {
-        for (auto &t : th_) t.join();
-        th_.clear();
+        if (coord_.joinable()) coord_.join();
+    }
+    // Whether every buffer was registered (valid after join).
+    bool pinned() const
+    {
+        if (pinned_.empty()) return false;
+        for (bool b : pinned_)
+            if (!b) return false;
+        return true;
     }
     ~Prefault() { join(); }
 
 private:
-    std::vector<std::thread> th_;
+    std::thread coord_;
+    std::vector<bool> pinned_;
 };
 
-std::mutex g_host_mu;
-HostBufs g_host_cache;
+// Page-locked host arrays (base pointer -> bytes) and the host cache live
+// in objects that are never destroyed: nothing of theirs runs at exit,
+// when the CUDA runtime may already be gone.
+struct PinRegistry {
+    std::mutex mu;
+    std::map<const void *, uint64_t> arrays;
+    uint64_t bytes = 0;
+};
+PinRegistry &pins()
+{
+    static PinRegistry *r = new PinRegistry;
+    return *r;
+}
+
+uint64_t pin_limit()
+{
+    const long pages = sysconf(_SC_PHYS_PAGES), pg = sysconf(_SC_PAGESIZE);
+    return pages > 0 && pg > 0 ? (uint64_t)pages * (uint64_t)pg / 4 : 0;
+}
+
+struct HostCache {
+    std::mutex mu;
+    HostBufs bufs;
+};
+HostCache &host_cache()
+{
+    static HostCache *c = new HostCache;
+    return *c;
+}
 constexpr uint64_t kHostCacheMaxBytes = 32ull << 30;
 
 }  // namespace
 
+bool host_pin(uint32_t *p, uint64_t bytes)
+{
+    if (!p || !bytes) return false;
+    PinRegistry &r = pins();
+    {
+        std::lock_guard<std::mutex> lk(r.mu);
+        if (r.arrays.count(p) || r.bytes + bytes > pin_limit()) return false;
+        r.bytes += bytes;  // reserved while registering
+    }
+    // portable: the registering thread's current device need not be the graph's
+    const bool ok = cudaHostRegister(p, bytes, cudaHostRegisterPortable) == cudaSuccess;
+    std::lock_guard<std::mutex> lk(r.mu);
+    if (ok) {
+        r.arrays[p] = bytes;
+    } else {
+        cudaGetLastError();
+        r.bytes -= bytes;
+    }
+    return ok;
+}
+
+void HostArrayDelete::operator()(uint32_t *p) const
+{
+    if (!p) return;
+    PinRegistry &r = pins();
+    bool was = false;
+    {
+        std::lock_guard<std::mutex> lk(r.mu);
+        auto it = r.arrays.find(p);
+        if (it != r.arrays.end()) {
+            r.bytes -= it->second;
+            r.arrays.erase(it);
+            was = true;
+        }
+    }
+    if (was && cudaHostUnregister(p) != cudaSuccess) cudaGetLastError();
+    delete[] p;
+}
+
 bool host_cache_take(uint64_t need, HostBufs &out)
 {
-    std::lock_guard<std::mutex> lk(g_host_mu);
-    if (!g_host_cache.names || g_host_cache.cap < need) return false;
-    out = std::move(g_host_cache);
-    g_host_cache = HostBufs();
+    HostCache &c = host_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (!c.bufs.names || c.bufs.cap < need) return false;
+    out = std::move(c.bufs);
+    c.bufs = HostBufs();
     return true;
 }
 
@@ -126,20 +213,22 @@ void host_cache_put(HostBufs &&b)
 {
     if (!b.names || !b.counts || b.cap * 8 > kHostCacheMaxBytes) return;
     HostBufs old;
+    HostCache &c = host_cache();
     {
-        std::lock_guard<std::mutex> lk(g_host_mu);
-        if (g_host_cache.names && g_host_cache.cap > b.cap) return;  // keep the larger pair
-        old = std::move(g_host_cache);
-        g_host_cache = std::move(b);
+        std::lock_guard<std::mutex> lk(c.mu);
+        if (c.bufs.names && c.bufs.cap > b.cap) return;  // keep the larger pair
+        old = std::move(c.bufs);
+        c.bufs = std::move(b);
     }
 }  // the replaced pair is freed outside the lock
 
 void trim_host_cache()
 {
     HostBufs old;
-    std::lock_guard<std::mutex> lk(g_host_mu);
-    old = std::move(g_host_cache);
-    g_host_cache = HostBufs();
+    HostCache &c = host_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    old = std::move(c.bufs);
+    c.bufs = HostBufs();
 }
 
 namespace {
@@ -367,24 +456,37 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
             est += std::min<uint64_t>(g->dg.n, (uint64_t)(1.5 * (double)wq[i].budget) + 64);
         if (est * 8 >= (64ull << 20)) {
             HostBufs hb;
+            bool fresh = false;
             if (host_cache_take(est, hb)) {
                 // a freed batch's buffers: only the part never faulted in needs it
                 wr.c.pre_names = std::move(hb.names);
                 wr.c.pre_counts = std::move(hb.counts);
                 wr.c.pre_cap = hb.cap;
                 wr.c.pre_touched = std::min(hb.touched, est);
+                wr.c.pre_pinned = hb.pinned;
             } else {
                 wr.c.pre_names.reset(new (std::nothrow) uint32_t[est]);
                 wr.c.pre_counts.reset(new (std::nothrow) uint32_t[est]);
                 wr.c.pre_cap = est;
                 wr.c.pre_touched = 0;
+                wr.c.pre_pinned = false;
+                fresh = true;
             }
             if (wr.c.pre_names && wr.c.pre_counts) {
                 const uint64_t t0 = wr.c.pre_touched;
-                if (t0 < est)
-                    early.start({{wr.c.pre_names.get() + t0, (est - t0) * 4},
-                                 {wr.c.pre_counts.get() + t0, (est - t0) * 4}});
-                wr.c.pre_join = [&early] { early.join(); };
+                if (fresh) {
+                    // touch, then register the whole arrays, while the device walks
+                    early.start({{wr.c.pre_names.get(), est * 4}, {wr.c.pre_counts.get(), est * 4}}, true);
+                    wr.c.pre_join = [&early, &wr] {
+                        early.join();
+                        wr.c.pre_pinned = early.pinned();
+                    };
+                } else {
+                    if (t0 < est)
+                        early.start({{wr.c.pre_names.get() + t0, (est - t0) * 4},
+                                     {wr.c.pre_counts.get() + t0, (est - t0) * 4}});
+                    wr.c.pre_join = [&early] { early.join(); };
+                }
             } else {
                 wr.c.pre_names.reset();
                 wr.c.pre_counts.reset();
@@ -460,6 +562,7 @@ int assemble(ptw_batch *b, std::vector<WaveResult> &waves)
         b->counts = std::move(waves[0].c.counts);
         b->buf_cap = waves[0].c.cap;
         b->buf_touched = waves[0].c.touched;
+        b->buf_pinned = waves[0].c.pinned;
         return PTW_OK;
     }
     if (!total) return PTW_OK;
@@ -592,10 +695,15 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             out->counts = std::move(out->pre_counts);
             out->h_names = out->names.get();
             out->h_counts = out->counts.get();
-            release_tail(out->h_names, n_out * 4, out->pre_cap * 4);
-            release_tail(out->h_counts, n_out * 4, out->pre_cap * 4);
             out->cap = out->pre_cap;
-            out->touched = n_out;  // the tail's pages were handed back
+            out->pinned = out->pre_pinned;
+            if (out->pinned) {
+                out->touched = out->pre_cap;  // registered pages stay resident
+            } else {
+                release_tail(out->h_names, n_out * 4, out->pre_cap * 4);
+                release_tail(out->h_counts, n_out * 4, out->pre_cap * 4);
+                out->touched = n_out;  // the tail's pages were handed back
+            }
         } else {
             if (out->pre_join) out->pre_join();
             out->pre_names.reset();
@@ -926,6 +1034,7 @@ try {
         hb.counts = std::move(b->counts);
         hb.cap = b->buf_cap;
         hb.touched = b->buf_touched;
+        hb.pinned = b->buf_pinned;
         host_cache_put(std::move(hb));
     }
     delete b;

@@ -278,30 +278,44 @@ uint32_t batch_top_k(const ptw_batch *b);
 // h_names / h_counts point at wherever they landed.  top_k > 0 keeps the
 // top_k largest counts of every table instead, ordered by count descending
 // and then by name (seg then delimits the kept entries).
+// Host result array (new[]); page-locked with CUDA when host_pin took it,
+// unregistered by the deleter before it is freed.
+struct HostArrayDelete {
+    void operator()(uint32_t *p) const;
+};
+using HostArray = std::unique_ptr<uint32_t[], HostArrayDelete>;
+// Registers [p, p + bytes) of a HostArray with CUDA (page-locked), within a
+// process-wide limit of a quarter of the host memory; false when refused.
+bool host_pin(uint32_t *p, uint64_t bytes);
+
 struct Compacted {
     uint32_t top_k = 0;
     uint64_t n = 0;
     std::vector<uint64_t> seg;
-    std::unique_ptr<uint32_t[]> names, counts;
+    HostArray names, counts;
     std::function<uint32_t *(uint64_t)> sink;
     uint32_t *h_names = nullptr, *h_counts = nullptr;
     // Optional host buffers of pre_cap entries, allocated before the walk
     // and faulted in on host threads while it runs (pre_join waits for
     // that); adopted when the lists fit, the unused tail handed back.
-    std::unique_ptr<uint32_t[]> pre_names, pre_counts;
+    HostArray pre_names, pre_counts;
     uint64_t pre_cap = 0;
     uint64_t pre_touched = 0;  // leading entries of pre_* already faulted in before this call
+    bool pre_pinned = false;   // pre_* are page-locked (known after pre_join)
     std::function<void()> pre_join;
-    // Capacity of names / counts in entries, and how many leading entries
-    // are faulted in (a freed batch hands them to the host cache).
+    // Capacity of names / counts in entries, how many leading entries are
+    // faulted in, and whether they are page-locked (a freed batch hands
+    // them to the host cache).
     uint64_t cap = 0, touched = 0;
+    bool pinned = false;
 };
 // Host result buffers of the last freed batch, kept faulted in so that the
 // next batch's copies land in touched pages (batch.cu).  take() hands them
 // over when they hold at least `need` entries; trim_host_cache() frees them.
 struct HostBufs {
-    std::unique_ptr<uint32_t[]> names, counts;
+    HostArray names, counts;
     uint64_t cap = 0, touched = 0;
+    bool pinned = false;
 };
 bool host_cache_take(uint64_t need, HostBufs &out);
 void host_cache_put(HostBufs &&b);
