@@ -632,8 +632,9 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     PTW_CUDA(db.alloc(&d_seg, nt + 1));
     PTW_CUDA(db.alloc(&d_fill, nt));
     PTW_CUDA(db.alloc(&d_tch, nt + 1));
-    PTW_CUDA(db.alloc(&d_cc, std::max<uint64_t>(nch, 1)));
-    PTW_CUDA(db.alloc(&d_hc, std::max<uint64_t>(nch, 1)));
+    const uint64_t npc = nch * 8;  // warp pieces: 8 per chunk
+    PTW_CUDA(db.alloc(&d_cc, std::max<uint64_t>(npc, 1)));
+    PTW_CUDA(db.alloc(&d_hc, std::max<uint64_t>(npc, 1)));
     PTW_CUDA(cudaMemcpyAsync(d_base, h_base, nt * 8ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_cap, h_cap, nt * 4ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_dense, dense_flags.data(), nt, cudaMemcpyHostToDevice, st));
@@ -658,14 +659,14 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     }, st));
     PTW_CUDA(cudaMemcpyAsync(out->seg.data(), d_seg, (nt + 1) * 8ull, cudaMemcpyDeviceToHost, st));
     if (!k && nch) {
-        // output position of every dense chunk, sort-input position of every hash chunk
-        PTW_CUDA(db.alloc(&d_pos, nch));
-        PTW_CUDA(db.alloc(&d_hpos, nch));
+        // output position of every dense piece, sort-input position of every hash piece
+        PTW_CUDA(db.alloc(&d_pos, npc));
+        PTW_CUDA(db.alloc(&d_hpos, npc));
         PTW_CUDA(cub_call([&](void *t, size_t &b) {
-            return cub::DeviceScan::ExclusiveSum(t, b, d_cc, d_pos, (int64_t)nch, st);
+            return cub::DeviceScan::ExclusiveSum(t, b, d_cc, d_pos, (int64_t)npc, st);
         }, st));
         PTW_CUDA(cub_call([&](void *t, size_t &b) {
-            return cub::DeviceScan::ExclusiveSum(t, b, d_hc, d_hpos, (int64_t)nch, st);
+            return cub::DeviceScan::ExclusiveSum(t, b, d_hc, d_hpos, (int64_t)npc, st);
         }, st));
     }
     PTW_CUDA(cudaStreamSynchronize(st));

@@ -281,23 +281,24 @@ struct Chunk {
     const uint4 *p;       // the chunk's first 16-byte word
 };
 
-__device__ __forceinline__ Chunk block_chunk(const unsigned long long *slots, const unsigned long long *t_base,
-                                             const uint32_t *t_len, const uint8_t *t_dense,
-                                             const unsigned long long *tch, uint32_t nt, uint32_t *s_t)
+__device__ __forceinline__ uint32_t chunk_table(const unsigned long long *tch, uint32_t nt)
 {
-    if (threadIdx.x == 0) {
-        const unsigned long long b = blockIdx.x;
-        uint32_t lo = 0, hi = nt;  // tch[lo] <= b < tch[hi]
-        while (hi - lo > 1) {
-            const uint32_t mid = lo + (hi - lo) / 2;
-            if (tch[mid] <= b) lo = mid;
-            else hi = mid;
-        }
-        *s_t = lo;
+    const unsigned long long b = blockIdx.x;
+    uint32_t lo = 0, hi = nt;  // tch[lo] <= b < tch[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (tch[mid] <= b) lo = mid;
+        else hi = mid;
     }
-    __syncthreads();
+    return lo;
+}
+
+__device__ __forceinline__ Chunk chunk_of(uint32_t t, const unsigned long long *slots,
+                                          const unsigned long long *t_base, const uint32_t *t_len,
+                                          const uint8_t *t_dense, const unsigned long long *tch)
+{
     Chunk c;
-    c.t = *s_t;
+    c.t = t;
     c.dense = t_dense[c.t] != 0;
     const uint32_t per = c.dense ? kChunkBytes / 4 : kChunkBytes / 8;
     c.first = (uint64_t)(blockIdx.x - tch[c.t]) * per;
@@ -305,6 +306,27 @@ __device__ __forceinline__ Chunk block_chunk(const unsigned long long *slots, co
     c.n = (uint32_t)(left < per ? left : per);
     c.p = reinterpret_cast<const uint4 *>(slots + t_base[c.t]) + (c.dense ? c.first / 4 : c.first / 2);
     return c;
+}
+
+// The block's chunk: thread 0 looks the table up, the block synchronises.
+__device__ __forceinline__ Chunk block_chunk(const unsigned long long *slots, const unsigned long long *t_base,
+                                             const uint32_t *t_len, const uint8_t *t_dense,
+                                             const unsigned long long *tch, uint32_t nt, uint32_t *s_t)
+{
+    if (threadIdx.x == 0) *s_t = chunk_table(tch, nt);
+    __syncthreads();
+    return chunk_of(*s_t, slots, t_base, t_len, t_dense, tch);
+}
+
+// The same for one warp, without a block-wide synchronisation.
+__device__ __forceinline__ Chunk warp_chunk(const unsigned long long *slots, const unsigned long long *t_base,
+                                            const uint32_t *t_len, const uint8_t *t_dense,
+                                            const unsigned long long *tch, uint32_t nt)
+{
+    uint32_t t = 0;
+    if ((threadIdx.x & 31) == 0) t = chunk_table(tch, nt);
+    t = __shfl_sync(kBFull, t, 0);
+    return chunk_of(t, slots, t_base, t_len, t_dense, tch);
 }
 
 // Word j of the lane: chunk word w = warp * 32 * kLaneVecs + j * 32 + lane
@@ -334,9 +356,11 @@ __device__ __forceinline__ void word_entry(const uint4 &x, int e, uint32_t &coun
     }
 }
 
-// Pass 1: occupied entries per chunk (cc, and hc for hash tables only) and
-// per table (cnt); with HIST also each table's histogram of count_bin over
-// its occupied entries (hist[t * kCountBins + bin]), for top-k selection.
+// Pass 1: occupied entries per warp piece of a chunk (cc[b * 8 + warp], and
+// hc for hash tables only; the pieces in this order are the tables' entries
+// in order) and per table (cnt); with HIST also each table's histogram of
+// count_bin over its occupied entries (hist[t * kCountBins + bin]), for
+// top-k selection.
 template <int EPV, bool HIST>
 __device__ __forceinline__ uint32_t count_chunk(const Chunk &c, uint32_t *h)
 {
@@ -373,13 +397,16 @@ __global__ void __launch_bounds__(256) k_tabs_count(const unsigned long long *sl
     const Chunk c = block_chunk(slots, t_base, t_len, t_dense, tch, nt, &s_t);  // synchronises
     uint32_t k = c.dense ? count_chunk<4, HIST>(c, h) : count_chunk<2, HIST>(c, h);
     for (int o = 16; o; o >>= 1) k += __shfl_xor_sync(kBFull, k, o);
-    if ((threadIdx.x & 31) == 0) warp_n[threadIdx.x >> 5] = k;
+    if ((threadIdx.x & 31) == 0) {
+        const uint64_t wi = (uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+        warp_n[threadIdx.x >> 5] = k;
+        cc[wi] = k;
+        hc[wi] = c.dense ? 0u : k;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t tot = 0;
         for (int w = 0; w < 8; ++w) tot += warp_n[w];
-        cc[blockIdx.x] = tot;
-        hc[blockIdx.x] = c.dense ? 0u : tot;
         if (tot) atomicAdd(&cnt[c.t], (unsigned long long)tot);
     }
     if (HIST)
@@ -395,18 +422,18 @@ __global__ void __launch_bounds__(256) k_tabs_count(const unsigned long long *sl
 //  Top-k (TOPK true): entries whose count bin is at least thr[t] go to the
 //  sort input as (t, ~count, name) keys (by_count) or (t << name_bits |
 //  name) keys with counts, at sseg[t] + a block reservation on fill[t].
-// pos and hpos are exclusive scans of pass 1's cc and hc over the chunks in
-// table order, so pos[b] is also the output position of a dense chunk.
-// Ranks come from a warp scan of per-word counts packed one byte per word,
-// then warp totals through shared memory; each warp stages its kept entries
-// (name, count) in rank order in shared memory, so the stores to global
-// memory are whole coalesced rows.
+// pos and hpos are exclusive scans of pass 1's cc and hc over the warp
+// pieces in table order, so pos[b * 8 + warp] is also the output position of
+// a dense piece.  Warps work on their own: ranks come from a warp scan of
+// per-word counts packed one byte per word, top-k reserves per warp, and
+// each warp stages its kept entries (name, count) in rank order in its part
+// of shared memory, so the stores to global memory are whole coalesced rows
+// and the kernel has no block-wide synchronisation.
 constexpr uint32_t kWarpStage = 32 * kLaneVecs * 4;
 
 template <int EPV, bool TOPK>
-__device__ __forceinline__ void place_chunk(const Chunk &c, uint32_t thr, uint32_t *warp_n,
-                                            unsigned long long *s_base, uint32_t *s_nm, uint32_t *s_ct,
-                                            unsigned long long *__restrict__ fill, unsigned long long base_full,
+__device__ __forceinline__ void place_chunk(const Chunk &c, uint32_t thr, uint32_t *s_nm, uint32_t *s_ct,
+                                            unsigned long long *__restrict__ fill, unsigned long long base,
                                             const uint32_t *__restrict__ int2name,
                                             const uint32_t *__restrict__ idx_names, int name_bits, bool by_count,
                                             uint32_t *__restrict__ out_name, uint32_t *__restrict__ out_cnt,
@@ -416,6 +443,16 @@ __device__ __forceinline__ void place_chunk(const Chunk &c, uint32_t thr, uint32
     load_chunk<EPV>(c, v);
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t w0 = warp * (32 * kLaneVecs) + lane;
+    // A dense piece's names are contiguous and do not depend on its
+    // counters: they are loaded together with them (16 bytes per whole word).
+    uint4 nv[kLaneVecs];
+#pragma unroll
+    for (uint32_t j = 0; j < kLaneVecs; ++j) {
+        const uint32_t x = (w0 + 32 * j) * EPV;
+        nv[j] = EPV == 4 && x + 4 <= c.n
+                    ? ld_stream_u4(reinterpret_cast<const uint4 *>(idx_names + c.first + x))
+                    : make_uint4(0u, 0u, 0u, 0u);
+    }
     uint32_t km = 0;  // kept entries, bit j * EPV + e
     unsigned long long packed = 0;
 #pragma unroll
@@ -432,21 +469,20 @@ __device__ __forceinline__ void place_chunk(const Chunk &c, uint32_t thr, uint32
         packed |= (unsigned long long)n_j << (8 * j);
     }
     // Names of the kept entries, all loads issued before any is used (they
-    // land while the ranks are scanned): a dense chunk's names are
-    // contiguous (16-byte loads of idx_names where the word lies inside the
-    // table), a hash slot's name is int2name[key].
+    // land while the ranks are scanned): for a dense piece from the names
+    // loaded above (scalar loads for the table's last, partial word), for a
+    // hash slot int2name[key].
     uint32_t nm[kLaneVecs][EPV];
 #pragma unroll
     for (uint32_t j = 0; j < kLaneVecs; ++j) {
         const uint32_t wm = (km >> (j * EPV)) & ((1u << EPV) - 1u);
         const uint64_t x0 = c.first + (uint64_t)(w0 + 32 * j) * EPV;
         if (EPV == 4) {
-            if (wm != 0 && (w0 + 32 * j) * EPV + 4 <= c.n) {
-                const uint4 q = ld_stream_u4(reinterpret_cast<const uint4 *>(idx_names + x0));
-                nm[j][0] = q.x;
-                nm[j][1] = q.y;
-                nm[j][2 % EPV] = q.z;
-                nm[j][3 % EPV] = q.w;
+            if ((w0 + 32 * j) * EPV + 4 <= c.n) {
+                nm[j][0] = nv[j].x;
+                nm[j][1] = nv[j].y;
+                nm[j][2 % EPV] = nv[j].z;
+                nm[j][3 % EPV] = nv[j].w;
             } else {
 #pragma unroll
                 for (int e = 0; e < EPV; ++e) nm[j][e] = (wm >> e) & 1u ? idx_names[x0 + e] : 0u;
@@ -472,22 +508,13 @@ __device__ __forceinline__ void place_chunk(const Chunk &c, uint32_t thr, uint32
     uint32_t wsum = 0;
 #pragma unroll
     for (uint32_t j = 0; j < kLaneVecs; ++j) wsum += (uint32_t)(tot >> (8 * j)) & 0xFFu;
-    if (lane == 0) warp_n[warp] = wsum;
-    __syncthreads();
-    uint32_t before = 0, all = 0;
-#pragma unroll
-    for (uint32_t w = 0; w < 8; ++w) {
-        const uint32_t x = warp_n[w];
-        before += w < warp ? x : 0u;
-        all += x;
-    }
     if (TOPK) {
-        if (threadIdx.x == 0) *s_base = all ? atomicAdd(&fill[c.t], (unsigned long long)all) : 0ull;
-        __syncthreads();
-        base_full += *s_base;
+        unsigned long long r0 = 0;
+        if (lane == 0 && wsum) r0 = atomicAdd(&fill[c.t], (unsigned long long)wsum);
+        base += __shfl_sync(kBFull, r0, 0);
     }
     // stage in warp-local rank order, then write whole rows
-    uint32_t *wn = s_nm + warp * kWarpStage, *wc = s_ct + warp * kWarpStage;
+    uint32_t *wn = s_nm, *wc = s_ct;  // this warp's part of shared memory
     uint32_t jb = 0;
 #pragma unroll
     for (uint32_t j = 0; j < kLaneVecs; ++j) {
@@ -504,7 +531,7 @@ __device__ __forceinline__ void place_chunk(const Chunk &c, uint32_t thr, uint32
         jb += (uint32_t)(tot >> (8 * j)) & 0xFFu;
     }
     __syncwarp();
-    const unsigned long long p = base_full + before;
+    const unsigned long long p = base;
     const unsigned long long tagged = (unsigned long long)c.t << (by_count ? 32 + name_bits : name_bits);
     for (uint32_t i = lane; i < wsum; i += 32) {
         const uint32_t name = wn[i], cnt = wc[i];
@@ -530,20 +557,20 @@ __global__ void __launch_bounds__(256, 4) k_tabs_place(const unsigned long long 
                                                        uint32_t *h_cnt, unsigned long long *key_out,
                                                        uint32_t *cnt_out)
 {
-    __shared__ uint32_t s_t;
-    __shared__ uint32_t warp_n[8];
-    __shared__ unsigned long long s_base;
     __shared__ uint32_t s_nm[8 * kWarpStage], s_ct[8 * kWarpStage];
-    const Chunk c = block_chunk(slots, t_base, t_len, t_dense, tch, nt, &s_t);  // synchronises
+    const uint32_t warp = threadIdx.x >> 5;
+    const Chunk c = warp_chunk(slots, t_base, t_len, t_dense, tch, nt);
     const uint32_t thr = TOPK ? t_thr[c.t] : 0u;
-    if (TOPK && sseg[c.t + 1] == sseg[c.t]) return;  // nothing kept in this table (block-uniform)
-    const unsigned long long base = TOPK ? sseg[c.t] : c.dense ? pos[blockIdx.x] : hpos[blockIdx.x];
+    if (TOPK && sseg[c.t + 1] == sseg[c.t]) return;  // nothing kept in this table (warp-uniform)
+    const uint64_t wi = (uint64_t)blockIdx.x * 8 + warp;
+    const unsigned long long base = TOPK ? sseg[c.t] : c.dense ? pos[wi] : hpos[wi];
+    uint32_t *wn = s_nm + warp * kWarpStage, *wc = s_ct + warp * kWarpStage;
     if (c.dense)
-        place_chunk<4, TOPK>(c, thr, warp_n, &s_base, s_nm, s_ct, fill, base, int2name, idx_names, name_bits,
-                             by_count, out_name, out_cnt, key_out, cnt_out);
+        place_chunk<4, TOPK>(c, thr, wn, wc, fill, base, int2name, idx_names, name_bits, by_count, out_name,
+                             out_cnt, key_out, cnt_out);
     else
-        place_chunk<2, TOPK>(c, thr, warp_n, &s_base, s_nm, s_ct, fill, base, int2name, idx_names, name_bits,
-                             by_count, h_name, h_cnt, key_out, cnt_out);
+        place_chunk<2, TOPK>(c, thr, wn, wc, fill, base, int2name, idx_names, name_bits, by_count, h_name, h_cnt,
+                             key_out, cnt_out);
 }
 
 // Top-k selection, threshold: the lowest bin thr[i] such that the entries in
