@@ -635,12 +635,6 @@ __global__ void k_place_hash(const uint32_t *name, const uint32_t *cnt, uint64_t
     }
 }
 
-__global__ void k_key_names(const unsigned long long *key, uint64_t n, unsigned long long mask, uint32_t *name)
-{
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        name[i] = (uint32_t)(key[i] & mask);
-}
-
 // Top-k, step 1: key (table << 32 | ~count) with the name as value, from the
 // (table << name_bits | name) keys and counts of the name-ordered lists.
 __global__ void k_count_keys(const unsigned long long *key, const uint32_t *cnt, uint64_t n, int name_bits,
