@@ -682,11 +682,13 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     }
     out->n = n_out;
     if (n_ent) {
+        bool dst_pinned = false;  // the host lists are page-locked: copies run asynchronously
         if (out->sink) {
             uint32_t *base = out->sink(n_out);
             if (!base) return fail(PTW_ENOMEM, "host staging of results failed");
             out->h_names = base;
             out->h_counts = base + n_out;
+            dst_pinned = true;  // the sink hands out page-locked staging
         } else if (out->pre_names && n_out <= out->pre_cap) {
             // the buffers faulted in during the walk hold the lists
             const double tj = timing ? clk() : 0.0;
@@ -698,6 +700,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             out->h_counts = out->counts.get();
             out->cap = out->pre_cap;
             out->pinned = out->pre_pinned;
+            dst_pinned = out->pinned;
             if (out->pinned) {
                 out->touched = out->pre_cap;  // registered pages stay resident
             } else {
@@ -721,6 +724,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
         while (name_bits < 32 && (1ull << name_bits) < g->dg.id_bound) ++name_bits;
         while ((1ull << q_bits) < nt) ++q_bits;
         uint32_t *o_name = nullptr, *o_cnt = nullptr;
+        bool copied = false;  // the lists already reached the host (range copies)
         if (k) {
             // Top-k.  A histogram of each large table's counts (exact below
             // 256, 16 bins per octave above) gives the lowest bin that still
@@ -750,8 +754,8 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             PTW_CUDA(db.alloc(&s_cnt, n_sel));
             // (table, ~count, name) in 64 bits: one sort, keys only
             const bool packed = q_bits + 32 + name_bits <= 64;
-            k_tabs_place<true><<<(unsigned)nch, 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_tch, nt, nullptr,
-                                                             nullptr, d_thr, d_sseg, d_fill, g->dg.int2name,
+            k_tabs_place<true><<<(unsigned)nch, 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_tch, nt, 0ull,
+                                                             nullptr, nullptr, d_thr, d_sseg, d_fill, g->dg.int2name,
                                                              g->dg.names, name_bits, packed, nullptr, nullptr,
                                                              nullptr, nullptr, e_key, e_cnt);
             PTW_CUDA(cudaGetLastError());
@@ -808,38 +812,102 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
                 PTW_CUDA(db.alloc(&d_hseg, nt + 1));
                 PTW_CUDA(cudaMemcpyAsync(d_hseg, hseg.data(), (nt + 1) * 8ull, cudaMemcpyHostToDevice, st));
             }
-            // Pass 2: dense tables straight to the output, hash tables to their ranges.
-            k_tabs_place<false><<<(unsigned)nch, 256, 0, st>>>(d_slots, d_base, d_cap, d_dense, d_tch, nt, d_pos,
-                                                              d_hpos, nullptr, nullptr, nullptr, g->dg.int2name,
-                                                              g->dg.names, name_bits, false, o_name, o_cnt, h_name,
-                                                              h_cnt, nullptr, nullptr);
-            PTW_CUDA(cudaGetLastError());
-            if (n_hash) {
-                // segmented sorts over runs of whole tables of under 2^31 entries each
-                for (uint32_t t0 = 0; t0 < nt;) {
-                    uint32_t t1 = t0 + 1;
-                    while (t1 < nt && hseg[t1 + 1] - hseg[t0] < (1ull << 31)) ++t1;
-                    const uint64_t items = hseg[t1] - hseg[t0];
-                    if (items) {
-                        if (items >= (1ull << 31)) return fail(PTW_EINVAL, "a hash table holds 2^31 entries or more");
-                        std::vector<unsigned long long> rel(t1 - t0 + 1);
-                        for (uint32_t i = t0; i <= t1; ++i) rel[i - t0] = hseg[i] - hseg[t0];
-                        unsigned long long *d_rel;
-                        PTW_CUDA(db.alloc(&d_rel, rel.size()));
-                        PTW_CUDA(cudaMemcpyAsync(d_rel, rel.data(), rel.size() * 8ull, cudaMemcpyHostToDevice, st));
-                        const uint64_t o = hseg[t0];
-                        PTW_CUDA(cub_call([&](void *t, size_t &b) {
-                            return cub::DeviceSegmentedSort::SortPairs(t, b, h_name + o, s_name + o, h_cnt + o,
-                                                                       s_cnt + o, (int)items, (int)(t1 - t0), d_rel,
-                                                                       d_rel + 1, st);
-                        }, st));
-                    }
-                    t0 = t1;
+            // Pass 2 and the hash sorts run over R ranges of consecutive tables
+            // with about equal entries.  The lists of a range are final once
+            // its kernels end, and they are a contiguous piece of the output
+            // (tables are in output order), so with page-locked host lists
+            // each range's copy to the host runs on a second stream while the
+            // next range compacts.
+            const uint32_t R = dst_pinned && n_ent >= (16ull << 20) ? 4u : 1u;
+            std::vector<uint32_t> tb(R + 1, nt);
+            tb[0] = 0;
+            for (uint32_t r = 1; r < R; ++r) {
+                const uint64_t want = n_ent * r / R;
+                tb[r] = (uint32_t)(std::upper_bound(out->seg.begin(), out->seg.begin() + nt + 1, want) -
+                                   out->seg.begin() - 1);
+                tb[r] = std::max(tb[r], tb[r - 1]);
+            }
+            cudaStream_t cs = st;
+            if (R > 1) {
+                if (!g->copy_stream) PTW_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+                cs = g->copy_stream;
+            }
+            // On any return, copies still reading the device lists end before
+            // those are freed (the frees are ordered on st, not on cs).
+            struct CopyWait {
+                cudaStream_t s;
+                bool on;
+                ~CopyWait()
+                {
+                    if (on) cudaStreamSynchronize(s);
                 }
-                const unsigned hg = (unsigned)std::min<uint64_t>((n_hash + 255) / 256, (uint64_t)g->num_sms * 32);
-                k_place_hash<<<std::max(hg, 1u), 256, 0, st>>>(s_name, s_cnt, n_hash, d_hseg, nt, d_seg, o_name,
-                                                              o_cnt);
+            } copy_wait{cs, R > 1};
+            std::vector<cudaEvent_t> evs;
+            struct EvFree {
+                std::vector<cudaEvent_t> &e;
+                ~EvFree()
+                {
+                    for (cudaEvent_t x : e) cudaEventDestroy(x);
+                }
+            } ev_free{evs};
+            for (uint32_t r = 0; r < R; ++r) {
+                const uint32_t t0 = tb[r], t1 = tb[r + 1];
+                if (t0 >= t1) continue;
+                const unsigned long long c0 = tch[t0], c1 = tch[t1];
+                if (c1 > c0)
+                    k_tabs_place<false><<<(unsigned)(c1 - c0), 256, 0, st>>>(
+                        d_slots, d_base, d_cap, d_dense, d_tch, nt, c0, d_pos, d_hpos, nullptr, nullptr, nullptr,
+                        g->dg.int2name, g->dg.names, name_bits, false, o_name, o_cnt, h_name, h_cnt, nullptr, nullptr);
                 PTW_CUDA(cudaGetLastError());
+                if (hseg[t1] > hseg[t0]) {
+                    // segmented sorts over runs of whole tables of under 2^31 entries each
+                    for (uint32_t u0 = t0; u0 < t1;) {
+                        uint32_t u1 = u0 + 1;
+                        while (u1 < t1 && hseg[u1 + 1] - hseg[u0] < (1ull << 31)) ++u1;
+                        const uint64_t items = hseg[u1] - hseg[u0];
+                        if (items) {
+                            if (items >= (1ull << 31))
+                                return fail(PTW_EINVAL, "a hash table holds 2^31 entries or more");
+                            std::vector<unsigned long long> rel(u1 - u0 + 1);
+                            for (uint32_t i = u0; i <= u1; ++i) rel[i - u0] = hseg[i] - hseg[u0];
+                            unsigned long long *d_rel;
+                            PTW_CUDA(db.alloc(&d_rel, rel.size()));
+                            PTW_CUDA(cudaMemcpyAsync(d_rel, rel.data(), rel.size() * 8ull, cudaMemcpyHostToDevice,
+                                                     st));
+                            const uint64_t o = hseg[u0];
+                            PTW_CUDA(cub_call([&](void *t, size_t &b) {
+                                return cub::DeviceSegmentedSort::SortPairs(t, b, h_name + o, s_name + o, h_cnt + o,
+                                                                           s_cnt + o, (int)items, (int)(u1 - u0),
+                                                                           d_rel, d_rel + 1, st);
+                            }, st));
+                        }
+                        u0 = u1;
+                    }
+                    const uint64_t nh = hseg[t1] - hseg[t0];
+                    const unsigned hg = (unsigned)std::min<uint64_t>((nh + 255) / 256, (uint64_t)g->num_sms * 32);
+                    k_place_hash<<<std::max(hg, 1u), 256, 0, st>>>(s_name, s_cnt, hseg[t0], hseg[t1], d_hseg, nt,
+                                                                  d_seg, o_name, o_cnt);
+                    PTW_CUDA(cudaGetLastError());
+                }
+                if (R > 1) {
+                    const uint64_t e0 = out->seg[t0], e1 = out->seg[t1];
+                    cudaEvent_t ev;
+                    PTW_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+                    evs.push_back(ev);
+                    PTW_CUDA(cudaEventRecord(ev, st));
+                    PTW_CUDA(cudaStreamWaitEvent(cs, ev, 0));
+                    if (e1 > e0) {
+                        PTW_CUDA(cudaMemcpyAsync(out->h_names + e0, o_name + e0, (e1 - e0) * 4,
+                                                 cudaMemcpyDeviceToHost, cs));
+                        PTW_CUDA(cudaMemcpyAsync(out->h_counts + e0, o_cnt + e0, (e1 - e0) * 4,
+                                                 cudaMemcpyDeviceToHost, cs));
+                    }
+                }
+            }
+            if (R > 1) {
+                // copies issued; wait for them here (the device buffers they read are freed below)
+                PTW_CUDA(cudaStreamSynchronize(cs));
+                copied = true;
             }
         }
         const double tj2 = timing ? clk() : 0.0;
@@ -849,8 +917,10 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             PTW_CUDA(cudaStreamSynchronize(st));
             t1 = clk();
         }
-        PTW_CUDA(cudaMemcpyAsync(out->h_names, o_name, n_out * 4, cudaMemcpyDeviceToHost, st));
-        PTW_CUDA(cudaMemcpyAsync(out->h_counts, o_cnt, n_out * 4, cudaMemcpyDeviceToHost, st));
+        if (!copied) {
+            PTW_CUDA(cudaMemcpyAsync(out->h_names, o_name, n_out * 4, cudaMemcpyDeviceToHost, st));
+            PTW_CUDA(cudaMemcpyAsync(out->h_counts, o_cnt, n_out * 4, cudaMemcpyDeviceToHost, st));
+        }
         PTW_CUDA(cudaStreamSynchronize(st));
         if (timing) t2 = clk();
     }

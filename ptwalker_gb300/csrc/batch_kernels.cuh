@@ -281,9 +281,8 @@ struct Chunk {
     const uint4 *p;       // the chunk's first 16-byte word
 };
 
-__device__ __forceinline__ uint32_t chunk_table(const unsigned long long *tch, uint32_t nt)
+__device__ __forceinline__ uint32_t chunk_table(const unsigned long long *tch, uint32_t nt, unsigned long long b)
 {
-    const unsigned long long b = blockIdx.x;
     uint32_t lo = 0, hi = nt;  // tch[lo] <= b < tch[hi]
     while (hi - lo > 1) {
         const uint32_t mid = lo + (hi - lo) / 2;
@@ -293,7 +292,7 @@ __device__ __forceinline__ uint32_t chunk_table(const unsigned long long *tch, u
     return lo;
 }
 
-__device__ __forceinline__ Chunk chunk_of(uint32_t t, const unsigned long long *slots,
+__device__ __forceinline__ Chunk chunk_of(uint32_t t, unsigned long long b, const unsigned long long *slots,
                                           const unsigned long long *t_base, const uint32_t *t_len,
                                           const uint8_t *t_dense, const unsigned long long *tch)
 {
@@ -301,7 +300,7 @@ __device__ __forceinline__ Chunk chunk_of(uint32_t t, const unsigned long long *
     c.t = t;
     c.dense = t_dense[c.t] != 0;
     const uint32_t per = c.dense ? kChunkBytes / 4 : kChunkBytes / 8;
-    c.first = (uint64_t)(blockIdx.x - tch[c.t]) * per;
+    c.first = (uint64_t)(b - tch[c.t]) * per;
     const uint64_t left = t_len[c.t] - c.first;
     c.n = (uint32_t)(left < per ? left : per);
     c.p = reinterpret_cast<const uint4 *>(slots + t_base[c.t]) + (c.dense ? c.first / 4 : c.first / 2);
@@ -313,20 +312,20 @@ __device__ __forceinline__ Chunk block_chunk(const unsigned long long *slots, co
                                              const uint32_t *t_len, const uint8_t *t_dense,
                                              const unsigned long long *tch, uint32_t nt, uint32_t *s_t)
 {
-    if (threadIdx.x == 0) *s_t = chunk_table(tch, nt);
+    if (threadIdx.x == 0) *s_t = chunk_table(tch, nt, blockIdx.x);
     __syncthreads();
-    return chunk_of(*s_t, slots, t_base, t_len, t_dense, tch);
+    return chunk_of(*s_t, blockIdx.x, slots, t_base, t_len, t_dense, tch);
 }
 
-// The same for one warp, without a block-wide synchronisation.
-__device__ __forceinline__ Chunk warp_chunk(const unsigned long long *slots, const unsigned long long *t_base,
-                                            const uint32_t *t_len, const uint8_t *t_dense,
-                                            const unsigned long long *tch, uint32_t nt)
+// Chunk b for one warp, without a block-wide synchronisation.
+__device__ __forceinline__ Chunk warp_chunk(unsigned long long b, const unsigned long long *slots,
+                                            const unsigned long long *t_base, const uint32_t *t_len,
+                                            const uint8_t *t_dense, const unsigned long long *tch, uint32_t nt)
 {
     uint32_t t = 0;
-    if ((threadIdx.x & 31) == 0) t = chunk_table(tch, nt);
+    if ((threadIdx.x & 31) == 0) t = chunk_table(tch, nt, b);
     t = __shfl_sync(kBFull, t, 0);
-    return chunk_of(t, slots, t_base, t_len, t_dense, tch);
+    return chunk_of(t, b, slots, t_base, t_len, t_dense, tch);
 }
 
 // Word j of the lane: chunk word w = warp * 32 * kLaneVecs + j * 32 + lane
@@ -545,10 +544,13 @@ __device__ __forceinline__ void place_chunk(const Chunk &c, uint32_t thr, uint32
     }
 }
 
+// Block i of a launch works on chunk chunk0 + i (a launch may cover the
+// chunks of a range of tables).
 template <bool TOPK>
 __global__ void __launch_bounds__(256, 4) k_tabs_place(const unsigned long long *slots, const unsigned long long *t_base,
                                                        const uint32_t *t_len, const uint8_t *t_dense,
                                                        const unsigned long long *tch, uint32_t nt,
+                                                       unsigned long long chunk0,
                                                        const unsigned long long *pos, const unsigned long long *hpos,
                                                        const uint32_t *t_thr, const unsigned long long *sseg,
                                                        unsigned long long *fill, const uint32_t *int2name,
@@ -559,10 +561,11 @@ __global__ void __launch_bounds__(256, 4) k_tabs_place(const unsigned long long 
 {
     __shared__ uint32_t s_nm[8 * kWarpStage], s_ct[8 * kWarpStage];
     const uint32_t warp = threadIdx.x >> 5;
-    const Chunk c = warp_chunk(slots, t_base, t_len, t_dense, tch, nt);
+    const unsigned long long b = chunk0 + blockIdx.x;
+    const Chunk c = warp_chunk(b, slots, t_base, t_len, t_dense, tch, nt);
     const uint32_t thr = TOPK ? t_thr[c.t] : 0u;
     if (TOPK && sseg[c.t + 1] == sseg[c.t]) return;  // nothing kept in this table (warp-uniform)
-    const uint64_t wi = (uint64_t)blockIdx.x * 8 + warp;
+    const uint64_t wi = b * 8 + warp;
     const unsigned long long base = TOPK ? sseg[c.t] : c.dense ? pos[wi] : hpos[wi];
     uint32_t *wn = s_nm + warp * kWarpStage, *wc = s_ct + warp * kWarpStage;
     if (c.dense)
@@ -617,12 +620,15 @@ __global__ void k_tabs_thresh(const unsigned long long *cnt, const uint32_t *his
     }
 }
 
-// Hash entries j, sorted by name within their table t's range [hseg[t],
-// hseg[t + 1]), go to position seg[t] + (j - hseg[t]) of the output.
-__global__ void k_place_hash(const uint32_t *name, const uint32_t *cnt, uint64_t n, const unsigned long long *hseg,
-                             uint32_t nt, const unsigned long long *seg, uint32_t *out_name, uint32_t *out_cnt)
+// Hash entries j in [j0, j1), sorted by name within their table t's range
+// [hseg[t], hseg[t + 1]), go to position seg[t] + (j - hseg[t]) of the
+// output.
+__global__ void k_place_hash(const uint32_t *name, const uint32_t *cnt, uint64_t j0, uint64_t j1,
+                             const unsigned long long *hseg, uint32_t nt, const unsigned long long *seg,
+                             uint32_t *out_name, uint32_t *out_cnt)
 {
-    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t j = j0 + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < j1;
+         j += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t lo = 0, hi = nt;  // hseg[lo] <= j < hseg[hi]
         while (hi - lo > 1) {
             const uint32_t mid = lo + (hi - lo) / 2;

@@ -57,11 +57,12 @@ def test_batch_bit_exact_per_query(gpu, G16, s16_canon, app):
 
 def test_reused_host_result_buffers(gpu, G16, s16_canon):
     """Batches large enough for host result buffers sized before the walk
-    (8 M entries and up): a freed batch's buffers are reused by the next
-    batch, whose lists must still equal the replay, and results still held
-    are not touched by later batches."""
+    (8 M entries and up) and for copies overlapping compaction range by
+    range (16 M entries and up, page-locked lists): a freed batch's buffers
+    are reused by the next batch, whose lists must still equal the replay in
+    every range, and results still held are not touched by later batches."""
     rng = np.random.default_rng(17)
-    nq = 200  # about 11 M entries estimated: above the 8 M of the sized-before-the-walk path
+    nq = 700  # about 25 K distinct vertices per query: 17 M entries written
     sources = rng.integers(0, G16.n, nq)
     budgets = np.full(nq, 60000)
     first = gpu.ppr_batch(G16, sources, budgets, sp=0.2, seed=3)
@@ -70,7 +71,8 @@ def test_reused_host_result_buffers(gpu, G16, s16_canon):
     first.close()                                   # buffers go to the host cache
     second = gpu.ppr_batch(G16, sources, budgets, sp=0.2, seed=4)   # reuses them
     held = gpu.ppr_batch(G16, sources[:40], budgets[:40], sp=0.2, seed=5)
-    for i in (0, 57, nq - 1):
+    assert second.entries >= 16 << 20
+    for i in (0, 57, 180, 349, 420, 555, nq - 1):
         want = replay_query(s16_canon, int(sources[i]), i, int(budgets[i]), 0.2, 4, "visits")
         assert sparse_equal(second, i, want), i
     second.close()
