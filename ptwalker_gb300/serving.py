@@ -36,28 +36,35 @@ class Server:
         q = C.Query(int(source), int(query_id), int(budget))
         C.check(self._lib.ptw_serve_submit(self._h, ctypes.byref(q)))
 
-    def step(self, take=True):
+    def step(self, take=True, copy=True):
         """One admission + tick; returns the list of completed results as
         dicts with keys query_id, source, budget, names, counts, submit_s,
         admit_s, done_s.  take=False leaves them on the server for a later
-        results() call."""
+        results() call; copy=False as in results()."""
         nd, na, npd = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
         C.check(self._lib.ptw_serve_step(self._h, ctypes.byref(nd), ctypes.byref(na), ctypes.byref(npd)))
         self.n_active, self.n_pending = int(na.value), int(npd.value)
-        return self.results() if take else []
+        return self.results(copy) if take else []
 
-    def results(self):
-        """Takes every completed result the server holds."""
+    def results(self, copy=True):
+        """Takes every completed result the server holds.  copy=False gives
+        names and counts as read-only views of the server's page-locked
+        staging (no copy), valid until the next step()."""
         out = []
         r = C.ServeResult()
         pn, pc = ctypes.POINTER(ctypes.c_uint32)(), ctypes.POINTER(ctypes.c_uint32)()
         while self._lib.ptw_serve_poll(self._h, ctypes.byref(r)) == 1:
             ne = int(r.n_entries)
             if ne:
-                # one copy out of the pinned block the device wrote the entries to
+                # the entries sit in the page-locked block the device wrote them to
                 C.check(self._lib.ptw_serve_view(self._h, ctypes.byref(pn), ctypes.byref(pc)))
-                names = np.ctypeslib.as_array(pn, shape=(ne,)).copy()
-                counts = np.ctypeslib.as_array(pc, shape=(ne,)).copy()
+                names = np.ctypeslib.as_array(pn, shape=(ne,))
+                counts = np.ctypeslib.as_array(pc, shape=(ne,))
+                if copy:
+                    names, counts = names.copy(), counts.copy()
+                else:
+                    names.flags.writeable = False
+                    counts.flags.writeable = False
             else:
                 names = np.empty(0, dtype=np.uint32)
                 counts = np.empty(0, dtype=np.uint32)
@@ -123,7 +130,7 @@ def open_loop(server, sources, budgets, rate, seed=0, query_id0=0, keep_results=
             time.sleep(min(arrive[nxt] - now, 0.002))
             if nxt < n and arrive[nxt] > server.clock():
                 continue
-        for r in server.step():
+        for r in server.step(copy=keep_results):
             i = r["query_id"] - query_id0
             lat[i] = r["done_s"] - arrive[i]
             done_at[i] = r["done_s"]

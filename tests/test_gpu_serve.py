@@ -179,3 +179,17 @@ def test_serving_top_k(gpu, G16, s16_canon):
         keep = nz[order][:k]
         assert np.array_equal(r["names"], keep.astype(np.uint32)), r["query_id"]
         assert np.array_equal(r["counts"], dense[keep]), r["query_id"]
+
+
+def test_result_views_without_copy(gpu, G16, s16_canon):
+    """step(copy=False) hands out read-only views of the page-locked staging:
+    they hold the same lists as the replay until the next step."""
+    with gpu.Server(G16, sp=0.2, seed=6) as srv:
+        for i, (s, b) in enumerate([(3, 3000), (77, 5000), (1024, 2000), (46000, 4000)]):
+            srv.submit(s, b, 40 + i)
+        got = 0
+        while got < 4:
+            for r in srv.step(copy=False):
+                assert not r["names"].flags.writeable and not r["counts"].flags.writeable
+                check(r, s16_canon, 0.2, 6)   # before the next step
+                got += 1
