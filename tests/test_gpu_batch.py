@@ -224,3 +224,29 @@ def test_batch_and_serving_with_extended_columns(gpu, G16, s16_canon, app):
             assert np.array_equal(got[i]["names"], nz) and np.array_equal(got[i]["counts"], want[nz]), i
     finally:
         G16.tune = saved
+
+
+@pytest.mark.parametrize("case", range(6))
+def test_random_batches_equal_replay(gpu, G16, s16_canon, case):
+    """Random batch shapes through compaction: hash and dense tables mixed,
+    full lists and top-k, visit and endpoint apps, tiny and large budgets,
+    repeated sources; every query equals its replay alone."""
+    rng = np.random.default_rng(100 + case)
+    nq = int(rng.integers(1, 120))
+    app = ["visits", "endpoint"][case % 2]
+    k = [0, 1, 7, 100, 0, 0][case]
+    src = rng.integers(0, G16.n, nq).astype(np.uint32)
+    src[rng.random(nq) < 0.2] = src[0]                        # some queries share a source
+    bud = np.exp(rng.uniform(0, np.log(60000), nq)).astype(np.int64)
+    qids = rng.permutation(1 << 20)[:nq].astype(np.uint32)
+    sp = float(rng.choice([0.1, 0.2, 0.5]))
+    res = gpu.ppr_batch(G16, src, bud, sp=sp, seed=case, app=app, query_ids=qids, top_k=k)
+    for i in rng.choice(nq, min(nq, 12), replace=False):
+        dense = replay_query(s16_canon, int(src[i]), int(qids[i]), int(bud[i]), sp, case, app)
+        if k:
+            want_n, want_c = top_k_of(dense, k)
+            names, counts = res.query(i)
+            assert np.array_equal(names, want_n) and np.array_equal(counts, want_c), (case, i)
+        else:
+            assert sparse_equal(res, i, dense), (case, i)
+    res.close()
