@@ -138,3 +138,29 @@ def test_cfg_builder():
     assert api.Tune.from_c(t.to_c()).as_dict() == t.as_dict()
     with pytest.raises(ValueError):
         api._host_ptr(np.zeros(4, dtype=np.uint32)[::2])
+
+
+def test_integration_examples_compile(tmp_path):
+    """The C++ binding and serving examples of INTEGRATION.md compile against
+    include/ptw.h as written."""
+    import subprocess
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    blocks = re.findall(r"```cpp\n(.*?)```", text, re.S)
+    binding = [b for b in blocks if "ptw_walk.hpp" in b]
+    serving = [b for b in blocks if "ptw_serve_cfg cfg{}" in b]
+    assert binding and serving
+    src = binding[0] + """
+static void consume(uint64_t, const uint32_t *, const uint32_t *, uint64_t) {}
+int main() {
+    PtwGraph G("graph.txt", false);
+    std::vector<uint32_t> c = ptw_walk_counts(G, 10, 0.15, 1, {});
+    uint32_t source_name = 1, query_id = 2;
+""" + serving[0] + """
+    return 0;
+}
+"""
+    f = tmp_path / "example.cpp"
+    f.write_text(src)
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(f)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
