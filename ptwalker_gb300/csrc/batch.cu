@@ -365,6 +365,7 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
              std::vector<WaveResult> &waves, std::vector<uint32_t> &overflow, uint64_t *moves_out,
              float *walk_ms)
 {
+    NvtxRange nvtx("run_wave");
     cudaStream_t st = g->stream;
     const uint32_t nq = (uint32_t)wq.size();
     const bool timing = std::getenv("PTW_TIMING") != nullptr;
@@ -595,6 +596,7 @@ uint32_t batch_top_k(const ptw_batch *b) { return b->top_k; }
 int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned long long *h_base,
                    const uint32_t *h_cap, const uint8_t *h_dense, uint32_t nt, Compacted *out)
 {
+    NvtxRange nvtx("compact_tables");
     out->n = 0;
     out->seg.assign(nt + 1, 0);
     out->names.reset();
@@ -963,6 +965,7 @@ using namespace ptw;
 extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t nq, const ptw_batch_cfg *cfg,
                              ptw_batch **out)
 try {
+    NvtxRange nvtx("ptw_ppr_batch");
     if (!g || !cfg || !out) return fail(PTW_EINVAL, "null argument");
     *out = nullptr;
     if (nq && !h_queries) return fail(PTW_EINVAL, "null query table");

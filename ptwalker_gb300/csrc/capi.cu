@@ -435,6 +435,7 @@ extern "C" const char *ptw_version(void) { return "ptwalker_gb300 0.1 (sm_103a)"
 
 extern "C" int ptw_graph_load(const char *path, int32_t fmt, int32_t as_undirected, ptw_graph **out)
 try {
+    NvtxRange nvtx("ptw_graph_load");
     if (!path || !out) return fail(PTW_EINVAL, "null argument");
     if (fmt != PTW_FMT_BINARY && fmt != PTW_FMT_TEXT) return fail(PTW_EINVAL, "unknown graph format");
     std::vector<uint32_t> src, dst;
@@ -466,6 +467,7 @@ inline char *put_u32(char *p, uint32_t x)
 
 extern "C" int ptw_graph_save(const ptw_graph *g, const char *path, int32_t fmt)
 try {
+    NvtxRange nvtx("ptw_graph_save");
     if (!g || !path) return fail(PTW_EINVAL, "null argument");
     if (fmt != PTW_FMT_BINARY && fmt != PTW_FMT_TEXT) return fail(PTW_EINVAL, "unknown graph format");
     const uint64_t m = g->dg.m;
@@ -520,6 +522,7 @@ try {
 extern "C" int ptw_graph_from_edges(const uint32_t *h_src, const uint32_t *h_dst, uint64_t m,
                                     int32_t as_undirected, ptw_graph **out)
 try {
+    NvtxRange nvtx("ptw_graph_from_edges");
     return upload_and_build(h_src, h_dst, m, as_undirected != 0, out);
 } catch (...) {
     return host_exception();
@@ -528,6 +531,7 @@ try {
 extern "C" int ptw_graph_from_csr(const uint64_t *h_row_ptr, const uint32_t *h_col, uint32_t n,
                                   const uint32_t *h_names, ptw_graph **out)
 try {
+    NvtxRange nvtx("ptw_graph_from_csr");
     if (!out) return fail(PTW_EINVAL, "null output handle");
     *out = nullptr;
     if (!h_row_ptr || n == 0) return fail(PTW_EINVAL, "CSR needs n >= 1 rows and a row_ptr array");
@@ -559,6 +563,7 @@ try {
 extern "C" int ptw_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
                               uint64_t seed, int32_t clean, ptw_graph **out)
 try {
+    NvtxRange nvtx("ptw_graph_rmat");
     if (!out) return fail(PTW_EINVAL, "null output handle");
     *out = nullptr;
     if (scale < 1 || scale > 31) return fail(PTW_EINVAL, "scale must be in [1, 31]");
@@ -601,6 +606,7 @@ try {
 
 extern "C" int ptw_graph_chung_lu(uint32_t n, double gamma, double mean_degree, uint64_t seed, ptw_graph **out)
 try {
+    NvtxRange nvtx("ptw_graph_chung_lu");
     if (!out) return fail(PTW_EINVAL, "null output handle");
     *out = nullptr;
     if (n < 2) return fail(PTW_EINVAL, "n must be >= 2");
@@ -669,6 +675,7 @@ try {
 extern "C" int ptw_pagerank_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_counts,
                                 ptw_walk_stats *stats)
 try {
+    NvtxRange nvtx("ptw_pagerank_dev");
     int rc = check_cfg(g, cfg, true);
     if (rc) return rc;
     if (!d_counts) return fail(PTW_EINVAL, "null counts buffer");
@@ -684,6 +691,7 @@ try {
 extern "C" int ptw_pagerank(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_counts,
                             ptw_walk_stats *stats)
 try {
+    NvtxRange nvtx("ptw_pagerank");
     int rc = check_cfg(g, cfg, true);
     if (rc) return rc;
     if (!h_counts) return fail(PTW_EINVAL, "null counts buffer");
@@ -705,6 +713,7 @@ try {
 // in flight; each has its own device by-name buffer.
 extern "C" int ptw_pagerank_submit(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_counts, uint64_t *ticket)
 try {
+    NvtxRange nvtx("ptw_pagerank_submit");
     int rc = check_cfg(g, cfg, true);
     if (rc) return rc;
     if (!h_counts || !ticket) return fail(PTW_EINVAL, "null counts buffer or ticket");
@@ -744,6 +753,7 @@ try {
 
 extern "C" int ptw_pagerank_wait(ptw_graph *g, uint64_t ticket, ptw_walk_stats *stats)
 try {
+    NvtxRange nvtx("ptw_pagerank_wait");
     if (!g) return fail(PTW_EINVAL, "null graph");
     AsyncSlot *a = nullptr;
     for (AsyncSlot &x : g->async)
@@ -770,6 +780,7 @@ try {
 extern "C" int ptw_rwr_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_pairs,
                            ptw_walk_stats *stats)
 try {
+    NvtxRange nvtx("ptw_rwr_dev");
     int rc = check_cfg(g, cfg, true);
     if (rc) return rc;
     if (!d_pairs && cfg->n_walkers) return fail(PTW_EINVAL, "null pairs buffer");
@@ -785,6 +796,7 @@ try {
 
 extern "C" int ptw_rwr(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *h_pairs, ptw_walk_stats *stats)
 try {
+    NvtxRange nvtx("ptw_rwr");
     int rc = check_cfg(g, cfg, true);
     if (rc) return rc;
     if (!h_pairs && cfg->n_walkers) return fail(PTW_EINVAL, "null pairs buffer");
@@ -806,6 +818,7 @@ try {
 extern "C" int ptw_deepwalk_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *d_paths,
                                 ptw_walk_stats *stats)
 try {
+    NvtxRange nvtx("ptw_deepwalk_dev");
     int rc = check_cfg(g, cfg, false);
     if (rc) return rc;
     if (!d_paths && cfg->n_walkers && L) return fail(PTW_EINVAL, "null paths buffer");
@@ -833,6 +846,7 @@ try {
 extern "C" int ptw_deepwalk(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *h_paths,
                             ptw_walk_stats *stats)
 try {
+    NvtxRange nvtx("ptw_deepwalk");
     int rc = check_cfg(g, cfg, false);
     if (rc) return rc;
     if (!h_paths && cfg->n_walkers && L) return fail(PTW_EINVAL, "null paths buffer");
@@ -864,6 +878,7 @@ try {
 
 extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tune *best)
 try {
+    NvtxRange nvtx("ptw_autotune");
     if (!g) return fail(PTW_EINVAL, "null graph");
     if (!(sp > 0.0 && sp <= 1.0)) return fail(PTW_EINVAL, "sp must be in (0, 1]");
     PTW_CUDA(cudaSetDevice(g->device));

@@ -145,6 +145,7 @@ using namespace ptw;
 
 extern "C" int ptw_batch_l1(ptw_graph *g, const ptw_batch *b, double sp, int32_t app, double tol, double *h_l1)
 try {
+    NvtxRange nvtx("ptw_batch_l1");
     if (!g || !b || !h_l1) return fail(PTW_EINVAL, "null argument");
     if (!(sp > 0.0 && sp < 1.0)) return fail(PTW_EINVAL, "sp must be in (0, 1)");
     if (app != PTW_APP_VISITS && app != PTW_APP_ENDPOINT) return fail(PTW_EINVAL, "unknown app");

@@ -132,6 +132,7 @@ using namespace ptw;
 extern "C" int ptw_pagerank_noalloc(const ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_counts,
                                     void *cuda_stream)
 try {
+    NvtxRange nvtx("ptw_pagerank_noalloc");
     if (!g || !cfg || !d_counts) return fail(PTW_EINVAL, "null argument");
     if (g->dg.n > PTW_NOALLOC_MAX_VERTICES)
         return fail(PTW_EINVAL, "graph has " + std::to_string(g->dg.n) +

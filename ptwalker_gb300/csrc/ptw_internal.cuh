@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/ptw.h"
+#include <nvtx3/nvToolsExt.h>
 
 // Philox counter words that separate the purposes of a draw.
 #define PTW_TAG_WALK 0x57414C4Bu  // "WALK": one draw per move
@@ -21,6 +22,15 @@
 #define PTW_TAG_CHUNGLU 0x43484C55u // "CHLU": Chung-Lu endpoints
 
 namespace ptw {
+
+// Names a host-side span for profilers (NVTX ranges; nothing is recorded
+// unless a profiler is attached).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Records msg as the calling thread's last error and returns code.
 int fail(int code, const std::string &msg);

@@ -244,6 +244,7 @@ std::shared_ptr<PinnedBlock> pinned_block(ptw_server *s, uint64_t words)
 // and releases the tables; the caller removes them from s->active.
 int collect(ptw_server *s, const std::vector<size_t> &fin)
 {
+    NvtxRange nvtx("serve_collect");
     if (fin.empty()) return PTW_OK;
     std::vector<unsigned long long> base(fin.size());
     std::vector<uint32_t> cap(fin.size());
@@ -292,6 +293,7 @@ using namespace ptw;
 
 extern "C" int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server **out)
 try {
+    NvtxRange nvtx("ptw_serve_open");
     if (!g || !cfg || !out) return fail(PTW_EINVAL, "null argument");
     *out = nullptr;
     if (!(cfg->sp >= 0.0 && cfg->sp <= 1.0)) return fail(PTW_EINVAL, "sp must be in [0, 1]");
@@ -402,6 +404,7 @@ try {
 
 extern "C" int ptw_serve_step(ptw_server *s, uint32_t *n_done, uint32_t *n_active, uint32_t *n_pending)
 try {
+    NvtxRange nvtx("ptw_serve_step");
     if (!s) return fail(PTW_EINVAL, "null server");
     PTW_CUDA(cudaSetDevice(s->g->device));
     const double t_enter = now_s(s);
