@@ -250,9 +250,10 @@ typedef struct ptw_batch_cfg {
     uint32_t max_moves;   /* 0 = unbounded */
     uint64_t table_bytes; /* device memory for the count tables of one wave; 0 = 1/4 of free */
     double table_factor;  /* hash-table slots per expected counted position; 0 = 2.  A query
-                             whose hash table would take at least 4n bytes counts into a dense
-                             array of n 32-bit counters instead; a query whose hash table fills
-                             is run again with a dense array, so results never depend on it */
+                             whose hash table would take at least 4n bytes counts into a
+                             dense array of n 32-bit counters instead; a query
+                             whose hash table fills is run again with a dense array, so results
+                             never depend on it */
     uint32_t top_k;       /* 0 = every visited vertex, by name; k > 0 = each query's k largest
                              counts, by count descending then name (selected on the device) */
     uint32_t reserved;

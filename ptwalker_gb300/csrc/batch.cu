@@ -938,11 +938,12 @@ uint64_t table_slots(double sp, uint32_t max_moves, int32_t app, double factor, 
 
 TableSize dense_table(uint32_t n) { return TableSize{((uint64_t)n + 1) / 2, true}; }
 
-TableSize count_table(double sp, uint32_t max_moves, int32_t app, double factor, uint64_t budget, uint32_t n)
+TableSize count_table(double sp, uint32_t max_moves, int32_t app, double factor, uint64_t budget, uint32_t n,
+                      uint32_t dense_ratio)
 {
     const uint64_t hash = table_slots(sp, max_moves, app, factor, budget, n);
     const TableSize d = dense_table(n);
-    if (d.slots <= hash) return d;
+    if (d.slots <= dense_ratio * hash) return d;
     return TableSize{hash, false};
 }
 
@@ -992,7 +993,10 @@ try {
         all[i].src = g->h_idx2int[p - g->h_names];
         all[i].qid = q.query_id;
         all[i].budget = q.budget;
-        const TableSize ts = count_table(cfg->sp, cfg->max_moves, cfg->app, cfg->table_factor, q.budget, n);
+        // Dense when not larger than the hash table (a cut at twice its bytes
+        // was 3% faster on the scale-22 batch but 7% slower in the serving
+        // loop's top-k compaction).
+        const TableSize ts = count_table(cfg->sp, cfg->max_moves, cfg->app, cfg->table_factor, q.budget, n, 1u);
         all[i].cap = ts.slots;
         all[i].dense = ts.dense;
     }

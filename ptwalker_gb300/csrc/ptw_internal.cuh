@@ -339,13 +339,15 @@ void trim_host_cache();
 int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned long long *h_base,
                    const uint32_t *h_cap, const uint8_t *h_dense, uint32_t nt, Compacted *out);
 // The count table of a query: an open-addressing hash table sized from its
-// budget, or, when that would take at least as many bytes, a dense array of
-// n 32-bit counters (which cannot fill).  slots = 64-bit slots it occupies.
+// budget, or, when the dense array of n 32-bit counters (which cannot fill)
+// takes at most dense_ratio times its bytes, that array.  slots = 64-bit
+// slots it occupies.
 struct TableSize {
     uint64_t slots;
     bool dense;
 };
-TableSize count_table(double sp, uint32_t max_moves, int32_t app, double factor, uint64_t budget, uint32_t n);
+TableSize count_table(double sp, uint32_t max_moves, int32_t app, double factor, uint64_t budget, uint32_t n,
+                      uint32_t dense_ratio);
 TableSize dense_table(uint32_t n);
 // Splits [j0[i], j0[i] + count[i]) of every query entry i into walker
 // descriptors {entry, first rank, count}, ordered round-robin within groups

@@ -416,7 +416,7 @@ try {
         Pending &pd = s->pending.front();
         const TableSize ts = pd.full ? dense_table(n)
                                      : count_table(s->cfg.sp, s->cfg.max_moves, s->cfg.app, s->cfg.table_factor,
-                                                   pd.q.budget, n);
+                                                   pd.q.budget, n, 1u);
         const uint64_t cap = ts.slots;
         uint64_t off = 0;
         if (!s->buddy.alloc(cap, &off)) {

@@ -71,14 +71,17 @@ def test_alone_and_in_the_mix(gpu, G16, s16_canon, use_graph):
 
 
 def test_admission_waits_for_table_memory(gpu, G16, s16_canon):
-    sp, seed = 0.25, 5
+    seed = 5
     n = G16.n
-    # Arena of 2^17 64-bit slots.  A 5000-walker query would need a 2^16-slot
-    # hash table, so it counts into a dense array of n 32-bit counters instead
-    # ((n + 1) / 2 slots, a 2^15 buddy block): four fit at once.  A 1500-walker
-    # query keeps a 2^14-slot hash table: eight fit at once.
+    # Arena of 2^17 64-bit slots.  A 5000-walker query at sp 0.25 would need a
+    # 2^16-slot hash table, so it counts into a dense array of n 32-bit
+    # counters instead ((n + 1) / 2 slots, a 2^15 buddy block): four fit at
+    # once.  A 1300-walker query at sp 0.5 keeps a 2^13-slot hash table (dense
+    # would be more than twice its size): sixteen fit at once.  Both budgets
+    # exceed a tick's smallest share (1024 walkers), so queries stay active
+    # across ticks.
     assert 2 ** 14 < (n + 1) // 2 <= 2 ** 15
-    for budget, fit, nq in ((5000, 4, 8), (1500, 8, 16)):
+    for budget, fit, nq, sp in ((5000, 4, 8, 0.25), (1300, 16, 24, 0.5)):
         with gpu.Server(G16, sp=sp, seed=seed, tick_walkers=8192, table_bytes=8 << 17) as srv:
             for k in range(nq):
                 srv.submit(100 + k, budget, k)
