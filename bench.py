@@ -266,9 +266,11 @@ def loguniform_budgets(n, lo, hi, seed):
 
 def bench_batch(args, ptw):
     """Config: R-MAT scale 22, 4096 degree-proportional sources (seed 2),
-    budgets log-uniform in [1e3, 1e6] (seed 3), sp 0.2; one timed batch
-    call after one untimed call of the same size (reported as
-    cold_seconds)."""
+    budgets log-uniform in [1e3, 1e6] (seed 3), sp 0.2; three timed batch
+    calls (seeds 7, 8, 9; the median is reported, all three are listed)
+    after one untimed call of the same size (reported as cold_seconds).
+    The copy of results to the host slows down in some calls on some hosts,
+    which a single call would report as the batch's speed."""
     import numpy as np
     G = ptw.Graph.rmat(args.batch_scale, 16, 0.57, 0.19, 0.19, seed=1, clean=True)
     src = degree_sources(G, args.batch_queries, 2)
@@ -279,16 +281,21 @@ def bench_batch(args, ptw):
     t0 = time.perf_counter()
     ptw.ppr_batch(G, src, bud, sp=0.2, seed=6).close()
     cold = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    res = ptw.ppr_batch(G, src, bud, sp=0.2, seed=7)
-    wall = time.perf_counter() - t0
+    walls, res = [], None
+    for k in range(3):
+        if res is not None:
+            res.close()
+        t0 = time.perf_counter()
+        res = ptw.ppr_batch(G, src, bud, sp=0.2, seed=7 + k)
+        walls.append(time.perf_counter() - t0)
+    wall = float(np.median(walls))
     sub = np.arange(0, args.batch_queries, max(1, args.batch_queries // 64))[:64]
     one = ptw.ppr_batch(G, src[sub], bud[sub], sp=0.2, seed=7, query_ids=sub.astype(np.uint32))
     l1 = one.l1(tol=1e-10)
     out = {"graph": "rmat-s%d" % args.batch_scale, "vertices": G.n, "edges": G.m,
            "queries": int(args.batch_queries), "walkers": int(res.walkers), "moves": int(res.moves),
            "entries": int(res.entries), "seconds": wall, "queries_per_s": args.batch_queries / wall,
-           "cold_seconds": cold,
+           "cold_seconds": cold, "seconds_each": walls,
            "steps_per_s": res.moves / wall, "device_ms": res.ms, "walk_kernel_ms": res.kernel_ms,
            "walk_kernel_steps_per_s": res.moves / (res.kernel_ms / 1000.0),
            "fp64_l1_sample": {"queries": int(len(sub)), "p50": float(np.median(l1)),
