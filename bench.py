@@ -266,10 +266,11 @@ def loguniform_budgets(n, lo, hi, seed):
 
 def bench_batch(args, ptw):
     """Config: R-MAT scale 22, 4096 degree-proportional sources (seed 2),
-    budgets log-uniform in [1e3, 1e6] (seed 3), sp 0.2; three timed batch
-    calls (seeds 7, 8, 9; the median is reported, all three are listed)
-    after one untimed call of the same size (reported as cold_seconds).
-    The copy of results to the host slows down in some calls on some hosts,
+    budgets log-uniform in [1e3, 1e6] (seed 3), sp 0.2; five timed batch
+    calls (seeds 7-11; the median is reported, all five are listed) after
+    one untimed call of the same size (reported as cold_seconds).  The copy
+    of results to the host slows down in some calls on some hosts (by
+    0.05-0.35 s, whatever the copy path, more as the host gets busier),
     which a single call would report as the batch's speed."""
     import numpy as np
     G = ptw.Graph.rmat(args.batch_scale, 16, 0.57, 0.19, 0.19, seed=1, clean=True)
@@ -282,7 +283,7 @@ def bench_batch(args, ptw):
     ptw.ppr_batch(G, src, bud, sp=0.2, seed=6).close()
     cold = time.perf_counter() - t0
     walls, res = [], None
-    for k in range(3):
+    for k in range(5):
         if res is not None:
             res.close()
         t0 = time.perf_counter()
