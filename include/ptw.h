@@ -123,7 +123,7 @@ const char *ptw_version(void);
 /* Device memory that batched queries and serving free goes back to a pool
  * that keeps up to a quarter of the device memory mapped between calls, so
  * the next call reuses it instead of mapping tens of GB again.  This hands
- * that cached memory back to the driver (after waiting for the device).  An
+ * that cached memory back to the CUDA driver (after waiting for the device).  An
  * engine allocation that finds the device full trims and retries by itself;
  * call this before allocating elsewhere in the process when memory is short.
  * The reference's MemoryPool likewise holds every allocation until the pool

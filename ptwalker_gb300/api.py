@@ -292,7 +292,7 @@ def probe_gather(array_bytes=2 << 30, chains=8):
 
 def trim_memory():
     """Hands the device memory the engine keeps cached between batched and
-    served calls back to the driver (ptw_trim_memory)."""
+    served calls back to the CUDA driver (ptw_trim_memory)."""
     C.check(C.load().ptw_trim_memory())
 
 

@@ -76,7 +76,7 @@ cudaError_t pooled_alloc_async(void **p, size_t bytes, cudaStream_t st)
             // Memory freed to the pool stays mapped up to this much across
             // synchronisations: a batch of thousands of queries allocates and
             // frees tens of GB of count tables per call, and handing them back
-            // to the driver at every synchronisation costs about 1.5 ms per GB
+            // to the CUDA driver at every synchronisation costs about 1.5 ms per GB
             // to unmap and as much again to map on the next call.
             uint64_t keep = std::max<uint64_t>(1ull << 30, (uint64_t)total_b / 4);
             e = cudaMemPoolSetAttribute(np, cudaMemPoolAttrReleaseThreshold, &keep);

@@ -258,7 +258,7 @@ int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uin
 // pool hands memory back at each one), for count tables and the short-lived
 // buffers of every result compaction.  Freed with cudaFreeAsync.
 cudaError_t pooled_alloc_async(void **p, size_t bytes, cudaStream_t st);
-// Hands the pools' cached memory back to the driver.
+// Hands the pools' cached memory back to the CUDA driver.
 void trim_pools();
 // cudaMalloc that, when the device is out of memory, trims the pools and
 // retries once.
