@@ -60,16 +60,6 @@ def test_training_on_gpu_reduces_loss(gpu):
     m.close()
 
 
-def test_budget_labels_interpolate_the_grid():
-    from ptwalker_gb300 import learned
-    grid = np.array([1000, 2000, 4000, 8000])
-    errs = np.array([[0.4, 0.28, 0.2, 0.14], [0.1, 0.07, 0.05, 0.035], [1.0, 0.9, 0.8, 0.7]])
-    lb = learned.needed_budget(errs, grid, 0.2)
-    assert abs(np.exp(lb[0]) - 4000) < 1e-6
-    assert np.exp(lb[1]) < 1000          # below the grid: extrapolated down
-    assert np.exp(lb[2]) > 8000          # above the grid: extrapolated up
-
-
 @pytest.mark.parametrize("draw", ["degree", "uniform"])
 def test_learned_budgets_vs_fixed_budget(gpu, G16, draw):
     """Held-out queries: learned budgets reach the fixed budget's

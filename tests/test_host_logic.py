@@ -1,6 +1,7 @@
 """Host-side logic on the CPU: the open-loop load generator of the serving
 layer, driven by a fake server that completes every submitted query one
-tick after it was submitted."""
+tick after it was submitted; the learned-budget labels (log-log
+interpolation of the error curve) and the sparse L1 between two results."""
 import time
 
 import numpy as np
@@ -58,3 +59,27 @@ def test_open_loop_keeps_results_with_copies():
     assert sorted(r["results"]) == list(range(n))
     assert all(r["results"][i]["source"] == i + 7 for i in range(n))
     assert all(srv.copy_flags)
+
+
+def test_budget_labels_interpolate_the_grid():
+    from ptwalker_gb300 import learned
+    grid = np.array([1000, 2000, 4000, 8000])
+    errs = np.array([[0.4, 0.28, 0.2, 0.14], [0.1, 0.07, 0.05, 0.035], [1.0, 0.9, 0.8, 0.7]])
+    lb = learned.needed_budget(errs, grid, 0.2)
+    assert abs(np.exp(lb[0]) - 4000) < 1e-6
+    assert np.exp(lb[1]) < 1000          # below the grid: extrapolated down
+    assert np.exp(lb[2]) > 8000          # above the grid: extrapolated up
+
+
+def test_sparse_l1_equals_dense_l1():
+    from ptwalker_gb300 import learned
+    rng = np.random.default_rng(5)
+    for _ in range(50):
+        n = int(rng.integers(1, 200))
+        a = rng.integers(0, 4, n) * (rng.random(n) < 0.5)
+        b = rng.integers(0, 4, n) * (rng.random(n) < 0.5)
+        na, nb = np.nonzero(a)[0].astype(np.uint32), np.nonzero(b)[0].astype(np.uint32)
+        got = learned.sparse_l1(na, a[na].astype(np.uint32), nb, b[nb].astype(np.uint32))
+        pa = a / max(a.sum(), 1)
+        pb = b / max(b.sum(), 1)
+        assert abs(got - np.abs(pa - pb).sum()) < 1e-12
