@@ -409,14 +409,17 @@ void ptw_mlp_free(ptw_mlp *m);
  * whose pool allocator owns all device memory, or a context where an
  * allocation or its implied synchronisation is not allowed).  Same results
  * as ptw_pagerank_dev: counts by name into the caller's d_counts[id_bound],
- * issued on cuda_stream (NULL = the graph's stream), asynchronous.
+ * issued on cuda_stream (NULL = the graph's stream), asynchronous.  On
+ * another stream the walk waits for work already queued on the graph's
+ * stream, and the graph's stream (so ptw_graph_free too) waits for the walk.
  * Limits: graphs of at most PTW_NOALLOC_MAX_VERTICES vertices (PTW_EINVAL
  * beyond), per-vertex or uniform starts only.  The per-vertex counters and
  * the walker cursor live in one fixed device array inside the library
  * (about 16 MiB on every GPU that loads it, held until exit).  The first call
- * on a device looks up that array's address: make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race
- * and must be serialised. */
+ * on a device looks up that array's address and creates two ordering
+ * events: make it before any stream capture, and do not call this again
+ * after cudaDeviceReset in the same process.  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised. */
 #define PTW_NOALLOC_MAX_VERTICES (1u << 22)
 int ptw_pagerank_noalloc(const ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_counts,
                          void *cuda_stream);

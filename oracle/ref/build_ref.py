@@ -10,7 +10,11 @@ CMakeLists.txt:39-58 (-O3, OpenMP, PROFILE_LEVEL=PROFILE_BRIEF) minus the
 host-specific -march=native / -mclflushopt, so the binary builds on x86_64
 and aarch64 alike.
 
-Usage: python oracle/ref/build_ref.py [--ref /path/to/reference] [--force]
+The reference tree is named by --ref or by the environment variable
+PTW_REFERENCE_DIR; without either nothing is built (an existing binary is
+still returned).
+
+Usage: python oracle/ref/build_ref.py --ref /path/to/reference [--force]
 """
 import os
 import subprocess
@@ -19,12 +23,18 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(os.path.dirname(HERE), "_ref")
 BIN = os.path.join(OUT_DIR, "ptw_ref_walk")
-DEFAULT_REF = "/root/reference"
+REF_ENV = "PTW_REFERENCE_DIR"
 
 
-def build(ref=DEFAULT_REF, force=False):
-    """Returns the binary path, or None when the reference tree is absent."""
-    if not os.path.isdir(os.path.join(ref, "src", "core")):
+def reference_dir(ref=None):
+    """The reference tree: the argument, else $PTW_REFERENCE_DIR, else None."""
+    return ref or os.environ.get(REF_ENV) or None
+
+
+def build(ref=None, force=False):
+    """Returns the binary path, or None when no reference tree is named."""
+    ref = reference_dir(ref)
+    if not ref or not os.path.isdir(os.path.join(ref, "src", "core")):
         return BIN if os.path.exists(BIN) else None
     srcs = [os.path.join(HERE, "ref_walk.cpp")]
     shim = os.path.join(HERE, "shim")
@@ -47,7 +57,7 @@ def build(ref=DEFAULT_REF, force=False):
 
 
 if __name__ == "__main__":
-    ref = DEFAULT_REF
+    ref = None
     if "--ref" in sys.argv:
         ref = sys.argv[sys.argv.index("--ref") + 1]
     print(build(ref, force="--force" in sys.argv))

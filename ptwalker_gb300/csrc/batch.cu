@@ -967,12 +967,11 @@ extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t 
                              ptw_batch **out)
 try {
     NvtxRange nvtx("ptw_ppr_batch");
-    if (!g || !cfg || !out) return fail(PTW_EINVAL, "null argument");
+    if (!cfg) return fail(PTW_EINVAL, "null argument");
+    if (const int rc0 = check_stop(cfg->sp, cfg->max_moves)) return rc0;
+    if (!g || !out) return fail(PTW_EINVAL, "null argument");
     *out = nullptr;
     if (nq && !h_queries) return fail(PTW_EINVAL, "null query table");
-    if (!(cfg->sp >= 0.0 && cfg->sp <= 1.0)) return fail(PTW_EINVAL, "sp must be in [0, 1]");
-    if (cfg->sp == 0.0 && cfg->max_moves == 0)
-        return fail(PTW_EINVAL, "sp = 0 needs max_moves > 0 (walks would never end)");
     if (cfg->app != PTW_APP_VISITS && cfg->app != PTW_APP_ENDPOINT) return fail(PTW_EINVAL, "unknown app");
     PTW_CUDA(cudaSetDevice(g->device));
     const bool timing = std::getenv("PTW_TIMING") != nullptr;
@@ -1012,7 +1011,7 @@ try {
     b->queries.assign(h_queries, h_queries + nq);
     std::vector<WaveResult> waves;
     std::vector<uint32_t> overflow;
-    const uint64_t thr = cfg->sp >= 1.0 ? (1ull << 32) : (uint64_t)(cfg->sp * 4294967296.0);
+    const uint64_t thr = stop_threshold(cfg->sp);
     uint64_t moves = 0;
     float walk_ms = 0;
     PTW_CUDA(cudaEventRecord(g->ev[3], g->stream));

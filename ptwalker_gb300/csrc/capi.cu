@@ -41,6 +41,14 @@ int host_exception()
     }
 }
 
+int check_stop(double sp, uint32_t max_moves)
+{
+    if (!(sp >= 0.0 && sp <= 1.0)) return fail(PTW_EINVAL, "sp must be in [0, 1]");
+    if (stop_threshold(sp) == 0 && max_moves == 0)
+        return fail(PTW_EINVAL, "sp below 2^-32 (sp = 0 included) needs max_moves > 0: walks would never end");
+    return PTW_OK;
+}
+
 int cuda_fail(cudaError_t e, const char *what)
 {
     const int code = (e == cudaErrorMemoryAllocation) ? PTW_ENOMEM : PTW_ECUDA;
@@ -266,14 +274,12 @@ int upload_and_build(const uint32_t *h_src, const uint32_t *h_dst, uint64_t m, b
 
 int check_cfg(const ptw_graph *g, const ptw_walk_cfg *cfg, bool needs_sp)
 {
-    if (!g) return fail(PTW_EINVAL, "null graph");
     if (!cfg) return fail(PTW_EINVAL, "null walk configuration");
-    if (needs_sp) {
-        if (!(cfg->sp >= 0.0 && cfg->sp <= 1.0))
-            return fail(PTW_EINVAL, "sp must be in [0, 1]");
-        if (cfg->sp == 0.0 && cfg->max_moves == 0)
-            return fail(PTW_EINVAL, "sp = 0 needs max_moves > 0 (walks would never end)");
+    if (needs_sp) {  // checked before the graph, so it needs no device
+        const int rc = check_stop(cfg->sp, cfg->max_moves);
+        if (rc) return rc;
     }
+    if (!g) return fail(PTW_EINVAL, "null graph");
     if (cfg->start_mode < PTW_START_PER_VERTEX || cfg->start_mode > PTW_START_SOURCES)
         return fail(PTW_EINVAL, "unknown start_mode");
     if (cfg->start_mode == PTW_START_SOURCES && (cfg->n_sources == 0 || !cfg->h_sources))
@@ -322,18 +328,12 @@ int stage_bytes(ptw_graph *g, size_t bytes, void **out)
     return PTW_OK;
 }
 
-uint64_t threshold(double sp)
-{
-    if (sp >= 1.0) return 1ull << 32;
-    return (uint64_t)(sp * 4294967296.0);
-}
-
 WalkLaunch make_launch(const ptw_walk_cfg *cfg)
 {
     WalkLaunch wl;
     wl.w_begin = cfg->first_walker;
     wl.w_end = wl.w_begin + cfg->n_walkers;
-    wl.thr = threshold(cfg->sp);
+    wl.thr = stop_threshold(cfg->sp);
     wl.seed = cfg->seed;
     wl.start_mode = cfg->start_mode;
     wl.n_sources = cfg->start_mode == PTW_START_SOURCES ? cfg->n_sources : 0;
@@ -880,7 +880,8 @@ extern "C" int ptw_autotune(ptw_graph *g, double sp, uint64_t n_walkers, ptw_tun
 try {
     NvtxRange nvtx("ptw_autotune");
     if (!g) return fail(PTW_EINVAL, "null graph");
-    if (!(sp > 0.0 && sp <= 1.0)) return fail(PTW_EINVAL, "sp must be in (0, 1]");
+    if (!(sp > 0.0 && sp <= 1.0) || stop_threshold(sp) == 0)
+        return fail(PTW_EINVAL, "sp must be in [2^-32, 1]");
     PTW_CUDA(cudaSetDevice(g->device));
     ptw_walk_cfg cfg{};
     cfg.n_walkers = n_walkers ? n_walkers : g->dg.n;

@@ -70,6 +70,21 @@ void parallel_for_threads(unsigned n, F fn)
     if (err) std::rethrow_exception(err);
 }
 
+// Stop threshold of the termination draw: a walker stops after a move iff
+// the draw's 32-bit word u satisfies u < floor(sp * 2^32); sp = 1 stops
+// after every move.
+inline uint64_t stop_threshold(double sp)
+{
+    if (sp >= 1.0) return 1ull << 32;
+    return (uint64_t)(sp * 4294967296.0);
+}
+
+// Validates a stop probability and move cap: sp in [0, 1], and a walk that
+// can end.  A threshold of 0 (sp below 2^-32, sp = 0 included) never stops
+// a walker, so without max_moves a walk on a graph whose vertices all have
+// out-edges would never return.
+int check_stop(double sp, uint32_t max_moves);
+
 #define PTW_CUDA(call)                                   \
     do {                                                 \
         cudaError_t _e = (call);                         \

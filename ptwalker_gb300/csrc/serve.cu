@@ -294,11 +294,10 @@ using namespace ptw;
 extern "C" int ptw_serve_open(ptw_graph *g, const ptw_serve_cfg *cfg, ptw_server **out)
 try {
     NvtxRange nvtx("ptw_serve_open");
-    if (!g || !cfg || !out) return fail(PTW_EINVAL, "null argument");
+    if (!cfg) return fail(PTW_EINVAL, "null argument");
+    if (const int rc0 = check_stop(cfg->sp, cfg->max_moves)) return rc0;
+    if (!g || !out) return fail(PTW_EINVAL, "null argument");
     *out = nullptr;
-    if (!(cfg->sp >= 0.0 && cfg->sp <= 1.0)) return fail(PTW_EINVAL, "sp must be in [0, 1]");
-    if (cfg->sp == 0.0 && cfg->max_moves == 0)
-        return fail(PTW_EINVAL, "sp = 0 needs max_moves > 0 (walks would never end)");
     if (cfg->app != PTW_APP_VISITS && cfg->app != PTW_APP_ENDPOINT) return fail(PTW_EINVAL, "unknown app");
     PTW_CUDA(cudaSetDevice(g->device));
     ptw_server *s = new (std::nothrow) ptw_server();
@@ -308,7 +307,7 @@ try {
     if (!s->cfg.tick_walkers) s->cfg.tick_walkers = 1ull << 23;
     if (!s->cfg.max_active) s->cfg.max_active = 4096;
     s->S = s->cfg.max_active;
-    s->thr = cfg->sp >= 1.0 ? (1ull << 32) : (uint64_t)(cfg->sp * 4294967296.0);
+    s->thr = stop_threshold(cfg->sp);
     s->t0 = std::chrono::steady_clock::now();
     uint64_t bytes = cfg->table_bytes;
     if (!bytes) {

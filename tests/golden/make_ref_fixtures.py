@@ -13,8 +13,9 @@ The reference's RNG is seeded from std::random_device, so these are one
 draw of its output; the tests compare them statistically (z-scores against
 the FP64 expectation).  Re-running this script gives different counts.
 
-Usage (from the repo root, with the reference tree present):
-    python tests/golden/make_ref_fixtures.py
+Usage (from the repo root; the reference tree is named as for
+oracle/ref/build_ref.py):
+    PTW_REFERENCE_DIR=/path/to/reference python tests/golden/make_ref_fixtures.py
 """
 import json
 import os
@@ -51,7 +52,7 @@ def run_ref(binary, path, W, sp, threads=8):
 def main():
     binary = build_ref.build()
     if binary is None:
-        raise SystemExit("reference tree not found; cannot build the reference binary")
+        raise SystemExit("no reference tree: set PTW_REFERENCE_DIR (or build with oracle/ref/build_ref.py --ref)")
     with tempfile.TemporaryDirectory() as td:
         # scale-16 R-MAT
         s, d = oracle.rmat_clean_edges(16, 16, 0.57, 0.19, 0.19, 1)

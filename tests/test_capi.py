@@ -164,3 +164,33 @@ int main() {
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(f)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_walks_that_cannot_end_are_rejected_without_gpu():
+    """A stop probability below 2^-32 (0 included) gives a stop threshold of 0:
+    without max_moves such a walk would never end on a graph whose vertices
+    all have out-edges.  Every entry point rejects it before touching a
+    graph or the device; with max_moves it passes that check (and then
+    fails on the null graph).  Nothing is launched."""
+    lib = _capi.load()
+    tiny = 2.0 ** -33
+    for sp, max_moves, ok in ((0.0, 0, False), (tiny, 0, False), (tiny, 3, True), (0.0, 3, True),
+                              (-0.1, 5, False), (1.5, 0, False)):
+        cfg = _capi.WalkCfg()
+        cfg.n_walkers, cfg.sp, cfg.max_moves = 10, sp, max_moves
+        for fn in (lambda: lib.ptw_pagerank(None, ctypes.byref(cfg), None, None),
+                   lambda: lib.ptw_pagerank_dev(None, ctypes.byref(cfg), None, None),
+                   lambda: lib.ptw_rwr(None, ctypes.byref(cfg), None, None),
+                   lambda: lib.ptw_pagerank_noalloc(None, ctypes.byref(cfg), None, None)):
+            assert fn() == _capi.PTW_EINVAL
+            err = lib.ptw_last_error()
+            assert (b"null" in err) == ok, (sp, max_moves, err)
+        bc = _capi.BatchCfg()
+        bc.sp, bc.max_moves = sp, max_moves
+        assert lib.ptw_ppr_batch(None, None, 0, ctypes.byref(bc), None) == _capi.PTW_EINVAL
+        assert (b"null" in lib.ptw_last_error()) == ok
+        sc = _capi.ServeCfg()
+        sc.sp, sc.max_moves = sp, max_moves
+        assert lib.ptw_serve_open(None, ctypes.byref(sc), None) == _capi.PTW_EINVAL
+        assert (b"null" in lib.ptw_last_error()) == ok
+    assert lib.ptw_autotune(None, tiny, 0, None) == _capi.PTW_EINVAL

@@ -1,11 +1,16 @@
 """Parity at the benchmark's own sizes.
 
-R-MAT scale 22 (2.4 M vertices, 128 M CSR entries) is small enough for the
-oracle's C pipeline to build and replay in seconds, so the GPU graph, count
-walk, DeepWalk paths and batched queries are compared with it bit for bit.
-At scale 24 (the headline workload) the checks are size-independent
-properties: every position counted once (sum of counts = walkers + moves),
-every start vertex visited, and walker shards summing to the whole run.
+R-MAT scale 22 (2.4 M vertices, 128 M CSR entries) and scale 24 (8.9 M
+vertices, 521 M CSR entries: the headline workload) are both built by the
+oracle's C pipeline in seconds and replayed on all host threads, so the GPU
+graph, full one-walker-per-vertex count walks, DeepWalk path samples and
+batched queries are compared with the replay bit for bit.  At scale 24 the
+count walk is checked under the launch configurations the bench runs (the
+autotuned one with the 8.3 GB extended column copy, and the plain-column
+alternative), and the DeepWalk samples start at walker ids above 2^23 and
+2^32 so the start map and the column offsets are exercised over the whole
+id and edge range.  Size-independent properties (every position counted
+once, walker shards summing to the whole run) are checked as well.
 """
 import os
 
@@ -13,7 +18,7 @@ import numpy as np
 import pytest
 
 import oracle
-from oracle.replay import START_PER_VERTEX, START_SOURCES
+from oracle.replay import START_PER_VERTEX, START_SOURCES, START_UNIFORM
 
 pytestmark = pytest.mark.gpu
 NT = os.cpu_count() or 1
@@ -79,19 +84,92 @@ def test_s22_batched_queries_bit_exact(gpu, s22):
         res.close()
 
 
-def test_s24_count_walk_properties(gpu):
+# Launch configurations of the scale-24 bench: the autotuned pick (block 512,
+# ILP 4, chunk 64, 8192 hot counters, L2 hints, extended columns for walks
+# and paths), the runner-up (block 1024, ILP 2, plain columns) and the
+# library default.
+S24_TUNES = {
+    "bench": dict(block=512, ilp=4, chunk=64, hot_k=8192, cache_hints=1, ext_columns=3, paths_ilp=2),
+    "plain_1024x2": dict(block=1024, ilp=2, chunk=256, hot_k=8192, cache_hints=1, ext_columns=0,
+                         paths_ilp=2, paths_named=1),
+    "default": dict(),
+}
+
+
+@pytest.fixture(scope="module")
+def s24(gpu):
+    G = gpu.Graph.rmat(24, 16, 0.57, 0.19, 0.19, seed=1, clean=True)
+    canon = oracle.rmat_clean_csr(24, 16, 0.57, 0.19, 0.19, 1, NT)
+    yield G, canon
+    G.close()
+
+
+def _set_tune(gpu, G, name):
+    G.tune = gpu.Tune(**S24_TUNES[name])
+
+
+def test_s24_graph_equals_oracle(s24):
+    G, canon = s24
+    names, row_ptr, col = G.export_csr()
+    assert G.n == canon.n and G.m == canon.m
+    assert G.m > 500_000_000 and G.n > 2 ** 23
+    assert np.array_equal(names, canon.names)
+    assert np.array_equal(row_ptr, canon.row_ptr)
+    assert np.array_equal(col, canon.col)
+
+
+@pytest.mark.parametrize("tune", sorted(S24_TUNES))
+def test_s24_pagerank_bit_exact(gpu, s24, tune):
+    """The headline workload itself: W = |V| walkers, one per vertex, sp 0.15."""
+    G, canon = s24
+    _set_tune(gpu, G, tune)
+    got, st = gpu.pagerank(G, G.n, 0.15, 41, "per_vertex", stats=True)
+    want, moves = oracle.replay_counts(canon, 0, G.n, 0.15, 41, START_PER_VERTEX, threads=NT)
+    assert st.moves == moves
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("tune", ["bench", "plain_1024x2"])
+def test_s24_uniform_starts_high_ids_bit_exact(gpu, s24, tune):
+    """Uniform starts (start vertex = mulhi(draw, n) over 8.9 M vertices) for
+    a million walkers whose ids lie above 2^32."""
+    G, canon = s24
+    _set_tune(gpu, G, tune)
+    W, w0 = 1_000_000, (1 << 32) + 12_345
+    got, st = gpu.pagerank(G, W, 0.2, 43, "uniform", first_walker=w0, stats=True)
+    want, moves = oracle.replay_counts(canon, w0, w0 + W, 0.2, 43, START_UNIFORM, threads=NT)
+    assert st.moves == moves
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("tune", ["bench", "plain_1024x2"])
+def test_s24_deepwalk_sample_bit_exact(gpu, s24, tune):
+    """L = 80 path samples of 8,192 walkers at several walker-id offsets:
+    the start, past 2^23, wrapping past |V| (per-vertex starts take the id
+    modulo |V|) and above 2^33."""
+    G, canon = s24
+    _set_tune(gpu, G, tune)
+    W, L = 8192, 80
+    for w0 in (0, 4_000_000, (1 << 23) + 777, G.n - 3000, (1 << 33) + 5):
+        got = gpu.deepwalk(G, W, L, 6, "per_vertex", first_walker=w0)
+        want = oracle.replay_paths(canon, w0, w0 + W, L, 6, START_PER_VERTEX, threads=NT)
+        assert np.array_equal(got, want), w0
+
+
+def test_s24_count_walk_properties(gpu, s24):
     import torch
-    with gpu.Graph.rmat(24, 16, 0.57, 0.19, 0.19, seed=1, clean=True) as G:
-        n = G.n
-        full = torch.empty(G.id_bound, dtype=torch.int32, device="cuda")
-        _, st = gpu.pagerank(G, n, 0.15, 77, "per_vertex", out=full, stats=True)
-        f = full.cpu().numpy().view(np.uint32)
-        assert int(f.astype(np.uint64).sum()) == n + st.moves   # every position counted once
-        assert int(f.min()) >= 1                                  # every start counted
-        # two walker shards, summed, equal the whole run
-        a = torch.empty_like(full)
-        b = torch.empty_like(full)
-        half = n // 2
-        gpu.pagerank(G, half, 0.15, 77, "per_vertex", out=a)
-        gpu.pagerank(G, n - half, 0.15, 77, "per_vertex", out=b, first_walker=half)
-        assert torch.equal(a.to(torch.int64) + b.to(torch.int64), full.to(torch.int64))
+    G, _ = s24
+    _set_tune(gpu, G, "bench")
+    n = G.n
+    full = torch.empty(G.id_bound, dtype=torch.int32, device="cuda")
+    _, st = gpu.pagerank(G, n, 0.15, 77, "per_vertex", out=full, stats=True)
+    f = full.cpu().numpy().view(np.uint32)
+    assert int(f.astype(np.uint64).sum()) == n + st.moves   # every position counted once
+    assert int(f.min()) >= 1                                  # every start counted
+    # two walker shards, summed, equal the whole run
+    a = torch.empty_like(full)
+    b = torch.empty_like(full)
+    half = n // 2
+    gpu.pagerank(G, half, 0.15, 77, "per_vertex", out=a)
+    gpu.pagerank(G, n - half, 0.15, 77, "per_vertex", out=b, first_walker=half)
+    assert torch.equal(a.to(torch.int64) + b.to(torch.int64), full.to(torch.int64))
