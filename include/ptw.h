@@ -256,10 +256,31 @@ typedef struct ptw_batch_cfg {
                              never depend on it */
     uint32_t top_k;       /* 0 = every visited vertex, by name; k > 0 = each query's k largest
                              counts, by count descending then name (selected on the device) */
-    uint32_t reserved;
+    uint32_t flags;       /* PTW_BATCH_* bits */
 } ptw_batch_cfg;
 
+/* The result lists stay in device memory for a GPU consumer (no copy to the
+ * host): read them with ptw_batch_view_device; ptw_batch_export copies them
+ * to the host on demand. */
+#define PTW_BATCH_DEVICE_RESULTS 1u
+
 typedef struct ptw_batch ptw_batch; /* the sparse results of one batch (host memory) */
+
+/* Launch parameters of the batched walker kernel (ptw_ppr_batch only; the
+ * serving loop keeps the defaults).  Zero fields take the defaults. */
+typedef struct ptw_batch_tune {
+    uint32_t desc_walkers;  /* walker ranks per work descriptor, 32 .. 65536; 0 = 256 */
+    uint32_t blocks_per_sm; /* walker-kernel blocks (256 threads) per SM; 0 = as many as fit */
+    uint64_t group_bytes;   /* descriptors interleave over groups of consecutive queries whose
+                               count tables add up to about this many bytes, group after group;
+                               0 = 384 MiB; UINT64_MAX = all queries in one group */
+    uint32_t dense_ratio;   /* a query counts into a dense array of n counters when that takes
+                               at most this many times its hash table's bytes; 0 = 1 */
+    int32_t ext_columns;    /* 1 = walk the extended column copy, 2 = the plain columns,
+                               0 = as bit 0 of the graph's walk tune */
+} ptw_batch_tune;
+int ptw_graph_set_batch_tune(ptw_graph *g, const ptw_batch_tune *t);
+int ptw_graph_get_batch_tune(const ptw_graph *g, ptw_batch_tune *t);
 
 /* Runs nq queries: the reference runs one source per process
  * (src/core/ppr.cpp:121-138 hard-codes internal id 0); here a device query
@@ -277,11 +298,40 @@ int ptw_batch_export(const ptw_batch *b, uint64_t *h_offsets, uint32_t *h_names,
  * valid until ptw_batch_free. */
 int ptw_batch_view(const ptw_batch *b, const uint64_t **offsets, const uint32_t **names,
                    const uint32_t **counts);
+/* Device pointers of a batch run with PTW_BATCH_DEVICE_RESULTS: d_offsets
+ * [nq + 1] (uint64), d_names / d_counts [entries], valid until
+ * ptw_batch_free.  PTW_EINVAL for a batch whose results are on the host.
+ * (ptw_batch_view of such a batch returns the host offsets and NULL lists.) */
+int ptw_batch_view_device(const ptw_batch *b, const uint64_t **d_offsets, const uint32_t **d_names,
+                          const uint32_t **d_counts);
+
+/* Where the time of a batch call went.  Device phases are CUDA-event
+ * intervals on the call's streams, summed over waves; host phases are wall
+ * clock.  No counterpart in the reference. */
+typedef struct ptw_batch_phases {
+    double call_ms;        /* host: the whole ptw_ppr_batch call */
+    double plan_ms;        /* host: query table and walker descriptors */
+    double device_ms;      /* device: first upload to the last result copy */
+    double upload_ms;      /* device: query table and descriptor uploads, count-table clear */
+    double walk_ms;        /* device: the walker kernel */
+    double count_ms;       /* device: compaction pass 1 (entries per chunk and table) and its scans */
+    double place_ms;       /* device: compaction pass 2, hash-table sorts and placement (or top-k) */
+    double copy_ms;        /* device: result copies to the host, summed over copies */
+    double copy_tail_ms;   /* device: end of the last compaction kernel to the end of the last copy */
+    double host_pages_ms;  /* host: waiting for result pages to be faulted in / page-locked */
+    uint64_t copy_bytes;   /* bytes copied device -> host */
+    uint32_t waves;        /* walker launches (waves, plus reruns of overflowed queries) */
+    uint32_t reruns;       /* queries rerun with a dense array after their hash table filled */
+} ptw_batch_phases;
+int ptw_batch_get_phases(const ptw_batch *b, ptw_batch_phases *out);
+
 /* Frees a batch.  Its host result arrays (when large) are kept, already
  * faulted in and page-locked, for the next batch's results (one pair, up
  * to 32 GB); ptw_trim_memory hands them back.  Large result arrays are
  * page-locked while the device walks (within a quarter of the host memory
- * for all of them), so their copies from the device run at a steady rate. */
+ * for all of them), so their copies from the device run at a steady rate.
+ * Device-resident results go back to the library's memory pool at once:
+ * finish (synchronise) every read of them first. */
 void ptw_batch_free(ptw_batch *b);
 
 /* FP64 oracle on the device: for each source name, the exact expected count
@@ -423,6 +473,17 @@ void ptw_mlp_free(ptw_mlp *m);
 #define PTW_NOALLOC_MAX_VERTICES (1u << 22)
 int ptw_pagerank_noalloc(const ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_counts,
                          void *cuda_stream);
+
+/* Autotuner of the batched kernel (the idea of the reference's per-setting
+ * step-cost cache, src/core/mini_bmk.hpp:62-117): runs the caller's batch
+ * (q, nq, cfg; results kept on the device and discarded) under candidate
+ * ptw_batch_tune values and times the device phases from the first upload
+ * to the end of compaction.  Descriptor size x group bytes first, then
+ * blocks per SM x dense ratio x column layout around the best, then the
+ * three fastest again in interleaved rounds.  Stores the fastest in the
+ * graph and returns it; *best_ms (may be NULL) gets its median time. */
+int ptw_autotune_batch(ptw_graph *g, const ptw_query *q, uint32_t nq, const ptw_batch_cfg *cfg,
+                       ptw_batch_tune *best, double *best_ms);
 
 /* Autotuner (the idea of the sampler micro-benchmark cache,
  * src/core/mini_bmk.hpp:62-117): times the count walk over candidate

@@ -52,7 +52,24 @@ class Query(ctypes.Structure):
 class BatchCfg(ctypes.Structure):
     _fields_ = [("sp", ctypes.c_double), ("seed", ctypes.c_uint64), ("app", ctypes.c_int32),
                 ("max_moves", ctypes.c_uint32), ("table_bytes", ctypes.c_uint64),
-                ("table_factor", ctypes.c_double), ("top_k", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("table_factor", ctypes.c_double), ("top_k", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
+
+
+PTW_BATCH_DEVICE_RESULTS = 1
+
+
+class BatchPhases(ctypes.Structure):
+    _fields_ = [("call_ms", ctypes.c_double), ("plan_ms", ctypes.c_double), ("device_ms", ctypes.c_double),
+                ("upload_ms", ctypes.c_double), ("walk_ms", ctypes.c_double), ("count_ms", ctypes.c_double),
+                ("place_ms", ctypes.c_double), ("copy_ms", ctypes.c_double), ("copy_tail_ms", ctypes.c_double),
+                ("host_pages_ms", ctypes.c_double), ("copy_bytes", ctypes.c_uint64), ("waves", ctypes.c_uint32),
+                ("reruns", ctypes.c_uint32)]
+
+
+class BatchTune(ctypes.Structure):
+    _fields_ = [("desc_walkers", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
+                ("group_bytes", ctypes.c_uint64), ("dense_ratio", ctypes.c_uint32),
+                ("ext_columns", ctypes.c_int32)]
 
 
 class ServeStats(ctypes.Structure):
@@ -137,6 +154,13 @@ SIGNATURES = [
     ("ptw_batch_view", ctypes.c_int, [_G, ctypes.POINTER(_u64p), ctypes.POINTER(_u32p),
                                       ctypes.POINTER(_u32p)]),
     ("ptw_batch_free", None, [_G]),
+    ("ptw_batch_view_device", ctypes.c_int, [_G, ctypes.POINTER(_u64p), ctypes.POINTER(_u32p),
+                                             ctypes.POINTER(_u32p)]),
+    ("ptw_batch_get_phases", ctypes.c_int, [_G, ctypes.POINTER(BatchPhases)]),
+    ("ptw_graph_set_batch_tune", ctypes.c_int, [_G, ctypes.POINTER(BatchTune)]),
+    ("ptw_graph_get_batch_tune", ctypes.c_int, [_G, ctypes.POINTER(BatchTune)]),
+    ("ptw_autotune_batch", ctypes.c_int, [_G, ctypes.POINTER(Query), ctypes.c_uint32, ctypes.POINTER(BatchCfg),
+                                          ctypes.POINTER(BatchTune), ctypes.POINTER(ctypes.c_double)]),
     ("ptw_batch_l1", ctypes.c_int, [_G, _G, ctypes.c_double, ctypes.c_int32, ctypes.c_double,
                                     ctypes.POINTER(ctypes.c_double)]),
     ("ptw_serve_open", ctypes.c_int, [_G, ctypes.POINTER(ServeCfg), _GP]),

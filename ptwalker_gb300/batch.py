@@ -13,11 +13,60 @@ from . import _capi as C
 
 APPS = {"visits": C.PTW_APP_VISITS, "endpoint": C.PTW_APP_ENDPOINT}
 
+PHASE_FIELDS = [f for f, _ in C.BatchPhases._fields_]
+
+
+class _DeviceArray:
+    """A device array the library owns, exposed through the CUDA array
+    interface so torch.as_tensor wraps it without a copy."""
+
+    def __init__(self, ptr, n, typestr):
+        self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 2}
+
+
+class BatchTune:
+    """Launch parameters of the batched walker kernel (ptw_batch_tune)."""
+
+    FIELDS = [f for f, _ in C.BatchTune._fields_]
+
+    def __init__(self, desc_walkers=0, blocks_per_sm=0, group_bytes=0, dense_ratio=0, ext_columns=0):
+        self.desc_walkers, self.blocks_per_sm, self.group_bytes = desc_walkers, blocks_per_sm, group_bytes
+        self.dense_ratio, self.ext_columns = dense_ratio, ext_columns
+
+    def to_c(self):
+        return C.BatchTune(int(self.desc_walkers), int(self.blocks_per_sm), int(self.group_bytes),
+                           int(self.dense_ratio), int(self.ext_columns))
+
+    @classmethod
+    def from_c(cls, t):
+        return cls(t.desc_walkers, t.blocks_per_sm, t.group_bytes, t.dense_ratio, t.ext_columns)
+
+    def as_dict(self):
+        return {f: int(getattr(self, f)) for f in self.FIELDS}
+
+    def __repr__(self):
+        return "BatchTune(%s)" % ", ".join("%s=%s" % kv for kv in self.as_dict().items())
+
+
+def get_batch_tune(graph):
+    t = C.BatchTune()
+    C.check(graph._lib.ptw_graph_get_batch_tune(graph.handle, ctypes.byref(t)))
+    return BatchTune.from_c(t)
+
+
+def set_batch_tune(graph, tune):
+    t = tune.to_c()
+    C.check(graph._lib.ptw_graph_set_batch_tune(graph.handle, ctypes.byref(t)))
+
 
 class BatchResult:
-    """Sparse per-query results, held in host memory by the library."""
+    """Sparse per-query results, held in host memory by the library (or, for
+    a batch run with device_results=True, in device memory: d_offsets,
+    d_names and d_counts are then zero-copy torch views of it and names /
+    counts are None)."""
 
-    def __init__(self, graph, handle, sources, budgets, query_ids, sp, app):
+    def __init__(self, graph, handle, sources, budgets, query_ids, sp, app, device_results=False):
         self._lib = C.load()
         self._h = handle
         self.graph = graph
@@ -39,7 +88,21 @@ class BatchResult:
         pc = ctypes.POINTER(ctypes.c_uint32)()
         C.check(self._lib.ptw_batch_view(self._h, ctypes.byref(po), ctypes.byref(pn), ctypes.byref(pc)))
         self.offsets = np.ctypeslib.as_array(po, shape=(self.nq + 1,))
-        if self.entries:
+        self.device_results = device_results
+        self.d_offsets = self.d_names = self.d_counts = None
+        if device_results:
+            import torch
+            C.check(self._lib.ptw_batch_view_device(self._h, ctypes.byref(po), ctypes.byref(pn),
+                                                    ctypes.byref(pc)))
+            self.d_offsets = torch.as_tensor(_DeviceArray(ctypes.addressof(po.contents), self.nq + 1, "<u8"),
+                                             device="cuda")
+            if self.entries:
+                self.d_names = torch.as_tensor(_DeviceArray(ctypes.addressof(pn.contents), self.entries, "<u4"),
+                                               device="cuda")
+                self.d_counts = torch.as_tensor(_DeviceArray(ctypes.addressof(pc.contents), self.entries, "<u4"),
+                                                device="cuda")
+            self.names = self.counts = None
+        elif self.entries:
             self.names = np.ctypeslib.as_array(pn, shape=(self.entries,))
             self.counts = np.ctypeslib.as_array(pc, shape=(self.entries,))
         else:
@@ -48,7 +111,28 @@ class BatchResult:
 
     def query(self, i):
         a, b = int(self.offsets[i]), int(self.offsets[i + 1])
+        if self.device_results:
+            if b == a:
+                return np.empty(0, dtype=np.uint32), np.empty(0, dtype=np.uint32)
+            return (self.d_names[a:b].cpu().numpy().view(np.uint32),
+                    self.d_counts[a:b].cpu().numpy().view(np.uint32))
         return self.names[a:b], self.counts[a:b]
+
+    def export(self):
+        """(offsets, names, counts) copied into new host arrays (ptw_batch_export)."""
+        off = np.empty(self.nq + 1, dtype=np.uint64)
+        names = np.empty(self.entries, dtype=np.uint32)
+        counts = np.empty(self.entries, dtype=np.uint32)
+        C.check(self._lib.ptw_batch_export(self._h, off.ctypes.data_as(C._u64p), names.ctypes.data_as(C._u32p),
+                                           counts.ctypes.data_as(C._u32p)))
+        return off, names, counts
+
+    def phases(self):
+        """Where the call's time went (ptw_batch_get_phases): device phases
+        from CUDA events, host phases from the wall clock; milliseconds."""
+        p = C.BatchPhases()
+        C.check(self._lib.ptw_batch_get_phases(self._h, ctypes.byref(p)))
+        return {f: (float(getattr(p, f)) if f.endswith("_ms") else int(getattr(p, f))) for f in PHASE_FIELDS}
 
     def dense(self, i, size=None):
         names, counts = self.query(i)
@@ -68,6 +152,7 @@ class BatchResult:
         """Frees the results; the arrays of this object are no longer valid."""
         if self._h:
             self.offsets = self.names = self.counts = None
+            self.d_offsets = self.d_names = self.d_counts = None
             self._lib.ptw_batch_free(self._h)
             self._h = None
 
@@ -78,8 +163,36 @@ class BatchResult:
             pass
 
 
+def _queries(sources, budgets, query_ids):
+    sources = np.atleast_1d(np.asarray(sources, dtype=np.uint32))
+    budgets = np.broadcast_to(np.asarray(budgets, dtype=np.uint64), sources.shape).copy()
+    if query_ids is None:
+        query_ids = np.arange(sources.shape[0], dtype=np.uint32)
+    query_ids = np.asarray(query_ids, dtype=np.uint32)
+    nq = sources.shape[0]
+    qs = (C.Query * max(nq, 1))()
+    for i in range(nq):
+        qs[i].source = int(sources[i])
+        qs[i].query_id = int(query_ids[i])
+        qs[i].budget = int(budgets[i])
+    return sources, budgets, query_ids, qs
+
+
+def autotune_batch(graph, sources, budgets, sp=0.2, seed=0, app="visits", query_ids=None, max_moves=0,
+                   top_k=0):
+    """Times this batch under candidate BatchTune values (ptw_autotune_batch),
+    keeps the fastest in the graph; returns (tune, median device ms)."""
+    sources, budgets, query_ids, qs = _queries(sources, budgets, query_ids)
+    cfg = C.BatchCfg(float(sp), int(seed) & 0xFFFFFFFFFFFFFFFF, APPS[app], int(max_moves), 0, 0.0, int(top_k), 0)
+    t = C.BatchTune()
+    ms = ctypes.c_double()
+    C.check(graph._lib.ptw_autotune_batch(graph.handle, qs, sources.shape[0], ctypes.byref(cfg), ctypes.byref(t),
+                                          ctypes.byref(ms)))
+    return BatchTune.from_c(t), float(ms.value)
+
+
 def ppr_batch(graph, sources, budgets, sp=0.2, seed=0, app="visits", query_ids=None, max_moves=0,
-              table_bytes=0, table_factor=0.0, top_k=0):
+              table_bytes=0, table_factor=0.0, top_k=0, device_results=False):
     sources = np.atleast_1d(np.asarray(sources, dtype=np.uint32))
     budgets = np.broadcast_to(np.asarray(budgets, dtype=np.uint64), sources.shape).copy()
     if query_ids is None:
@@ -92,7 +205,8 @@ def ppr_batch(graph, sources, budgets, sp=0.2, seed=0, app="visits", query_ids=N
         qs[i].query_id = int(query_ids[i])
         qs[i].budget = int(budgets[i])
     cfg = C.BatchCfg(float(sp), int(seed) & 0xFFFFFFFFFFFFFFFF, APPS[app], int(max_moves),
-                     int(table_bytes), float(table_factor), int(top_k))
+                     int(table_bytes), float(table_factor), int(top_k),
+                     C.PTW_BATCH_DEVICE_RESULTS if device_results else 0)
     h = ctypes.c_void_p()
     C.check(graph._lib.ptw_ppr_batch(graph.handle, qs, nq, ctypes.byref(cfg), ctypes.byref(h)))
-    return BatchResult(graph, h, sources, budgets, query_ids, sp, app)
+    return BatchResult(graph, h, sources, budgets, query_ids, sp, app, device_results=device_results)

@@ -52,6 +52,12 @@ struct ptw_batch {
     bool buf_pinned = false;                // page-locked
     ptw_walk_stats stats{};
     uint32_t top_k = 0;  // results hold each query's top_k largest counts only
+    // Device-resident results (PTW_BATCH_DEVICE_RESULTS): lists and offsets
+    // in the library's device pool instead of names / counts.
+    bool device = false;
+    int device_id = 0;
+    ptw::PoolArray d_names, d_counts, d_offsets;  // d_offsets holds nq + 1 uint64 (as 2 words each)
+    ptw_batch_phases phases{};
 };
 
 namespace ptw {
@@ -67,9 +73,81 @@ struct WaveResult {
 }  // namespace ptw
 
 namespace ptw {
+
+int PhaseTimer::begin(int phase, cudaStream_t s)
+{
+    Span sp{phase, nullptr, nullptr};
+    if (cudaEventCreate(&sp.a) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    if (cudaEventCreate(&sp.b) != cudaSuccess) {
+        cudaGetLastError();
+        cudaEventDestroy(sp.a);
+        return -1;
+    }
+    if (cudaEventRecord(sp.a, s) != cudaSuccess) cudaGetLastError();
+    spans.push_back(sp);
+    return (int)spans.size() - 1;
+}
+
+void PhaseTimer::end(int span, cudaStream_t s)
+{
+    if (span < 0) return;
+    if (cudaEventRecord(spans[span].b, s) != cudaSuccess) cudaGetLastError();
+    if (spans[span].phase == kPlace) last_place = span;
+    if (spans[span].phase == kCopy) last_copy = span;
+}
+
+void PhaseTimer::sums(double out[kPhases], double *copy_tail_ms) const
+{
+    for (int k = 0; k < kPhases; ++k) out[k] = 0;
+    for (const Span &sp : spans) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, sp.a, sp.b) == cudaSuccess) out[sp.phase] += ms;
+        else cudaGetLastError();
+    }
+    *copy_tail_ms = 0;
+    if (last_place >= 0 && last_copy >= 0) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, spans[last_place].b, spans[last_copy].b) == cudaSuccess)
+            *copy_tail_ms = std::max(0.0f, ms);
+        else
+            cudaGetLastError();
+    }
+}
+
+PhaseTimer::~PhaseTimer()
+{
+    for (Span &sp : spans) {
+        cudaEventDestroy(sp.a);
+        cudaEventDestroy(sp.b);
+    }
+}
+
 namespace {
 
 constexpr uint64_t kMaxBudget = 1ull << 28;
+
+// Effective batch launch parameters (zero fields of ptw_batch_tune take the
+// defaults).
+struct BatchTune {
+    uint32_t desc_walkers, blocks_per_sm, dense_ratio;
+    uint64_t group_bytes;
+    bool ext;
+};
+
+BatchTune effective_tune(const ptw_graph *g)
+{
+    const ptw_batch_tune &t = g->btune;
+    BatchTune e;
+    e.desc_walkers = t.desc_walkers ? t.desc_walkers : kDescWalkers;
+    e.blocks_per_sm = t.blocks_per_sm;
+    e.dense_ratio = t.dense_ratio ? t.dense_ratio : 1u;
+    e.group_bytes = t.group_bytes == 0 ? kGroupBytes : t.group_bytes == ~0ull ? 0ull : t.group_bytes;
+    e.ext = t.ext_columns == 1 ? true : t.ext_columns == 2 ? false : (g->tune.ext_columns & 1) != 0;
+    return e;
+}
 
 // Faults in the pages of fresh host buffers from several threads.  A
 // device-to-host copy into pages the process has never touched takes the
@@ -287,7 +365,7 @@ struct WaveQuery {
 }  // namespace
 
 // Splits [j0, j0 + count) of every entry into descriptors of at most
-// kDescWalkers ranks.  Entries are cut into consecutive groups whose tables
+// dw ranks.  Entries are cut into consecutive groups whose tables
 // add up to about group_bytes (0 = one group); descriptors go round-robin
 // over the entries of a group, and groups follow one another.  Warps take
 // descriptors in order, so the count tables being written at any moment are
@@ -296,7 +374,7 @@ struct WaveQuery {
 // on 4096 queries at R-MAT scale 22 with 384 MB groups).
 uint64_t interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<uint64_t> &count,
                                 const std::vector<uint64_t> &table_bytes, uint64_t group_bytes,
-                                std::unique_ptr<uint3[]> &desc, unsigned threads)
+                                std::unique_ptr<uint3[]> &desc, unsigned threads, uint32_t dw)
 {
     const uint32_t ne = (uint32_t)count.size();
     std::vector<uint32_t> gb;  // first entry of each group, then ne
@@ -315,7 +393,7 @@ uint64_t interleave_descriptors(const std::vector<uint64_t> &j0, const std::vect
     std::vector<uint64_t> goff(ng + 1, 0);  // first descriptor of each group
     for (size_t k = 0; k < ng; ++k) {
         uint64_t d = 0;
-        for (uint32_t i = gb[k]; i < gb[k + 1]; ++i) d += (count[i] + kDescWalkers - 1) / kDescWalkers;
+        for (uint32_t i = gb[k]; i < gb[k + 1]; ++i) d += (count[i] + dw - 1) / dw;
         goff[k + 1] = goff[k] + d;
     }
     desc.reset(new uint3[std::max<uint64_t>(goff[ng], 1)]);  // not value-initialised
@@ -327,9 +405,9 @@ uint64_t interleave_descriptors(const std::vector<uint64_t> &j0, const std::vect
         uint3 *o = out + goff[k];
         for (uint64_t r = 0; !live.empty(); ++r) {
             size_t keep = 0;
-            const uint64_t off = r * kDescWalkers;
+            const uint64_t off = r * dw;
             for (uint32_t i : live) {
-                const uint64_t c = std::min<uint64_t>(kDescWalkers, count[i] - off);
+                const uint64_t c = std::min<uint64_t>(dw, count[i] - off);
                 *o++ = make_uint3(i, (uint32_t)(j0[i] + off), (uint32_t)c);
                 if (off + c < count[i]) live[keep++] = i;
             }
@@ -354,7 +432,7 @@ void interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<u
                             std::vector<uint3> &desc)
 {
     std::unique_ptr<uint3[]> buf;
-    const uint64_t n = interleave_descriptors(j0, count, table_bytes, group_bytes, buf, 1);
+    const uint64_t n = interleave_descriptors(j0, count, table_bytes, group_bytes, buf, 1, kDescWalkers);
     desc.assign(buf.get(), buf.get() + n);
 }
 
@@ -363,14 +441,16 @@ namespace {
 // Runs one wave; stores each query's sorted entries in per-query host lists.
 int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg *cfg, uint64_t thr,
              std::vector<WaveResult> &waves, std::vector<uint32_t> &overflow, uint64_t *moves_out,
-             float *walk_ms)
+             float *walk_ms, PhaseTimer *ph)
 {
     NvtxRange nvtx("run_wave");
     cudaStream_t st = g->stream;
     const uint32_t nq = (uint32_t)wq.size();
+    const BatchTune bt = effective_tune(g);
+    const bool device_results = (cfg->flags & PTW_BATCH_DEVICE_RESULTS) != 0;
     const bool timing = std::getenv("PTW_TIMING") != nullptr;
     auto clk = [] { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
-    const double t_enter = timing ? clk() : 0.0;
+    const double t_enter = clk();
     double t_plan = 0, t_setup = 0;
     std::vector<unsigned long long> h_tab(nq + 1);
     std::vector<uint32_t> h_src(nq), h_qid(nq), h_mask(nq), h_cap(nq);
@@ -388,10 +468,13 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     std::unique_ptr<uint3[]> h_desc;
     std::vector<uint64_t> tbytes(nq);
     for (uint32_t i = 0; i < nq; ++i) tbytes[i] = wq[i].cap * 8;
-    const uint64_t nd = interleave_descriptors(j0, cnt, tbytes, kGroupBytes, h_desc,
-                                               std::min(16u, std::max(1u, std::thread::hardware_concurrency())));
-    if (timing) t_plan = clk();
+    const uint64_t nd = interleave_descriptors(j0, cnt, tbytes, bt.group_bytes, h_desc,
+                                               std::min(16u, std::max(1u, std::thread::hardware_concurrency())),
+                                               bt.desc_walkers);
+    t_plan = clk();
+    ph->plan_ms += 1e3 * (t_plan - t_enter);
     const uint64_t n_slots = h_tab[nq];
+    const int sp_up = ph->begin(PhaseTimer::kUpload, st);
     DevBuf db(st);
     unsigned long long *d_tab, *d_slots, *d_ctrl;
     uint32_t *d_src, *d_qid, *d_mask, *d_flag;
@@ -412,6 +495,7 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     PTW_CUDA(cudaMemsetAsync(d_flag, 0, nq * 4ull, st));
     PTW_CUDA(cudaMemsetAsync(d_ctrl, 0, 16, st));
     PTW_CUDA(cudaMemsetAsync(d_slots, 0, n_slots * 8, st));
+    ph->end(sp_up, st);
     if (timing) {
         PTW_CUDA(cudaStreamSynchronize(st));
         t_setup = clk();
@@ -420,7 +504,7 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     BatchArgs a;
     a.adj = g->dg.adj;
     a.col = g->dg.col;
-    const bool ext = (g->tune.ext_columns & 1) && ensure_ext_columns(g);
+    const bool ext = bt.ext && ensure_ext_columns(g);
     a.col_ext = g->dg.col_ext;
     a.int2idx = g->dg.int2idx;
     a.ext_idx = g->dg.id_bound == g->dg.n ? 1u : 0u;  // names 0..n-1
@@ -442,7 +526,9 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     int per_sm = 0;
     const void *kfn = ext ? (const void *)k_batch<true> : (const void *)k_batch<false>;
     PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 256, 0));
-    uint64_t grid = (uint64_t)g->num_sms * std::max(per_sm, 1);
+    per_sm = std::max(per_sm, 1);
+    if (bt.blocks_per_sm) per_sm = std::min<int>(per_sm, (int)bt.blocks_per_sm);
+    uint64_t grid = (uint64_t)g->num_sms * per_sm;
     grid = std::min<uint64_t>(grid, std::max<uint64_t>(1, (nd + 7) / 8));
     // Full lists: host buffers of an estimated size are faulted in on host
     // threads while the walk runs (about 1.1 distinct entries per walker on
@@ -450,8 +536,10 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     // fit.
     WaveResult wr;
     wr.c.top_k = cfg->top_k;
+    wr.c.device = device_results;
+    wr.c.ph = ph;
     Prefault early;
-    if (cfg->top_k == 0) {
+    if (cfg->top_k == 0 && !device_results) {
         uint64_t est = 0;
         for (uint32_t i = 0; i < nq; ++i)
             est += std::min<uint64_t>(g->dg.n, (uint64_t)(1.5 * (double)wq[i].budget) + 64);
@@ -496,10 +584,12 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
         }
     }
     PTW_CUDA(cudaEventRecord(g->ev[0], st));
+    const int sp_walk = ph->begin(PhaseTimer::kWalk, st);
     {
         void *kargs[] = {&a};
         PTW_CUDA(cudaLaunchKernel(kfn, dim3((unsigned)grid), dim3(256), kargs, 0, st));
     }
+    ph->end(sp_walk, st);
     PTW_CUDA(cudaEventRecord(g->ev[1], st));
     PTW_CUDA(cudaGetLastError());
     std::vector<uint32_t> h_flag(nq);
@@ -537,7 +627,9 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
 
 // Concatenates the waves' entries in caller query order.  One wave holding
 // every query in order (the common case) is adopted without a copy.
-int assemble(ptw_batch *b, std::vector<WaveResult> &waves)
+// Device-resident results are concatenated on the device (one copy per
+// query segment when there is more than one wave).
+int assemble(ptw_graph *g, ptw_batch *b, std::vector<WaveResult> &waves)
 {
     const uint32_t nq = b->nq;
     std::vector<const WaveResult *> src_w(nq, nullptr);
@@ -558,6 +650,29 @@ int assemble(ptw_batch *b, std::vector<WaveResult> &waves)
     bool adopt = waves.size() == 1 && waves[0].idx.size() == nq;
     if (adopt)
         for (uint32_t k = 0; k < nq; ++k) adopt = adopt && waves[0].idx[k] == k && !waves[0].overflow[k];
+    if (b->device) {
+        cudaStream_t st = g->stream;
+        if (adopt) {
+            b->d_names = std::move(waves[0].c.d_names);
+            b->d_counts = std::move(waves[0].c.d_counts);
+        } else if (total) {
+            PTW_CUDA(b->d_names.alloc(total, st));
+            PTW_CUDA(b->d_counts.alloc(total, st));
+            for (uint32_t i = 0; i < nq; ++i) {
+                const WaveResult *w = src_w[i];
+                const uint64_t len = b->offsets[i + 1] - b->offsets[i];
+                if (!w || !len) continue;
+                const uint64_t a = w->c.seg[src_i[i]];
+                PTW_CUDA(cudaMemcpyAsync(b->d_names.p + b->offsets[i], w->c.d_names.p + a, len * 4,
+                                         cudaMemcpyDeviceToDevice, st));
+                PTW_CUDA(cudaMemcpyAsync(b->d_counts.p + b->offsets[i], w->c.d_counts.p + a, len * 4,
+                                         cudaMemcpyDeviceToDevice, st));
+            }
+        }
+        PTW_CUDA(b->d_offsets.alloc(2ull * (nq + 1), st));
+        PTW_CUDA(cudaMemcpyAsync(b->d_offsets.p, b->offsets.data(), (nq + 1) * 8ull, cudaMemcpyHostToDevice, st));
+        return PTW_OK;
+    }
     if (adopt) {
         b->names = std::move(waves[0].c.names);
         b->counts = std::move(waves[0].c.counts);
@@ -608,6 +723,13 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     auto clk = [] { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
     const double t0 = timing ? (cudaStreamSynchronize(st), clk()) : 0.0;
     double t1 = 0, t2 = 0, t_join = 0;
+    PhaseTimer no_timer;
+    PhaseTimer *ph = out->ph ? out->ph : &no_timer;
+    struct PagesWait {  // host time spent waiting for result pages, added up on every return
+        PhaseTimer *ph;
+        double &ms;
+        ~PagesWait() { ph->host_pages_ms += 1e3 * ms; }
+    } pages_wait{ph, t_join};
     Prefault prefault;  // joined before the copies (and on any early return)
     std::vector<uint8_t> dense_flags(nt, 0);
     if (h_dense) dense_flags.assign(h_dense, h_dense + nt);
@@ -637,6 +759,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     const uint64_t npc = nch * 8;  // warp pieces: 8 per chunk
     PTW_CUDA(db.alloc(&d_cc, std::max<uint64_t>(npc, 1)));
     PTW_CUDA(db.alloc(&d_hc, std::max<uint64_t>(npc, 1)));
+    const int sp_count = ph->begin(PhaseTimer::kCount, st);
     PTW_CUDA(cudaMemcpyAsync(d_base, h_base, nt * 8ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_cap, h_cap, nt * 4ull, cudaMemcpyHostToDevice, st));
     PTW_CUDA(cudaMemcpyAsync(d_dense, dense_flags.data(), nt, cudaMemcpyHostToDevice, st));
@@ -671,6 +794,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             return cub::DeviceScan::ExclusiveSum(t, b, d_hc, d_hpos, (int64_t)npc, st);
         }, st));
     }
+    ph->end(sp_count, st);
     PTW_CUDA(cudaStreamSynchronize(st));
     const uint64_t n_ent = out->seg[nt];
     // top-k: every table keeps its min(k, entries) largest counts
@@ -685,7 +809,12 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
     out->n = n_out;
     if (n_ent) {
         bool dst_pinned = false;  // the host lists are page-locked: copies run asynchronously
-        if (out->sink) {
+        if (out->device) {
+            // the lists stay on the device: no host buffers, no copies
+            if (out->pre_join) out->pre_join();
+            out->pre_names.reset();
+            out->pre_counts.reset();
+        } else if (out->sink) {
             uint32_t *base = out->sink(n_out);
             if (!base) return fail(PTW_ENOMEM, "host staging of results failed");
             out->h_names = base;
@@ -693,9 +822,9 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             dst_pinned = true;  // the sink hands out page-locked staging
         } else if (out->pre_names && n_out <= out->pre_cap) {
             // the buffers faulted in during the walk hold the lists
-            const double tj = timing ? clk() : 0.0;
+            const double tj = clk();
             out->pre_join();
-            if (timing) t_join = clk() - tj;
+            t_join = clk() - tj;
             out->names = std::move(out->pre_names);
             out->counts = std::move(out->pre_counts);
             out->h_names = out->names.get();
@@ -722,6 +851,20 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             out->cap = out->touched = n_out;
             prefault.start({{out->h_names, n_out * 4}, {out->h_counts, n_out * 4}});
         }
+        // The output lists: scratch of this call, or, for device-resident
+        // results, arrays the results keep.
+        auto alloc_out = [&](uint32_t **name, uint32_t **cnt, uint64_t count) -> cudaError_t {
+            if (!out->device) {
+                cudaError_t e = db.alloc(name, count);
+                return e != cudaSuccess ? e : db.alloc(cnt, count);
+            }
+            cudaError_t e = out->d_names.alloc(count, st);
+            if (e != cudaSuccess) return e;
+            e = out->d_counts.alloc(count, st);
+            *name = out->d_names.p;
+            *cnt = out->d_counts.p;
+            return e;
+        };
         int name_bits = 1, q_bits = 1;
         while (name_bits < 32 && (1ull << name_bits) < g->dg.id_bound) ++name_bits;
         while ((1ull << q_bits) < nt) ++q_bits;
@@ -736,6 +879,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             // (ties by name) and the first k are kept.
             uint32_t *d_thr;
             unsigned long long *d_sel, *d_sseg;
+            const int sp_place = ph->begin(PhaseTimer::kPlace, st);
             PTW_CUDA(db.alloc(&d_thr, nt));
             PTW_CUDA(db.alloc(&d_sel, nt));
             PTW_CUDA(db.alloc(&d_sseg, nt + 1));
@@ -763,8 +907,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             PTW_CUDA(cudaGetLastError());
             unsigned long long *d_kseg;
             PTW_CUDA(db.alloc(&d_kseg, nt + 1));
-            PTW_CUDA(db.alloc(&o_name, n_out));
-            PTW_CUDA(db.alloc(&o_cnt, n_out));
+            PTW_CUDA(alloc_out(&o_name, &o_cnt, n_out));
             PTW_CUDA(cudaMemcpyAsync(d_kseg, kseg.data(), (nt + 1) * 8ull, cudaMemcpyHostToDevice, st));
             const unsigned sg = (unsigned)std::min<uint64_t>((n_sel + 255) / 256, (uint64_t)g->num_sms * 32);
             if (packed) {
@@ -791,6 +934,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
                                                               o_cnt);
             }
             PTW_CUDA(cudaGetLastError());
+            ph->end(sp_place, st);
             out->seg = kseg;
         } else {
             // Full lists by name.  Dense tables are already in name order:
@@ -798,8 +942,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             // put their entries into one range per table, each range is
             // sorted by name (a segmented sort of 32-bit names), and the
             // ranges are copied into their output segments.
-            PTW_CUDA(db.alloc(&o_name, n_ent));
-            PTW_CUDA(db.alloc(&o_cnt, n_ent));
+            PTW_CUDA(alloc_out(&o_name, &o_cnt, n_ent));
             std::vector<uint64_t> hseg(nt + 1, 0);
             for (uint32_t i = 0; i < nt; ++i)
                 hseg[i + 1] = hseg[i] + (dense_flags[i] ? 0 : out->seg[i + 1] - out->seg[i]);
@@ -820,7 +963,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
             // (tables are in output order), so with page-locked host lists
             // each range's copy to the host runs on a second stream while the
             // next range compacts.
-            const uint32_t R = dst_pinned && n_ent >= (16ull << 20) ? 4u : 1u;
+            const uint32_t R = !out->device && dst_pinned && n_ent >= (16ull << 20) ? 4u : 1u;
             std::vector<uint32_t> tb(R + 1, nt);
             tb[0] = 0;
             for (uint32_t r = 1; r < R; ++r) {
@@ -852,6 +995,7 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
                     for (cudaEvent_t x : e) cudaEventDestroy(x);
                 }
             } ev_free{evs};
+            const int sp_place = ph->begin(PhaseTimer::kPlace, st);
             for (uint32_t r = 0; r < R; ++r) {
                 const uint32_t t0 = tb[r], t1 = tb[r + 1];
                 if (t0 >= t1) continue;
@@ -899,29 +1043,36 @@ int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned lon
                     PTW_CUDA(cudaEventRecord(ev, st));
                     PTW_CUDA(cudaStreamWaitEvent(cs, ev, 0));
                     if (e1 > e0) {
+                        const int sp_copy = ph->begin(PhaseTimer::kCopy, cs);
                         PTW_CUDA(cudaMemcpyAsync(out->h_names + e0, o_name + e0, (e1 - e0) * 4,
                                                  cudaMemcpyDeviceToHost, cs));
                         PTW_CUDA(cudaMemcpyAsync(out->h_counts + e0, o_cnt + e0, (e1 - e0) * 4,
                                                  cudaMemcpyDeviceToHost, cs));
+                        ph->end(sp_copy, cs);
+                        ph->copy_bytes += (e1 - e0) * 8;
                     }
                 }
             }
+            ph->end(sp_place, st);
             if (R > 1) {
                 // copies issued; wait for them here (the device buffers they read are freed below)
                 PTW_CUDA(cudaStreamSynchronize(cs));
                 copied = true;
             }
         }
-        const double tj2 = timing ? clk() : 0.0;
+        const double tj2 = clk();
         prefault.join();
-        if (timing) t_join += clk() - tj2;
+        t_join += clk() - tj2;
         if (timing) {
             PTW_CUDA(cudaStreamSynchronize(st));
             t1 = clk();
         }
-        if (!copied) {
+        if (!copied && !out->device) {
+            const int sp_copy = ph->begin(PhaseTimer::kCopy, st);
             PTW_CUDA(cudaMemcpyAsync(out->h_names, o_name, n_out * 4, cudaMemcpyDeviceToHost, st));
             PTW_CUDA(cudaMemcpyAsync(out->h_counts, o_cnt, n_out * 4, cudaMemcpyDeviceToHost, st));
+            ph->end(sp_copy, st);
+            ph->copy_bytes += n_out * 8;
         }
         PTW_CUDA(cudaStreamSynchronize(st));
         if (timing) t2 = clk();
@@ -973,12 +1124,15 @@ try {
     *out = nullptr;
     if (nq && !h_queries) return fail(PTW_EINVAL, "null query table");
     if (cfg->app != PTW_APP_VISITS && cfg->app != PTW_APP_ENDPOINT) return fail(PTW_EINVAL, "unknown app");
+    if (cfg->flags & ~PTW_BATCH_DEVICE_RESULTS) return fail(PTW_EINVAL, "unknown batch flags");
     PTW_CUDA(cudaSetDevice(g->device));
     const bool timing = std::getenv("PTW_TIMING") != nullptr;
     auto clk = [] { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
-    const double t_enter = timing ? clk() : 0.0;
+    const double t_enter = clk();
     double t_waves = 0, t_asm = 0;
     const uint32_t n = g->dg.n;
+    const BatchTune bt = effective_tune(g);
+    PhaseTimer ph;
     std::vector<WaveQuery> all(nq);
     for (uint32_t i = 0; i < nq; ++i) {
         const ptw_query &q = h_queries[i];
@@ -995,7 +1149,8 @@ try {
         // Dense when not larger than the hash table (a cut at twice its bytes
         // was 3% faster on the scale-22 batch but 7% slower in the serving
         // loop's top-k compaction).
-        const TableSize ts = count_table(cfg->sp, cfg->max_moves, cfg->app, cfg->table_factor, q.budget, n, 1u);
+        const TableSize ts = count_table(cfg->sp, cfg->max_moves, cfg->app, cfg->table_factor, q.budget, n,
+                                         bt.dense_ratio);
         all[i].cap = ts.slots;
         all[i].dense = ts.dense;
     }
@@ -1009,6 +1164,8 @@ try {
     if (!b) return fail(PTW_ENOMEM, "host allocation failed");
     b->nq = nq;
     b->queries.assign(h_queries, h_queries + nq);
+    b->device = (cfg->flags & PTW_BATCH_DEVICE_RESULTS) != 0;
+    b->device_id = g->device;
     std::vector<WaveResult> waves;
     std::vector<uint32_t> overflow;
     const uint64_t thr = stop_threshold(cfg->sp);
@@ -1024,7 +1181,7 @@ try {
             bytes += all[i].cap * 8;
             wave.push_back(all[i++]);
         }
-        rc = run_wave(g, wave, cfg, thr, waves, overflow, &moves, &walk_ms);
+        rc = run_wave(g, wave, cfg, thr, waves, overflow, &moves, &walk_ms, &ph);
     }
     // Queries whose hash table filled run again with a dense array (which
     // cannot fill).
@@ -1036,12 +1193,12 @@ try {
         w.cap = d.slots;
         w.dense = true;
         uint64_t m2 = 0;
-        rc = run_wave(g, {w}, cfg, thr, waves, overflow, &m2, &walk_ms);
+        rc = run_wave(g, {w}, cfg, thr, waves, overflow, &m2, &walk_ms, &ph);
         if (rc == PTW_OK && !overflow.empty()) rc = fail(PTW_EFULL, "count table overflow in a dense array");
     }
-    if (timing) t_waves = clk();
-    if (rc == PTW_OK) rc = assemble(b, waves);
-    if (timing) t_asm = clk();
+    t_waves = clk();
+    if (rc == PTW_OK) rc = assemble(g, b, waves);
+    t_asm = clk();
     if (rc != PTW_OK) {
         delete b;
         return rc;
@@ -1058,6 +1215,25 @@ try {
     PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[3], g->ev[2]));
     b->stats.total_ms = ms;
     b->stats.kernel_ms = walk_ms;  // walker kernels only; total_ms includes compaction and copies
+    // the device arrays outlive this call and possibly the graph's stream:
+    // everything on it has completed, so they are freed on the default stream
+    b->d_names.st = b->d_counts.st = b->d_offsets.st = nullptr;
+    double sums[PhaseTimer::kPhases], tail = 0;
+    ph.sums(sums, &tail);
+    ptw_batch_phases &P = b->phases;
+    P.plan_ms = ph.plan_ms;
+    P.device_ms = ms;
+    P.upload_ms = sums[PhaseTimer::kUpload];
+    P.walk_ms = sums[PhaseTimer::kWalk];
+    P.count_ms = sums[PhaseTimer::kCount];
+    P.place_ms = sums[PhaseTimer::kPlace];
+    P.copy_ms = sums[PhaseTimer::kCopy];
+    P.copy_tail_ms = tail;
+    P.host_pages_ms = ph.host_pages_ms;
+    P.copy_bytes = ph.copy_bytes;
+    P.waves = (uint32_t)waves.size();
+    P.reruns = (uint32_t)again.size();
+    P.call_ms = 1e3 * (clk() - t_enter);
     if (timing)
         std::fprintf(stderr, "[ptw] batch of %u queries: %zu waves in %.1f ms, assemble %.1f ms, call %.1f ms\n", nq,
                      waves.size(), 1e3 * (t_waves - t_enter), 1e3 * (t_asm - t_waves), 1e3 * (clk() - t_enter));
@@ -1083,6 +1259,13 @@ try {
     if (!b) return fail(PTW_EINVAL, "null batch");
     const uint64_t n = b->offsets.empty() ? 0 : b->offsets.back();
     if (h_offsets) std::memcpy(h_offsets, b->offsets.data(), b->offsets.size() * 8);
+    if (b->device) {
+        if (!n || (!h_names && !h_counts)) return PTW_OK;
+        PTW_CUDA(cudaSetDevice(b->device_id));
+        if (h_names) PTW_CUDA(cudaMemcpy(h_names, b->d_names.p, n * 4, cudaMemcpyDeviceToHost));
+        if (h_counts) PTW_CUDA(cudaMemcpy(h_counts, b->d_counts.p, n * 4, cudaMemcpyDeviceToHost));
+        return PTW_OK;
+    }
     if (h_names && n) std::memcpy(h_names, b->names.get(), n * 4);
     if (h_counts && n) std::memcpy(h_counts, b->counts.get(), n * 4);
     return PTW_OK;
@@ -1095,8 +1278,30 @@ extern "C" int ptw_batch_view(const ptw_batch *b, const uint64_t **offsets, cons
 try {
     if (!b) return fail(PTW_EINVAL, "null batch");
     if (offsets) *offsets = b->offsets.data();
-    if (names) *names = b->names.get();
-    if (counts) *counts = b->counts.get();
+    if (names) *names = b->device ? nullptr : b->names.get();
+    if (counts) *counts = b->device ? nullptr : b->counts.get();
+    return PTW_OK;
+} catch (...) {
+    return host_exception();
+}
+
+extern "C" int ptw_batch_view_device(const ptw_batch *b, const uint64_t **d_offsets, const uint32_t **d_names,
+                                     const uint32_t **d_counts)
+try {
+    if (!b) return fail(PTW_EINVAL, "null batch");
+    if (!b->device) return fail(PTW_EINVAL, "the batch's results are in host memory (run without PTW_BATCH_DEVICE_RESULTS)");
+    if (d_offsets) *d_offsets = reinterpret_cast<const uint64_t *>(b->d_offsets.p);
+    if (d_names) *d_names = b->d_names.p;
+    if (d_counts) *d_counts = b->d_counts.p;
+    return PTW_OK;
+} catch (...) {
+    return host_exception();
+}
+
+extern "C" int ptw_batch_get_phases(const ptw_batch *b, ptw_batch_phases *out)
+try {
+    if (!b || !out) return fail(PTW_EINVAL, "null argument");
+    *out = b->phases;
     return PTW_OK;
 } catch (...) {
     return host_exception();
@@ -1105,6 +1310,16 @@ try {
 extern "C" void ptw_batch_free(ptw_batch *b)
 try {
     if (!b) return;
+    if (b->device) {  // the pool memory goes back on the batch's device
+        int prev = 0;
+        const bool have_prev = cudaGetDevice(&prev) == cudaSuccess;
+        cudaSetDevice(b->device_id);
+        b->d_names.reset();
+        b->d_counts.reset();
+        b->d_offsets.reset();
+        if (have_prev) cudaSetDevice(prev);
+        cudaGetLastError();
+    }
     if (b->names && b->buf_cap) {
         HostBufs hb;
         hb.names = std::move(b->names);
@@ -1118,4 +1333,133 @@ try {
 } catch (...) {
     delete b;
     host_exception();
+}
+
+extern "C" int ptw_graph_set_batch_tune(ptw_graph *g, const ptw_batch_tune *t)
+try {
+    if (!g || !t) return fail(PTW_EINVAL, "null argument");
+    if (t->desc_walkers && (t->desc_walkers < 32 || t->desc_walkers > 65536))
+        return fail(PTW_EINVAL, "batch tune: desc_walkers must be 0 or in [32, 65536]");
+    if (t->blocks_per_sm > 64) return fail(PTW_EINVAL, "batch tune: blocks_per_sm must be in [0, 64]");
+    if (t->dense_ratio > 64) return fail(PTW_EINVAL, "batch tune: dense_ratio must be in [0, 64]");
+    if (t->ext_columns < 0 || t->ext_columns > 2) return fail(PTW_EINVAL, "batch tune: ext_columns must be 0, 1 or 2");
+    g->btune = *t;
+    return PTW_OK;
+} catch (...) {
+    return host_exception();
+}
+
+extern "C" int ptw_graph_get_batch_tune(const ptw_graph *g, ptw_batch_tune *t)
+try {
+    if (!g || !t) return fail(PTW_EINVAL, "null argument");
+    *t = g->btune;
+    return PTW_OK;
+} catch (...) {
+    return host_exception();
+}
+
+extern "C" int ptw_autotune_batch(ptw_graph *g, const ptw_query *q, uint32_t nq, const ptw_batch_cfg *cfg,
+                                  ptw_batch_tune *best, double *best_ms)
+try {
+    NvtxRange nvtx("ptw_autotune_batch");
+    if (!g || !cfg || (nq && !q)) return fail(PTW_EINVAL, "null argument");
+    if (nq == 0) return fail(PTW_EINVAL, "the autotuner needs at least one query");
+    ptw_batch_cfg c = *cfg;
+    c.flags |= PTW_BATCH_DEVICE_RESULTS;  // results are discarded: no copies to the host
+    const ptw_batch_tune saved = g->btune;
+    // Device time of the whole batch under tune t: first upload to the end
+    // of compaction (ev[3] -> ev[2] of the call).
+    auto time_one = [&](const ptw_batch_tune &t, double *ms) -> int {
+        int rc = ptw_graph_set_batch_tune(g, &t);
+        if (rc) return rc;
+        ptw_batch *b = nullptr;
+        rc = ptw_ppr_batch(g, q, nq, &c, &b);
+        if (rc) return rc;
+        *ms = b->phases.device_ms;
+        ptw_batch_free(b);
+        return PTW_OK;
+    };
+    struct Cand {
+        ptw_batch_tune t;
+        double ms;
+    };
+    std::vector<Cand> all;
+    double warm = 0;
+    int rc = time_one(saved, &warm);  // maps the pool's memory, builds column copies
+    if (rc) {
+        g->btune = saved;
+        return rc;
+    }
+    const ptw_batch_tune base = saved;
+    auto run = [&](ptw_batch_tune t) -> int {
+        double ms = 0;
+        const int r = time_one(t, &ms);
+        if (r == PTW_OK) all.push_back({t, ms});
+        return r;
+    };
+    // Stage 1: descriptor size x group bytes.
+    for (uint32_t dw : {128u, 256u, 512u, 1024u})
+        for (uint64_t gbytes : {128ull << 20, 384ull << 20, 1024ull << 20, ~0ull}) {
+            if (rc) break;
+            ptw_batch_tune t = base;
+            t.desc_walkers = dw;
+            t.group_bytes = gbytes;
+            t.blocks_per_sm = 0;
+            t.dense_ratio = 1;
+            t.ext_columns = 0;
+            rc = run(t);
+        }
+    auto fastest = [&]() {
+        return *std::min_element(all.begin(), all.end(), [](const Cand &a, const Cand &b) { return a.ms < b.ms; });
+    };
+    // Stage 2: blocks per SM x dense ratio x column layout around the best.
+    if (rc == PTW_OK && !all.empty()) {
+        const ptw_batch_tune b1 = fastest().t;
+        for (uint32_t bps : {0u, 4u, 6u})
+            for (uint32_t dr : {1u, 2u})
+                for (int32_t ext : {1, 2}) {
+                    if (rc) break;
+                    ptw_batch_tune t = b1;
+                    t.blocks_per_sm = bps;
+                    t.dense_ratio = dr;
+                    t.ext_columns = ext;
+                    rc = run(t);
+                }
+    }
+    if (rc != PTW_OK || all.empty()) {
+        g->btune = saved;
+        return rc ? rc : fail(PTW_EINVAL, "no batch tune could be timed");
+    }
+    // Stage 3: the three fastest again, three interleaved rounds; median.
+    std::sort(all.begin(), all.end(), [](const Cand &a, const Cand &b) { return a.ms < b.ms; });
+    const size_t top = std::min<size_t>(3, all.size());
+    std::vector<std::vector<double>> again(top);
+    for (int round = 0; round < 3 && rc == PTW_OK; ++round)
+        for (size_t i = 0; i < top && rc == PTW_OK; ++i) {
+            double ms = 0;
+            rc = time_one(all[i].t, &ms);
+            again[i].push_back(ms);
+        }
+    if (rc != PTW_OK) {
+        g->btune = saved;
+        return rc;
+    }
+    size_t pick = 0;
+    double pick_ms = 0;
+    for (size_t i = 0; i < top; ++i) {
+        std::vector<double> v = again[i];
+        v.push_back(all[i].ms);
+        std::sort(v.begin(), v.end());
+        const double med = v[v.size() / 2];
+        if (i == 0 || med < pick_ms) {
+            pick = i;
+            pick_ms = med;
+        }
+    }
+    g->btune = all[pick].t;
+    if (best) *best = all[pick].t;
+    if (best_ms) *best_ms = pick_ms;
+    return PTW_OK;
+} catch (...) {
+    return host_exception();
 }

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <exception>
 #include <functional>
 #include <memory>
@@ -229,6 +230,7 @@ struct ptw_graph {
     int device = 0;
     int num_sms = 0;
     ptw_tune tune{};
+    ptw_batch_tune btune{};  // zero fields: defaults (see ptw_batch_tune)
     uint64_t device_bytes = 0;
     int ext_users = 0;  // open servers reading the extended columns (kept while > 0)
     ptw::AsyncSlot async[2];             // pipelined count walks in flight
@@ -313,8 +315,72 @@ using HostArray = std::unique_ptr<uint32_t[], HostArrayDelete>;
 // process-wide limit of a quarter of the host memory; false when refused.
 bool host_pin(uint32_t *p, uint64_t bytes);
 
+// CUDA-event intervals of the phases of a batch call on the device
+// timeline (several spans of one phase add up), plus host-side waits.
+struct PhaseTimer {
+    enum { kUpload, kWalk, kCount, kPlace, kCopy, kPhases };
+    struct Span {
+        int phase;
+        cudaEvent_t a, b;
+    };
+    std::vector<Span> spans;
+    double host_pages_ms = 0, plan_ms = 0;
+    uint64_t copy_bytes = 0;
+    int last_place = -1, last_copy = -1;  // span indices
+    // Opens a span of `phase` by recording an event on s; returns its index
+    // (-1 when no event could be created: the span is then not timed).
+    int begin(int phase, cudaStream_t s);
+    void end(int span, cudaStream_t s);
+    // Milliseconds per phase (after the recorded work has completed).
+    void sums(double out[kPhases], double *copy_tail_ms) const;
+    PhaseTimer() = default;
+    PhaseTimer(const PhaseTimer &) = delete;
+    PhaseTimer &operator=(const PhaseTimer &) = delete;
+    ~PhaseTimer();
+};
+
+// Device memory from the library's pool, freed on a stream when dropped.
+struct PoolArray {
+    uint32_t *p = nullptr;
+    cudaStream_t st = nullptr;
+    PoolArray() = default;
+    PoolArray(const PoolArray &) = delete;
+    PoolArray &operator=(const PoolArray &) = delete;
+    PoolArray(PoolArray &&o) noexcept : p(o.p), st(o.st) { o.p = nullptr; }
+    PoolArray &operator=(PoolArray &&o) noexcept
+    {
+        if (this != &o) {
+            reset();
+            p = o.p;
+            st = o.st;
+            o.p = nullptr;
+        }
+        return *this;
+    }
+    cudaError_t alloc(uint64_t count, cudaStream_t s)
+    {
+        reset();
+        st = s;
+        void *q = nullptr;
+        const cudaError_t e = pooled_alloc_async(&q, std::max<uint64_t>(count, 1) * 4, s);
+        p = (uint32_t *)q;
+        return e;
+    }
+    void reset()
+    {
+        if (p) cudaFreeAsync(p, st);
+        p = nullptr;
+    }
+    ~PoolArray() { reset(); }
+};
+
 struct Compacted {
     uint32_t top_k = 0;
+    // Device-resident results: the lists stay in d_names / d_counts (no host
+    // buffers, no copy).
+    bool device = false;
+    PoolArray d_names, d_counts;
+    PhaseTimer *ph = nullptr;  // phase spans of the call (may be null)
     uint64_t n = 0;
     std::vector<uint64_t> seg;
     HostArray names, counts;
@@ -371,11 +437,12 @@ TableSize dense_table(uint32_t n);
 void interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<uint64_t> &count,
                             const std::vector<uint64_t> &table_bytes, uint64_t group_bytes,
                             std::vector<uint3> &desc);
-// The same into a new buffer, groups filled on up to `threads` host threads
-// when there are many descriptors; returns the number of descriptors.
+// The same into a new buffer with descriptors of at most desc_walkers ranks,
+// groups filled on up to `threads` host threads when there are many
+// descriptors; returns the number of descriptors.
 uint64_t interleave_descriptors(const std::vector<uint64_t> &j0, const std::vector<uint64_t> &count,
                                 const std::vector<uint64_t> &table_bytes, uint64_t group_bytes,
-                                std::unique_ptr<uint3[]> &desc, unsigned threads);
+                                std::unique_ptr<uint3[]> &desc, unsigned threads, uint32_t desc_walkers);
 // Count-table bytes per descriptor group: about 3x the 129 MB L2.
 constexpr uint64_t kGroupBytes = 384ull << 20;
 
