@@ -18,8 +18,8 @@ removed (synthetic, built on the device).  Each step uses a new seed.
             the next step walks
   roofline  random-gather bound: 64 B per move (row record + column
             sector) + 32 B per counted visit, against the measured HBM peak;
-            traffic = the ncu DRAM bytes per move of the committed scale-24
-            capture times this run's moves per launch; gather_peak = random
+            traffic = the ncu DRAM bytes per move of the scale-24 capture of
+            the same column layout times this run's moves per launch; gather_peak = random
             4-byte loads/s this GPU serves from a 2 GB array, measured here
   cpu_baseline  the oracle port (C, all host threads) on a bounded sample of
             the same workload
@@ -240,22 +240,22 @@ def degree_sources(G, n, seed):
     return names[col[e]]
 
 
-TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_walk_dram_bytes_rmat-s24.md")
+# DRAM bytes per move of the count walk on R-MAT scale 24, W = |V|, sp 0.15:
+# ncu dram__bytes_read.sum + dram__bytes_write.sum over two launches of each
+# launch configuration, divided by the moves of a launch (one-pass capture
+# of the full-size bench command; profiles/k_walk_dram_bytes_rmat-s24.md).
+TRAFFIC_PER_MOVE_S24 = {True: 125.0, False: 130.1}  # extended columns / plain columns
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per move of k_walk at R-MAT scale 24 "
+                  "(two launches of the %s-column configuration, profiles/k_walk_dram_bytes_rmat-s24.md), "
+                  "times this run's moves per launch")
 
 
-def traffic_per_move(scale):
-    """DRAM bytes per move of the walk kernel from the committed ncu summary
-    (its line `dram_bytes_per_move: X`), for the scale it was captured at."""
-    if scale != 24 or not os.path.exists(TRAFFIC_PROFILE):
+def traffic_per_move(scale, ext):
+    """DRAM bytes per move of the walk kernel at the bench workload, for the
+    column layout the launch reads; None at other scales."""
+    if scale != 24:
         return None
-    for ln in open(TRAFFIC_PROFILE):
-        if ln.startswith("dram_bytes_per_move:"):
-            return float(ln.split(":", 1)[1])
-    return None
-
-
-def per_move_src(scale):
-    return "ncu dram__bytes_read.sum + dram__bytes_write.sum per move, %s" % os.path.relpath(TRAFFIC_PROFILE, ROOT)
+    return TRAFFIC_PER_MOVE_S24[bool(ext)]
 
 
 def loguniform_budgets(n, lo, hi, seed):
@@ -650,10 +650,11 @@ def run_ours(args):
     # DRAM bytes per walk launch: the ncu capture's bytes per move at this
     # workload (committed summary) times this run's moves per launch.
     traffic, traffic_src = None, None
-    per_move = traffic_per_move(args.scale)
+    ext_walk = bool(tune.ext_columns & 1)
+    per_move = traffic_per_move(args.scale, ext_walk)
     if per_move:
         traffic = per_move * sum(moves) / len(moves)
-        traffic_src = per_move_src(args.scale)
+        traffic_src = TRAFFIC_SOURCE % ("extended" if ext_walk else "plain")
     # Random-gather ceiling measured on this GPU: a move is one dependent
     # random gather into the column array (2 GB > L2), so moves/s over this
     # rate is the kernel's share of what random access can deliver.
