@@ -69,7 +69,9 @@ def parse():
     p.add_argument("--no-batch", action="store_true", help="skip the batched-PPR side line")
     p.add_argument("--no-serve", action="store_true", help="skip the serving side line")
     p.add_argument("--no-ingest", action="store_true", help="skip the edge-list ingest side line")
-    p.add_argument("--learned", action="store_true", help="add the learned-budget side line (minutes)")
+    p.add_argument("--no-learned", action="store_true", help="skip the learned-budget side line")
+    p.add_argument("--learned-train", type=int, default=4096, help="training queries of the learned line")
+    p.add_argument("--learned-test", type=int, default=4096, help="held-out queries of the learned line")
     p.add_argument("--batch-scale", type=int, default=22)
     p.add_argument("--batch-queries", type=int, default=4096)
     p.add_argument("--serve-n", type=int, default=8_400_000)
@@ -428,14 +430,40 @@ def bench_serve(args, ptw):
 
 
 def bench_learned(args, ptw):
+    """Learned walker budgets against the fixed plain budget of 1e6 walkers
+    per query (sp 0.2), scored by the FP64 oracle on held-out queries, on
+    three workloads: R-MAT scale 22 with degree-proportional sources (the
+    configuration's own: args.learned_train training and args.learned_test
+    held-out queries), R-MAT scale 22 with uniform sources and the Chung-Lu
+    serving graph (half the training and half the held-out queries).  Each
+    line gives the gain at equal 90th-percentile L1 and at equal mean L1,
+    and the ceiling the needed budgets themselves allow for each."""
     import numpy as np
     from ptwalker_gb300 import learned
+    out = {"fixed_budget": 1_000_000, "sp": 0.2, "workloads": []}
+    nt, ne = args.learned_train, args.learned_test
+
+    def one(name, G, train, test):
+        t0 = time.perf_counter()
+        r = learned.evaluate(G, train, test, b_fix=1_000_000, sp=0.2, seed=5, epochs=300)
+        r.pop("train_loss", None)
+        r.update(workload=name, vertices=G.n, edges=G.m, seconds=time.perf_counter() - t0)
+        out["workloads"].append(r)
+
     G = ptw.Graph.rmat(args.batch_scale, 16, 0.57, 0.19, 0.19, seed=1, clean=True)
-    train = degree_sources(G, 1024, 21)
-    test = degree_sources(G, 512, 22)
-    r = learned.evaluate(G, train, test, b_fix=100000, sp=0.2, seed=5, epochs=300)
+    one("rmat-s%d degree-proportional sources" % args.batch_scale, G, degree_sources(G, nt, 21),
+        degree_sources(G, ne, 22))
+    names = G.export_csr()[0]
+    rng = np.random.default_rng(23)
+    one("rmat-s%d uniform sources" % args.batch_scale, G, names[rng.integers(0, G.n, nt // 2)],
+        names[rng.integers(0, G.n, ne // 2)])
     G.close()
-    return r
+    G = ptw.Graph.chung_lu(args.serve_n, 2.1, 32.0, seed=1)
+    names = G.export_csr()[0]
+    one("chung-lu n=%d uniform sources" % args.serve_n, G, names[rng.integers(0, G.n, nt // 2)],
+        names[rng.integers(0, G.n, ne // 2)])
+    G.close()
+    return out
 
 
 # ---- our arm ----------------------------------------------------------------------
@@ -705,7 +733,7 @@ def run_ours(args):
     if rank == 0 and world == 1:
         for key, flag, fn in (("batched_ppr", args.no_batch, bench_batch), ("serving", args.no_serve, bench_serve),
                               ("ingest", args.no_ingest, bench_ingest),
-                              ("learned_budgets", not args.learned, bench_learned)):
+                              ("learned_budgets", args.no_learned, bench_learned)):
             if flag:
                 continue
             try:

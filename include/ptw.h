@@ -341,6 +341,18 @@ void ptw_batch_free(ptw_batch *b);
  * query i of batch b (both normalised to sum 1).  h_l1[nq].  PTW_EINVAL for
  * a batch run with top_k > 0 (its lists are truncated). */
 int ptw_batch_l1(ptw_graph *g, const ptw_batch *b, double sp, int32_t app, double tol, double *h_l1);
+/* The same for nb batches over the same query sources (e.g. one query table
+ * run with two budget rules), sharing one power iteration per 32 sources:
+ * h_l1[j * nq + i] for query i of batch bs[j].  The truncated series is
+ * within about 2 tol of the exact expectation in L1.  No counterpart in the
+ * reference. */
+int ptw_batch_l1_many(ptw_graph *g, const ptw_batch *const *bs, uint32_t nb, double sp, int32_t app, double tol,
+                      double *h_l1);
+/* L1 distance between the normalised counts of query i of batch a and of
+ * batch ref (same query sources), h_l1[nq]: e.g. a low-budget estimate
+ * against a high-budget one of the same query ids.  No counterpart in the
+ * reference. */
+int ptw_batch_l1_pair(ptw_graph *g, const ptw_batch *a, const ptw_batch *ref, double *h_l1);
 
 /* ---- serving loop with continuous batching ----------------------------- */
 

@@ -163,6 +163,9 @@ SIGNATURES = [
                                           ctypes.POINTER(BatchTune), ctypes.POINTER(ctypes.c_double)]),
     ("ptw_batch_l1", ctypes.c_int, [_G, _G, ctypes.c_double, ctypes.c_int32, ctypes.c_double,
                                     ctypes.POINTER(ctypes.c_double)]),
+    ("ptw_batch_l1_many", ctypes.c_int, [_G, ctypes.POINTER(ctypes.c_void_p), ctypes.c_uint32, ctypes.c_double,
+                                         ctypes.c_int32, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    ("ptw_batch_l1_pair", ctypes.c_int, [_G, _G, _G, ctypes.POINTER(ctypes.c_double)]),
     ("ptw_serve_open", ctypes.c_int, [_G, ctypes.POINTER(ServeCfg), _GP]),
     ("ptw_serve_submit", ctypes.c_int, [_G, ctypes.POINTER(Query)]),
     ("ptw_serve_step", ctypes.c_int, [_G, _u32p, _u32p, _u32p]),

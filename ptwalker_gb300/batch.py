@@ -140,12 +140,20 @@ class BatchResult:
         out[names] = counts
         return out
 
-    def l1(self, tol=1e-10):
+    def l1(self, tol=1e-6):
         """Per-query L1 between the normalised counts and the FP64 expected
-        counts (device power iteration, ptw_batch_l1)."""
+        counts (device power iteration to residual tol, ptw_batch_l1)."""
         out = np.empty(self.nq, dtype=np.float64)
         C.check(self._lib.ptw_batch_l1(self.graph.handle, self._h, self.sp, APPS[self.app], tol,
                                        out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
+
+    def l1_vs(self, ref):
+        """Per-query L1 between this batch's normalised counts and those of
+        ref, a batch over the same sources (ptw_batch_l1_pair)."""
+        out = np.empty(self.nq, dtype=np.float64)
+        C.check(self._lib.ptw_batch_l1_pair(self.graph.handle, self._h, ref._h,
+                                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return out
 
     def close(self):
@@ -161,6 +169,17 @@ class BatchResult:
             self.close()
         except Exception:
             pass
+
+
+def l1_many(graph, results, tol=1e-6):
+    """FP64-oracle L1 of several batches over the same sources, one power
+    iteration shared by all (ptw_batch_l1_many); returns [len(results), nq]."""
+    r0 = results[0]
+    hs = (ctypes.c_void_p * len(results))(*[r._h.value if hasattr(r._h, "value") else r._h for r in results])
+    out = np.empty((len(results), r0.nq), dtype=np.float64)
+    C.check(graph._lib.ptw_batch_l1_many(graph.handle, hs, len(results), r0.sp, APPS[r0.app], tol,
+                                         out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    return out
 
 
 def _queries(sources, budgets, query_ids):

@@ -707,6 +707,7 @@ uint64_t next_pow2(uint64_t x)
 
 const ptw_query *batch_queries(const ptw_batch *b) { return b->queries.data(); }
 uint32_t batch_top_k(const ptw_batch *b) { return b->top_k; }
+bool batch_device(const ptw_batch *b) { return b->device; }
 
 int compact_tables(ptw_graph *g, unsigned long long *d_slots, const unsigned long long *h_base,
                    const uint32_t *h_cap, const uint8_t *h_dense, uint32_t nt, Compacted *out)

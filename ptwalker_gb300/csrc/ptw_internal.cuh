@@ -297,6 +297,7 @@ bool ensure_ext_columns(ptw_graph *g);
 // The query table a batch was run with (batch.cu).
 const ptw_query *batch_queries(const ptw_batch *b);
 uint32_t batch_top_k(const ptw_batch *b);
+bool batch_device(const ptw_batch *b);  // results are device-resident
 
 // (name, count) lists of nt tables in host memory: table i owns entries
 // [seg[i], seg[i+1]), sorted by name.  Without a sink the lists land in the

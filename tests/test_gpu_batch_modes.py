@@ -126,3 +126,33 @@ def test_autotune_batch(gpu, G16):
         b.close()
     finally:
         gpu.set_batch_tune(G16, saved)
+
+
+def test_shared_fp64_l1_and_pair_l1(gpu, G16):
+    """ptw_batch_l1_many scores several batches over the same sources with
+    one power iteration: each row equals that batch scored alone.
+    ptw_batch_l1_pair (summed on the device) equals the L1 of the exported
+    lists computed on the host."""
+    from ptwalker_gb300 import learned
+    from ptwalker_gb300.batch import l1_many
+    rng = np.random.default_rng(15)
+    sources, budgets, qids = _batch(rng, G16, nq=40)
+    a = gpu.ppr_batch(G16, sources, budgets, sp=0.2, seed=4, query_ids=qids)
+    b = gpu.ppr_batch(G16, sources, budgets // 3 + 1, sp=0.2, seed=4, query_ids=qids, device_results=True)
+    ref = gpu.ppr_batch(G16, sources, 4 * budgets, sp=0.2, seed=4, query_ids=qids, device_results=True)
+    both = l1_many(G16, [a, b], tol=1e-9)
+    assert np.allclose(both[0], a.l1(tol=1e-9), rtol=0, atol=1e-12)
+    assert np.allclose(both[1], b.l1(tol=1e-9), rtol=0, atol=1e-12)
+    for x in (a, b):
+        got = x.l1_vs(ref)
+        o1, n1, c1 = x.export()
+        o2, n2, c2 = ref.export()
+        want = np.array([learned.sparse_l1(n1[o1[i]:o1[i + 1]], c1[o1[i]:o1[i + 1]],
+                                           n2[o2[i]:o2[i + 1]], c2[o2[i]:o2[i + 1]]) for i in range(len(sources))])
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-9)
+    assert np.allclose(ref.l1_vs(ref), 0.0, atol=1e-12)
+    other = gpu.ppr_batch(G16, sources[::-1].copy(), budgets, sp=0.2, seed=4)
+    with pytest.raises(gpu.PTWError):
+        a.l1_vs(other)
+    for x in (a, b, ref, other):
+        x.close()
