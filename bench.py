@@ -63,7 +63,7 @@ def parse():
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--tune", default=None,
                    help="block,ilp,chunk,hot_k[,min_blocks[,paths_ilp[,cache_hints[,paths_named[,ext_columns"
-                        "[,gather_slots]]]]]]: "
+                        "[,gather_slots[,warp_agg]]]]]]]: "
                         "fixed launch parameters "
                         "(skips the autotuner)")
     p.add_argument("--no-batch", action="store_true", help="skip the batched-PPR side line")
@@ -168,12 +168,20 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-# ---- CPU baseline (oracle port) ---------------------------------------------
+# ---- CPU baseline ---------------------------------------------------------------
+
+# Partition size of the partitioned port: a core's L2 (1 MB on Grace).
+PORT_PART_BYTES = 1 << 20
+PORT_KIND = ("partitioned port: the reference's partition sweeps with per-(thread, partition) walker pools "
+             "(src/core/solver.hpp:222-493) restated in C with OpenMP (oracle/partitioned.c), Philox draws, "
+             "counts equal to the oracle's")
+
 
 def cpu_port_run(canon, sp, seed, n_walkers, threads):
     import oracle
     t0 = time.perf_counter()
-    _, moves = oracle.replay_counts(canon, 0, n_walkers, sp, seed, 0, threads=threads)
+    _, moves, _ = oracle.partitioned_counts(canon, 0, n_walkers, sp, seed, 0, threads=threads,
+                                            part_bytes=PORT_PART_BYTES)
     dt = time.perf_counter() - t0
     return moves, dt
 
@@ -478,7 +486,7 @@ def get_tune(G, ptw, args, dev_name):
     if args.tune:
         v = [int(x) for x in args.tune.split(",")]
         names = ["block", "ilp", "chunk", "hot_k", "min_blocks", "paths_ilp", "cache_hints", "paths_named",
-                 "ext_columns", "gather_slots"]
+                 "ext_columns", "gather_slots", "warp_agg"]
         G.tune = ptw.Tune(**dict(zip(names, v)))
         return G.tune, "fixed"
     path = tune_cache_path()

@@ -114,7 +114,9 @@ typedef struct ptw_tune {
                               move an asynchronous 16-byte gather (cp.async) into shared memory,
                               so a thread keeps that many gathers in flight without registers.
                               Uses the extended column copy and a 16-byte record per vertex. */
-    int32_t reserved;
+    int32_t warp_agg;      /* count walks: 1 = lanes of a warp that visit the same vertex in the
+                              same move merge their visits (__match_any_sync) into one reduction;
+                              0 = one reduction per visit.  Needs min_blocks 0, gather_slots 0 */
 } ptw_tune;
 
 const char *ptw_last_error(void);

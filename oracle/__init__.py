@@ -7,6 +7,8 @@ Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 Contents
   * ``oracle.c`` (built to ``oracle/_build/liboracle.so``): Philox4x32-10,
     raw R-MAT edges, walker replay for counts / endpoints / paths.
+  * ``partitioned.c``: the same count walks scheduled the reference's way
+    (partition sweeps, per-partition walker pools); the timed CPU baseline.
   * ``graph.py``: canonical graph layout (names, CSR in index space) and the
     R-MAT clean-up pipeline, restating the reference loader's semantics.
   * ``power.py``: FP64 power iteration and the exact expected-visit formulas.
@@ -33,6 +35,7 @@ from .replay import (  # noqa: F401
     replay_counts,
     replay_pairs,
     replay_paths,
+    partitioned_counts,
     sp_threshold,
     TAG_WALK,
     TAG_START,

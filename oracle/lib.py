@@ -5,6 +5,7 @@ import subprocess
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _SRC = os.path.join(_HERE, "oracle.c")
+_SRCS = [_SRC, os.path.join(_HERE, "partitioned.c")]
 _OUT_DIR = os.path.join(_HERE, "_build")
 _SO = os.path.join(_OUT_DIR, "liboracle.so")
 _lib = None
@@ -14,10 +15,10 @@ def build_lib(force=False):
     """Compile oracle.c with gcc + OpenMP; returns the .so path."""
     os.makedirs(_OUT_DIR, exist_ok=True)
     if (not force and os.path.exists(_SO)
-            and os.path.getmtime(_SO) >= os.path.getmtime(_SRC)):
+            and all(os.path.getmtime(_SO) >= os.path.getmtime(f) for f in _SRCS)):
         return _SO
     tmp = _SO + ".tmp%d" % os.getpid()
-    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-std=c11", _SRC, "-o", tmp]
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-std=c11", *_SRCS, "-o", tmp]
     subprocess.check_call(cmd)
     os.replace(tmp, _SO)
     return _SO
@@ -52,6 +53,10 @@ def load_lib():
                                        ctypes.POINTER(ctypes.c_uint64),
                                        ctypes.POINTER(u64p), ctypes.POINTER(u32p)]
     lib.ora_rmat_clean_csr.restype = ctypes.c_int
+    lib.ora_partitioned_walks.argtypes = [u64p, u32p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64,
+                                          ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, u32p, ctypes.c_uint32,
+                                          ctypes.c_uint32, ctypes.c_uint64, u32p, ctypes.c_int, u64p]
+    lib.ora_partitioned_walks.restype = ctypes.c_uint64
     lib.ora_free.argtypes = [ctypes.c_void_p]
     lib.ora_free.restype = None
     _lib = lib

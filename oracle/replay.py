@@ -85,3 +85,22 @@ def replay_paths(g, w_begin, w_end, L, seed, start_mode=START_PER_VERTEX,
         w_begin, w_end, L, seed, start_mode, _p(src_arr, ctypes.c_uint32), n_src,
         _p(paths, ctypes.c_int32), threads)
     return paths
+
+
+def partitioned_counts(g, w_begin, w_end, sp, seed, start_mode=START_PER_VERTEX, sources=None, max_moves=0,
+                       threads=1, part_bytes=1 << 20):
+    """The same visit counts as replay_counts, computed the way the reference
+    schedules its walkers (partition sweeps with per-partition pools,
+    partitioned.c): the timed CPU baseline.  Returns (counts, moves, info)
+    with info = {partitions, sweeps, migrations}."""
+    lib = load_lib()
+    counts = np.zeros(g.n, dtype=np.uint32)
+    src_arr, n_src = _sources_arg(g, start_mode, sources)
+    info = np.zeros(3, dtype=np.uint64)
+    total = lib.ora_partitioned_walks(
+        _p(g.row_ptr, ctypes.c_uint64), _p(g.col, ctypes.c_uint32), g.n, w_begin, w_end, sp_threshold(sp), seed,
+        start_mode, _p(src_arr, ctypes.c_uint32), n_src, max_moves, int(part_bytes),
+        _p(counts, ctypes.c_uint32), threads, _p(info, ctypes.c_uint64))
+    if total == (1 << 64) - 1:
+        raise MemoryError("partitioned walk: host memory ran out")
+    return counts, int(total), {"partitions": int(info[0]), "sweeps": int(info[1]), "migrations": int(info[2])}

@@ -103,7 +103,7 @@ class Tune(ctypes.Structure):
                 ("min_blocks", ctypes.c_int32), ("paths_ilp", ctypes.c_int32),
                 ("cache_hints", ctypes.c_int32), ("paths_named", ctypes.c_int32),
                 ("ext_columns", ctypes.c_int32), ("gather_slots", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("warp_agg", ctypes.c_int32)]
 
 
 # Every symbol include/ptw.h declares: (name, restype, argtypes).

@@ -55,28 +55,28 @@ class Tune:
     """Launch parameters of the walk kernels (see ptw_tune in include/ptw.h)."""
 
     def __init__(self, block=256, ilp=2, chunk=256, hot_k=0, blocks_per_sm=0, min_blocks=0,
-                 paths_ilp=2, cache_hints=1, paths_named=1, ext_columns=0, gather_slots=0):
+                 paths_ilp=2, cache_hints=1, paths_named=1, ext_columns=0, gather_slots=0, warp_agg=0):
         self.block, self.ilp, self.chunk = block, ilp, chunk
         self.hot_k, self.blocks_per_sm, self.min_blocks = hot_k, blocks_per_sm, min_blocks
         self.paths_ilp, self.cache_hints, self.paths_named = paths_ilp, cache_hints, paths_named
-        self.ext_columns, self.gather_slots = ext_columns, gather_slots
+        self.ext_columns, self.gather_slots, self.warp_agg = ext_columns, gather_slots, warp_agg
 
     def to_c(self):
         return C.Tune(self.block, self.ilp, self.chunk, self.hot_k, self.blocks_per_sm,
                       self.min_blocks, self.paths_ilp, self.cache_hints, self.paths_named,
-                      self.ext_columns, self.gather_slots, 0)
+                      self.ext_columns, self.gather_slots, self.warp_agg)
 
     @classmethod
     def from_c(cls, t):
         return cls(t.block, t.ilp, t.chunk, t.hot_k, t.blocks_per_sm, t.min_blocks, t.paths_ilp,
-                   t.cache_hints, t.paths_named, t.ext_columns, t.gather_slots)
+                   t.cache_hints, t.paths_named, t.ext_columns, t.gather_slots, t.warp_agg)
 
     def as_dict(self):
         return dict(block=self.block, ilp=self.ilp, chunk=self.chunk, hot_k=self.hot_k,
                     blocks_per_sm=self.blocks_per_sm, min_blocks=self.min_blocks,
                     paths_ilp=self.paths_ilp, cache_hints=self.cache_hints,
                     paths_named=self.paths_named, ext_columns=self.ext_columns,
-                    gather_slots=self.gather_slots)
+                    gather_slots=self.gather_slots, warp_agg=self.warp_agg)
 
     def __repr__(self):
         return "Tune(%s)" % ", ".join("%s=%s" % kv for kv in self.as_dict().items())

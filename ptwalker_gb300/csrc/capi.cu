@@ -971,6 +971,20 @@ try {
                     }
     if (cand.empty()) return fail(PTW_EINVAL, "no walk configuration launches on this device");
     std::sort(cand.begin(), cand.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+    // warp-aggregated visits for the three fastest register-resident candidates
+    {
+        std::vector<ptw_tune> agg;
+        for (const auto &c : cand)
+            if (agg.size() < 3 && c.second.min_blocks == 0 && c.second.gather_slots == 0) agg.push_back(c.second);
+        for (ptw_tune t : agg) {
+            t.warp_agg = 1;
+            float med = 0;
+            int rc = time_walk(t, 3, &med);
+            if (rc) return rc;
+            if (med > 0) cand.push_back({med, t});
+        }
+        std::sort(cand.begin(), cand.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+    }
     cand.resize(std::min<size_t>(cand.size(), 6));
     std::vector<float> sum(cand.size(), 0.f);
     for (int round = 0; round < 3; ++round)

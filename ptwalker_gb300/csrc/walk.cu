@@ -81,7 +81,25 @@ __device__ __forceinline__ void count_visit(const WalkArgs &a, uint32_t *s_hot, 
     else red_add_hint(&a.counts[v], 1u, pol);
 }
 
-template <bool ENDPOINT, int ILP, bool HOT, bool EXT>
+// Warp-aggregated visit (all 32 lanes call it): lanes with `on` set count
+// vertex v; lanes counting the same non-hot vertex merge into one reduction
+// of the group's size by its lowest lane.
+template <bool HOT>
+__device__ __forceinline__ void count_visit_agg(const WalkArgs &a, uint32_t *s_hot, uint32_t v, bool on,
+                                                uint32_t lt_mask, uint64_t pol)
+{
+    const bool hot = HOT && v < a.hot_k;
+    const unsigned m = __ballot_sync(kFull, on && !hot);
+    if (!on) return;
+    if (hot) {
+        atomicAdd(&s_hot[v], 1u);
+        return;
+    }
+    const unsigned grp = __match_any_sync(m, v);
+    if ((grp & lt_mask) == 0) red_add_hint(&a.counts[v], (uint32_t)__popc(grp), pol);
+}
+
+template <bool ENDPOINT, int ILP, bool HOT, bool EXT, bool AGG = false>
 __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
 {
     if (HOT) {
@@ -179,29 +197,35 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
         }
 #pragma unroll
         for (int k = 0; k < ILP; ++k) {
-            if (!act[k]) continue;
-            bool done;
-            if (rec[k].y == 0) {
-                done = true;  // no out-edge: the walk ends here
-            } else {
-                v[k] = nb[k];
-                if (EXT) {
-                    rec[k] = nrec[k];
-                    have[k] = true;
+            bool counted = false;  // AGG: this lane moved and counts v[k] below
+            if (act[k]) {
+                bool done;
+                if (rec[k].y == 0) {
+                    done = true;  // no out-edge: the walk ends here
+                } else {
+                    v[k] = nb[k];
+                    if (EXT) {
+                        rec[k] = nrec[k];
+                        have[k] = true;
+                    }
+                    ++step[k];
+                    ++moves;
+                    if (!ENDPOINT) {
+                        if (AGG) counted = true;
+                        else count_visit<HOT>(a, s_hot, v[k], pol_keep);
+                    }
+                    done = (uint64_t)r[k].y < a.thr || (a.max_moves && step[k] >= a.max_moves);
                 }
-                ++step[k];
-                ++moves;
-                if (!ENDPOINT) count_visit<HOT>(a, s_hot, v[k], pol_keep);
-                done =(uint64_t)r[k].y < a.thr || (a.max_moves && step[k] >= a.max_moves);
-            }
-            if (done) {
-                if (ENDPOINT) {
-                    const uint64_t j = wid[k] - a.w_begin;
-                    *reinterpret_cast<uint2 *>(&a.pairs[2 * j]) =
-                        make_uint2(a.int2name[s0[k]], a.int2name[v[k]]);
+                if (done) {
+                    if (ENDPOINT) {
+                        const uint64_t j = wid[k] - a.w_begin;
+                        *reinterpret_cast<uint2 *>(&a.pairs[2 * j]) =
+                            make_uint2(a.int2name[s0[k]], a.int2name[v[k]]);
+                    }
+                    act[k] = false;
                 }
-                act[k] = false;
             }
+            if (AGG && !ENDPOINT) count_visit_agg<HOT>(a, s_hot, v[k], counted, lt_mask, pol_keep);
         }
     }
 
@@ -223,6 +247,14 @@ __global__ void k_walk(const WalkArgs a)
 {
     extern __shared__ uint32_t s_hot[];
     walk_body<ENDPOINT, ILP, HOT, EXT>(a, s_hot);
+}
+
+// Count walks with warp-aggregated visits (tune.warp_agg).
+template <int ILP, bool HOT, bool EXT>
+__global__ void k_walk_agg(const WalkArgs a)
+{
+    extern __shared__ uint32_t s_hot[];
+    walk_body<false, ILP, HOT, EXT, true>(a, s_hot);
 }
 
 // Register caps so that two blocks fit on an SM, for more walkers in flight:
@@ -595,6 +627,21 @@ void *pick_walk_async(bool endpoint, bool hot, int slots)
     return hot ? (void *)k_walk_async<false, true, 8> : (void *)k_walk_async<false, false, 8>;
 }
 
+template <bool H, bool X> void *agg_fn(int ilp)
+{
+    switch (ilp) {
+    case 1: return (void *)k_walk_agg<1, H, X>;
+    case 4: return (void *)k_walk_agg<4, H, X>;
+    default: return (void *)k_walk_agg<2, H, X>;
+    }
+}
+
+void *pick_walk_agg(int ilp, bool hot, bool ext)
+{
+    if (ext) return hot ? agg_fn<true, true>(ilp) : agg_fn<false, true>(ilp);
+    return hot ? agg_fn<true, false>(ilp) : agg_fn<false, false>(ilp);
+}
+
 // min_blocks 2 picks the register cap by block size (checked by check_tune).
 void *pick_walk(bool endpoint, int ilp, bool hot, int min_blocks, int block, bool ext)
 {
@@ -680,6 +727,9 @@ int check_tune(const ptw_tune &t)
     if (t.gather_slots != 0 && t.gather_slots != 8 && t.gather_slots != 16)
         return fail(PTW_EINVAL, "tune.gather_slots must be 0, 8 or 16");
     if (t.gather_slots && t.block > 256) return fail(PTW_EINVAL, "tune.gather_slots needs tune.block <= 256");
+    if (t.warp_agg != 0 && t.warp_agg != 1) return fail(PTW_EINVAL, "tune.warp_agg must be 0 or 1");
+    if (t.warp_agg && (t.min_blocks == 2 || t.gather_slots))
+        return fail(PTW_EINVAL, "tune.warp_agg needs min_blocks 0 and gather_slots 0");
     return PTW_OK;
 }
 
@@ -716,7 +766,8 @@ int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t)
     a.col_ext = g->dg.col_ext;
     a.vtx_ext = g->dg.vtx_ext;
     void *fn = slots ? pick_walk_async(wl.endpoint, hot, t.gather_slots)
-                     : pick_walk(wl.endpoint, t.ilp, hot, t.min_blocks, t.block, ext);
+               : (t.warp_agg && !wl.endpoint) ? pick_walk_agg(t.ilp, hot, ext)
+                                              : pick_walk(wl.endpoint, t.ilp, hot, t.min_blocks, t.block, ext);
     const size_t smem = slots ? async_smem(t.gather_slots, t.block, a.hot_k) : hot ? (size_t)a.hot_k * 4 : 0;
     if (smem > 227 * 1024) return fail(PTW_EINVAL, "tune.gather_slots x tune.block x hot_k need too much shared memory");
     if (smem > 48 * 1024)

@@ -79,6 +79,10 @@ def test_ppr_sources_and_query_ids(gpu, G16, s16_canon, sources, W, qid):
     dict(block=128, ilp=2, chunk=7, hot_k=0, gather_slots=8),
     dict(block=64, ilp=1, chunk=256, hot_k=100, gather_slots=8, cache_hints=0),
     dict(block=256, ilp=4, chunk=4096, hot_k=10000, gather_slots=16),
+    dict(block=512, ilp=4, chunk=64, hot_k=8192, cache_hints=1, ext_columns=1, warp_agg=1),
+    dict(block=1024, ilp=2, chunk=256, hot_k=8192, cache_hints=1, warp_agg=1),
+    dict(block=96, ilp=1, chunk=3, hot_k=0, warp_agg=1),
+    dict(block=256, ilp=2, chunk=64, hot_k=50, cache_hints=0, ext_columns=1, warp_agg=1),
 ])
 def test_launch_parameters_do_not_change_results(gpu, G16, s16_canon, tune):
     saved = G16.tune
@@ -98,6 +102,8 @@ def test_invalid_tune_rejected(gpu, G16):
         G16.tune = gpu.Tune(ilp=3)
     with pytest.raises(gpu.PTWError):
         G16.tune = gpu.Tune(gather_slots=4)
+    with pytest.raises(gpu.PTWError):
+        G16.tune = gpu.Tune(block=512, warp_agg=1, min_blocks=2)
     with pytest.raises(gpu.PTWError):
         G16.tune = gpu.Tune(block=512, gather_slots=8)
     saved = G16.tune

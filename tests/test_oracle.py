@@ -90,6 +90,26 @@ def test_paths_are_walks_and_prefix_of_counts(s16_canon):
             assert paths[j, moves[j]] == pairs[j, 1]
 
 
+@pytest.mark.parametrize("part_bytes", [1 << 12, 1 << 16, 1 << 20, 1 << 40])
+def test_partitioned_port_equals_replay(s16_canon, part_bytes):
+    """The timed CPU baseline (partition sweeps with per-(thread, partition)
+    walker pools, partitioned.c) counts exactly what the replay counts, for
+    every start mode, with move caps, across partition sizes and thread
+    counts (from thousands of partitions down to one)."""
+    g = s16_canon
+    from oracle.replay import START_PER_VERTEX, START_SOURCES, START_UNIFORM
+    cases = [(0, g.n, 0.15, 31, START_PER_VERTEX, None, 0),
+             (1 << 33, (1 << 33) + 60000, 0.3, 9, START_UNIFORM, None, 4),
+             (5 << 32, (5 << 32) + 40000, 0.2, 3, START_SOURCES, [int(g.names[5]), int(g.names[17]), int(g.names[99])], 0)]
+    for w0, w1, sp, seed, mode, src, mm in cases:
+        want, mv = oracle.replay_counts(g, w0, w1, sp, seed, mode, src, max_moves=mm, threads=4)
+        for th in (1, 3):
+            got, m2, info = oracle.partitioned_counts(g, w0, w1, sp, seed, mode, src, max_moves=mm, threads=th,
+                                                      part_bytes=part_bytes)
+            assert m2 == mv and np.array_equal(got, want), (part_bytes, th, mode)
+            assert info["partitions"] >= 1 and info["sweeps"] >= 1
+
+
 def test_dead_end_semantics():
     # 0 -> 1 -> 2, vertex 2 has no out-edge
     g = oracle.canonical_from_edges([0, 1], [1, 2])
