@@ -177,6 +177,18 @@ PORT_KIND = ("partitioned port: the reference's partition sweeps with per-(threa
              "counts equal to the oracle's")
 
 
+# The reference's own binary cannot run on the GPU host (its sources are not
+# there; no cross compiler here).  oracle/ref/calibrate.py timed it beside the
+# ports on one 8-core x86 host (R-MAT, W = |V|, sp 0.15, uniform starts, median
+# of 3): reference binary / partitioned port = 1.26 at scale 16 (54.9 vs
+# 43.6 M steps/s) and 2.10 at scale 20 (100.1 vs 47.7 M steps/s); at scale 22
+# the binary aborts with glibc heap corruption, so no larger figure exists.
+PORT_CALIBRATION = {"host": "x86_64, 8 cores (the build container)", "script": "oracle/ref/calibrate.py",
+                    "reference_over_partitioned_port": {"rmat-s16": 1.26, "rmat-s20": 2.10,
+                                                        "rmat-s22": "reference binary aborts (heap corruption)"},
+                    "reference_over_atomic_port": {"rmat-s16": 1.38, "rmat-s20": 3.18}}
+
+
 def cpu_port_run(canon, sp, seed, n_walkers, threads):
     import oracle
     t0 = time.perf_counter()
@@ -211,6 +223,7 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     canon = oracle.rmat_clean_csr(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed, threads)
+    oracle.replay.degree_relabelled(canon, threads)  # graph-load work, as in the reference
     build_s = time.perf_counter() - t0
     # each step a bounded sample, sized so that warm-up + timed steps take
     # about 90 s of walking whatever K and W are (at most 2 s per step)
@@ -230,6 +243,7 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": config(args, world), "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "port": PORT_KIND, "calibration": PORT_CALIBRATION,
                          "sample": "first %d of %d walkers per step (per-vertex starts) of the same "
                                    "workload; graph built on the host in %.1f s"
                                    % (S, canon.n, build_s)},
@@ -706,8 +720,10 @@ def run_ours(args):
         import oracle
         canon = oracle.CanonicalGraph(names=names, row_ptr=row_ptr, col=col)
         threads = os.cpu_count() or 1
+        oracle.replay.degree_relabelled(canon, threads)  # graph-load work, as in the reference
         S, mv, dt = cpu_port_sample(canon, args.sp, 4242, threads, target_s=3.0)
-        cpu = {"value": mv / dt, "unit": UNIT, "cores": threads, "kind": "port",
+        cpu = {"value": mv / dt, "unit": UNIT, "cores": threads, "kind": "port", "port": PORT_KIND,
+               "calibration": PORT_CALIBRATION,
                "sample": "first %d of %d walkers (per-vertex starts) of the same workload, %d moves "
                          "in %.2f s" % (S, n, mv, dt)}
 

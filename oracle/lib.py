@@ -53,10 +53,12 @@ def load_lib():
                                        ctypes.POINTER(ctypes.c_uint64),
                                        ctypes.POINTER(u64p), ctypes.POINTER(u32p)]
     lib.ora_rmat_clean_csr.restype = ctypes.c_int
-    lib.ora_partitioned_walks.argtypes = [u64p, u32p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64,
+    lib.ora_partitioned_walks.argtypes = [u64p, u32p, ctypes.c_uint32, u32p, ctypes.c_uint64, ctypes.c_uint64,
                                           ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, u32p, ctypes.c_uint32,
                                           ctypes.c_uint32, ctypes.c_uint64, u32p, ctypes.c_int, u64p]
     lib.ora_partitioned_walks.restype = ctypes.c_uint64
+    lib.ora_degree_relabel.argtypes = [u64p, u32p, ctypes.c_uint32, u32p, u64p, u32p, ctypes.c_int]
+    lib.ora_degree_relabel.restype = ctypes.c_int
     lib.ora_free.argtypes = [ctypes.c_void_p]
     lib.ora_free.restype = None
     _lib = lib

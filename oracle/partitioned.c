@@ -15,9 +15,13 @@
  * touched only by the thread sweeping it, so counting needs no atomics, and
  * its rows and counters stay in that core's caches while it is swept.
  *
- * Here: partitions are ranges of 2^k consecutive vertex indices, k chosen so
- * that a partition's row offsets, counters and column entries take about
- * part_bytes on average; walkers are 16-byte records kept in pools per
+ * Here: the vertices are relabelled by descending degree (as the reference
+ * does when it loads a graph, src/core/graph.hpp:515-628), so the hubs that
+ * most walkers stand on share partitions; partitions are ranges of
+ * consecutive ids cut so that a partition's row offsets, counters and column
+ * entries take about part_bytes (a hub whose row alone is larger gets a
+ * partition of its own, as the reference's hub partitions do,
+ * src/core/graph.hpp:159-169); walkers are 16-byte records kept in pools per
  * (thread, partition), as in the reference.  The draws are the oracle's
  * Philox stream (oracle.c), and every position is counted once when the
  * walker is processed there, so the counts and the move total equal
@@ -98,6 +102,18 @@ static inline uint32_t start_index(uint64_t wid, uint32_t n, int start_mode, con
     return sources[mulhi(w[0], n_sources)];
 }
 
+/* the partition holding id v: the last p with bounds[p] <= v */
+static inline uint32_t part_of(const uint32_t *bounds, uint32_t P, uint32_t v)
+{
+    uint32_t lo = 0, hi = P; /* bounds[lo] <= v < bounds[hi] */
+    while (hi - lo > 1) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (bounds[mid] <= v) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 static inline int thread_id(void)
 {
 #ifdef _OPENMP
@@ -109,17 +125,21 @@ static inline int thread_id(void)
 
 /*
  * Count walks of walkers [w_begin, w_end) (semantics of ora_replay_walks).
- * counts[n] is overwritten.  info[3] (may be NULL): partitions, sweeps,
- * walkers moved between partitions.  Returns the total number of moves, or
- * UINT64_MAX when host memory runs out.
+ * The graph may be relabelled: perm (NULL = none) maps a canonical vertex
+ * index to its id in row_ptr / col, whose rows keep the canonical order of
+ * their neighbours (so neighbour rank r is the same neighbour); start
+ * indices are mapped through it, sources are given relabelled.  counts[n]
+ * (by relabelled id) is overwritten.  info[3] (may be NULL): partitions,
+ * sweeps, walkers moved between partitions.  Returns the total number of
+ * moves, or UINT64_MAX when host memory runs out.
  *
  * Pools: cur[t * P + p] holds the walkers thread t handed to partition p in
  * the previous sweep.  A sweep takes partitions dynamically; the thread that
  * takes p advances the walkers of every thread's pool for p and appends each
  * walker that crosses into partition q to its own pool nxt[self * P + q].
  */
-uint64_t ora_partitioned_walks(const uint64_t *row_ptr, const uint32_t *col, uint32_t n, uint64_t w_begin,
-                               uint64_t w_end, uint64_t thr, uint64_t seed, int start_mode,
+uint64_t ora_partitioned_walks(const uint64_t *row_ptr, const uint32_t *col, uint32_t n, const uint32_t *perm,
+                               uint64_t w_begin, uint64_t w_end, uint64_t thr, uint64_t seed, int start_mode,
                                const uint32_t *sources, uint32_t n_sources, uint32_t max_moves,
                                uint64_t part_bytes, uint32_t *counts, int n_threads, uint64_t *info)
 {
@@ -128,17 +148,29 @@ uint64_t ora_partitioned_walks(const uint64_t *row_ptr, const uint32_t *col, uin
     memset(counts, 0, (size_t)n * sizeof *counts);
     if (info) info[0] = info[1] = info[2] = 0;
     if (n == 0 || W == 0) return 0;
-    /* partition size: 2^k vertices of (8 + 4) bytes plus their columns */
-    const double per_vertex = 12.0 + 4.0 * (double)row_ptr[n] / (double)n;
-    int k = 0;
-    while (k < 31 && (double)(2ull << k) * per_vertex <= (double)(part_bytes ? part_bytes : 1)) ++k;
-    const uint32_t P = (uint32_t)(((uint64_t)n + (1ull << k) - 1) >> k);
+    /* partitions: consecutive ids while the bytes (12 per vertex, 4 per
+     * column entry) stay within part_bytes; bounds[p] = first id of p */
+    const uint64_t budget = part_bytes ? part_bytes : 1;
+    uint32_t *bounds = (uint32_t *)malloc(((size_t)n + 1) * sizeof *bounds);
+    uint32_t P = 0;
+    if (bounds) {
+        uint64_t bytes = 0;
+        for (uint32_t v = 0; v < n; ++v) {
+            const uint64_t b = 12 + 4 * (row_ptr[v + 1] - row_ptr[v]);
+            if (v == 0 || bytes + b > budget) {
+                bounds[P++] = v;
+                bytes = 0;
+            }
+            bytes += b;
+        }
+        bounds[P] = n;
+    }
     const size_t NP = (size_t)T * P;
-    pool_t *cur = (pool_t *)calloc(NP, sizeof *cur);
-    pool_t *nxt = (pool_t *)calloc(NP, sizeof *nxt);
+    pool_t *cur = (pool_t *)calloc(NP ? NP : 1, sizeof *cur);
+    pool_t *nxt = (pool_t *)calloc(NP ? NP : 1, sizeof *nxt);
     uint64_t *moves = (uint64_t *)calloc((size_t)T * 8, sizeof *moves); /* one cache line per thread */
     uint64_t total = UINT64_MAX, sweeps = 0, migrations = 0;
-    int ok = cur && nxt && moves;
+    int ok = bounds && cur && nxt && moves;
 
     if (ok) {
         /* each thread places a static slice of the walkers at their starts */
@@ -149,9 +181,10 @@ uint64_t ora_partitioned_walks(const uint64_t *row_ptr, const uint32_t *col, uin
 #pragma omp for schedule(static)
             for (int64_t i = 0; i < (int64_t)W; ++i) {
                 const uint64_t wid = w_begin + (uint64_t)i;
-                const uint32_t v = start_index(wid, n, start_mode, sources, n_sources, seed);
+                uint32_t v = start_index(wid, n, start_mode, sources, n_sources, seed);
+                if (perm && start_mode != 2) v = perm[v];
                 const walker_t x = {wid, v, 0u};
-                ok &= push(&mine[v >> k], x);
+                ok &= push(&mine[part_of(bounds, P, v)], x);
             }
         }
     }
@@ -165,6 +198,7 @@ uint64_t ora_partitioned_walks(const uint64_t *row_ptr, const uint32_t *col, uin
             uint64_t mv = 0;
 #pragma omp for schedule(dynamic, 1)
             for (int64_t p = 0; p < (int64_t)P; ++p) {
+                const uint32_t lo = bounds[p], span = bounds[p + 1] - bounds[p];
                 for (int t = 0; t < T; ++t) {
                     pool_t *in = &cur[(size_t)t * P + p];
                     for (size_t i = 0; i < in->n; ++i) {
@@ -181,9 +215,9 @@ uint64_t ora_partitioned_walks(const uint64_t *row_ptr, const uint32_t *col, uin
                             ++step;
                             ++mv;
                             stop = (uint64_t)r[1] < thr || (max_moves && step >= max_moves);
-                            if ((v >> k) != (uint32_t)p) { /* into another partition's pool */
+                            if (v - lo >= span) { /* into another partition's pool */
                                 const walker_t y = {x.wid, v, (step << 1) | (uint32_t)stop};
-                                ok &= push(&out[v >> k], y);
+                                ok &= push(&out[part_of(bounds, P, v)], y);
                                 break;
                             }
                             counts[v]++;
@@ -210,10 +244,55 @@ uint64_t ora_partitioned_walks(const uint64_t *row_ptr, const uint32_t *col, uin
         info[1] = sweeps;
         info[2] = migrations;
     }
+    free(bounds);
     for (size_t i = 0; cur && i < NP; ++i) free(cur[i].w);
     for (size_t i = 0; nxt && i < NP; ++i) free(nxt[i].w);
     free(cur);
     free(nxt);
     free(moves);
     return total;
+}
+
+/*
+ * The graph relabelled by descending degree, ties by index (graph-load work
+ * of the partitioned walks): perm[canonical index] = new id; row_ptr_out
+ * [n + 1] and col_out [m] hold the relabelled CSR, each row keeping the
+ * canonical order of its neighbours.  Returns 0, or -1 when host memory runs
+ * out.
+ */
+int ora_degree_relabel(const uint64_t *row_ptr, const uint32_t *col, uint32_t n, uint32_t *perm,
+                       uint64_t *row_ptr_out, uint32_t *col_out, int n_threads)
+{
+    const int T = n_threads < 1 ? 1 : n_threads;
+    uint64_t maxdeg = 0;
+    for (uint32_t v = 0; v < n; ++v) {
+        const uint64_t d = row_ptr[v + 1] - row_ptr[v];
+        if (d > maxdeg) maxdeg = d;
+    }
+    /* counting sort by degree, descending; stable, so ties stay in index order */
+    uint64_t *first = (uint64_t *)calloc(maxdeg + 2, sizeof *first);
+    uint32_t *order = (uint32_t *)malloc(((size_t)n + 1) * sizeof *order);
+    if (!first || !order) {
+        free(first);
+        free(order);
+        return -1;
+    }
+    for (uint32_t v = 0; v < n; ++v) first[maxdeg - (row_ptr[v + 1] - row_ptr[v]) + 1]++;
+    for (uint64_t d = 1; d <= maxdeg + 1; ++d) first[d] += first[d - 1];
+    for (uint32_t v = 0; v < n; ++v) {
+        const uint64_t slot = first[maxdeg - (row_ptr[v + 1] - row_ptr[v])]++;
+        order[slot] = v;
+        perm[v] = (uint32_t)slot;
+    }
+    row_ptr_out[0] = 0;
+    for (uint32_t j = 0; j < n; ++j) row_ptr_out[j + 1] = row_ptr_out[j] + (row_ptr[order[j] + 1] - row_ptr[order[j]]);
+#pragma omp parallel for schedule(dynamic, 4096) num_threads(T)
+    for (int64_t j = 0; j < (int64_t)n; ++j) {
+        const uint32_t v = order[j];
+        const uint64_t a = row_ptr[v], len = row_ptr[v + 1] - a, o = row_ptr_out[j];
+        for (uint64_t e = 0; e < len; ++e) col_out[o + e] = perm[col[a + e]];
+    }
+    free(first);
+    free(order);
+    return 0;
 }

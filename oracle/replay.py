@@ -87,20 +87,48 @@ def replay_paths(g, w_begin, w_end, L, seed, start_mode=START_PER_VERTEX,
     return paths
 
 
+def degree_relabelled(g, threads=None):
+    """The graph relabelled by descending degree (ties by index), rows
+    keeping the canonical order of their neighbours: (perm, row_ptr, col)
+    with perm[canonical index] = new id (ora_degree_relabel).  Cached on g:
+    it is graph-load work, kept out of the timed region as the reference's
+    own relabelling is."""
+    cached = getattr(g, "_degree_relabelled", None)
+    if cached is not None:
+        return cached
+    import os
+    lib = load_lib()
+    perm = np.empty(g.n, dtype=np.uint32)
+    row_ptr = np.empty(g.n + 1, dtype=np.uint64)
+    col = np.empty(g.m, dtype=np.uint32)
+    rc = lib.ora_degree_relabel(_p(g.row_ptr, ctypes.c_uint64), _p(g.col, ctypes.c_uint32), g.n,
+                                _p(perm, ctypes.c_uint32), _p(row_ptr, ctypes.c_uint64), _p(col, ctypes.c_uint32),
+                                threads or os.cpu_count() or 1)
+    if rc:
+        raise MemoryError("degree relabelling: host memory ran out")
+    g._degree_relabelled = (perm, row_ptr, col)
+    return g._degree_relabelled
+
+
 def partitioned_counts(g, w_begin, w_end, sp, seed, start_mode=START_PER_VERTEX, sources=None, max_moves=0,
                        threads=1, part_bytes=1 << 20):
     """The same visit counts as replay_counts, computed the way the reference
-    schedules its walkers (partition sweeps with per-partition pools,
-    partitioned.c): the timed CPU baseline.  Returns (counts, moves, info)
-    with info = {partitions, sweeps, migrations}."""
+    schedules its walkers (degree-sorted relabelling, partition sweeps with
+    per-(thread, partition) pools, partitioned.c): the timed CPU baseline.
+    Returns (counts by canonical index, moves, info) with info =
+    {partitions, sweeps, migrations}."""
     lib = load_lib()
+    perm, row_ptr, col = degree_relabelled(g)
     counts = np.zeros(g.n, dtype=np.uint32)
     src_arr, n_src = _sources_arg(g, start_mode, sources)
+    if src_arr is not None:
+        src_arr = np.ascontiguousarray(perm[src_arr], dtype=np.uint32)
     info = np.zeros(3, dtype=np.uint64)
     total = lib.ora_partitioned_walks(
-        _p(g.row_ptr, ctypes.c_uint64), _p(g.col, ctypes.c_uint32), g.n, w_begin, w_end, sp_threshold(sp), seed,
-        start_mode, _p(src_arr, ctypes.c_uint32), n_src, max_moves, int(part_bytes),
+        _p(row_ptr, ctypes.c_uint64), _p(col, ctypes.c_uint32), g.n, _p(perm, ctypes.c_uint32), w_begin, w_end,
+        sp_threshold(sp), seed, start_mode, _p(src_arr, ctypes.c_uint32), n_src, max_moves, int(part_bytes),
         _p(counts, ctypes.c_uint32), threads, _p(info, ctypes.c_uint64))
     if total == (1 << 64) - 1:
         raise MemoryError("partitioned walk: host memory ran out")
-    return counts, int(total), {"partitions": int(info[0]), "sweeps": int(info[1]), "migrations": int(info[2])}
+    return counts[perm], int(total), {"partitions": int(info[0]), "sweeps": int(info[1]),
+                                      "migrations": int(info[2])}
