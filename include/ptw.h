@@ -291,6 +291,20 @@ int ptw_graph_get_batch_tune(const ptw_graph *g, ptw_batch_tune *t);
  * (vertex name, count) pairs per query, sorted by name. */
 int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t nq, const ptw_batch_cfg *cfg,
                   ptw_batch **out);
+/* The same batch, resumable (no counterpart in the reference; its walks
+ * restart from scratch).  Each completed wave's lists are appended to the
+ * file at checkpoint_path (created when absent) before the next wave runs;
+ * a call finds the waves already in the file and runs only the queries
+ * without results.  At most max_waves waves run per call (0 = no limit):
+ * while queries remain, the call returns PTW_OK with *out = NULL, and a
+ * later call (or a new process) continues.  Draws depend on (seed, query
+ * id, walker rank) only, so the final results equal one uninterrupted
+ * ptw_ppr_batch call bit for bit.  The file is tied to the graph, the
+ * configuration and the query table: another batch's file is PTW_EINVAL.
+ * Host results only (no PTW_BATCH_DEVICE_RESULTS).  The caller deletes
+ * the file when done. */
+int ptw_ppr_batch_resumable(ptw_graph *g, const ptw_query *h_queries, uint32_t nq, const ptw_batch_cfg *cfg,
+                            const char *checkpoint_path, uint32_t max_waves, ptw_batch **out);
 /* Number of queries, total (name, count) entries, and walk statistics. */
 int ptw_batch_info(const ptw_batch *b, uint32_t *nq, uint64_t *entries, ptw_walk_stats *stats);
 /* h_offsets[nq + 1]: query i owns entries [h_offsets[i], h_offsets[i+1]).
@@ -428,6 +442,19 @@ int ptw_serve_get_stats(const ptw_server *s, ptw_serve_stats *out);
 /* Seconds since ptw_serve_open on the server's clock. */
 double ptw_serve_clock(const ptw_server *s);
 void ptw_serve_close(ptw_server *s);
+/* Saves a server's state between steps (no counterpart in the reference,
+ * which has no server): its configuration, clock and statistics, the
+ * pending queries, the active queries with the walker ranks run so far and
+ * their count tables, and the finished results not yet taken.  Written to
+ * path.tmp, then renamed over path. */
+int ptw_serve_save(const ptw_server *s, const char *path);
+/* Opens a server on graph g (the graph the state was saved from, else
+ * PTW_EINVAL) in the saved state; the clock continues from the saved one.
+ * Draws depend on (seed, query id, walker rank) only, so every query
+ * finishes with the same counts as on the server that was saved.
+ * PTW_ENOMEM when the table arena here cannot hold the saved active
+ * queries (a smaller table_bytes or less free device memory). */
+int ptw_serve_restore(ptw_graph *g, const char *path, ptw_server **out);
 
 /* Synthetic Chung-Lu power-law graph built on the device: n vertices with
  * expected degrees proportional to (i + 1)^(-1/(gamma-1)), mean degree

@@ -27,7 +27,7 @@ from .api import (  # noqa: F401
 )
 
 from .batch import (BatchResult, BatchTune, autotune_batch, get_batch_tune, ppr_batch,  # noqa: F401,E402
-                    set_batch_tune)
+                    ppr_batch_resumable, set_batch_tune)
 from .serving import Server, open_loop  # noqa: F401,E402
 
 __version__ = "0.1.0"

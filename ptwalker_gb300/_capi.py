@@ -148,6 +148,8 @@ SIGNATURES = [
     ("ptw_pagerank_noalloc", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), _vp, _vp]),
     ("ptw_ppr_batch", ctypes.c_int, [_G, ctypes.POINTER(Query), ctypes.c_uint32,
                                      ctypes.POINTER(BatchCfg), _GP]),
+    ("ptw_ppr_batch_resumable", ctypes.c_int, [_G, ctypes.POINTER(Query), ctypes.c_uint32,
+                                               ctypes.POINTER(BatchCfg), ctypes.c_char_p, ctypes.c_uint32, _GP]),
     ("ptw_batch_info", ctypes.c_int, [_G, ctypes.POINTER(ctypes.c_uint32), _u64p,
                                       ctypes.POINTER(WalkStats)]),
     ("ptw_batch_export", ctypes.c_int, [_G, _u64p, _u32p, _u32p]),
@@ -175,6 +177,8 @@ SIGNATURES = [
     ("ptw_serve_get_stats", ctypes.c_int, [_G, ctypes.POINTER(ServeStats)]),
     ("ptw_serve_clock", ctypes.c_double, [_G]),
     ("ptw_serve_close", None, [_G]),
+    ("ptw_serve_save", ctypes.c_int, [_G, ctypes.c_char_p]),
+    ("ptw_serve_restore", ctypes.c_int, [_G, ctypes.c_char_p, _GP]),
     ("ptw_graph_chung_lu", ctypes.c_int, [ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_uint64, _GP]),
     ("ptw_source_features", ctypes.c_int, [_G, _u32p, ctypes.c_uint32, _f32p]),

@@ -210,6 +210,23 @@ def autotune_batch(graph, sources, budgets, sp=0.2, seed=0, app="visits", query_
     return BatchTune.from_c(t), float(ms.value)
 
 
+def ppr_batch_resumable(graph, sources, budgets, checkpoint, sp=0.2, seed=0, app="visits", query_ids=None,
+                        max_moves=0, table_bytes=0, table_factor=0.0, top_k=0, max_waves=0):
+    """ppr_batch with its completed waves kept in the file `checkpoint`
+    (ptw_ppr_batch_resumable): runs at most max_waves waves (0 = all) and
+    returns None while queries remain, the BatchResult once all are done.
+    A later call, in this process or another, continues from the file."""
+    sources, budgets, query_ids, qs = _queries(sources, budgets, query_ids)
+    cfg = C.BatchCfg(float(sp), int(seed) & 0xFFFFFFFFFFFFFFFF, APPS[app], int(max_moves),
+                     int(table_bytes), float(table_factor), int(top_k), 0)
+    h = ctypes.c_void_p()
+    C.check(graph._lib.ptw_ppr_batch_resumable(graph.handle, qs, sources.shape[0], ctypes.byref(cfg),
+                                               str(checkpoint).encode(), int(max_waves), ctypes.byref(h)))
+    if not h.value:
+        return None
+    return BatchResult(graph, h, sources, budgets, query_ids, sp, app)
+
+
 def ppr_batch(graph, sources, budgets, sp=0.2, seed=0, app="visits", query_ids=None, max_moves=0,
               table_bytes=0, table_factor=0.0, top_k=0, device_results=False):
     sources = np.atleast_1d(np.asarray(sources, dtype=np.uint32))

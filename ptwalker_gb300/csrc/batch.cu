@@ -1115,10 +1115,172 @@ uint64_t table_slots(double sp, uint32_t max_moves, int32_t app, double factor, 
 
 using namespace ptw;
 
-extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t nq, const ptw_batch_cfg *cfg,
-                             ptw_batch **out)
-try {
-    NvtxRange nvtx("ptw_ppr_batch");
+namespace ptw {
+namespace {
+
+// ---- checkpoint file of a resumable batch ------------------------------------
+//
+// Header: magic "PTWBCK1\0", then a 64-bit key of everything the results
+// depend on (graph: n, m, id bound and its names; configuration: sp, seed,
+// app, max_moves, top_k; every query's source, id and budget).  Then one
+// record per completed wave:
+//   u32 'WAVE', u32 rerun (1 = dense rerun of overflowed queries),
+//   u32 k_ok, u32 k_overflow, u64 moves (first-pass waves only), u64 entries,
+//   u32 idx_ok[k_ok], u32 idx_overflow[k_overflow], u64 seg[k_ok + 1],
+//   u32 names[entries], u32 counts[entries], u32 'DONE'.
+// A record cut short (the process ended while writing it) is ignored and
+// overwritten by the next append.
+constexpr uint32_t kCkWave = 0x45564157u, kCkDone = 0x454E4F44u;
+const char kCkMagic[8] = {'P', 'T', 'W', 'B', 'C', 'K', '1', '\0'};
+
+struct Fnv {
+    uint64_t h = 1469598103934665603ull;
+    void add(const void *p, size_t n)
+    {
+        const unsigned char *c = (const unsigned char *)p;
+        for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
+    }
+    template <typename T> void val(const T &x) { add(&x, sizeof x); }
+};
+
+uint64_t checkpoint_key(const ptw_graph *g, const ptw_query *q, uint32_t nq, const ptw_batch_cfg *cfg)
+{
+    Fnv f;
+    f.val(g->dg.n);
+    f.val(g->dg.m);
+    f.val(g->dg.id_bound);
+    f.add(g->h_names, (size_t)g->dg.n * 4);
+    f.val(cfg->sp);
+    f.val(cfg->seed);
+    f.val(cfg->app);
+    f.val(cfg->max_moves);
+    f.val(cfg->top_k);
+    f.val(nq);
+    for (uint32_t i = 0; i < nq; ++i) {
+        f.val(q[i].source);
+        f.val(q[i].query_id);
+        f.val(q[i].budget);
+    }
+    return f.h;
+}
+
+struct Checkpoint {
+    FILE *f = nullptr;
+    long good = 0;  // end of the last complete record
+    ~Checkpoint()
+    {
+        if (f) std::fclose(f);
+    }
+};
+
+template <typename T> bool rd(FILE *f, T *p, size_t n = 1) { return std::fread(p, sizeof(T), n, f) == n; }
+
+// Opens (or creates) the checkpoint and loads its completed waves: their
+// results become WaveResults, their queries are marked done, and queries
+// that overflowed (and have no result yet) are marked for the dense rerun.
+int checkpoint_open(const char *path, uint64_t key, uint32_t nq, Checkpoint &ck, std::vector<WaveResult> &waves,
+                    std::vector<char> &done, std::vector<char> &dense_next, uint64_t *moves, uint32_t *n_waves)
+{
+    done.assign(nq, 0);
+    dense_next.assign(nq, 0);
+    ck.f = std::fopen(path, "r+b");
+    if (!ck.f) {
+        ck.f = std::fopen(path, "w+b");
+        if (!ck.f) return fail(PTW_EIO, std::string("cannot create checkpoint ") + path);
+        if (std::fwrite(kCkMagic, 1, 8, ck.f) != 8 || std::fwrite(&key, 8, 1, ck.f) != 1 || std::fflush(ck.f))
+            return fail(PTW_EIO, std::string("cannot write checkpoint ") + path);
+        ck.good = 16;
+        return PTW_OK;
+    }
+    char magic[8];
+    uint64_t k = 0;
+    if (!rd(ck.f, magic, 8) || std::memcmp(magic, kCkMagic, 8) || !rd(ck.f, &k))
+        return fail(PTW_EINVAL, std::string(path) + " is not a batch checkpoint");
+    if (k != key)
+        return fail(PTW_EINVAL, std::string(path) + " is the checkpoint of another batch (queries, "
+                                                     "configuration or graph differ)");
+    ck.good = 16;
+    for (;;) {
+        uint32_t hdr[4];
+        uint64_t mv = 0, ne = 0;
+        if (!rd(ck.f, hdr, 4) || hdr[0] != kCkWave || !rd(ck.f, &mv) || !rd(ck.f, &ne)) break;
+        const uint32_t k_ok = hdr[2], k_ovf = hdr[3];
+        if (k_ok > nq || k_ovf > nq) break;
+        std::vector<uint32_t> ok(k_ok), ovf(k_ovf);
+        WaveResult w;
+        w.c.seg.resize(k_ok + 1ull);
+        if (!rd(ck.f, ok.data(), k_ok) || !rd(ck.f, ovf.data(), k_ovf) || !rd(ck.f, w.c.seg.data(), k_ok + 1ull))
+            break;
+        if (w.c.seg[k_ok] != ne) break;
+        w.c.names.reset(new uint32_t[std::max<uint64_t>(ne, 1)]);
+        w.c.counts.reset(new uint32_t[std::max<uint64_t>(ne, 1)]);
+        uint32_t tail = 0;
+        if (!rd(ck.f, w.c.names.get(), ne) || !rd(ck.f, w.c.counts.get(), ne) || !rd(ck.f, &tail) ||
+            tail != kCkDone)
+            break;
+        bool valid = true;
+        for (uint32_t i : ok) valid = valid && i < nq;
+        for (uint32_t i : ovf) valid = valid && i < nq;
+        if (!valid) break;
+        w.c.n = w.c.cap = w.c.touched = ne;
+        w.c.h_names = w.c.names.get();
+        w.c.h_counts = w.c.counts.get();
+        w.idx = ok;
+        w.overflow.assign(k_ok, 0);
+        for (uint32_t i : ok) done[i] = 1;
+        for (uint32_t i : ovf) dense_next[i] = 1;
+        if (!hdr[1]) *moves += mv;
+        ++*n_waves;
+        waves.push_back(std::move(w));
+        ck.good = std::ftell(ck.f);
+    }
+    for (uint32_t i = 0; i < nq; ++i)
+        if (done[i]) dense_next[i] = 0;
+    return PTW_OK;
+}
+
+// Appends the last wave of `waves` (its completed queries and those that
+// overflowed) as one record, cutting off any partial record first.
+int checkpoint_append(Checkpoint &ck, const WaveResult &w, bool rerun, uint64_t moves)
+{
+    std::vector<uint32_t> ok, ovf;
+    std::vector<uint64_t> seg(1, 0);
+    for (size_t k = 0; k < w.idx.size(); ++k) {
+        if (w.overflow[k]) {
+            ovf.push_back(w.idx[k]);
+            continue;
+        }
+        ok.push_back(w.idx[k]);
+        seg.push_back(seg.back() + (w.c.seg[k + 1] - w.c.seg[k]));
+    }
+    if (std::fflush(ck.f) || ftruncate(fileno(ck.f), ck.good) || std::fseek(ck.f, ck.good, SEEK_SET))
+        return fail(PTW_EIO, "cannot position the batch checkpoint");
+    const uint32_t hdr[4] = {kCkWave, rerun ? 1u : 0u, (uint32_t)ok.size(), (uint32_t)ovf.size()};
+    const uint64_t ne = seg.back();
+    bool good = std::fwrite(hdr, 4, 4, ck.f) == 4 && std::fwrite(&moves, 8, 1, ck.f) == 1 &&
+                std::fwrite(&ne, 8, 1, ck.f) == 1 && std::fwrite(ok.data(), 4, ok.size(), ck.f) == ok.size() &&
+                std::fwrite(ovf.data(), 4, ovf.size(), ck.f) == ovf.size() &&
+                std::fwrite(seg.data(), 8, seg.size(), ck.f) == seg.size();
+    for (int pass = 0; pass < 2 && good; ++pass) {
+        const uint32_t *src = pass == 0 ? w.c.h_names : w.c.h_counts;
+        for (size_t k = 0; k < w.idx.size() && good; ++k) {
+            if (w.overflow[k]) continue;
+            const uint64_t len = w.c.seg[k + 1] - w.c.seg[k];
+            good = std::fwrite(src + w.c.seg[k], 4, len, ck.f) == len;
+        }
+    }
+    good = good && std::fwrite(&kCkDone, 4, 1, ck.f) == 1 && std::fflush(ck.f) == 0 && fsync(fileno(ck.f)) == 0;
+    if (!good) return fail(PTW_EIO, "cannot write the batch checkpoint");
+    ck.good = std::ftell(ck.f);
+    return PTW_OK;
+}
+
+// The batch, optionally resumable: with ckpt_path, completed waves are read
+// from and appended to that file, and at most max_waves (0 = all) waves run
+// in this call; *out stays null while queries remain.
+int batch_impl(ptw_graph *g, const ptw_query *h_queries, uint32_t nq, const ptw_batch_cfg *cfg,
+               const char *ckpt_path, uint32_t max_waves, ptw_batch **out)
+{
     if (!cfg) return fail(PTW_EINVAL, "null argument");
     if (const int rc0 = check_stop(cfg->sp, cfg->max_moves)) return rc0;
     if (!g || !out) return fail(PTW_EINVAL, "null argument");
@@ -1172,30 +1334,65 @@ try {
     const uint64_t thr = stop_threshold(cfg->sp);
     uint64_t moves = 0;
     float walk_ms = 0;
+    // a resumable batch: completed waves come from its checkpoint
+    Checkpoint ck;
+    std::vector<char> done(nq, 0), dense_next(nq, 0);
+    uint32_t waves_loaded = 0, waves_run = 0;
+    if (ckpt_path) {
+        const int rc0 = checkpoint_open(ckpt_path, checkpoint_key(g, h_queries, nq, cfg), nq, ck, waves, done,
+                                        dense_next, &moves, &waves_loaded);
+        if (rc0) {
+            delete b;
+            return rc0;
+        }
+    }
+    auto budget_left = [&] { return max_waves == 0 || waves_run < max_waves; };
     PTW_CUDA(cudaEventRecord(g->ev[3], g->stream));
     int rc = PTW_OK;
     // Waves in query order, admitted while their tables fit the budget.
-    for (uint32_t i = 0; i < nq && rc == PTW_OK;) {
+    uint32_t i = 0;
+    auto skip_done = [&] {
+        while (i < nq && (done[i] || dense_next[i])) ++i;
+    };
+    skip_done();
+    while (i < nq && rc == PTW_OK && budget_left()) {
         std::vector<WaveQuery> wave;
         uint64_t bytes = 0;
         while (i < nq && (wave.empty() || bytes + all[i].cap * 8 <= budget_bytes) && wave.size() < (1u << 20)) {
             bytes += all[i].cap * 8;
             wave.push_back(all[i++]);
+            skip_done();
         }
-        rc = run_wave(g, wave, cfg, thr, waves, overflow, &moves, &walk_ms, &ph);
+        uint64_t mv = 0;
+        rc = run_wave(g, wave, cfg, thr, waves, overflow, &mv, &walk_ms, &ph);
+        moves += mv;
+        ++waves_run;
+        if (rc == PTW_OK && ckpt_path) rc = checkpoint_append(ck, waves.back(), false, mv);
     }
     // Queries whose hash table filled run again with a dense array (which
     // cannot fill).
     std::vector<uint32_t> again;
     again.swap(overflow);
-    for (size_t k = 0; k < again.size() && rc == PTW_OK; ++k) {
-        WaveQuery w = all[again[k]];
+    for (uint32_t q = 0; q < nq; ++q)
+        if (dense_next[q]) again.push_back(q);
+    std::sort(again.begin(), again.end());
+    size_t reran = 0;
+    for (; reran < again.size() && rc == PTW_OK && budget_left(); ++reran) {
+        WaveQuery w = all[again[reran]];
         const TableSize d = dense_table(n);
         w.cap = d.slots;
         w.dense = true;
         uint64_t m2 = 0;
         rc = run_wave(g, {w}, cfg, thr, waves, overflow, &m2, &walk_ms, &ph);
+        ++waves_run;
         if (rc == PTW_OK && !overflow.empty()) rc = fail(PTW_EFULL, "count table overflow in a dense array");
+        if (rc == PTW_OK && ckpt_path) rc = checkpoint_append(ck, waves.back(), true, 0);
+    }
+    if (rc == PTW_OK && (i < nq || reran < again.size())) {
+        // the wave limit was reached with queries left: progress is in the checkpoint
+        PTW_CUDA(cudaStreamSynchronize(g->stream));
+        delete b;
+        return PTW_OK;
     }
     t_waves = clk();
     if (rc == PTW_OK) rc = assemble(g, b, waves);
@@ -1232,7 +1429,7 @@ try {
     P.copy_tail_ms = tail;
     P.host_pages_ms = ph.host_pages_ms;
     P.copy_bytes = ph.copy_bytes;
-    P.waves = (uint32_t)waves.size();
+    P.waves = (uint32_t)waves.size() - waves_loaded;
     P.reruns = (uint32_t)again.size();
     P.call_ms = 1e3 * (clk() - t_enter);
     if (timing)
@@ -1240,6 +1437,30 @@ try {
                      waves.size(), 1e3 * (t_waves - t_enter), 1e3 * (t_asm - t_waves), 1e3 * (clk() - t_enter));
     *out = b;
     return PTW_OK;
+}
+
+}  // namespace
+}  // namespace ptw
+
+extern "C" int ptw_ppr_batch(ptw_graph *g, const ptw_query *h_queries, uint32_t nq, const ptw_batch_cfg *cfg,
+                             ptw_batch **out)
+try {
+    NvtxRange nvtx("ptw_ppr_batch");
+    return batch_impl(g, h_queries, nq, cfg, nullptr, 0, out);
+} catch (...) {
+    return host_exception();
+}
+
+extern "C" int ptw_ppr_batch_resumable(ptw_graph *g, const ptw_query *h_queries, uint32_t nq,
+                                       const ptw_batch_cfg *cfg, const char *checkpoint_path, uint32_t max_waves,
+                                       ptw_batch **out)
+try {
+    NvtxRange nvtx("ptw_ppr_batch_resumable");
+    if (out) *out = nullptr;
+    if (!checkpoint_path) return fail(PTW_EINVAL, "null checkpoint path");
+    if (cfg && (cfg->flags & PTW_BATCH_DEVICE_RESULTS))
+        return fail(PTW_EINVAL, "a resumable batch keeps its results on the host (no PTW_BATCH_DEVICE_RESULTS)");
+    return batch_impl(g, h_queries, nq, cfg, checkpoint_path, max_waves, out);
 } catch (...) {
     return host_exception();
 }

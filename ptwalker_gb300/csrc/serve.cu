@@ -11,10 +11,14 @@
 // finish within the tick, so a query is done once all its ranks have run.
 // Draws depend on (query id, rank) only: a query's counts are the same
 // however its ranks are split across ticks and whatever runs beside it.
+#include <unistd.h>
+
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cstring>
 #include <deque>
+#include <string>
 #include <map>
 #include <vector>
 
@@ -603,4 +607,221 @@ try {
     delete s;
 } catch (...) {
     host_exception();
+}
+
+// ---- checkpoint / resume ------------------------------------------------------
+//
+// File: magic "PTWSRV1\0", a 64-bit key of the graph (n, m, id bound, names),
+// the configuration (ptw_serve_cfg), the server clock and statistics, then
+//   pending queries: ptw_query, u8 full, f64 submit_s
+//   active queries:  ptw_query, u8 full, f64 submit_s, f64 admit_s,
+//                    u64 ranks run, u8 dense, u64 table slots, the table
+//   finished results not taken: ptw_serve_result, names[n], counts[n]
+// and a closing magic.
+
+namespace ptw {
+namespace {
+
+const char kSrvMagic[8] = {'P', 'T', 'W', 'S', 'R', 'V', '1', '\0'};
+
+uint64_t graph_key(const ptw_graph *g)
+{
+    uint64_t h = 1469598103934665603ull;
+    auto add = [&](const void *p, size_t n) {
+        const unsigned char *c = (const unsigned char *)p;
+        for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
+    };
+    add(&g->dg.n, sizeof g->dg.n);
+    add(&g->dg.m, sizeof g->dg.m);
+    add(&g->dg.id_bound, sizeof g->dg.id_bound);
+    add(g->h_names, (size_t)g->dg.n * 4);
+    return h;
+}
+
+struct File {
+    FILE *f = nullptr;
+    bool ok = true;
+    ~File()
+    {
+        if (f) std::fclose(f);
+    }
+    template <typename T> void put(const T *p, size_t n = 1)
+    {
+        ok = ok && std::fwrite(p, sizeof(T), n, f) == n;
+    }
+    template <typename T> void get(T *p, size_t n = 1)
+    {
+        ok = ok && std::fread(p, sizeof(T), n, f) == n;
+    }
+};
+
+}  // namespace
+}  // namespace ptw
+
+extern "C" int ptw_serve_save(const ptw_server *s, const char *path)
+try {
+    NvtxRange nvtx("ptw_serve_save");
+    if (!s || !path) return fail(PTW_EINVAL, "null argument");
+    PTW_CUDA(cudaSetDevice(s->g->device));
+    PTW_CUDA(cudaStreamSynchronize(s->g->stream));
+    const std::string tmp = std::string(path) + ".tmp";
+    File out;
+    out.f = std::fopen(tmp.c_str(), "wb");
+    if (!out.f) return fail(PTW_EIO, "cannot create " + tmp);
+    const uint64_t key = graph_key(s->g);
+    const double clock = now_s(s);
+    const uint64_t counts[3] = {s->pending.size(), s->active.size(), s->done.size()};
+    out.put(kSrvMagic, 8);
+    out.put(&key);
+    out.put(&s->cfg);
+    out.put(&clock);
+    out.put(&s->st);
+    out.put(counts, 3);
+    for (const Pending &p : s->pending) {
+        const uint8_t full = p.full ? 1 : 0;
+        out.put(&p.q);
+        out.put(&full);
+        out.put(&p.submit_s);
+    }
+    std::vector<unsigned long long> tab;
+    for (const Active &a : s->active) {
+        const uint8_t full = a.p.full ? 1 : 0, dense = a.dense ? 1 : 0;
+        out.put(&a.p.q);
+        out.put(&full);
+        out.put(&a.p.submit_s);
+        out.put(&a.admit_s);
+        out.put(&a.started);
+        out.put(&dense);
+        out.put(&a.cap);
+        tab.resize(a.cap);
+        PTW_CUDA(cudaMemcpy(tab.data(), s->arena + a.off, a.cap * 8, cudaMemcpyDeviceToHost));
+        out.put(tab.data(), tab.size());
+    }
+    for (const Done &d : s->done) {
+        out.put(&d.r);
+        out.put(d.names, d.r.n_entries);
+        out.put(d.counts, d.r.n_entries);
+    }
+    out.put(kSrvMagic, 8);
+    out.ok = out.ok && std::fflush(out.f) == 0 && fsync(fileno(out.f)) == 0;
+    std::fclose(out.f);
+    out.f = nullptr;
+    if (!out.ok || std::rename(tmp.c_str(), path) != 0) {
+        std::remove(tmp.c_str());
+        return fail(PTW_EIO, std::string("cannot write the server checkpoint ") + path);
+    }
+    return PTW_OK;
+} catch (...) {
+    return host_exception();
+}
+
+extern "C" int ptw_serve_restore(ptw_graph *g, const char *path, ptw_server **out)
+try {
+    NvtxRange nvtx("ptw_serve_restore");
+    if (!g || !path || !out) return fail(PTW_EINVAL, "null argument");
+    *out = nullptr;
+    File in;
+    in.f = std::fopen(path, "rb");
+    if (!in.f) return fail(PTW_EIO, std::string("cannot open ") + path);
+    char magic[8];
+    uint64_t key = 0, counts[3] = {0, 0, 0};
+    ptw_serve_cfg cfg{};
+    double clock = 0;
+    ptw_serve_stats st{};
+    in.get(magic, 8);
+    if (!in.ok || std::memcmp(magic, kSrvMagic, 8)) return fail(PTW_EINVAL, std::string(path) + " is not a server checkpoint");
+    in.get(&key);
+    if (!in.ok || key != graph_key(g))
+        return fail(PTW_EINVAL, std::string(path) + " was saved from a server on another graph");
+    in.get(&cfg);
+    in.get(&clock);
+    in.get(&st);
+    in.get(counts, 3);
+    if (!in.ok) return fail(PTW_EIO, std::string("truncated server checkpoint ") + path);
+    ptw_server *s = nullptr;
+    int rc = ptw_serve_open(g, &cfg, &s);
+    if (rc) return rc;
+    auto bail = [&](int code) {
+        ptw_serve_close(s);
+        return code;
+    };
+    // the clock continues from the saved one (latencies leave the downtime out)
+    s->t0 = std::chrono::steady_clock::now() -
+            std::chrono::duration_cast<std::chrono::steady_clock::duration>(std::chrono::duration<double>(clock));
+    s->st = st;
+    const uint32_t n = g->dg.n;
+    auto source_id = [&](uint32_t name, uint32_t *id) -> bool {
+        const uint32_t *p = std::lower_bound(g->h_names, g->h_names + n, name);
+        if (p == g->h_names + n || *p != name) return false;
+        *id = g->h_idx2int[p - g->h_names];
+        return true;
+    };
+    for (uint64_t i = 0; i < counts[0]; ++i) {
+        Pending p;
+        uint8_t full = 0;
+        in.get(&p.q);
+        in.get(&full);
+        in.get(&p.submit_s);
+        p.full = full != 0;
+        if (!in.ok || !source_id(p.q.source, &p.src)) return bail(fail(PTW_EIO, "bad pending query in checkpoint"));
+        s->pending.push_back(p);
+    }
+    std::vector<unsigned long long> tab;
+    for (uint64_t i = 0; i < counts[1]; ++i) {
+        Active a;
+        uint8_t full = 0, dense = 0;
+        in.get(&a.p.q);
+        in.get(&full);
+        in.get(&a.p.submit_s);
+        in.get(&a.admit_s);
+        in.get(&a.started);
+        in.get(&dense);
+        in.get(&a.cap);
+        a.p.full = full != 0;
+        a.dense = dense != 0;
+        if (!in.ok || !source_id(a.p.q.source, &a.p.src) || a.started > a.p.q.budget || a.cap == 0 ||
+            a.cap > s->buddy.capacity())
+            return bail(fail(PTW_EIO, "bad active query in checkpoint"));
+        tab.resize(a.cap);
+        in.get(tab.data(), tab.size());
+        if (!in.ok) return bail(fail(PTW_EIO, "truncated server checkpoint"));
+        if (s->active.size() >= s->S || !s->buddy.alloc(a.cap, &a.off))
+            return bail(fail(PTW_ENOMEM, "the restored server's table arena cannot hold the saved active queries"));
+        cudaError_t e = cudaMemcpy(s->arena + a.off, tab.data(), a.cap * 8, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return bail(cuda_fail(e, "restoring a count table"));
+        s->active.push_back(a);
+    }
+    // finished results: read, then staged together in one pinned block
+    std::vector<ptw_serve_result> rs(counts[2]);
+    std::vector<std::vector<uint32_t>> lists(counts[2]);
+    uint64_t words = 0;
+    for (uint64_t i = 0; i < counts[2]; ++i) {
+        in.get(&rs[i]);
+        if (!in.ok || rs[i].n_entries > n) return bail(fail(PTW_EIO, "truncated server checkpoint"));
+        lists[i].resize(2 * rs[i].n_entries);
+        in.get(lists[i].data(), lists[i].size());
+        words += lists[i].size();
+    }
+    if (!in.ok) return bail(fail(PTW_EIO, "truncated server checkpoint"));
+    if (counts[2]) {
+        std::shared_ptr<PinnedBlock> blk = pinned_block(s, std::max<uint64_t>(words, 1));
+        if (!blk) return bail(fail(PTW_ENOMEM, "pinned result staging"));
+        uint64_t at = 0;
+        for (uint64_t i = 0; i < counts[2]; ++i) {
+            Done d;
+            d.r = rs[i];
+            d.blk = blk;
+            std::memcpy(blk->p + at, lists[i].data(), lists[i].size() * 4);
+            d.names = blk->p + at;
+            d.counts = blk->p + at + rs[i].n_entries;
+            at += lists[i].size();
+            s->done.push_back(std::move(d));
+        }
+    }
+    in.get(magic, 8);
+    if (!in.ok || std::memcmp(magic, kSrvMagic, 8)) return bail(fail(PTW_EIO, "truncated server checkpoint"));
+    *out = s;
+    return PTW_OK;
+} catch (...) {
+    return host_exception();
 }

@@ -29,6 +29,23 @@ class Server:
         self.n_active = 0
         self.n_pending = 0
 
+    def save(self, path):
+        """Writes the server's state between steps (ptw_serve_save)."""
+        C.check(self._lib.ptw_serve_save(self._h, str(path).encode()))
+
+    @classmethod
+    def restore(cls, graph, path):
+        """A server on `graph` in the state saved at `path` (ptw_serve_restore)."""
+        obj = cls.__new__(cls)
+        obj._lib = C.load()
+        obj.graph = graph
+        h = ctypes.c_void_p()
+        C.check(obj._lib.ptw_serve_restore(graph.handle, str(path).encode(), ctypes.byref(h)))
+        obj._h = h
+        st = obj.stats()
+        obj.n_active, obj.n_pending = st["active"], st["pending"]
+        return obj
+
     def clock(self):
         return float(self._lib.ptw_serve_clock(self._h))
 
