@@ -4,6 +4,7 @@
     python -m ptwalker_gb300.profile_workloads deepwalk --scale 22 --walk-len 80
     python -m ptwalker_gb300.profile_workloads batch --scale 20 --queries 512
     python -m ptwalker_gb300.profile_workloads exact --scale 18
+    python -m ptwalker_gb300.profile_workloads learned --scale 18 --queries 256
     python -m ptwalker_gb300.profile_workloads mlp
     python -m ptwalker_gb300.profile_workloads build --scale 22
     python -m ptwalker_gb300.profile_workloads serve --n 8400000 --queries 600 --top-k 1000
@@ -21,7 +22,7 @@ import numpy as np
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("what", choices=["pagerank", "deepwalk", "batch", "exact", "mlp", "build", "serve"])
+    p.add_argument("what", choices=["pagerank", "deepwalk", "batch", "exact", "learned", "mlp", "build", "serve"])
     p.add_argument("--scale", type=int, default=22)
     p.add_argument("--walk-len", type=int, default=80)
     p.add_argument("--queries", type=int, default=512)
@@ -110,6 +111,17 @@ def main(argv=None):
         res = ptw.ppr_batch(G, src, 1000, sp=0.2, seed=1)
         l1 = res.l1(tol=1e-9)
         out.update(l1_p50=float(np.median(l1)))
+    elif a.what == "learned":
+        # the learned-budget evaluation at a small size: labels by pairwise
+        # L1 of device-resident batches, training, three held-out runs scored
+        # by one shared FP64 pass
+        from ptwalker_gb300 import learned
+        names, row_ptr, col = G.export_csr()
+        rng = np.random.default_rng(3)
+        tr = names[col[rng.integers(0, G.m, a.queries)]]
+        te = names[col[rng.integers(0, G.m, a.queries)]]
+        r = learned.evaluate(G, tr, te, b_fix=int(a.budget_max), sp=0.2, seed=5, epochs=100)
+        out.update(gain=r["gain"], ceiling=r["label_ceiling"], stage_seconds=r["stage_seconds"])
     out["seconds"] = time.perf_counter() - t0
     G.close()
     print(json.dumps(out))
