@@ -442,7 +442,9 @@ def bench_serve(args, ptw):
     for k, (rate, top_k) in enumerate(runs):
         src = rng.integers(0, G.n, args.serve_queries)
         bud = loguniform_budgets(args.serve_queries, 1e3, args.serve_budget_max, 10 + k)
-        with ptw.Server(G, sp=0.2, seed=3, tick_walkers=args.serve_tick, use_graph=True, top_k=top_k) as srv:
+        # full vectors: reserve the page-locked result staging the largest ticks need
+        with ptw.Server(G, sp=0.2, seed=3, tick_walkers=args.serve_tick, use_graph=True, top_k=top_k,
+                        staging_mb=0 if top_k else 1024) as srv:
             r = ptw.open_loop(srv, src, bud, rate=rate, seed=k, query_id0=k << 20)
             st = srv.stats()
         line = {kk: r[kk] for kk in ("rate", "n", "qps", "p50_ms", "p99_ms", "mean_ms")}

@@ -394,7 +394,11 @@ typedef struct ptw_serve_cfg {
     uint32_t use_graph;     /* 1 = replay the tick as a CUDA graph */
     double table_factor;    /* as in ptw_batch_cfg */
     uint32_t top_k;         /* as in ptw_batch_cfg */
-    uint32_t reserved;
+    uint32_t staging_mb;    /* page-locked host staging for results, reserved at open, in MiB;
+                               0 = 32.  It grows (doubling) when a tick's results need more:
+                               a server that returns full vectors (top_k = 0) should reserve
+                               what its largest ticks need (hundreds of MB) to keep the growth
+                               out of its first ticks */
 } ptw_serve_cfg;
 
 typedef struct ptw_serve_result {

@@ -88,7 +88,7 @@ class ServeCfg(ctypes.Structure):
                 ("max_moves", ctypes.c_uint32), ("table_bytes", ctypes.c_uint64),
                 ("tick_walkers", ctypes.c_uint64), ("max_active", ctypes.c_uint32),
                 ("use_graph", ctypes.c_uint32), ("table_factor", ctypes.c_double),
-                ("top_k", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("top_k", ctypes.c_uint32), ("staging_mb", ctypes.c_uint32)]
 
 
 class ServeResult(ctypes.Structure):

@@ -373,8 +373,10 @@ try {
             if (e != cudaSuccess) rc = cuda_fail(e, "server events");
         }
         if (rc == PTW_OK && cfg->use_graph) rc = build_tick_graph(s);
-        // one staging block up front, so the first results do not wait for it
-        if (rc == PTW_OK && !pinned_block(s, 1)) rc = fail(PTW_ENOMEM, "pinned result staging");
+        // one staging block up front (cfg.staging_mb), so the first results do not wait for it
+        const uint64_t staging_words = (uint64_t)cfg->staging_mb << 18;  // MiB -> 4-byte words
+        if (rc == PTW_OK && !pinned_block(s, std::max<uint64_t>(staging_words, 1)))
+            rc = fail(PTW_ENOMEM, "pinned result staging");
     }
     if (rc != PTW_OK) {
         ptw_serve_close(s);

@@ -17,12 +17,12 @@ from .batch import APPS
 
 class Server:
     def __init__(self, graph, sp=0.2, seed=0, app="visits", max_moves=0, table_bytes=0,
-                 tick_walkers=0, max_active=0, use_graph=True, table_factor=0.0, top_k=0):
+                 tick_walkers=0, max_active=0, use_graph=True, table_factor=0.0, top_k=0, staging_mb=0):
         self._lib = C.load()
         self.graph = graph
         cfg = C.ServeCfg(float(sp), int(seed) & 0xFFFFFFFFFFFFFFFF, APPS[app], int(max_moves),
                          int(table_bytes), int(tick_walkers), int(max_active), int(bool(use_graph)),
-                         float(table_factor), int(top_k))
+                         float(table_factor), int(top_k), int(staging_mb))
         h = ctypes.c_void_p()
         C.check(self._lib.ptw_serve_open(graph.handle, ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
