@@ -341,13 +341,12 @@ typedef struct ptw_batch_phases {
 } ptw_batch_phases;
 int ptw_batch_get_phases(const ptw_batch *b, ptw_batch_phases *out);
 
-/* Frees a batch.  Its host result arrays (when large) are kept, already
- * faulted in and page-locked, for the next batch's results (one pair, up
- * to 32 GB); ptw_trim_memory hands them back.  Large result arrays are
- * page-locked while the device walks (within a quarter of the host memory
- * for all of them), so their copies from the device run at a steady rate.
- * Device-resident results go back to the library's memory pool at once:
- * finish (synchronise) every read of them first. */
+/* Frees a batch and its result arrays.  Large host result arrays are
+ * allocated for each batch and faulted in and page-locked while the device
+ * walks (within a quarter of the host memory for all of them), so their
+ * copies from the device run at link speed; freeing them takes a few ms
+ * per GB.  Device-resident results go back to the library's memory pool at
+ * once: finish (synchronise) every read of them first. */
 void ptw_batch_free(ptw_batch *b);
 
 /* FP64 oracle on the device: for each source name, the exact expected count

@@ -48,8 +48,6 @@ struct ptw_batch {
     std::vector<ptw_query> queries;
     std::vector<uint64_t> offsets;  // [nq + 1]
     ptw::HostArray names, counts;
-    uint64_t buf_cap = 0, buf_touched = 0;  // entries allocated / faulted in
-    bool buf_pinned = false;                // page-locked
     ptw_walk_stats stats{};
     uint32_t top_k = 0;  // results hold each query's top_k largest counts only
     // Device-resident results (PTW_BATCH_DEVICE_RESULTS): lists and offsets
@@ -225,17 +223,6 @@ uint64_t pin_limit()
     return pages > 0 && pg > 0 ? (uint64_t)pages * (uint64_t)pg / 4 : 0;
 }
 
-struct HostCache {
-    std::mutex mu;
-    HostBufs bufs;
-};
-HostCache &host_cache()
-{
-    static HostCache *c = new HostCache;
-    return *c;
-}
-constexpr uint64_t kHostCacheMaxBytes = 32ull << 30;
-
 }  // namespace
 
 bool host_pin(uint32_t *p, uint64_t bytes)
@@ -275,38 +262,6 @@ void HostArrayDelete::operator()(uint32_t *p) const
     }
     if (was && cudaHostUnregister(p) != cudaSuccess) cudaGetLastError();
     delete[] p;
-}
-
-bool host_cache_take(uint64_t need, HostBufs &out)
-{
-    HostCache &c = host_cache();
-    std::lock_guard<std::mutex> lk(c.mu);
-    if (!c.bufs.names || c.bufs.cap < need) return false;
-    out = std::move(c.bufs);
-    c.bufs = HostBufs();
-    return true;
-}
-
-void host_cache_put(HostBufs &&b)
-{
-    if (!b.names || !b.counts || b.cap * 8 > kHostCacheMaxBytes) return;
-    HostBufs old;
-    HostCache &c = host_cache();
-    {
-        std::lock_guard<std::mutex> lk(c.mu);
-        if (c.bufs.names && c.bufs.cap > b.cap) return;  // keep the larger pair
-        old = std::move(c.bufs);
-        c.bufs = std::move(b);
-    }
-}  // the replaced pair is freed outside the lock
-
-void trim_host_cache()
-{
-    HostBufs old;
-    HostCache &c = host_cache();
-    std::lock_guard<std::mutex> lk(c.mu);
-    old = std::move(c.bufs);
-    c.bufs = HostBufs();
 }
 
 namespace {
@@ -544,38 +499,21 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
         for (uint32_t i = 0; i < nq; ++i)
             est += std::min<uint64_t>(g->dg.n, (uint64_t)(1.5 * (double)wq[i].budget) + 64);
         if (est * 8 >= (64ull << 20)) {
-            HostBufs hb;
-            bool fresh = false;
-            if (host_cache_take(est, hb)) {
-                // a freed batch's buffers: only the part never faulted in needs it
-                wr.c.pre_names = std::move(hb.names);
-                wr.c.pre_counts = std::move(hb.counts);
-                wr.c.pre_cap = hb.cap;
-                wr.c.pre_touched = std::min(hb.touched, est);
-                wr.c.pre_pinned = hb.pinned;
-            } else {
-                wr.c.pre_names.reset(new (std::nothrow) uint32_t[est]);
-                wr.c.pre_counts.reset(new (std::nothrow) uint32_t[est]);
-                wr.c.pre_cap = est;
-                wr.c.pre_touched = 0;
-                wr.c.pre_pinned = false;
-                fresh = true;
-            }
+            // Fresh arrays every call, faulted in and page-locked on host
+            // threads while the device walks.  Arrays kept from an earlier
+            // batch and reused (registered once) took copies 2-40x slower in
+            // some calls on some hosts (5 of 12 calls on one host, where 12
+            // calls into fresh arrays all copied at 193 GB/s).
+            wr.c.pre_names.reset(new (std::nothrow) uint32_t[est]);
+            wr.c.pre_counts.reset(new (std::nothrow) uint32_t[est]);
+            wr.c.pre_cap = est;
+            wr.c.pre_pinned = false;
             if (wr.c.pre_names && wr.c.pre_counts) {
-                const uint64_t t0 = wr.c.pre_touched;
-                if (fresh) {
-                    // touch, then register the whole arrays, while the device walks
-                    early.start({{wr.c.pre_names.get(), est * 4}, {wr.c.pre_counts.get(), est * 4}}, true);
-                    wr.c.pre_join = [&early, &wr] {
-                        early.join();
-                        wr.c.pre_pinned = early.pinned();
-                    };
-                } else {
-                    if (t0 < est)
-                        early.start({{wr.c.pre_names.get() + t0, (est - t0) * 4},
-                                     {wr.c.pre_counts.get() + t0, (est - t0) * 4}});
-                    wr.c.pre_join = [&early] { early.join(); };
-                }
+                early.start({{wr.c.pre_names.get(), est * 4}, {wr.c.pre_counts.get(), est * 4}}, true);
+                wr.c.pre_join = [&early, &wr] {
+                    early.join();
+                    wr.c.pre_pinned = early.pinned();
+                };
             } else {
                 wr.c.pre_names.reset();
                 wr.c.pre_counts.reset();
@@ -676,16 +614,12 @@ int assemble(ptw_graph *g, ptw_batch *b, std::vector<WaveResult> &waves)
     if (adopt) {
         b->names = std::move(waves[0].c.names);
         b->counts = std::move(waves[0].c.counts);
-        b->buf_cap = waves[0].c.cap;
-        b->buf_touched = waves[0].c.touched;
-        b->buf_pinned = waves[0].c.pinned;
         return PTW_OK;
     }
     if (!total) return PTW_OK;
     b->names.reset(new (std::nothrow) uint32_t[total]);
     b->counts.reset(new (std::nothrow) uint32_t[total]);
     if (!b->names || !b->counts) return fail(PTW_ENOMEM, "host allocation of batch results failed");
-    b->buf_cap = b->buf_touched = total;  // every entry is written below
     for (uint32_t i = 0; i < nq; ++i) {
         const WaveResult *w = src_w[i];
         if (!w) continue;
@@ -1541,15 +1475,6 @@ try {
         b->d_offsets.reset();
         if (have_prev) cudaSetDevice(prev);
         cudaGetLastError();
-    }
-    if (b->names && b->buf_cap) {
-        HostBufs hb;
-        hb.names = std::move(b->names);
-        hb.counts = std::move(b->counts);
-        hb.cap = b->buf_cap;
-        hb.touched = b->buf_touched;
-        hb.pinned = b->buf_pinned;
-        host_cache_put(std::move(hb));
     }
     delete b;
 } catch (...) {

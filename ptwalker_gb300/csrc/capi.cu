@@ -425,7 +425,6 @@ try {
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(e, "synchronise before trimming");
     trim_pools();
-    trim_host_cache();
     return PTW_OK;
 } catch (...) {
     return host_exception();

@@ -392,7 +392,6 @@ struct Compacted {
     // that); adopted when the lists fit, the unused tail handed back.
     HostArray pre_names, pre_counts;
     uint64_t pre_cap = 0;
-    uint64_t pre_touched = 0;  // leading entries of pre_* already faulted in before this call
     bool pre_pinned = false;   // pre_* are page-locked (known after pre_join)
     std::function<void()> pre_join;
     // Capacity of names / counts in entries, how many leading entries are
@@ -401,17 +400,6 @@ struct Compacted {
     uint64_t cap = 0, touched = 0;
     bool pinned = false;
 };
-// Host result buffers of the last freed batch, kept faulted in so that the
-// next batch's copies land in touched pages (batch.cu).  take() hands them
-// over when they hold at least `need` entries; trim_host_cache() frees them.
-struct HostBufs {
-    HostArray names, counts;
-    uint64_t cap = 0, touched = 0;
-    bool pinned = false;
-};
-bool host_cache_take(uint64_t need, HostBufs &out);
-void host_cache_put(HostBufs &&b);
-void trim_host_cache();
 // Compacts nt count tables into *out (batch.cu).  Table i starts at slot
 // h_base[i] of d_slots, an even slot (16-byte aligned; callers use 128-byte
 // lines); a hash table (h_dense[i] == 0, or h_dense NULL) has h_cap[i]

@@ -55,12 +55,12 @@ def test_batch_bit_exact_per_query(gpu, G16, s16_canon, app):
         assert res.moves == tot_moves
 
 
-def test_reused_host_result_buffers(gpu, G16, s16_canon):
-    """Batches large enough for host result buffers sized before the walk
-    (8 M entries and up) and for copies overlapping compaction range by
-    range (16 M entries and up, page-locked lists): a freed batch's buffers
-    are reused by the next batch, whose lists must still equal the replay in
-    every range, and results still held are not touched by later batches."""
+def test_large_batches_one_after_another(gpu, G16, s16_canon):
+    """Batches large enough for host result arrays sized, faulted in and
+    page-locked before the walk (8 M entries and up) and for copies
+    overlapping compaction range by range (16 M entries and up): a batch run
+    after another one was freed must still equal the replay in every range,
+    and results still held are not touched by later batches."""
     rng = np.random.default_rng(17)
     nq = 700  # about 25 K distinct vertices per query: 17 M entries written
     sources = rng.integers(0, G16.n, nq)
@@ -68,8 +68,8 @@ def test_reused_host_result_buffers(gpu, G16, s16_canon):
     first = gpu.ppr_batch(G16, sources, budgets, sp=0.2, seed=3)
     keep = [first.query(i) for i in (0, 1)]
     kept = [(a.copy(), b.copy()) for a, b in keep]
-    first.close()                                   # buffers go to the host cache
-    second = gpu.ppr_batch(G16, sources, budgets, sp=0.2, seed=4)   # reuses them
+    first.close()
+    second = gpu.ppr_batch(G16, sources, budgets, sp=0.2, seed=4)
     held = gpu.ppr_batch(G16, sources[:40], budgets[:40], sp=0.2, seed=5)
     assert second.entries >= 16 << 20
     for i in (0, 57, 180, 349, 420, 555, nq - 1):
