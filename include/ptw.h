@@ -224,6 +224,34 @@ int ptw_deepwalk(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *h_p
 int ptw_deepwalk_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *d_paths,
                      ptw_walk_stats *stats);
 
+/* Second-order (node2vec) walks.  The reference parses -p / -q
+ * (include/option.hpp:447-469) and prepares a neighbour query for them
+ * (src/core/graph.hpp:787-820) in src/core/node2vec.cpp:8-24; its test
+ * (src/test/debug/test_node2vec.cpp, third_party/knightking/test_node2vec.hpp:47-80)
+ * states the law: from v, reached from t, the next vertex x is drawn over
+ * v's out-edges with weight 1/p if x == t, 1 if x is an out-neighbour of t,
+ * 1/q otherwise; the first move is uniform.  n_walkers walks of L vertices
+ * (L-1 moves), written as names into h_paths[n_walkers * L] (row-major,
+ * int32), padded with -1 after a vertex without out-edges, as ptw_deepwalk.
+ * p and q must be positive and finite with max(1/p, 1, 1/q) / min(1/p, 1, 1/q)
+ * <= 1024 (PTW_EINVAL otherwise).  Needs the extended column copy (16 bytes
+ * per CSR entry, built on first use; PTW_ENOMEM when it does not fit).
+ * cfg->sp and cfg->max_moves are ignored. */
+typedef struct ptw_node2vec_stats {
+    uint64_t walkers;
+    uint64_t moves;    /* edge traversals */
+    uint64_t trials;   /* candidate draws (>= moves; rejected candidates included) */
+    uint64_t probes;   /* reads of the previous vertex's row by the neighbour test */
+    float kernel_ms;   /* device time of the walk kernel */
+    float total_ms;    /* device time of the whole call, copies included */
+} ptw_node2vec_stats;
+int ptw_node2vec(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, double p, double q,
+                 int32_t *h_paths, ptw_node2vec_stats *stats);
+/* Device variant: d_paths[n_walkers * L] on the graph's device; runs on the
+ * graph's stream and does not synchronise unless stats != NULL. */
+int ptw_node2vec_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, double p, double q,
+                     int32_t *d_paths, ptw_node2vec_stats *stats);
+
 /* Synchronise the graph's stream. */
 int ptw_graph_sync(ptw_graph *g);
 

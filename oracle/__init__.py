@@ -6,7 +6,8 @@ Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 
 Contents
   * ``oracle.c`` (built to ``oracle/_build/liboracle.so``): Philox4x32-10,
-    raw R-MAT edges, walker replay for counts / endpoints / paths.
+    raw R-MAT edges, walker replay for counts / endpoints / paths, and
+    second-order (node2vec) paths.
   * ``partitioned.c``: the same count walks scheduled the reference's way
     (partition sweeps, per-partition walker pools); the timed CPU baseline.
   * ``graph.py``: canonical graph layout (names, CSR in index space) and the
@@ -35,6 +36,8 @@ from .replay import (  # noqa: F401
     replay_counts,
     replay_pairs,
     replay_paths,
+    replay_node2vec,
+    n2v_thresholds,
     partitioned_counts,
     sp_threshold,
     TAG_WALK,

@@ -47,6 +47,13 @@ def load_lib():
                                      ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
                                      ctypes.c_int, u32p, ctypes.c_uint32, i32p, ctypes.c_int]
     lib.ora_replay_paths.restype = None
+    lib.ora_replay_node2vec.argtypes = [u64p, u32p, ctypes.c_uint32, ctypes.c_uint64,
+                                        ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_int, u32p,
+                                        ctypes.c_uint32, i32p, ctypes.c_int]
+    lib.ora_replay_node2vec.restype = ctypes.c_uint64
+    lib.ora_n2v_thresholds.argtypes = [ctypes.c_double, ctypes.c_double, u64p]
+    lib.ora_n2v_thresholds.restype = None
     lib.ora_rmat_clean_csr.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                        ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
                                        ctypes.c_int, ctypes.POINTER(ctypes.c_uint32),

@@ -327,3 +327,98 @@ void ora_replay_paths(const uint64_t *row_ptr, const uint32_t *col, uint32_t n,
         }
     }
 }
+
+/*
+ * Second-order (node2vec) walks.  The reference parses -p / -q
+ * (include/option.hpp:447-469), prepares its neighbour query for them
+ * (src/core/graph.hpp:787-820: Bloom filter, then binary search in the
+ * sorted row) and calls FMobSolver::set_node2vec (src/core/node2vec.cpp:8-24,
+ * src/core/solver.hpp:156-159), whose second-order step is commented out; its
+ * test (src/test/debug/test_node2vec.cpp, with the transition matrix of
+ * third_party/knightking/test_node2vec.hpp:47-80) states the law this replay
+ * follows, the node2vec law of Grover and Leskovec (KDD'16): from vertex v,
+ * reached from t, the next vertex x is drawn over the CSR row of v (multi-edges
+ * with multiplicity) with weight 1/p if x == t, 1 if x is an out-neighbour of
+ * t, 1/q otherwise.  The first move (no t yet) is uniform.
+ *
+ * Drawing is rejection sampling over the row (the method of KnightKing, Yang
+ * et al., SOSP'19): trial k of move `step` takes two 32-bit words of
+ *    draw(seed, wid, step, PTW_TAG_N2V + k/2): words (0, 1) for even k,
+ *    (2, 3) for odd k;
+ * the first word picks the candidate x = row[mulhi32(word, degree)], the
+ * second accepts it iff word < thr[class(x)], with
+ *    thr[c] = w_c >= M ? 2^32 : floor(w_c / M * 2^32),   M = max(1/p, 1, 1/q).
+ * The first move accepts trial 0.  Trial ORA_N2V_MAX_TRIALS - 1 is accepted
+ * whatever its draw, so a move always ends; callers keep max(w)/min(w) <=
+ * 1024, which makes reaching it less likely than 1e-27 per move.
+ * Paths are written as in ora_replay_paths; the return value is the number of
+ * trials (candidate draws) made.
+ */
+#define PTW_TAG_N2V 0x4E320000u /* "N2" + trial pair index */
+#define ORA_N2V_MAX_TRIALS 65536u
+
+void ora_n2v_thresholds(double p, double q, uint64_t thr[3])
+{
+    double w[3] = {1.0 / p, 1.0, 1.0 / q}; /* return, neighbour of t, other */
+    double m = w[0] > w[1] ? w[0] : w[1];
+    if (w[2] > m) m = w[2];
+    for (int c = 0; c < 3; c++)
+        thr[c] = w[c] >= m ? (uint64_t)1 << 32 : (uint64_t)(w[c] / m * 4294967296.0);
+}
+
+static int row_has(const uint64_t *row_ptr, const uint32_t *col, uint32_t t, uint32_t x)
+{
+    uint64_t lo = row_ptr[t], hi = row_ptr[t + 1];
+    while (lo < hi) {
+        uint64_t mid = lo + (hi - lo) / 2;
+        if (col[mid] < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo < row_ptr[t + 1] && col[lo] == x;
+}
+
+uint64_t ora_replay_node2vec(const uint64_t *row_ptr, const uint32_t *col, uint32_t n,
+                             uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
+                             double p, double q, int start_mode, const uint32_t *sources,
+                             uint32_t n_sources, int32_t *paths, int n_threads)
+{
+    uint64_t thr[3];
+    ora_n2v_thresholds(p, q, thr);
+    uint64_t trials_total = 0;
+#ifdef _OPENMP
+    if (n_threads < 1) n_threads = 1;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : trials_total) num_threads(n_threads)
+#endif
+    for (int64_t wi = (int64_t)w_begin; wi < (int64_t)w_end; wi++) {
+        uint64_t wid = (uint64_t)wi;
+        int32_t *row = paths + (wid - w_begin) * (uint64_t)L;
+        uint32_t v = start_index(wid, n, start_mode, sources, n_sources, seed);
+        if (L == 0) continue;
+        row[0] = (int32_t)v;
+        uint32_t t = 0;
+        int dead = 0;
+        for (uint32_t step = 0; step + 1 < L; step++) {
+            if (!dead) {
+                uint64_t b = row_ptr[v], deg = row_ptr[v + 1] - b;
+                if (deg == 0) {
+                    dead = 1;
+                } else {
+                    uint32_t w[4], x = 0;
+                    for (uint32_t k = 0;; k++) {
+                        if ((k & 1) == 0) draw(seed, wid, step, PTW_TAG_N2V + (k >> 1), w);
+                        uint32_t cu = w[(k & 1) * 2], au = w[(k & 1) * 2 + 1];
+                        x = col[b + mulhi32(cu, (uint32_t)deg)];
+                        trials_total++;
+                        if (step == 0 || k + 1 == ORA_N2V_MAX_TRIALS) break;
+                        int c = x == t ? 0 : row_has(row_ptr, col, t, x) ? 1 : 2;
+                        if ((uint64_t)au < thr[c]) break;
+                    }
+                    t = v;
+                    v = x;
+                }
+            }
+            row[step + 1] = dead ? -1 : (int32_t)v;
+        }
+    }
+    return trials_total;
+}

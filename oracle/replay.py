@@ -87,6 +87,30 @@ def replay_paths(g, w_begin, w_end, L, seed, start_mode=START_PER_VERTEX,
     return paths
 
 
+def replay_node2vec(g, w_begin, w_end, L, seed, p, q, start_mode=START_PER_VERTEX,
+                    sources=None, threads=1):
+    """Second-order (node2vec) walks, ora_replay_node2vec: ([walkers, L] int32
+    vertex indices, -1 after a dead end; number of candidate draws)."""
+    lib = load_lib()
+    nw = w_end - w_begin
+    paths = np.zeros((nw, L), dtype=np.int32)
+    src_arr, n_src = _sources_arg(g, start_mode, sources)
+    trials = lib.ora_replay_node2vec(
+        _p(g.row_ptr, ctypes.c_uint64), _p(g.col, ctypes.c_uint32), g.n,
+        w_begin, w_end, L, seed, float(p), float(q), start_mode, _p(src_arr, ctypes.c_uint32), n_src,
+        _p(paths, ctypes.c_int32), threads)
+    return paths, int(trials)
+
+
+def n2v_thresholds(p, q):
+    """Acceptance thresholds (return, neighbour of the previous vertex,
+    other) of the node2vec rejection draw, ora_n2v_thresholds."""
+    lib = load_lib()
+    thr = np.zeros(3, dtype=np.uint64)
+    lib.ora_n2v_thresholds(float(p), float(q), _p(thr, ctypes.c_uint64))
+    return [int(x) for x in thr]
+
+
 def degree_relabelled(g, threads=None):
     """The graph relabelled by descending degree (ties by index), rows
     keeping the canonical order of their neighbours: (perm, row_ptr, col)

@@ -14,6 +14,7 @@ from .api import (  # noqa: F401
     ppr,
     rwr,
     deepwalk,
+    node2vec,
     PageRankApp,
     PPRApp,
     RWRApp,

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 SO = os.path.join(OUT, "libptw.so")
-SOURCES = ["graph.cu", "walk.cu", "capi.cu", "noalloc.cu", "batch.cu", "exact.cu", "serve.cu", "mlp.cu", "probe.cu"]
+SOURCES = ["graph.cu", "walk.cu", "capi.cu", "noalloc.cu", "batch.cu", "exact.cu", "serve.cu", "mlp.cu", "probe.cu", "node2vec.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
               "--expt-relaxed-constexpr"]
@@ -73,7 +73,7 @@ def build(force=False, verbose=False, extra_flags=()):
 
 CLI_SRC = os.path.join(HERE, "cli", "ptw_cli.cpp")
 BIN_DIR = os.path.join(OUT, "bin")
-APPS = ("pagerank", "ppr", "PPR", "rwr", "RWR", "deepwalk")
+APPS = ("pagerank", "ppr", "PPR", "rwr", "RWR", "deepwalk", "node2vec")
 
 
 def build_cli():

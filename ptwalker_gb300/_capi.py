@@ -45,6 +45,12 @@ class WalkStats(ctypes.Structure):
                 ("total_ms", ctypes.c_float)]
 
 
+class Node2vecStats(ctypes.Structure):
+    _fields_ = [("walkers", ctypes.c_uint64), ("moves", ctypes.c_uint64),
+                ("trials", ctypes.c_uint64), ("probes", ctypes.c_uint64),
+                ("kernel_ms", ctypes.c_float), ("total_ms", ctypes.c_float)]
+
+
 class Query(ctypes.Structure):
     _fields_ = [("source", ctypes.c_uint32), ("query_id", ctypes.c_uint32), ("budget", ctypes.c_uint64)]
 
@@ -141,6 +147,10 @@ SIGNATURES = [
                                     ctypes.POINTER(WalkStats)]),
     ("ptw_deepwalk_dev", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), ctypes.c_uint32, _vp,
                                         ctypes.POINTER(WalkStats)]),
+    ("ptw_node2vec", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), ctypes.c_uint32, ctypes.c_double,
+                                    ctypes.c_double, _vp, ctypes.POINTER(Node2vecStats)]),
+    ("ptw_node2vec_dev", ctypes.c_int, [_G, ctypes.POINTER(WalkCfg), ctypes.c_uint32, ctypes.c_double,
+                                        ctypes.c_double, _vp, ctypes.POINTER(Node2vecStats)]),
     ("ptw_graph_sync", ctypes.c_int, [_G]),
     ("ptw_graph_set_stream", ctypes.c_int, [_G, _vp]),
     ("ptw_autotune", ctypes.c_int, [_G, ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(Tune)]),

@@ -390,6 +390,42 @@ def deepwalk(graph, n_walkers=None, walk_len=80, seed=0, start="per_vertex", sou
                 int(n_walkers) * int(walk_len), stats)
 
 
+class Node2vecStats:
+    def __init__(self, s):
+        self.walkers, self.moves = int(s.walkers), int(s.moves)
+        self.trials, self.probes = int(s.trials), int(s.probes)
+        self.kernel_ms, self.total_ms = float(s.kernel_ms), float(s.total_ms)
+
+    def __repr__(self):
+        return ("Node2vecStats(walkers=%d, moves=%d, trials=%d, probes=%d, kernel_ms=%.3f, total_ms=%.3f)"
+                % (self.walkers, self.moves, self.trials, self.probes, self.kernel_ms, self.total_ms))
+
+
+def node2vec(graph, n_walkers=None, walk_len=80, p=1.0, q=1.0, seed=0, start="per_vertex", sources=None,
+             out=None, first_walker=0, stats=False):
+    """int32[n_walkers, walk_len] second-order paths of names, -1 after a dead
+    end (src/core/node2vec.cpp with -p / -q, include/option.hpp:447-469): from
+    v, reached from t, the next vertex x has weight 1/p if x == t, 1 if x is a
+    neighbour of t, 1/q otherwise."""
+    n_walkers = graph.n if n_walkers is None else n_walkers
+    cfg, _keep = _cfg(n_walkers, 0.0, seed, start, sources, 0, first_walker)
+    if out is None:
+        out = np.empty((n_walkers, walk_len), dtype=np.int32)
+    itemsize = out.itemsize if isinstance(out, np.ndarray) else out.element_size()
+    if itemsize != 4 or _nelem(out) < int(n_walkers) * int(walk_len):
+        raise ValueError("output needs at least %d 4-byte elements" % (int(n_walkers) * int(walk_len)))
+    st = C.Node2vecStats()
+    stp = ctypes.byref(st) if stats else None
+    args = (graph.handle, ctypes.byref(cfg), int(walk_len), float(p), float(q))
+    if getattr(out, "is_cuda", False):
+        graph._before_device_call()
+        C.check(graph._lib.ptw_node2vec_dev(*args, _dev_ptr(out), stp))
+        graph._after_device_call()
+    else:
+        C.check(graph._lib.ptw_node2vec(*args, _host_ptr(out), stp))
+    return (out, Node2vecStats(st)) if stats else out
+
+
 # ---- app-template mirror (src/core/pagerank.cpp, ppr.cpp, RWR.cpp, deepwalk.cpp) ----
 
 class PageRankApp:
@@ -444,6 +480,14 @@ class Solver:
 
     def __init__(self, graph, mtcfg=None):
         self.graph = graph
+        self.is_node2vec = False
+        self.p = self.q = 1.0
+
+    def set_node2vec(self, p, q):
+        """FMobSolver::set_node2vec (solver.hpp:156-159): fixed-length walks
+        of this solver become second-order (node2vec) walks."""
+        self.is_node2vec = True
+        self.p, self.q = float(p), float(q)
 
 
 def walk(solver, walker_num, walk_len, mem_quota, app, walker_size=4196):
@@ -454,7 +498,10 @@ def walk(solver, walker_num, walk_len, mem_quota, app, walker_size=4196):
     g = solver.graph if isinstance(solver, Solver) else solver
     if isinstance(app, DeepWalkApp):
         start = "sources" if getattr(app, "start_vertices", None) else app.start
-        app.paths = deepwalk(g, walker_num, app.tp_, app.seed, start)
+        if getattr(solver, "is_node2vec", False):
+            app.paths = node2vec(g, walker_num, app.tp_, solver.p, solver.q, app.seed, start)
+        else:
+            app.paths = deepwalk(g, walker_num, app.tp_, app.seed, start)
         return app
     sources = app.start_vertices if app.start_vertices else None
     start = "sources" if sources else app.start

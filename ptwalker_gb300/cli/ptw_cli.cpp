@@ -6,11 +6,13 @@
 //             src/core/ppr.cpp:54; here the source is a vertex name)
 //   rwr       -f -g (-w | -e) [--sp P] (the reference fixes 0.5, RWR.cpp:122)
 //   deepwalk  -f -g (-w | -e) -l L
+//   node2vec  -f -g (-w | -e) -l L -p P -q Q  (src/core/node2vec.cpp,
+//             include/option.hpp:447-469)
 //
 // -t, -s, --mem, --socket-mapping, --ws and --db size CPU thread pools and
 // NUMA partitions in the reference; they are accepted and ignored.  Added:
 // --seed S, --start per_vertex|uniform, --out FILE (counts by name as u32, or
-// (start,end) pairs for rwr), --paths-out FILE (int32 [W, L] for deepwalk),
+// (start,end) pairs for rwr), --paths-out FILE (int32 [W, L] for deepwalk and node2vec),
 // --as-undirected.  The app is chosen by the executable name or by the
 // first argument (ptw_cli pagerank ...).  Like the reference apps, each
 // prints "ppr value %u" (here: the count of vertex name 0) on stdout.
@@ -28,18 +30,20 @@ namespace {
 struct Opts {
     std::string app, fmt, path, out, paths_out, start = "per_vertex";
     uint64_t walkers = 0, epochs = 0, seed = 0;
-    double sp = -1;
+    double sp = -1, p = -1, q = -1;
     long len = -1;
     long long source = -1;
     bool undirected = false;
 };
 
 const char *kUsage =
-    "usage: {pagerank|ppr|rwr|deepwalk} -f text|binary -g PATH (-w W | -e E) [--sp P] [-l L]\n"
+    "usage: {pagerank|ppr|rwr|deepwalk|node2vec} -f text|binary -g PATH (-w W | -e E) [--sp P] [-l L]\n"
+    "       [-p P -q Q (node2vec)]\n"
     "       [--source NAME] [--seed S] [--start per_vertex|uniform] [--out FILE]\n"
     "       [--paths-out FILE] [--as-undirected] [-t T -s S --mem G --socket-mapping M\n"
     "       --ws N --db D (accepted, ignored)]\n"
-    "The app is the program name (pagerank, ppr or PPR, rwr or RWR, deepwalk) or the first argument.\n";
+    "The app is the program name (pagerank, ppr or PPR, rwr or RWR, deepwalk, node2vec) or the first\n"
+    "argument.\n";
 
 int usage(const char *msg)
 {
@@ -81,7 +85,7 @@ int main(int argc, char **argv)
     Opts o;
     int i = 1;
     o.app = app_name(base_name(argv[0]));
-    if (o.app != "pagerank" && o.app != "ppr" && o.app != "rwr" && o.app != "deepwalk") {
+    if (o.app != "pagerank" && o.app != "ppr" && o.app != "rwr" && o.app != "deepwalk" && o.app != "node2vec") {
         if (argc < 2) return usage("missing app name");
         o.app = app_name(argv[1]);
         i = 2;
@@ -107,6 +111,8 @@ int main(int argc, char **argv)
         else if (a == "-e") o.epochs = std::strtoull(v.c_str(), nullptr, 10);
         else if (a == "--sp") o.sp = std::atof(v.c_str());
         else if (a == "-l") o.len = std::atol(v.c_str());
+        else if (a == "-p") o.p = std::atof(v.c_str());
+        else if (a == "-q") o.q = std::atof(v.c_str());
         else if (a == "--source") o.source = std::atoll(v.c_str());
         else if (a == "--seed") o.seed = std::strtoull(v.c_str(), nullptr, 10);
         else if (a == "--start") o.start = v;
@@ -128,7 +134,8 @@ int main(int argc, char **argv)
     if ((o.walkers == 0) == (o.epochs == 0)) return usage("give exactly one of -w and -e");
     if (o.app == "rwr" && o.sp < 0) o.sp = 0.5;
     if ((o.app == "pagerank" || o.app == "ppr") && o.sp <= 0) return usage("--sp is required");
-    if (o.app == "deepwalk" && o.len < 1) return usage("-l is required for deepwalk");
+    if ((o.app == "deepwalk" || o.app == "node2vec") && o.len < 1) return usage("-l is required for deepwalk and node2vec");
+    if (o.app == "node2vec" && (o.p <= 0 || o.q <= 0)) return usage("-p and -q are required for node2vec");
     if (o.app == "ppr" && o.source < 0) return usage("--source is required for ppr");
     if (o.start != "per_vertex" && o.start != "uniform") return usage("--start must be per_vertex or uniform");
 
@@ -169,6 +176,17 @@ int main(int argc, char **argv)
             value0 = pairs.empty() ? 0 : pairs[1];
             if (!o.out.empty() && !write_file(o.out, pairs.data(), pairs.size() * 4)) rc = PTW_EIO;
         }
+    } else if (o.app == "node2vec") {
+        std::vector<int32_t> paths(cfg.n_walkers * (uint64_t)o.len);
+        ptw_node2vec_stats ns;
+        std::memset(&ns, 0, sizeof(ns));
+        rc = check(ptw_node2vec(g, &cfg, (uint32_t)o.len, o.p, o.q, paths.data(), &ns), "node2vec");
+        st.walkers = ns.walkers;
+        st.moves = ns.moves;
+        st.kernel_ms = ns.kernel_ms;
+        st.total_ms = ns.total_ms;
+        if (!rc && !o.paths_out.empty() && !write_file(o.paths_out, paths.data(), paths.size() * 4))
+            rc = PTW_EIO;
     } else {
         std::vector<int32_t> paths(cfg.n_walkers * (uint64_t)o.len);
         rc = check(ptw_deepwalk(g, &cfg, (uint32_t)o.len, paths.data(), &st), "deepwalk");

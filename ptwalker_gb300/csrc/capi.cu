@@ -413,6 +413,59 @@ int run_paths(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *d_path
     return PTW_OK;
 }
 
+// Acceptance thresholds of the node2vec rejection draw: class weights
+// {1/p (return), 1 (neighbour of the previous vertex), 1/q (other)} over
+// their maximum M, as 32-bit fractions (2^32 = always accept).
+int n2v_thresholds(double p, double q, uint64_t thr[3])
+{
+    if (!(p > 0.0 && q > 0.0 && p < 1e300 && q < 1e300))
+        return fail(PTW_EINVAL, "node2vec p and q must be positive and finite");
+    const double w[3] = {1.0 / p, 1.0, 1.0 / q};
+    const double m = std::max(w[0], std::max(w[1], w[2]));
+    const double lo = std::min(w[0], std::min(w[1], w[2]));
+    if (m > 1024.0 * lo)
+        return fail(PTW_EINVAL, "node2vec needs max(1/p, 1, 1/q) <= 1024 * min(1/p, 1, 1/q)");
+    for (int c = 0; c < 3; ++c) thr[c] = w[c] >= m ? 1ull << 32 : (uint64_t)(w[c] / m * 4294967296.0);
+    return PTW_OK;
+}
+
+int run_node2vec(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, const uint64_t thr[3], int32_t *d_paths)
+{
+    int rc = upload_sources(g, cfg);
+    if (rc) return rc;
+    PTW_CUDA(cudaEventRecord(g->ev[3], g->stream));
+    PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 4 * sizeof(unsigned long long), g->stream));
+    if (cfg->n_walkers && L && !ensure_ext_columns(g))
+        return fail(PTW_ENOMEM, "node2vec needs the extended column copy (16 bytes per CSR entry), "
+                                "which does not fit in device memory");
+    PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
+    if (cfg->n_walkers && L) {
+        const uint64_t w0 = cfg->first_walker;
+        rc = launch_node2vec(g, w0, w0 + cfg->n_walkers, L, cfg->seed, cfg->start_mode,
+                             cfg->start_mode == PTW_START_SOURCES ? cfg->n_sources : 0, thr, d_paths);
+        if (rc) return rc;
+    }
+    PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
+    return PTW_OK;
+}
+
+int node2vec_stats(ptw_graph *g, const ptw_walk_cfg *cfg, ptw_node2vec_stats *stats)
+{
+    unsigned long long c[3];
+    PTW_CUDA(cudaMemcpyAsync(c, g->sc.ctrl + 1, sizeof(c), cudaMemcpyDeviceToHost, g->stream));
+    PTW_CUDA(cudaStreamSynchronize(g->stream));
+    stats->walkers = cfg->n_walkers;
+    stats->moves = c[0];
+    stats->trials = c[1];
+    stats->probes = c[2];
+    float ms = 0;
+    PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]));
+    stats->kernel_ms = ms;
+    PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[3], g->ev[2]));
+    stats->total_ms = ms;
+    return PTW_OK;
+}
+
 }  // namespace
 }  // namespace ptw
 
@@ -871,6 +924,52 @@ try {
         stats->total_ms = ms;
     }
     return PTW_OK;
+} catch (...) {
+    return host_exception();
+}
+
+extern "C" int ptw_node2vec_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, double p, double q,
+                                int32_t *d_paths, ptw_node2vec_stats *stats)
+try {
+    NvtxRange nvtx("ptw_node2vec_dev");
+    uint64_t thr[3];
+    int rc = n2v_thresholds(p, q, thr);
+    if (rc) return rc;
+    rc = check_cfg(g, cfg, false);
+    if (rc) return rc;
+    if (!d_paths && cfg->n_walkers && L) return fail(PTW_EINVAL, "null paths buffer");
+    if (g->dg.id_bound > 0x80000000u) return fail(PTW_EINVAL, "names above 2^31-1 do not fit int32 paths");
+    PTW_CUDA(cudaSetDevice(g->device));
+    rc = run_node2vec(g, cfg, L, thr, d_paths);
+    if (rc) return rc;
+    PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    return stats ? node2vec_stats(g, cfg, stats) : PTW_OK;
+} catch (...) {
+    return host_exception();
+}
+
+extern "C" int ptw_node2vec(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, double p, double q,
+                            int32_t *h_paths, ptw_node2vec_stats *stats)
+try {
+    NvtxRange nvtx("ptw_node2vec");
+    uint64_t thr[3];
+    int rc = n2v_thresholds(p, q, thr);
+    if (rc) return rc;
+    rc = check_cfg(g, cfg, false);
+    if (rc) return rc;
+    if (!h_paths && cfg->n_walkers && L) return fail(PTW_EINVAL, "null paths buffer");
+    if (g->dg.id_bound > 0x80000000u) return fail(PTW_EINVAL, "names above 2^31-1 do not fit int32 paths");
+    PTW_CUDA(cudaSetDevice(g->device));
+    const uint64_t bytes = cfg->n_walkers * (uint64_t)L * 4;
+    void *stage = nullptr;
+    rc = stage_bytes(g, bytes, &stage);
+    if (rc) return rc;
+    rc = run_node2vec(g, cfg, L, thr, (int32_t *)stage);
+    if (rc) return rc;
+    if (bytes) PTW_CUDA(cudaMemcpyAsync(h_paths, stage, bytes, cudaMemcpyDeviceToHost, g->stream));
+    PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    PTW_CUDA(cudaStreamSynchronize(g->stream));
+    return stats ? node2vec_stats(g, cfg, stats) : PTW_OK;
 } catch (...) {
     return host_exception();
 }

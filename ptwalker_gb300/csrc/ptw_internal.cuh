@@ -21,6 +21,7 @@
 #define PTW_TAG_START 0x53545254u // "STRT": start-vertex draw
 #define PTW_TAG_RMAT 0x524D4154u  // "RMAT": synthetic edge generation
 #define PTW_TAG_CHUNGLU 0x43484C55u // "CHLU": Chung-Lu endpoints
+#define PTW_TAG_N2V 0x4E320000u     // "N2" + trial pair index: node2vec candidate draws
 
 namespace ptw {
 
@@ -108,6 +109,24 @@ __device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1)
         k1 += 0xBB67AE85u;
     }
     return c;
+}
+
+// Start vertex (internal id) of walker wid: PTW_START_PER_VERTEX takes the
+// (wid mod n)-th vertex by name; PTW_START_UNIFORM draws a vertex with
+// Philox(ctr = (wid_lo, wid_hi, 0, "STRT")); PTW_START_SOURCES draws from the
+// source list the same way (one source needs no draw).
+__device__ __forceinline__ uint32_t walker_start(int start_mode, const uint32_t *start_map,
+                                                 const uint32_t *sources, uint32_t n, uint32_t n_sources,
+                                                 uint32_t key0, uint32_t key1, uint64_t wid)
+{
+    if (start_mode == PTW_START_PER_VERTEX) {
+        const uint32_t idx = wid < n ? (uint32_t)wid : (uint32_t)(wid % n);
+        return start_map[idx];
+    }
+    if (start_mode == PTW_START_SOURCES && n_sources == 1) return sources[0];
+    const uint4 r = philox(make_uint4((uint32_t)wid, (uint32_t)(wid >> 32), 0u, PTW_TAG_START), key0, key1);
+    if (start_mode == PTW_START_UNIFORM) return start_map[__umulhi(r.x, n)];
+    return sources[__umulhi(r.x, n_sources)];
 }
 
 // L2 eviction-priority policies (PTX createpolicy) for the gathers:
@@ -270,6 +289,12 @@ struct WalkLaunch {
 int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t);
 int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
                  int start_mode, uint32_t n_sources, int32_t *paths);
+// Second-order (node2vec) paths (node2vec.cu): thr = acceptance thresholds
+// {return, neighbour of the previous vertex, other}; needs the extended
+// column copy (PTW_ENOMEM when it does not fit).  Moves, candidate draws and
+// row probes accumulate in ctrl[1..3].
+int launch_node2vec(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
+                    int start_mode, uint32_t n_sources, const uint64_t thr[3], int32_t *paths);
 // Stream-ordered device allocation from a per-device pool that keeps up to
 // a quarter of the device memory cached across synchronisations (the default
 // pool hands memory back at each one), for count tables and the short-lived

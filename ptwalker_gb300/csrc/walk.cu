@@ -63,15 +63,7 @@ struct WalkArgs {
 
 __device__ __forceinline__ uint32_t start_vertex(const WalkArgs &a, uint64_t wid)
 {
-    if (a.start_mode == PTW_START_PER_VERTEX) {
-        const uint32_t idx = wid < a.n ? (uint32_t)wid : (uint32_t)(wid % a.n);
-        return a.start_map[idx];
-    }
-    if (a.start_mode == PTW_START_SOURCES && a.n_sources == 1) return a.sources[0];
-    const uint4 r = philox(make_uint4((uint32_t)wid, (uint32_t)(wid >> 32), 0u, PTW_TAG_START),
-                           a.key0, a.key1);
-    if (a.start_mode == PTW_START_UNIFORM) return a.start_map[__umulhi(r.x, a.n)];
-    return a.sources[__umulhi(r.x, a.n_sources)];
+    return walker_start(a.start_mode, a.start_map, a.sources, a.n, a.n_sources, a.key0, a.key1, wid);
 }
 
 template <bool HOT>
