@@ -704,7 +704,31 @@ def run_ours(args):
         deepwalk = {"walk_len": L, "walkers": n, "steps_per_s": dsteps / (dms / 1000.0),
                     "ms_per_step": dms, "achieved_gbs": dbytes / (dms / 1000.0) / 1e9,
                     "frac": dbytes / (dms / 1000.0) / 1e9 / peak,
-                    "path_bytes": 4 * n * L}
+                    "path_bytes": 4 * n * L,
+                    "kernel": "k_lane_paths" if tune.ext_columns & 2 else "k_paths"}
+        # node2vec side line (second-order walks, same walkers and length):
+        # algorithmic bytes = 64 B per candidate draw (row record + column
+        # sector, as a DeepWalk move) + 32 B per neighbour test (one filter
+        # sector) + 32 B per probe of the previous vertex's row + 4 B per
+        # path entry
+        node2vec = []
+        for p_, q_ in ((2.0, 0.5), (0.5, 2.0)):
+            _, st = ptw.node2vec(G, n, L, p_, q_, 5, out=paths, stats=True)
+            torch.cuda.synchronize()
+            d0.record(stream)
+            for k in range(reps):
+                ptw.node2vec(G, n, L, p_, q_, 60 + k, out=paths)
+            d1.record(stream)
+            torch.cuda.synchronize()
+            nms = d0.elapsed_time(d1) / reps
+            nbytes = 64 * st.trials + 32 * st.checks + 32 * st.probes + 4 * n * L
+            node2vec.append({"p": p_, "q": q_, "walk_len": L, "walkers": n, "ms_per_step": nms,
+                             "steps_per_s": st.moves / (nms / 1000.0),
+                             "trials_per_move": st.trials / st.moves, "checks_per_move": st.checks / st.moves,
+                             "probes_per_move": st.probes / st.moves,
+                             "achieved_gbs": nbytes / (nms / 1000.0) / 1e9,
+                             "frac": nbytes / (nms / 1000.0) / 1e9 / peak, "kernel": "k_lane_paths"})
+        deepwalk["node2vec"] = node2vec
         del paths
 
     # DRAM bytes per walk launch: the ncu capture's bytes per move at this

@@ -235,13 +235,15 @@ int ptw_deepwalk_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t 
  * int32), padded with -1 after a vertex without out-edges, as ptw_deepwalk.
  * p and q must be positive and finite with max(1/p, 1, 1/q) / min(1/p, 1, 1/q)
  * <= 1024 (PTW_EINVAL otherwise).  Needs the extended column copy (16 bytes
- * per CSR entry, built on first use; PTW_ENOMEM when it does not fit).
+ * per CSR entry) and an edge filter (a blocked Bloom filter, about 2 bytes
+ * per CSR entry), both built on first use (PTW_ENOMEM when they do not fit).
  * cfg->sp and cfg->max_moves are ignored. */
 typedef struct ptw_node2vec_stats {
     uint64_t walkers;
     uint64_t moves;    /* edge traversals */
     uint64_t trials;   /* candidate draws (>= moves; rejected candidates included) */
-    uint64_t probes;   /* reads of the previous vertex's row by the neighbour test */
+    uint64_t checks;   /* neighbour tests (edge-filter reads) */
+    uint64_t probes;   /* reads of the previous vertex's row by the tests the filter passed */
     float kernel_ms;   /* device time of the walk kernel */
     float total_ms;    /* device time of the whole call, copies included */
 } ptw_node2vec_stats;

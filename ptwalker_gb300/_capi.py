@@ -47,7 +47,7 @@ class WalkStats(ctypes.Structure):
 
 class Node2vecStats(ctypes.Structure):
     _fields_ = [("walkers", ctypes.c_uint64), ("moves", ctypes.c_uint64),
-                ("trials", ctypes.c_uint64), ("probes", ctypes.c_uint64),
+                ("trials", ctypes.c_uint64), ("checks", ctypes.c_uint64), ("probes", ctypes.c_uint64),
                 ("kernel_ms", ctypes.c_float), ("total_ms", ctypes.c_float)]
 
 

@@ -393,12 +393,13 @@ def deepwalk(graph, n_walkers=None, walk_len=80, seed=0, start="per_vertex", sou
 class Node2vecStats:
     def __init__(self, s):
         self.walkers, self.moves = int(s.walkers), int(s.moves)
-        self.trials, self.probes = int(s.trials), int(s.probes)
+        self.trials, self.checks, self.probes = int(s.trials), int(s.checks), int(s.probes)
         self.kernel_ms, self.total_ms = float(s.kernel_ms), float(s.total_ms)
 
     def __repr__(self):
-        return ("Node2vecStats(walkers=%d, moves=%d, trials=%d, probes=%d, kernel_ms=%.3f, total_ms=%.3f)"
-                % (self.walkers, self.moves, self.trials, self.probes, self.kernel_ms, self.total_ms))
+        return ("Node2vecStats(walkers=%d, moves=%d, trials=%d, checks=%d, probes=%d, kernel_ms=%.3f, "
+                "total_ms=%.3f)" % (self.walkers, self.moves, self.trials, self.checks, self.probes,
+                                    self.kernel_ms, self.total_ms))
 
 
 def node2vec(graph, n_walkers=None, walk_len=80, p=1.0, q=1.0, seed=0, start="per_vertex", sources=None,

@@ -434,10 +434,10 @@ int run_node2vec(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, const uint64
     int rc = upload_sources(g, cfg);
     if (rc) return rc;
     PTW_CUDA(cudaEventRecord(g->ev[3], g->stream));
-    PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 4 * sizeof(unsigned long long), g->stream));
-    if (cfg->n_walkers && L && !ensure_ext_columns(g))
-        return fail(PTW_ENOMEM, "node2vec needs the extended column copy (16 bytes per CSR entry), "
-                                "which does not fit in device memory");
+    PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 5 * sizeof(unsigned long long), g->stream));
+    if (cfg->n_walkers && L && !(ensure_ext_columns(g) && ensure_edge_filter(g)))
+        return fail(PTW_ENOMEM, "node2vec needs the extended column copy (16 bytes per CSR entry) and "
+                                "the edge filter (2 bytes per CSR entry), which do not fit in device memory");
     PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
     if (cfg->n_walkers && L) {
         const uint64_t w0 = cfg->first_walker;
@@ -451,13 +451,14 @@ int run_node2vec(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, const uint64
 
 int node2vec_stats(ptw_graph *g, const ptw_walk_cfg *cfg, ptw_node2vec_stats *stats)
 {
-    unsigned long long c[3];
+    unsigned long long c[4];
     PTW_CUDA(cudaMemcpyAsync(c, g->sc.ctrl + 1, sizeof(c), cudaMemcpyDeviceToHost, g->stream));
     PTW_CUDA(cudaStreamSynchronize(g->stream));
     stats->walkers = cfg->n_walkers;
     stats->moves = c[0];
     stats->trials = c[1];
-    stats->probes = c[2];
+    stats->checks = c[2];
+    stats->probes = c[3];
     float ms = 0;
     PTW_CUDA(cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]));
     stats->kernel_ms = ms;

@@ -351,6 +351,7 @@ void graph_release(ptw_graph *g)
     cudaFree(g->dg.col_named);
     cudaFree(g->dg.col_ext);
     cudaFree(g->dg.vtx_ext);
+    cudaFree(g->dg.edge_filter);
     cudaFree(g->sc.counts);
     cudaFree(g->sc.ctrl);
     cudaFree(g->sc.sources);

@@ -9,7 +9,7 @@
 // the next vertex x is drawn over v's row with weight 1/p if x == t, 1 if x
 // is an out-neighbour of t, 1/q otherwise; the first move is uniform.
 //
-// k_node2vec draws by rejection over v's row.  Trial k of move s takes two
+// k_lane_paths draws by rejection over v's row.  Trial k of move s takes two
 // words of Philox(ctr = (wid_lo, wid_hi, s, "N2" + k/2)) -- (x, y) for even
 // k, (z, w) for odd k --, reads the candidate's extended column entry
 // {id, first column, degree, name} (one 16-byte gather: the candidate's own
@@ -17,9 +17,15 @@
 // threshold of the candidate's class.  Most trials are decided without the
 // neighbour query: a return to t is known from the id, a word below both
 // the neighbour and the other threshold accepts and a word above both
-// rejects.  Only the words between them search t's row for the candidate's
-// name (rows are in ascending name order), all groups of a lane searching in
-// step so their probes are in flight together.  Trial 65535 is accepted
+// rejects.  Only the words between them ask whether the candidate x is an
+// out-neighbour of t, the way the reference's has_neighbor does
+// (src/core/graph.hpp:811-820): a Bloom filter over the edges first, then a
+// binary search of t's row for x's name (rows are in ascending name order)
+// only when the filter does not rule the edge out.  The filter is blocked:
+// one 32-byte block per edge key, one bit in each of its 8 words, so a test
+// is one sector read; at 16 bits per edge about 0.1% of non-edges pass it.
+// All groups of a lane test and search in step, so their reads are in
+// flight together.  Trial 65535 is accepted
 // whatever its word, so every move ends; the host keeps max(w) / min(w) <=
 // 1024, which puts that cap below 1e-27 per move.
 //
@@ -35,16 +41,59 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kN2vWarps = 4;                // warps per block
 constexpr uint32_t kN2vMaxTrials = 65536u;  // trials per move before the last is taken
 
+// MurmurHash3 64-bit finaliser (Appleby, public domain).
+__host__ __device__ __forceinline__ uint64_t fmix64(uint64_t k)
+{
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+
+// Filter block of the directed edge (u, v) (internal ids) and the bit of
+// each of its 8 words.
+struct FilterKey {
+    uint64_t block;
+    uint64_t bits;  // 5 bits per word
+};
+
+__device__ __forceinline__ FilterKey filter_key(uint32_t u, uint32_t v, uint64_t blocks)
+{
+    const uint64_t key = ((uint64_t)u << 32) | v;
+    return FilterKey{fmix64(key) & (blocks - 1), fmix64(key + 0x9E3779B97F4A7C15ull)};
+}
+
+// One warp per vertex: sets the bits of every out-edge.
+__global__ void k_build_edge_filter(const uint2 *__restrict__ adj, const uint32_t *__restrict__ col, uint32_t n,
+                                    uint64_t blocks, uint32_t *__restrict__ filter)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t u = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; u < n; u += warps) {
+        const uint2 r = adj[u];
+        for (uint32_t i = lane; i < r.y; i += 32) {
+            const FilterKey fk = filter_key((uint32_t)u, col[(uint64_t)r.x + i], blocks);
+            uint32_t *blk = filter + fk.block * 8;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) atomicOr(&blk[j], 1u << ((fk.bits >> (5 * j)) & 31));
+        }
+    }
+}
+
 struct N2vArgs {
-    const uint2 *__restrict__ adj;
+    const uint4 *__restrict__ vtx_ext;    // {id, first column, degree, name} per vertex
     const uint4 *__restrict__ col_ext;    // {id, first column, degree, name} per CSR entry
+    const uint32_t *__restrict__ filter;  // edge filter, filter_blocks blocks of 8 words
+    uint64_t filter_blocks;
     const uint32_t *__restrict__ start_map;
     const uint32_t *__restrict__ sources;
-    const uint32_t *__restrict__ int2name;
     int32_t *__restrict__ paths;
-    unsigned long long *__restrict__ ctrl;  // [1] moves, [2] candidate draws, [3] row probes
+    unsigned long long *__restrict__ ctrl;  // [0] walker cursor, [1] moves, [2] candidate draws, [3] neighbour tests, [4] row probes
     uint64_t w_begin, n_walk;
     uint64_t thr_ret, thr_nb, thr_out;    // acceptance thresholds (2^32 = always)
+    uint32_t tag;                         // draw tag: "N2" + trial pair, or "WALK"
     uint32_t n, L;
     uint32_t key0, key1;
     uint32_t n_sources;
@@ -52,148 +101,199 @@ struct N2vArgs {
     int hints;
 };
 
-// Name of CSR entry e, read from its extended column entry.
-__device__ __forceinline__ uint32_t entry_name(const uint4 *col_ext, uint64_t e, uint64_t pol)
-{
-    return ld_hint_u32(reinterpret_cast<const uint32_t *>(col_ext) + 4 * e + 3, pol);
-}
+// Walker slot states.
+enum : uint32_t { kIdle = 0, kDraw = 1, kFilter = 2, kSearch = 3 };
 
-// G groups of 32 consecutive walkers per warp, one walker of each group per
-// lane.
-template <int G>
-__global__ void __launch_bounds__(kN2vWarps * 32) k_node2vec(const N2vArgs a)
+// ILP walker slots per lane, each an independent state machine: every pass
+// of the loop issues one read per active slot -- a candidate's column entry
+// (kDraw), an edge-filter block (kFilter) or one entry of the previous
+// vertex's row (kSearch) -- and then consumes it, so a slot that rejects or
+// searches does not hold back the other lanes of its warp.  A slot whose
+// walk ends takes the next walker id from a warp-private range refilled
+// from one global cursor (ctrl[0]).  Each slot stages C path positions of
+// its walker in a shared-memory row and writes them out as one contiguous
+// segment of the walker's path row.  First-order DeepWalk
+// (src/core/deepwalk.cpp:25-28) runs through the same loop with every
+// threshold at 2^32 and draw tag "WALK": each move then accepts its first
+// candidate, the neighbour mulhi(x, degree) of
+// Philox(ctr = (wid_lo, wid_hi, s, "WALK")), the draw of the other walk
+// kernels.
+template <int ILP>
+__global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
 {
-    constexpr uint32_t C = G == 1 ? 32 : 16;
-    __shared__ int32_t stage[kN2vWarps][G][32][C + 1];
+    constexpr uint32_t C = 32;
+    __shared__ int32_t stage[kN2vWarps][ILP][32][C + 1];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t wib = threadIdx.x >> 5;
-    const uint64_t n_groups = (a.n_walk + 31) / 32;
-    const uint64_t warps = (uint64_t)gridDim.x * kN2vWarps;
+    const uint32_t lt_mask = (1u << lane) - 1u;
     const uint64_t pol_keep = l2_policy(a.hints ? 1 : 0);
     const uint64_t pol_stream = l2_policy(a.hints ? 2 : 0);
     const uint64_t thr_lo = a.thr_nb < a.thr_out ? a.thr_nb : a.thr_out;
     const uint64_t thr_hi = a.thr_nb < a.thr_out ? a.thr_out : a.thr_nb;
-    unsigned long long moves = 0, trials = 0, probes = 0;
+    const uint32_t chunk = 32 * ILP;
+    unsigned long long moves = 0, trials = 0, checks = 0, probes = 0;
 
-    for (uint64_t g0 = (blockIdx.x * (uint64_t)kN2vWarps + wib) * G; g0 < n_groups; g0 += warps * G) {
-        uint64_t wid[G];
-        uint32_t v[G], t[G], rows[G];
-        uint2 rec[G], trec[G];  // {first column, degree} of v and of t
-        bool dead[G];
+    uint64_t wid[ILP], fbits[ILP];
+    uint32_t st[ILP], v[ILP], t[ILP], p[ILP], c0[ILP], k[ILP], au[ILP], lo[ILP], hi[ILP], mid[ILP];
+    uint2 rec[ILP], trec[ILP];  // {first column, degree} of v and of t
+    uint4 r[ILP], cx[ILP];      // draw words; candidate {id, first column, degree, name}
 #pragma unroll
-        for (int g = 0; g < G; ++g) {
-            const uint64_t grp = g0 + g;
-            const uint64_t j = grp * 32 + lane;
-            const bool valid = j < a.n_walk;
-            wid[g] = a.w_begin + j;
-            rows[g] = grp < n_groups ? (uint32_t)(a.n_walk - grp * 32 < 32 ? a.n_walk - grp * 32 : 32) : 0;
-            v[g] = valid ? walker_start(a.start_mode, a.start_map, a.sources, a.n, a.n_sources, a.key0, a.key1,
-                                        wid[g])
-                         : 0;
-            dead[g] = !valid;
-            rec[g] = valid ? ld_hint_u2(&a.adj[v[g]], pol_keep) : make_uint2(0u, 0u);
-            t[g] = 0;
-            trec[g] = make_uint2(0u, 0u);
-            stage[wib][g][lane][0] = valid ? (int32_t)a.int2name[v[g]] : -1;
+    for (int s = 0; s < ILP; ++s) {
+        st[s] = kIdle;
+        wid[s] = fbits[s] = 0;
+        v[s] = t[s] = p[s] = c0[s] = k[s] = au[s] = lo[s] = hi[s] = mid[s] = 0;
+        rec[s] = trec[s] = make_uint2(0u, 0u);
+        r[s] = cx[s] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    uint64_t next = 0, end = 0;  // warp-uniform walker range [next, end) relative to w_begin
+    bool exhausted = false;
+
+    // Writes positions [c0, p) of slot s from its stage row.
+    auto flush = [&](int s) {
+        int32_t *dst = a.paths + (wid[s] - a.w_begin) * (uint64_t)a.L;
+        for (uint32_t i = c0[s]; i < p[s]; ++i) dst[i] = stage[wib][s][lane][i - c0[s]];
+        c0[s] = p[s];
+    };
+    // The walker of slot s stands at a vertex without out-edges: the rest
+    // of its path is -1.
+    auto finish_dead = [&](int s) {
+        int32_t *dst = a.paths + (wid[s] - a.w_begin) * (uint64_t)a.L;
+        for (uint32_t i = p[s]; i < a.L; ++i) dst[i] = -1;
+        st[s] = kIdle;
+    };
+
+    for (;;) {
+        // ---- refill idle slots ---------------------------------------------
+#pragma unroll
+        for (int s = 0; s < ILP; ++s) {
+            const unsigned need = __ballot_sync(kFull, st[s] == kIdle);
+            if (need == 0 || exhausted) continue;
+            const uint32_t n_need = __popc(need);
+            const uint32_t rank = __popc(need & lt_mask);
+            uint64_t my = ~0ull;
+            const uint32_t took = (uint32_t)(end - next < n_need ? end - next : n_need);
+            if (st[s] == kIdle && rank < took) my = next + rank;
+            next += took;
+            if (took < n_need) {
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd(&a.ctrl[0], (unsigned long long)chunk);
+                base = __shfl_sync(kFull, base, 0);
+                if (base >= a.n_walk) {
+                    exhausted = true;
+                    next = end = a.n_walk;
+                } else {
+                    next = base;
+                    end = base + chunk < a.n_walk ? base + chunk : a.n_walk;
+                    const uint32_t rest = n_need - took;
+                    const uint32_t take2 = (uint32_t)(end - next < rest ? end - next : rest);
+                    if (st[s] == kIdle && rank >= took && rank - took < take2) my = next + (rank - took);
+                    next += take2;
+                }
+            }
+            if (my != ~0ull) {
+                wid[s] = a.w_begin + my;
+                v[s] = walker_start(a.start_mode, a.start_map, a.sources, a.n, a.n_sources, a.key0, a.key1,
+                                    wid[s]);
+                const uint4 vx = ld_hint_u4(&a.vtx_ext[v[s]], pol_keep);  // {id, first column, degree, name}
+                rec[s] = make_uint2(vx.y, vx.z);
+                stage[wib][s][lane][0] = (int32_t)vx.w;
+                p[s] = 1;
+                c0[s] = 0;
+                k[s] = 0;
+                st[s] = kDraw;
+                if (a.L == 1 || rec[s].y == 0) {
+                    flush(s);
+                    finish_dead(s);
+                }
+            }
         }
-        uint32_t c0 = 0;
-        for (uint32_t p = 1; p <= a.L; ++p) {
-            if (p == a.L || p % C == 0) {
-                __syncwarp();
-                const uint32_t cols = p - c0;
+        bool any = false;
 #pragma unroll
-                for (int g = 0; g < G; ++g)
-                    for (uint32_t idx = lane; idx < rows[g] * cols; idx += 32) {
-                        const uint32_t rr = idx / cols, cc = idx - rr * cols;
-                        a.paths[((g0 + g) * 32 + rr) * (uint64_t)a.L + c0 + cc] = stage[wib][g][rr][cc];
-                    }
-                __syncwarp();
-                c0 = p;
-                if (p == a.L) break;
+        for (int s = 0; s < ILP; ++s) any |= st[s] != kIdle;
+        // walkers that end at their start (L = 1, no out-edge) leave every
+        // slot idle while ids remain: refill again
+        if (!__any_sync(kFull, any)) {
+            if (exhausted) break;
+            continue;
+        }
+
+        // ---- one read per active slot --------------------------------------
+        uint4 x[ILP], x2[ILP];
+#pragma unroll
+        for (int s = 0; s < ILP; ++s) {
+            if (st[s] == kDraw) {
+                if ((k[s] & 1) == 0)
+                    r[s] = philox(make_uint4((uint32_t)wid[s], (uint32_t)(wid[s] >> 32), p[s] - 1,
+                                             a.tag + (k[s] >> 1)),
+                                  a.key0, a.key1);
+                const uint32_t cu = (k[s] & 1) ? r[s].z : r[s].x;
+                au[s] = (k[s] & 1) ? r[s].w : r[s].y;
+                x[s] = ld_hint_u4(&a.col_ext[rec[s].x + __umulhi(cu, rec[s].y)], pol_stream);
+            } else if (st[s] == kFilter) {
+                const FilterKey fk = filter_key(t[s], cx[s].x, a.filter_blocks);
+                fbits[s] = fk.bits;
+                const uint4 *blk = reinterpret_cast<const uint4 *>(a.filter + fk.block * 8);
+                x[s] = ld_hint_u4(blk, pol_stream);
+                x2[s] = ld_hint_u4(blk + 1, pol_stream);
+            } else if (st[s] == kSearch) {
+                mid[s] = lo[s] + ((hi[s] - lo[s]) >> 1);
+                x[s] = ld_hint_u4(&a.col_ext[(uint64_t)trec[s].x + mid[s]], pol_stream);
             }
-            // move p-1: trials until one is accepted
-            bool pend[G];
-            uint32_t k[G], nm[G], au[G];
-            uint4 r[G], cx[G];
-            bool any = false;
+        }
+
+        // ---- consume ------------------------------------------------------
 #pragma unroll
-            for (int g = 0; g < G; ++g) {
-                if (!dead[g] && rec[g].y == 0) dead[g] = true;
-                pend[g] = !dead[g];
-                any |= pend[g];
-                k[g] = 0;
-                nm[g] = 0;
-            }
-            while (any) {
+        for (int s = 0; s < ILP; ++s) {
+            if (st[s] == kIdle) continue;
+            int verdict = -1;  // -1 undecided, 0 reject, 1 accept
+            if (st[s] == kDraw) {
+                cx[s] = x[s];
+                ++trials;
+                if (p[s] == 1 || k[s] + 1 == kN2vMaxTrials) verdict = 1;
+                else if (cx[s].x == t[s]) verdict = (uint64_t)au[s] < a.thr_ret;
+                else if ((uint64_t)au[s] < thr_lo) verdict = 1;
+                else if ((uint64_t)au[s] >= thr_hi) verdict = 0;
+                else st[s] = kFilter;
+            } else if (st[s] == kFilter) {
+                ++checks;
+                const uint32_t w[8] = {x[s].x, x[s].y, x[s].z, x[s].w, x2[s].x, x2[s].y, x2[s].z, x2[s].w};
+                bool pass = true;
 #pragma unroll
-                for (int g = 0; g < G; ++g) {
-                    if (!pend[g]) continue;
-                    if ((k[g] & 1) == 0)
-                        r[g] = philox(make_uint4((uint32_t)wid[g], (uint32_t)(wid[g] >> 32), p - 1,
-                                                 PTW_TAG_N2V + (k[g] >> 1)),
-                                      a.key0, a.key1);
-                    const uint32_t cu = (k[g] & 1) ? r[g].z : r[g].x;
-                    au[g] = (k[g] & 1) ? r[g].w : r[g].y;
-                    cx[g] = ld_hint_u4(&a.col_ext[rec[g].x + __umulhi(cu, rec[g].y)], pol_stream);
-                    ++trials;
+                for (int j = 0; j < 8; ++j) pass &= (w[j] >> ((fbits[s] >> (5 * j)) & 31)) & 1u;
+                if (!pass) {
+                    verdict = (uint64_t)au[s] < a.thr_out;
+                } else {
+                    lo[s] = 0;
+                    hi[s] = trec[s].y;
+                    st[s] = kSearch;
                 }
-                bool acc[G], chk[G];
-                uint32_t lo[G], hi[G];
-                bool searching = false;
-#pragma unroll
-                for (int g = 0; g < G; ++g) {
-                    acc[g] = false;
-                    chk[g] = false;
-                    if (!pend[g]) continue;
-                    if (p == 1 || k[g] + 1 == kN2vMaxTrials) acc[g] = true;
-                    else if (cx[g].x == t[g]) acc[g] = (uint64_t)au[g] < a.thr_ret;
-                    else if ((uint64_t)au[g] < thr_lo) acc[g] = true;
-                    else if ((uint64_t)au[g] >= thr_hi) acc[g] = false;
-                    else chk[g] = true;
-                    lo[g] = 0;
-                    hi[g] = chk[g] ? trec[g].y : 0;
-                    searching |= chk[g];
-                }
-                // is the candidate an out-neighbour of t?  Binary search of
-                // t's row by name, every searching group one probe per round.
-                bool found[G];
-#pragma unroll
-                for (int g = 0; g < G; ++g) found[g] = false;
-                while (searching) {
-                    searching = false;
-#pragma unroll
-                    for (int g = 0; g < G; ++g) {
-                        if (!chk[g] || found[g] || lo[g] >= hi[g]) continue;
-                        const uint32_t mid = lo[g] + ((hi[g] - lo[g]) >> 1);
-                        const uint32_t nmid = entry_name(a.col_ext, (uint64_t)trec[g].x + mid, pol_stream);
-                        ++probes;
-                        if (nmid == cx[g].w) found[g] = true;
-                        else if (nmid < cx[g].w) lo[g] = mid + 1;
-                        else hi[g] = mid;
-                        searching |= !found[g] && lo[g] < hi[g];
-                    }
-                }
-                any = false;
-#pragma unroll
-                for (int g = 0; g < G; ++g) {
-                    if (!pend[g]) continue;
-                    if (chk[g]) acc[g] = (uint64_t)au[g] < (found[g] ? a.thr_nb : a.thr_out);
-                    if (acc[g]) {
-                        pend[g] = false;
-                        t[g] = v[g];
-                        trec[g] = rec[g];
-                        v[g] = cx[g].x;
-                        rec[g] = make_uint2(cx[g].y, cx[g].z);
-                        nm[g] = cx[g].w;
-                        ++moves;
-                    } else {
-                        ++k[g];
-                        any = true;
-                    }
+            } else {
+                ++probes;
+                if (x[s].w == cx[s].w) {
+                    verdict = (uint64_t)au[s] < a.thr_nb;
+                } else {
+                    if (x[s].w < cx[s].w) lo[s] = mid[s] + 1;
+                    else hi[s] = mid[s];
+                    if (lo[s] >= hi[s]) verdict = (uint64_t)au[s] < a.thr_out;
                 }
             }
-#pragma unroll
-            for (int g = 0; g < G; ++g) stage[wib][g][lane][p - c0] = dead[g] ? -1 : (int32_t)nm[g];
+            if (verdict == 0) {
+                ++k[s];
+                st[s] = kDraw;
+            } else if (verdict == 1) {
+                t[s] = v[s];
+                trec[s] = rec[s];
+                v[s] = cx[s].x;
+                rec[s] = make_uint2(cx[s].y, cx[s].z);
+                stage[wib][s][lane][p[s] - c0[s]] = (int32_t)cx[s].w;
+                ++p[s];
+                ++moves;
+                k[s] = 0;
+                st[s] = kDraw;
+                if (p[s] == a.L || p[s] - c0[s] == C || rec[s].y == 0) flush(s);
+                if (p[s] == a.L) st[s] = kIdle;
+                else if (rec[s].y == 0) finish_dead(s);
+            }
         }
     }
 
@@ -201,37 +301,80 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_node2vec(const N2vArgs a)
     for (int o = 16; o; o >>= 1) {
         moves += __shfl_xor_sync(kFull, moves, o);
         trials += __shfl_xor_sync(kFull, trials, o);
+        checks += __shfl_xor_sync(kFull, checks, o);
         probes += __shfl_xor_sync(kFull, probes, o);
     }
     if (lane == 0) {
         if (moves) atomicAdd(&a.ctrl[1], moves);
         if (trials) atomicAdd(&a.ctrl[2], trials);
-        if (probes) atomicAdd(&a.ctrl[3], probes);
+        if (checks) atomicAdd(&a.ctrl[3], checks);
+        if (probes) atomicAdd(&a.ctrl[4], probes);
     }
 }
 
 }  // namespace
 
-int launch_node2vec(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
-                    int start_mode, uint32_t n_sources, const uint64_t thr[3], int32_t *paths)
+bool ensure_edge_filter(ptw_graph *g)
 {
-    if (!ensure_ext_columns(g))
-        return fail(PTW_ENOMEM, "node2vec needs the extended column copy (16 bytes per CSR entry), "
-                                "which does not fit in device memory");
+    if (g->dg.edge_filter) return true;
     const DeviceGraph &dg = g->dg;
-    N2vArgs a;
-    a.adj = dg.adj;
+    // 16 bits per edge, rounded up to a power of two of 32-byte blocks
+    uint64_t blocks = 1;
+    while (blocks * 16 < dg.m) blocks <<= 1;
+    uint32_t *f = nullptr;
+    if (device_malloc(&f, blocks * 32) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (cudaMemsetAsync(f, 0, blocks * 32, g->stream) != cudaSuccess) {
+        cudaFree(f);
+        return false;
+    }
+    const unsigned grid = (unsigned)std::min<uint64_t>((dg.n + 7) / 8, (uint64_t)g->num_sms * 64);
+    k_build_edge_filter<<<std::max(grid, 1u), 256, 0, g->stream>>>(dg.adj, dg.col, dg.n, blocks, f);
+    if (cudaGetLastError() != cudaSuccess) {
+        cudaFree(f);
+        return false;
+    }
+    g->dg.edge_filter = f;
+    g->dg.filter_blocks = blocks;
+    g->device_bytes += blocks * 32;
+    return true;
+}
+
+namespace {
+
+// Launches k_lane_paths<ILP>, ILP = 1, 2 or 4.
+int launch_lane_paths(ptw_graph *g, N2vArgs &a, int ilp)
+{
+    const void *fn = ilp == 1 ? (const void *)k_lane_paths<1>
+                              : ilp == 4 ? (const void *)k_lane_paths<4> : (const void *)k_lane_paths<2>;
+    int per_sm = 0;
+    PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kN2vWarps * 32, 0));
+    per_sm = std::max(per_sm, 1);
+    const uint64_t per_block = (uint64_t)kN2vWarps * 32 * ilp;  // walker slots per block
+    uint64_t grid = std::min<uint64_t>((uint64_t)g->num_sms * per_sm, (a.n_walk + per_block - 1) / per_block);
+    grid = std::max<uint64_t>(grid, 1);
+    void *args[] = {&a};
+    PTW_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kN2vWarps * 32), args, 0, g->stream));
+    return PTW_OK;
+}
+
+N2vArgs lane_args(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed, int start_mode,
+                  uint32_t n_sources, int32_t *paths)
+{
+    const DeviceGraph &dg = g->dg;
+    N2vArgs a{};
+    a.vtx_ext = dg.vtx_ext;
     a.col_ext = dg.col_ext;
+    a.filter = dg.edge_filter;
+    a.filter_blocks = dg.filter_blocks;
     a.start_map = dg.idx2int;
     a.sources = g->sc.sources;
-    a.int2name = dg.int2name;
     a.paths = paths;
     a.ctrl = g->sc.ctrl;
     a.w_begin = w_begin;
     a.n_walk = w_end - w_begin;
-    a.thr_ret = thr[0];
-    a.thr_nb = thr[1];
-    a.thr_out = thr[2];
     a.n = dg.n;
     a.L = L;
     a.key0 = (uint32_t)seed;
@@ -239,19 +382,36 @@ int launch_node2vec(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, 
     a.n_sources = n_sources;
     a.start_mode = start_mode;
     a.hints = g->tune.cache_hints;
-    const int G = g->tune.paths_ilp == 1 || g->tune.paths_ilp == 4 ? g->tune.paths_ilp : 2;
-    const void *fn = G == 1 ? (const void *)k_node2vec<1> : G == 4 ? (const void *)k_node2vec<4>
-                                                                    : (const void *)k_node2vec<2>;
-    int per_sm = 0;
-    PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kN2vWarps * 32, 0));
-    per_sm = std::max(per_sm, 1);
-    const uint64_t groups = (a.n_walk + 31) / 32;
-    const uint64_t per_block = (uint64_t)kN2vWarps * G;
-    uint64_t grid = std::min<uint64_t>((uint64_t)g->num_sms * per_sm, (groups + per_block - 1) / per_block);
-    grid = std::max<uint64_t>(grid, 1);
-    void *args[] = {&a};
-    PTW_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kN2vWarps * 32), args, 0, g->stream));
-    return PTW_OK;
+    return a;
+}
+
+}  // namespace
+
+int launch_node2vec(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
+                    int start_mode, uint32_t n_sources, const uint64_t thr[3], int32_t *paths)
+{
+    if (!ensure_ext_columns(g) || !ensure_edge_filter(g))
+        return fail(PTW_ENOMEM, "node2vec needs the extended column copy (16 bytes per CSR entry) and "
+                                "the edge filter (2 bytes per CSR entry), which do not fit in device memory");
+    N2vArgs a = lane_args(g, w_begin, w_end, L, seed, start_mode, n_sources, paths);
+    a.thr_ret = thr[0];
+    a.thr_nb = thr[1];
+    a.thr_out = thr[2];
+    a.tag = PTW_TAG_N2V;
+    // One slot per lane: with rejections the slots of a lane wait on each
+    // other's reads (R-MAT scale 24, p = 2, q = 0.5: 24.9 / 22.8 / 12.8 G
+    // moves/s with 1 / 2 / 4 slots).
+    return launch_lane_paths(g, a, 1);
+}
+
+int launch_lane_deepwalk(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
+                         int start_mode, uint32_t n_sources, int32_t *paths)
+{
+    PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 2 * sizeof(unsigned long long), g->stream));
+    N2vArgs a = lane_args(g, w_begin, w_end, L, seed, start_mode, n_sources, paths);
+    a.thr_ret = a.thr_nb = a.thr_out = 1ull << 32;  // every first candidate accepted
+    a.tag = PTW_TAG_WALK;
+    return launch_lane_paths(g, a, g->tune.paths_ilp == 1 || g->tune.paths_ilp == 4 ? g->tune.paths_ilp : 2);
 }
 
 }  // namespace ptw

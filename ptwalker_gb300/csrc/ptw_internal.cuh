@@ -211,6 +211,9 @@ struct DeviceGraph {
     uint4 *col_ext = nullptr;     // [m] {neighbour id, its first column, its degree, its name};
                                   // built on the first walk with tune.ext_columns
     uint4 *vtx_ext = nullptr;     // [n] {id, first column, degree, name}, built with col_ext
+    uint32_t *edge_filter = nullptr; // blocked Bloom filter of the directed edges (u, v): blocks of
+                                     // 8 words; built on the first node2vec walk
+    uint64_t filter_blocks = 0;      // a power of two
 };
 
 // Scratch owned by a graph handle and reused by every call.
@@ -295,6 +298,11 @@ int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uin
 // row probes accumulate in ctrl[1..3].
 int launch_node2vec(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
                     int start_mode, uint32_t n_sources, const uint64_t thr[3], int32_t *paths);
+// DeepWalk paths through the same per-lane loop (node2vec.cu); needs the
+// extended column copy, which the caller has built.  Clears ctrl[0..1]
+// (walker cursor, moves) first.
+int launch_lane_deepwalk(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
+                         int start_mode, uint32_t n_sources, int32_t *paths);
 // Stream-ordered device allocation from a per-device pool that keeps up to
 // a quarter of the device memory cached across synchronisations (the default
 // pool hands memory back at each one), for count tables and the short-lived
@@ -315,6 +323,10 @@ int launch_counts_by_name(ptw_graph *g, uint32_t *d_out);
 int check_tune(const ptw_tune &t);
 // Frees the column copies the graph's tune no longer reads.
 void drop_unused_columns(ptw_graph *g);
+// Builds the edge filter of node2vec's neighbour test on first use; false,
+// without an error, when it does not fit in device memory.
+bool ensure_edge_filter(ptw_graph *g);
+
 // Builds the extended column copy (and the per-vertex records) on first use;
 // false, without an error, when they do not fit in device memory.
 bool ensure_ext_columns(ptw_graph *g);

@@ -21,11 +21,12 @@
 // gather: the walker keeps {off, deg} of its vertex in registers and loads a
 // row record only at its start vertex.
 //
-// K3 k_paths: DeepWalk (src/core/deepwalk.cpp:25-28).  One walker per lane,
-// all walks the same length, so a warp stays converged.  Each warp stages the
-// next 32 path positions of its 32 walkers in shared memory and writes them
-// out row by row, so every store instruction writes 32 consecutive int32 of
-// one path row.
+// K3 k_paths: DeepWalk (src/core/deepwalk.cpp:25-28) on the plain or
+// name-paired columns.  One walker per lane, all walks the same length, so a
+// warp stays converged.  Each warp stages the next 32 path positions of its
+// 32 walkers in shared memory and writes them out row by row, so every store
+// instruction writes 32 consecutive int32 of one path row.  On the extended
+// columns DeepWalk runs in the per-lane loop of node2vec.cu.
 #include <algorithm>
 
 #include "ptw_internal.cuh"
@@ -429,7 +430,6 @@ struct PathArgs {
     const uint2 *__restrict__ adj;
     const uint32_t *__restrict__ col;
     const uint2 *__restrict__ col_named;  // {internal id, name} per column entry
-    const uint4 *__restrict__ col_ext;    // {internal id, first column, degree, name} per entry
     const uint32_t *__restrict__ start_map;
     const uint32_t *__restrict__ sources;
     const uint32_t *__restrict__ int2name;
@@ -448,8 +448,8 @@ constexpr int kPathWarps = 4;  // warps per block
 // lane), stepped together so a lane has G gathers in flight.  MODE 0 reads
 // the row record, the column entry and the neighbour's name (three random
 // reads per move); MODE 1 reads {internal id, name} pairs from col_named (two:
-// row record, pair); MODE 2 reads {id, first column, degree, name} from
-// col_ext and keeps the row record in registers (one).
+// row record, pair).  With the extended columns (one read per move) DeepWalk
+// runs in the per-lane loop of node2vec.cu instead.
 template <int G, int MODE>
 __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
 {
@@ -487,7 +487,6 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
             rows[g] = grp < n_groups ? (uint32_t)umin64(32, a.n_walk - grp * 32) : 0;
             v[g] = valid ? start_vertex(sa, wid[g]) : 0;
             dead[g] = !valid;
-            if (MODE == 2) rec[g] = valid ? ld_hint_u2(&a.adj[v[g]], pol_keep) : make_uint2(0u, 0u);
             stage[wib][g][lane][0] = valid ? (int32_t)a.int2name[v[g]] : -1;
         }
         uint32_t c0 = 0;  // path position of stage column 0
@@ -507,11 +506,9 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
                 c0 = p;
                 if (p == a.L) break;
             }
-            if (MODE != 2) {
 #pragma unroll
-                for (int g = 0; g < G; ++g)
-                    if (!dead[g]) rec[g] = ld_hint_u2(&a.adj[v[g]], pol_keep);
-            }
+            for (int g = 0; g < G; ++g)
+                if (!dead[g]) rec[g] = ld_hint_u2(&a.adj[v[g]], pol_keep);
             uint4 r[G];
 #pragma unroll
             for (int g = 0; g < G; ++g)
@@ -524,11 +521,6 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
                 if (!dead[g]) {
                     if (rec[g].y == 0) {
                         dead[g] = true;
-                    } else if (MODE == 2) {
-                        const uint4 cx = ld_hint_u4(&a.col_ext[rec[g].x + __umulhi(r[g].x, rec[g].y)], pol_stream);
-                        v[g] = cx.x;
-                        rec[g] = make_uint2(cx.y, cx.z);
-                        nm[g] = cx.w;
                     } else if (MODE == 1) {
                         const uint2 cn = ld_hint_u2(&a.col_named[rec[g].x + __umulhi(r[g].x, rec[g].y)], pol_stream);
                         v[g] = cn.x;
@@ -804,7 +796,6 @@ int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uin
     // name-paired columns, built once on the first path walk (8 bytes per
     // CSR entry); without either the kernel looks names up per move.
     const bool ext = (g->tune.ext_columns & 2) && ensure_ext_columns(g);
-    a.col_ext = g->dg.col_ext;
     bool named = !ext && g->tune.paths_named != 0;
     if (named && !g->dg.col_named) {
         uint2 *cn = nullptr;
@@ -820,11 +811,12 @@ int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uin
         }
     }
     a.col_named = g->dg.col_named;
+    // With extended columns the walkers run in the per-lane loop of
+    // node2vec.cu, each slot refilled as its walk ends (no warp lockstep).
+    if (ext) return launch_lane_deepwalk(g, w_begin, w_end, L, seed, start_mode, n_sources, paths);
     const int G = g->tune.paths_ilp == 1 || g->tune.paths_ilp == 4 ? g->tune.paths_ilp : 2;
     const void *fn;
-    if (ext)
-        fn = G == 1 ? (const void *)k_paths<1, 2> : G == 4 ? (const void *)k_paths<4, 2> : (const void *)k_paths<2, 2>;
-    else if (named)
+    if (named)
         fn = G == 1 ? (const void *)k_paths<1, 1> : G == 4 ? (const void *)k_paths<4, 1> : (const void *)k_paths<2, 1>;
     else
         fn = G == 1 ? (const void *)k_paths<1, 0> : G == 4 ? (const void *)k_paths<4, 0> : (const void *)k_paths<2, 0>;

@@ -2,7 +2,7 @@
 
 Paths must equal ora_replay_node2vec bit for bit under the same Philox
 stream, and so must the number of candidate draws, for every (p, q), start
-mode, walker-id offset and number of walker groups per warp; on a small
+mode, walker-id offset and launch tune; on a small
 undirected graph the GPU paths also follow the node2vec transition law that
 the reference's test checks (src/test/debug/test_node2vec.cpp,
 third_party/knightking/test_node2vec.hpp:47-80).
@@ -42,12 +42,13 @@ def test_node2vec_paths_bit_exact(gpu, G16, s16_canon, p, q):
     assert st.moves == int((want[:, 1:] >= 0).sum())
     assert st.trials == trials
     if p == 1.0 and q == 1.0:
-        assert st.trials == st.moves and st.probes == 0
+        assert st.trials == st.moves and st.checks == 0 and st.probes == 0
 
 
 @pytest.mark.parametrize("start,W,L,first", [("uniform", 5000, 33, 0), ("uniform", 777, 17, (1 << 33) + 5),
                                              ("per_vertex", 4097, 7, 123), ("sources", 3001, 25, 0),
-                                             ("per_vertex", 31, 1, 0), ("per_vertex", 100, 2, 0)])
+                                             ("per_vertex", 31, 1, 0), ("per_vertex", 100, 2, 0),
+                                             ("uniform", 400_000, 1, 7), ("uniform", 300_000, 2, 0)])
 def test_node2vec_start_modes_and_offsets(gpu, G16, s16_canon, start, W, L, first):
     sources = [0, 17, 4242] if start == "sources" else None
     got = gpu.node2vec(G16, W, L, 0.5, 2.0, seed=5, start=start, sources=sources, first_walker=first)
@@ -57,7 +58,7 @@ def test_node2vec_start_modes_and_offsets(gpu, G16, s16_canon, start, W, L, firs
 
 
 @pytest.mark.parametrize("paths_ilp,hints", [(1, 0), (2, 1), (4, 0), (4, 1)])
-def test_node2vec_groups_per_warp(gpu, G16, s16_canon, paths_ilp, hints):
+def test_node2vec_any_tune(gpu, G16, s16_canon, paths_ilp, hints):
     saved = G16.tune
     try:
         t = G16.tune
