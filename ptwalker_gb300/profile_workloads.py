@@ -2,6 +2,7 @@
 
     python -m ptwalker_gb300.profile_workloads pagerank --scale 22
     python -m ptwalker_gb300.profile_workloads deepwalk --scale 22 --walk-len 80
+    python -m ptwalker_gb300.profile_workloads node2vec --scale 22 --walk-len 80 --p 2 --q 0.5
     python -m ptwalker_gb300.profile_workloads batch --scale 20 --queries 512
     python -m ptwalker_gb300.profile_workloads exact --scale 18
     python -m ptwalker_gb300.profile_workloads learned --scale 18 --queries 256
@@ -22,12 +23,15 @@ import numpy as np
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("what", choices=["pagerank", "deepwalk", "batch", "exact", "learned", "mlp", "build", "serve"])
+    p.add_argument("what", choices=["pagerank", "deepwalk", "node2vec", "batch", "exact", "learned", "mlp", "build",
+                                    "serve"])
     p.add_argument("--scale", type=int, default=22)
     p.add_argument("--walk-len", type=int, default=80)
     p.add_argument("--queries", type=int, default=512)
     p.add_argument("--reps", type=int, default=3)
     p.add_argument("--sp", type=float, default=0.15)
+    p.add_argument("--p", type=float, default=2.0, help="node2vec return parameter")
+    p.add_argument("--q", type=float, default=0.5, help="node2vec in-out parameter")
     p.add_argument("--n", type=int, default=8_400_000, help="Chung-Lu vertices (serve)")
     p.add_argument("--top-k", type=int, default=1000)
     p.add_argument("--budget-max", type=float, default=1e5, help="batch: budgets log-uniform in [1e3, this]")
@@ -98,6 +102,14 @@ def main(argv=None):
             _, st = ptw.deepwalk(G, G.n, a.walk_len, 2 + k, out=paths, stats=True)
             ms.append(st.kernel_ms)
         out.update(kernel_ms=ms, steps=G.n * (a.walk_len - 1))
+    elif a.what == "node2vec":
+        paths = torch.empty((G.n, a.walk_len), dtype=torch.int32, device="cuda")
+        ptw.node2vec(G, G.n, a.walk_len, a.p, a.q, 1, out=paths)
+        ms = []
+        for k in range(a.reps):
+            _, st = ptw.node2vec(G, G.n, a.walk_len, a.p, a.q, 2 + k, out=paths, stats=True)
+            ms.append(st.kernel_ms)
+        out.update(kernel_ms=ms, moves=st.moves, trials=st.trials, checks=st.checks, probes=st.probes)
     elif a.what == "batch":
         names, row_ptr, col = G.export_csr()
         rng = np.random.default_rng(2)
