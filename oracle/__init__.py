@@ -38,6 +38,8 @@ from .replay import (  # noqa: F401
     replay_paths,
     replay_node2vec,
     n2v_thresholds,
+    n2v_fold,
+    simple_symmetric,
     partitioned_counts,
     sp_threshold,
     TAG_WALK,

@@ -50,8 +50,12 @@ def load_lib():
     lib.ora_replay_node2vec.argtypes = [u64p, u32p, ctypes.c_uint32, ctypes.c_uint64,
                                         ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_int, u32p,
-                                        ctypes.c_uint32, i32p, ctypes.c_int]
+                                        ctypes.c_uint32, ctypes.c_int, i32p, ctypes.c_int]
     lib.ora_replay_node2vec.restype = ctypes.c_uint64
+    lib.ora_n2v_fold.argtypes = [ctypes.c_double, ctypes.c_double, u64p]
+    lib.ora_n2v_fold.restype = ctypes.c_int
+    lib.ora_csr_simple_symmetric.argtypes = [u64p, u32p, ctypes.c_uint32]
+    lib.ora_csr_simple_symmetric.restype = ctypes.c_int
     lib.ora_n2v_thresholds.argtypes = [ctypes.c_double, ctypes.c_double, u64p]
     lib.ora_n2v_thresholds.restype = None
     lib.ora_rmat_clean_csr.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,

@@ -352,7 +352,8 @@ void ora_replay_paths(const uint64_t *row_ptr, const uint32_t *col, uint32_t n,
  * whatever its draw, so a move always ends; callers keep max(w)/min(w) <=
  * 1024, which makes reaching it less likely than 1e-27 per move.
  * Paths are written as in ora_replay_paths; the return value is the number of
- * trials (candidate draws) made.
+ * trials (candidate draws) made.  simple_symmetric (ora_csr_simple_symmetric
+ * of the graph) enables the outlier folding below for a small p.
  */
 #define PTW_TAG_N2V 0x4E320000u /* "N2" + trial pair index */
 #define ORA_N2V_MAX_TRIALS 65536u
@@ -364,6 +365,58 @@ void ora_n2v_thresholds(double p, double q, uint64_t thr[3])
     if (w[2] > m) m = w[2];
     for (int c = 0; c < 3; c++)
         thr[c] = w[c] >= m ? (uint64_t)1 << 32 : (uint64_t)(w[c] / m * 4294967296.0);
+}
+
+/*
+ * Outlier folding (KnightKing, Yang et al., SOSP'19) for a small p: when the
+ * return weight 1/p is the only largest weight, the envelope of the
+ * rejection draw is M' = max(1, 1/q) instead, and the return edge's excess
+ * (1/p - M') sits in an appendix beside the row.  On a graph whose rows hold
+ * no repeated neighbour and whose edges all have their reverse (a simple
+ * symmetric graph), t appears exactly once in the row of v, so the appendix
+ * has width a = (1/p - M') / M' slots.  In fixed point with 2^20 units per
+ * slot (a_fx = floor(a * 2^20)), trial words (cu, au) place the point
+ * pos = floor(cu * (deg * 2^20 + a_fx) / 2^32); pos >= deg * 2^20 returns to
+ * t at once, else the candidate is row[pos >> 20], accepted iff
+ * au < thr'[class], thr' the thresholds against M'.  thr[0..2] are thr',
+ * thr[3] = a_fx; ora_n2v_fold returns 0 (and leaves thr alone) when the
+ * return weight is not the only largest one.
+ */
+int ora_n2v_fold(double p, double q, uint64_t thr[4])
+{
+    double w[3] = {1.0 / p, 1.0, 1.0 / q};
+    double m = w[1] > w[2] ? w[1] : w[2];
+    if (!(w[0] > m)) return 0;
+    thr[0] = (uint64_t)1 << 32;
+    for (int c = 1; c < 3; c++)
+        thr[c] = w[c] >= m ? (uint64_t)1 << 32 : (uint64_t)(w[c] / m * 4294967296.0);
+    thr[3] = (uint64_t)((w[0] - m) / m * 1048576.0);
+    return 1;
+}
+
+/* 1 iff no row holds a repeated neighbour and every edge (u, v) has its
+ * reverse (v, u). */
+int ora_csr_simple_symmetric(const uint64_t *row_ptr, const uint32_t *col, uint32_t n)
+{
+    int ok = 1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4096) reduction(& : ok)
+#endif
+    for (int64_t ui = 0; ui < (int64_t)n; ui++) {
+        uint32_t u = (uint32_t)ui;
+        for (uint64_t e = row_ptr[u]; e < row_ptr[u + 1]; e++) {
+            if (e > row_ptr[u] && col[e] == col[e - 1]) ok = 0;
+            uint32_t v = col[e];
+            uint64_t lo = row_ptr[v], hi = row_ptr[v + 1];
+            while (lo < hi) {
+                uint64_t mid = lo + (hi - lo) / 2;
+                if (col[mid] < u) lo = mid + 1;
+                else hi = mid;
+            }
+            if (!(lo < row_ptr[v + 1] && col[lo] == u)) ok = 0;
+        }
+    }
+    return ok;
 }
 
 static int row_has(const uint64_t *row_ptr, const uint32_t *col, uint32_t t, uint32_t x)
@@ -380,10 +433,11 @@ static int row_has(const uint64_t *row_ptr, const uint32_t *col, uint32_t t, uin
 uint64_t ora_replay_node2vec(const uint64_t *row_ptr, const uint32_t *col, uint32_t n,
                              uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
                              double p, double q, int start_mode, const uint32_t *sources,
-                             uint32_t n_sources, int32_t *paths, int n_threads)
+                             uint32_t n_sources, int simple_symmetric, int32_t *paths, int n_threads)
 {
-    uint64_t thr[3];
+    uint64_t thr[4] = {0, 0, 0, 0};
     ora_n2v_thresholds(p, q, thr);
+    const int fold = simple_symmetric && ora_n2v_fold(p, q, thr);
     uint64_t trials_total = 0;
 #ifdef _OPENMP
     if (n_threads < 1) n_threads = 1;
@@ -407,8 +461,18 @@ uint64_t ora_replay_node2vec(const uint64_t *row_ptr, const uint32_t *col, uint3
                     for (uint32_t k = 0;; k++) {
                         if ((k & 1) == 0) draw(seed, wid, step, PTW_TAG_N2V + (k >> 1), w);
                         uint32_t cu = w[(k & 1) * 2], au = w[(k & 1) * 2 + 1];
-                        x = col[b + mulhi32(cu, (uint32_t)deg)];
                         trials_total++;
+                        if (fold && step > 0) {
+                            uint64_t tf = (deg << 20) + thr[3];
+                            uint64_t pos = (uint64_t)cu * (tf >> 32) + (((uint64_t)cu * (tf & 0xFFFFFFFFu)) >> 32);
+                            if (pos >= (deg << 20)) { /* the appendix: back to t */
+                                x = t;
+                                break;
+                            }
+                            x = col[b + (pos >> 20)];
+                        } else {
+                            x = col[b + mulhi32(cu, (uint32_t)deg)];
+                        }
                         if (step == 0 || k + 1 == ORA_N2V_MAX_TRIALS) break;
                         int c = x == t ? 0 : row_has(row_ptr, col, t, x) ? 1 : 2;
                         if ((uint64_t)au < thr[c]) break;

@@ -88,9 +88,11 @@ def replay_paths(g, w_begin, w_end, L, seed, start_mode=START_PER_VERTEX,
 
 
 def replay_node2vec(g, w_begin, w_end, L, seed, p, q, start_mode=START_PER_VERTEX,
-                    sources=None, threads=1):
+                    sources=None, threads=1, fold=None):
     """Second-order (node2vec) walks, ora_replay_node2vec: ([walkers, L] int32
-    vertex indices, -1 after a dead end; number of candidate draws)."""
+    vertex indices, -1 after a dead end; number of candidate draws).  The
+    outlier folding for a small p applies on simple symmetric graphs;
+    ``fold=False`` turns it off (a test's comparison)."""
     lib = load_lib()
     nw = w_end - w_begin
     paths = np.zeros((nw, L), dtype=np.int32)
@@ -98,8 +100,30 @@ def replay_node2vec(g, w_begin, w_end, L, seed, p, q, start_mode=START_PER_VERTE
     trials = lib.ora_replay_node2vec(
         _p(g.row_ptr, ctypes.c_uint64), _p(g.col, ctypes.c_uint32), g.n,
         w_begin, w_end, L, seed, float(p), float(q), start_mode, _p(src_arr, ctypes.c_uint32), n_src,
-        _p(paths, ctypes.c_int32), threads)
+        int(simple_symmetric(g) if fold is None else fold), _p(paths, ctypes.c_int32), threads)
     return paths, int(trials)
+
+
+def simple_symmetric(g):
+    """True iff no row of g repeats a neighbour and every edge has its
+    reverse (ora_csr_simple_symmetric); cached on g."""
+    cached = getattr(g, "_simple_symmetric", None)
+    if cached is None:
+        lib = load_lib()
+        cached = bool(lib.ora_csr_simple_symmetric(_p(g.row_ptr, ctypes.c_uint64), _p(g.col, ctypes.c_uint32),
+                                                   g.n))
+        g._simple_symmetric = cached
+    return cached
+
+
+def n2v_fold(p, q):
+    """(thresholds against M', a_fx) of the folded draw, or None when the
+    return weight is not the only largest one (ora_n2v_fold)."""
+    lib = load_lib()
+    thr = np.zeros(4, dtype=np.uint64)
+    if not lib.ora_n2v_fold(float(p), float(q), _p(thr, ctypes.c_uint64)):
+        return None
+    return [int(x) for x in thr[:3]], int(thr[3])
 
 
 def n2v_thresholds(p, q):

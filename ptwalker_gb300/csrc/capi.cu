@@ -429,7 +429,8 @@ int n2v_thresholds(double p, double q, uint64_t thr[3])
     return PTW_OK;
 }
 
-int run_node2vec(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, const uint64_t thr[3], int32_t *d_paths)
+int run_node2vec(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, double p, double q, const uint64_t thr[3],
+                 int32_t *d_paths)
 {
     int rc = upload_sources(g, cfg);
     if (rc) return rc;
@@ -442,7 +443,7 @@ int run_node2vec(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, const uint64
     if (cfg->n_walkers && L) {
         const uint64_t w0 = cfg->first_walker;
         rc = launch_node2vec(g, w0, w0 + cfg->n_walkers, L, cfg->seed, cfg->start_mode,
-                             cfg->start_mode == PTW_START_SOURCES ? cfg->n_sources : 0, thr, d_paths);
+                             cfg->start_mode == PTW_START_SOURCES ? cfg->n_sources : 0, p, q, thr, d_paths);
         if (rc) return rc;
     }
     PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
@@ -941,7 +942,7 @@ try {
     if (!d_paths && cfg->n_walkers && L) return fail(PTW_EINVAL, "null paths buffer");
     if (g->dg.id_bound > 0x80000000u) return fail(PTW_EINVAL, "names above 2^31-1 do not fit int32 paths");
     PTW_CUDA(cudaSetDevice(g->device));
-    rc = run_node2vec(g, cfg, L, thr, d_paths);
+    rc = run_node2vec(g, cfg, L, p, q, thr, d_paths);
     if (rc) return rc;
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
     return stats ? node2vec_stats(g, cfg, stats) : PTW_OK;
@@ -965,7 +966,7 @@ try {
     void *stage = nullptr;
     rc = stage_bytes(g, bytes, &stage);
     if (rc) return rc;
-    rc = run_node2vec(g, cfg, L, thr, (int32_t *)stage);
+    rc = run_node2vec(g, cfg, L, p, q, thr, (int32_t *)stage);
     if (rc) return rc;
     if (bytes) PTW_CUDA(cudaMemcpyAsync(h_paths, stage, bytes, cudaMemcpyDeviceToHost, g->stream));
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));

@@ -24,8 +24,21 @@
 // only when the filter does not rule the edge out.  The filter is blocked:
 // one 32-byte block per edge key, one bit in each of its 8 words, so a test
 // is one sector read; at 16 bits per edge about 0.1% of non-edges pass it.
-// All groups of a lane test and search in step, so their reads are in
-// flight together.  Trial 65535 is accepted
+// On a graph whose edges all have their reverse, the search takes the
+// shorter of the two rows (x in t's row, or t in x's row).
+//
+// Outlier folding (KnightKing, Yang et al., SOSP'19) for a small p: when
+// the return weight 1/p is the only largest weight and the graph is simple
+// and symmetric (t then appears exactly once in v's row), the envelope is
+// M' = max(1, 1/q) and the return edge's excess sits in an appendix of
+// a = (1/p - M') / M' slots beside the row.  In fixed point (2^20 units per
+// slot, a_fx = floor(a * 2^20)) the trial's first word places the point
+// pos = floor(cu * (degree * 2^20 + a_fx) / 2^32): pos >= degree * 2^20 goes
+// back to t with no read at all, else the candidate is entry pos >> 20,
+// accepted against thresholds relative to M'.  Without folding, p = 0.25,
+// q = 4 takes 13 candidate draws per move on R-MAT.
+//
+// Trial 65535 is accepted
 // whatever its word, so every move ends; the host keeps max(w) / min(w) <=
 // 1024, which puts that cap below 1e-27 per move.
 //
@@ -93,6 +106,9 @@ struct N2vArgs {
     unsigned long long *__restrict__ ctrl;  // [0] walker cursor, [1] moves, [2] candidate draws, [3] neighbour tests, [4] row probes
     uint64_t w_begin, n_walk;
     uint64_t thr_ret, thr_nb, thr_out;    // acceptance thresholds (2^32 = always)
+    uint64_t fold_fx;                     // appendix width a_fx (folding on when fold != 0)
+    uint32_t fold;
+    uint32_t sym;                         // every edge has its reverse: search the shorter row
     uint32_t tag;                         // draw tag: "N2" + trial pair, or "WALK"
     uint32_t n, L;
     uint32_t key0, key1;
@@ -135,6 +151,8 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
 
     uint64_t wid[ILP], fbits[ILP];
     uint32_t st[ILP], v[ILP], t[ILP], p[ILP], c0[ILP], k[ILP], au[ILP], lo[ILP], hi[ILP], mid[ILP];
+    uint32_t vname[ILP], tname[ILP], skey[ILP], soff[ILP];  // names of v and t; the searched row and key
+    bool appx[ILP];                                         // the draw fell in the appendix (back to t)
     uint2 rec[ILP], trec[ILP];  // {first column, degree} of v and of t
     uint4 r[ILP], cx[ILP];      // draw words; candidate {id, first column, degree, name}
 #pragma unroll
@@ -142,6 +160,8 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
         st[s] = kIdle;
         wid[s] = fbits[s] = 0;
         v[s] = t[s] = p[s] = c0[s] = k[s] = au[s] = lo[s] = hi[s] = mid[s] = 0;
+        vname[s] = tname[s] = skey[s] = soff[s] = 0;
+        appx[s] = false;
         rec[s] = trec[s] = make_uint2(0u, 0u);
         r[s] = cx[s] = make_uint4(0u, 0u, 0u, 0u);
     }
@@ -196,6 +216,7 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
                                     wid[s]);
                 const uint4 vx = ld_hint_u4(&a.vtx_ext[v[s]], pol_keep);  // {id, first column, degree, name}
                 rec[s] = make_uint2(vx.y, vx.z);
+                vname[s] = vx.w;
                 stage[wib][s][lane][0] = (int32_t)vx.w;
                 p[s] = 1;
                 c0[s] = 0;
@@ -228,7 +249,19 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
                                   a.key0, a.key1);
                 const uint32_t cu = (k[s] & 1) ? r[s].z : r[s].x;
                 au[s] = (k[s] & 1) ? r[s].w : r[s].y;
-                x[s] = ld_hint_u4(&a.col_ext[rec[s].x + __umulhi(cu, rec[s].y)], pol_stream);
+                uint32_t idx;
+                appx[s] = false;
+                if (a.fold && p[s] > 1) {
+                    const uint64_t deg_fx = (uint64_t)rec[s].y << 20;
+                    const uint64_t tf = deg_fx + a.fold_fx;
+                    const uint64_t pos = (uint64_t)cu * (tf >> 32) + (((uint64_t)cu * (tf & 0xFFFFFFFFull)) >> 32);
+                    appx[s] = pos >= deg_fx;
+                    idx = (uint32_t)(pos >> 20);
+                } else {
+                    idx = __umulhi(cu, rec[s].y);
+                }
+                if (appx[s]) x[s] = make_uint4(t[s], trec[s].x, trec[s].y, tname[s]);
+                else x[s] = ld_hint_u4(&a.col_ext[rec[s].x + idx], pol_stream);
             } else if (st[s] == kFilter) {
                 const FilterKey fk = filter_key(t[s], cx[s].x, a.filter_blocks);
                 fbits[s] = fk.bits;
@@ -237,7 +270,7 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
                 x2[s] = ld_hint_u4(blk + 1, pol_stream);
             } else if (st[s] == kSearch) {
                 mid[s] = lo[s] + ((hi[s] - lo[s]) >> 1);
-                x[s] = ld_hint_u4(&a.col_ext[(uint64_t)trec[s].x + mid[s]], pol_stream);
+                x[s] = ld_hint_u4(&a.col_ext[(uint64_t)soff[s] + mid[s]], pol_stream);
             }
         }
 
@@ -249,7 +282,7 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
             if (st[s] == kDraw) {
                 cx[s] = x[s];
                 ++trials;
-                if (p[s] == 1 || k[s] + 1 == kN2vMaxTrials) verdict = 1;
+                if (appx[s] || p[s] == 1 || k[s] + 1 == kN2vMaxTrials) verdict = 1;
                 else if (cx[s].x == t[s]) verdict = (uint64_t)au[s] < a.thr_ret;
                 else if ((uint64_t)au[s] < thr_lo) verdict = 1;
                 else if ((uint64_t)au[s] >= thr_hi) verdict = 0;
@@ -263,16 +296,26 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
                 if (!pass) {
                     verdict = (uint64_t)au[s] < a.thr_out;
                 } else {
+                    // search the shorter row: x in t's, or (every edge having
+                    // its reverse) t in x's
                     lo[s] = 0;
-                    hi[s] = trec[s].y;
+                    if (a.sym && cx[s].z < trec[s].y) {
+                        soff[s] = cx[s].y;
+                        hi[s] = cx[s].z;
+                        skey[s] = tname[s];
+                    } else {
+                        soff[s] = trec[s].x;
+                        hi[s] = trec[s].y;
+                        skey[s] = cx[s].w;
+                    }
                     st[s] = kSearch;
                 }
             } else {
                 ++probes;
-                if (x[s].w == cx[s].w) {
+                if (x[s].w == skey[s]) {
                     verdict = (uint64_t)au[s] < a.thr_nb;
                 } else {
-                    if (x[s].w < cx[s].w) lo[s] = mid[s] + 1;
+                    if (x[s].w < skey[s]) lo[s] = mid[s] + 1;
                     else hi[s] = mid[s];
                     if (lo[s] >= hi[s]) verdict = (uint64_t)au[s] < a.thr_out;
                 }
@@ -283,6 +326,8 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
             } else if (verdict == 1) {
                 t[s] = v[s];
                 trec[s] = rec[s];
+                tname[s] = vname[s];
+                vname[s] = cx[s].w;
                 v[s] = cx[s].x;
                 rec[s] = make_uint2(cx[s].y, cx[s].z);
                 stage[wib][s][lane][p[s] - c0[s]] = (int32_t)cx[s].w;
@@ -309,6 +354,33 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
         if (trials) atomicAdd(&a.ctrl[2], trials);
         if (checks) atomicAdd(&a.ctrl[3], checks);
         if (probes) atomicAdd(&a.ctrl[4], probes);
+    }
+}
+
+// One warp per vertex u: sets *bad when u's row repeats a neighbour or an
+// edge (u, v) has no reverse (binary search of v's row for u's name).
+__global__ void k_check_simple_symmetric(const uint2 *__restrict__ adj, const uint4 *__restrict__ col_ext,
+                                         const uint32_t *__restrict__ int2name, uint32_t n,
+                                         unsigned int *__restrict__ bad)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t u = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; u < n; u += warps) {
+        const uint2 r = adj[u];
+        const uint32_t nu = int2name[u];
+        for (uint32_t i = lane; i < r.y; i += 32) {
+            const uint64_t e = (uint64_t)r.x + i;
+            const uint4 c = col_ext[e];
+            bool fail = i > 0 && col_ext[e - 1].x == c.x;
+            uint32_t lo = 0, hi = c.z;
+            while (lo < hi) {
+                const uint32_t mid = lo + ((hi - lo) >> 1);
+                if (col_ext[(uint64_t)c.y + mid].w < nu) lo = mid + 1;
+                else hi = mid;
+            }
+            fail |= !(lo < c.z && col_ext[(uint64_t)c.y + lo].w == nu);
+            if (fail) atomicOr(bad, 1u);
+        }
     }
 }
 
@@ -339,6 +411,23 @@ bool ensure_edge_filter(ptw_graph *g)
     g->dg.edge_filter = f;
     g->dg.filter_blocks = blocks;
     g->device_bytes += blocks * 32;
+    if (g->dg.simple_symmetric < 0 && g->dg.col_ext) {
+        unsigned int *d_bad = nullptr;
+        unsigned int h_bad = 1;
+        if (device_malloc(&d_bad, sizeof(unsigned int)) == cudaSuccess) {
+            if (cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), g->stream) == cudaSuccess) {
+                k_check_simple_symmetric<<<std::max(grid, 1u), 256, 0, g->stream>>>(dg.adj, g->dg.col_ext, dg.int2name,
+                                                                                    dg.n, d_bad);
+                if (cudaGetLastError() == cudaSuccess &&
+                    cudaMemcpyAsync(&h_bad, d_bad, sizeof(h_bad), cudaMemcpyDeviceToHost, g->stream) == cudaSuccess &&
+                    cudaStreamSynchronize(g->stream) == cudaSuccess)
+                    g->dg.simple_symmetric = h_bad ? 0 : 1;
+            }
+            cudaFree(d_bad);
+        }
+        cudaGetLastError();
+        if (g->dg.simple_symmetric < 0) g->dg.simple_symmetric = 0;  // unknown: fold nothing
+    }
     return true;
 }
 
@@ -388,7 +477,7 @@ N2vArgs lane_args(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, ui
 }  // namespace
 
 int launch_node2vec(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
-                    int start_mode, uint32_t n_sources, const uint64_t thr[3], int32_t *paths)
+                    int start_mode, uint32_t n_sources, double p, double q, const uint64_t thr[3], int32_t *paths)
 {
     if (!ensure_ext_columns(g) || !ensure_edge_filter(g))
         return fail(PTW_ENOMEM, "node2vec needs the extended column copy (16 bytes per CSR entry) and "
@@ -397,6 +486,20 @@ int launch_node2vec(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, 
     a.thr_ret = thr[0];
     a.thr_nb = thr[1];
     a.thr_out = thr[2];
+    a.sym = g->dg.simple_symmetric == 1 ? 1u : 0u;
+    if (a.sym) {
+        // outlier folding when 1/p is the only largest weight: envelope
+        // M' = max(1, 1/q), thresholds against M', appendix a_fx
+        const double w[3] = {1.0 / p, 1.0, 1.0 / q};
+        const double m = std::max(w[1], w[2]);
+        if (w[0] > m) {
+            a.fold = 1;
+            a.thr_ret = 1ull << 32;
+            a.thr_nb = w[1] >= m ? 1ull << 32 : (uint64_t)(w[1] / m * 4294967296.0);
+            a.thr_out = w[2] >= m ? 1ull << 32 : (uint64_t)(w[2] / m * 4294967296.0);
+            a.fold_fx = (uint64_t)((w[0] - m) / m * 1048576.0);
+        }
+    }
     a.tag = PTW_TAG_N2V;
     // One slot per lane: with rejections the slots of a lane wait on each
     // other's reads (R-MAT scale 24, p = 2, q = 0.5: 24.9 / 22.8 / 12.8 G

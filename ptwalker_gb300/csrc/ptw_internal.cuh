@@ -214,6 +214,8 @@ struct DeviceGraph {
     uint32_t *edge_filter = nullptr; // blocked Bloom filter of the directed edges (u, v): blocks of
                                      // 8 words; built on the first node2vec walk
     uint64_t filter_blocks = 0;      // a power of two
+    int simple_symmetric = -1;       // 1: no row repeats a neighbour and every edge has its
+                                     // reverse; 0: not; -1: not checked yet (first node2vec walk)
 };
 
 // Scratch owned by a graph handle and reused by every call.
@@ -293,11 +295,13 @@ int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t);
 int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
                  int start_mode, uint32_t n_sources, int32_t *paths);
 // Second-order (node2vec) paths (node2vec.cu): thr = acceptance thresholds
-// {return, neighbour of the previous vertex, other}; needs the extended
-// column copy (PTW_ENOMEM when it does not fit).  Moves, candidate draws and
+// {return, neighbour of the previous vertex, other} for the envelope
+// max(1/p, 1, 1/q) (p and q pick the folded form on simple symmetric
+// graphs); needs the extended column copy (PTW_ENOMEM when it does not fit).  Moves, candidate draws and
 // row probes accumulate in ctrl[1..3].
 int launch_node2vec(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
-                    int start_mode, uint32_t n_sources, const uint64_t thr[3], int32_t *paths);
+                    int start_mode, uint32_t n_sources, double p, double q, const uint64_t thr[3],
+                    int32_t *paths);
 // DeepWalk paths through the same per-lane loop (node2vec.cu); needs the
 // extended column copy, which the caller has built.  Clears ctrl[0..1]
 // (walker cursor, moves) first.
@@ -323,8 +327,9 @@ int launch_counts_by_name(ptw_graph *g, uint32_t *d_out);
 int check_tune(const ptw_tune &t);
 // Frees the column copies the graph's tune no longer reads.
 void drop_unused_columns(ptw_graph *g);
-// Builds the edge filter of node2vec's neighbour test on first use; false,
-// without an error, when it does not fit in device memory.
+// Builds the edge filter of node2vec's neighbour test and checks whether
+// the graph is simple and symmetric, on first use; false, without an error,
+// when the filter does not fit in device memory.  Needs the extended columns.
 bool ensure_edge_filter(ptw_graph *g);
 
 // Builds the extended column copy (and the per-vertex records) on first use;

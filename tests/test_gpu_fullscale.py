@@ -9,7 +9,8 @@ count walk is checked under the launch configurations the bench runs (the
 autotuned one with the 8.3 GB extended column copy, and the plain-column
 alternative), and the DeepWalk samples start at walker ids above 2^23 and
 2^32 so the start map and the column offsets are exercised over the whole
-id and edge range.  Size-independent properties (every position counted
+id and edge range; so do node2vec samples, which also read the edge
+filter.  Size-independent properties (every position counted
 once, walker shards summing to the whole run) are checked as well.
 """
 import os
@@ -154,6 +155,20 @@ def test_s24_deepwalk_sample_bit_exact(gpu, s24, tune):
         got = gpu.deepwalk(G, W, L, 6, "per_vertex", first_walker=w0)
         want = oracle.replay_paths(canon, w0, w0 + W, L, 6, START_PER_VERTEX, threads=NT)
         assert np.array_equal(got, want), w0
+
+
+@pytest.mark.parametrize("p,q", [(2.0, 0.5), (0.5, 2.0)])
+def test_s24_node2vec_sample_bit_exact(gpu, s24, p, q):
+    """Second-order path samples on the 8.3 GB extended columns and the 1 GB
+    edge filter, at walker offsets past 2^23 and 2^33."""
+    G, canon = s24
+    _set_tune(gpu, G, "bench")
+    W, L = 8192, 80
+    for w0 in (0, (1 << 23) + 777, (1 << 33) + 5):
+        got, st = gpu.node2vec(G, W, L, p, q, 8, "per_vertex", first_walker=w0, stats=True)
+        want, trials = oracle.replay_node2vec(canon, w0, w0 + W, L, 8, p, q, START_PER_VERTEX, threads=NT)
+        assert np.array_equal(got, want), w0
+        assert st.trials == trials
 
 
 def test_s24_count_walk_properties(gpu, s24):

@@ -51,8 +51,32 @@ def exact_transitions(g, p, q):
     return out
 
 
+def test_fold_thresholds():
+    two32 = 1 << 32
+    assert oracle.n2v_fold(2.0, 0.5) is None      # return weight not the largest
+    assert oracle.n2v_fold(1.0, 1.0) is None      # not the only largest
+    assert oracle.n2v_fold(0.5, 0.5) is None      # ties with the other weight
+    assert oracle.n2v_fold(0.5, 2.0) == ([two32, two32, 1 << 31], 1 << 20)   # M' = 1, a = 1
+    assert oracle.n2v_fold(0.25, 0.5) == ([two32, 1 << 31, two32], 1 << 20)  # M' = 2, a = 1
+    assert oracle.n2v_fold(0.1, 4.0) == ([two32, two32, 1 << 30], 9 << 20)
+
+
+def test_simple_symmetric_detection():
+    g = undirected_graph(40, 200, seed=1)
+    assert oracle.simple_symmetric(g)
+    src, dst = np.array([0, 1, 1], np.uint32), np.array([1, 0, 2], np.uint32)
+    assert not oracle.simple_symmetric(oracle.canonical_from_edges(src, dst))      # 1 -> 2 has no reverse
+    src, dst = np.array([0, 0, 1], np.uint32), np.array([1, 1, 0], np.uint32)
+    assert not oracle.simple_symmetric(oracle.canonical_from_edges(src, dst))      # repeated neighbour
+    src, dst = np.array([0, 2], np.uint32), np.array([1, 2], np.uint32)
+    # symmetrising doubles the self-loop (2, 2): a repeated neighbour
+    assert not oracle.simple_symmetric(oracle.canonical_from_edges(src, dst, as_undirected=True))
+    src, dst = np.array([0, 1, 2], np.uint32), np.array([1, 0, 2], np.uint32)
+    assert oracle.simple_symmetric(oracle.canonical_from_edges(src, dst))          # one self-loop is its own reverse
+
+
 @pytest.mark.parametrize("e_num", [64, 232, 800])
-@pytest.mark.parametrize("p,q", [(0.5, 2.0), (2.0, 0.5), (10.0, 10.0)])
+@pytest.mark.parametrize("p,q", [(0.5, 2.0), (2.0, 0.5), (10.0, 10.0), (0.25, 4.0), (0.25, 0.5)])
 def test_replay_follows_node2vec_law(e_num, p, q):
     v_num = min(e_num // 2, 100 + e_num // 9)
     g = undirected_graph(v_num, e_num, seed=e_num)
@@ -89,6 +113,22 @@ def test_replay_follows_node2vec_law(e_num, p, q):
                 worst_z = max(worst_z, abs(f - pr) / np.sqrt(pr * (1 - pr) / total))
     assert variance < 1.0  # the reference's check allows 10.0
     assert worst_z < 6.0
+
+
+@pytest.mark.parametrize("p,q", [(0.5, 2.0), (0.25, 4.0)])
+def test_folding_keeps_the_law_with_fewer_draws(p, q):
+    g = undirected_graph(80, 600, seed=7)
+    assert oracle.simple_symmetric(g)
+    W, L = g.m * 20, 40
+    folded, t_fold = oracle.replay_node2vec(g, 0, W, L, 3, p, q, threads=4)
+    plain, t_plain = oracle.replay_node2vec(g, 0, W, L, 3, p, q, threads=4, fold=False)
+    assert t_fold < 0.75 * t_plain
+    # the same law: second-order transition frequencies agree within noise
+    def freq(paths):
+        t, v, x = paths[:, :-2].ravel(), paths[:, 1:-1].ravel(), paths[:, 2:].ravel()
+        back = (x == t).mean()
+        return back
+    assert abs(freq(folded) - freq(plain)) < 0.01
 
 
 def test_p_q_one_accepts_every_first_candidate():
