@@ -168,10 +168,19 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
     uint64_t next = 0, end = 0;  // warp-uniform walker range [next, end) relative to w_begin
     bool exhausted = false;
 
-    // Writes positions [c0, p) of slot s from its stage row.
+    // Writes positions [c0, p) of slot s from its stage row: 16-byte stores
+    // from the first 16-byte boundary of the path row on, single words
+    // around them.
     auto flush = [&](int s) {
         int32_t *dst = a.paths + (wid[s] - a.w_begin) * (uint64_t)a.L;
-        for (uint32_t i = c0[s]; i < p[s]; ++i) dst[i] = stage[wib][s][lane][i - c0[s]];
+        const int32_t *row = stage[wib][s][lane];
+        uint32_t i = c0[s];
+        for (; i < p[s] && (reinterpret_cast<uintptr_t>(dst + i) & 15); ++i) dst[i] = row[i - c0[s]];
+        for (; i + 4 <= p[s]; i += 4) {
+            const uint32_t o = i - c0[s];
+            *reinterpret_cast<int4 *>(dst + i) = make_int4(row[o], row[o + 1], row[o + 2], row[o + 3]);
+        }
+        for (; i < p[s]; ++i) dst[i] = row[i - c0[s]];
         c0[s] = p[s];
     };
     // The walker of slot s stands at a vertex without out-edges: the rest
