@@ -40,6 +40,7 @@ def test_struct_layouts(tmp_path):
                "ptw_walk_stats": _capi.WalkStats, "ptw_tune": _capi.Tune,
                "ptw_query": _capi.Query, "ptw_batch_cfg": _capi.BatchCfg,
                "ptw_serve_cfg": _capi.ServeCfg, "ptw_serve_result": _capi.ServeResult,
+               "ptw_node2vec_stats": _capi.Node2vecStats,
                "ptw_serve_stats": _capi.ServeStats, "ptw_batch_phases": _capi.BatchPhases,
                "ptw_batch_tune": _capi.BatchTune}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ptw.h"', "int main(void){"]
