@@ -23,7 +23,9 @@
 // binary search of t's row for x's name (rows are in ascending name order)
 // only when the filter does not rule the edge out.  The filter is blocked:
 // one 32-byte block per edge key, one bit in each of its 8 words, so a test
-// is one sector read; at 16 bits per edge about 0.1% of non-edges pass it.
+// is one sector read; at 16 bits per edge (15.5 edges per block at R-MAT
+// scale 24) a non-edge passes with probability E[(1 - (31/32)^k)^8] over
+// Poisson block loads k, about 0.1%.
 // On a graph whose edges all have their reverse, the search takes the
 // shorter of the two rows (x in t's row, or t in x's row).
 //
@@ -35,14 +37,14 @@
 // slot, a_fx = floor(a * 2^20)) the trial's first word places the point
 // pos = floor(cu * (degree * 2^20 + a_fx) / 2^32): pos >= degree * 2^20 goes
 // back to t with no read at all, else the candidate is entry pos >> 20,
-// accepted against thresholds relative to M'.  Without folding, p = 0.25,
-// q = 4 takes 13 candidate draws per move on R-MAT.
+// accepted against thresholds relative to M'.  On R-MAT scale 24, p = 0.25,
+// q = 4 takes 13.1 candidate draws per move without folding and 3.3 with it.
 //
-// Trial 65535 is accepted
-// whatever its word, so every move ends; the host keeps max(w) / min(w) <=
-// 1024, which puts that cap below 1e-27 per move.
+// Trial 65535 is accepted whatever its word, so every move ends; the host
+// keeps max(w) / min(w) <= 1024, which puts that cap below 1e-27 per move.
 //
-// Paths are staged in shared memory and written row by row as in k_paths.
+// Each walker's path is staged in a shared-memory row and written out in
+// segments of up to 32 positions.
 #include <algorithm>
 
 #include "ptw_internal.cuh"

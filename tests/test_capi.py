@@ -196,3 +196,16 @@ def test_walks_that_cannot_end_are_rejected_without_gpu():
         assert lib.ptw_serve_open(None, ctypes.byref(sc), None) == _capi.PTW_EINVAL
         assert (b"null" in lib.ptw_last_error()) == ok
     assert lib.ptw_autotune(None, tiny, 0, None) == _capi.PTW_EINVAL
+
+
+def test_cli_node2vec_flags_checked_before_any_gpu_work():
+    """node2vec takes the reference's -p / -q (include/option.hpp:447-469):
+    missing values are usage errors, found before the graph is loaded."""
+    import subprocess
+    from ptwalker_gb300 import _build
+    exe = os.path.join(_build.BIN_DIR, "node2vec")
+    for argv, msg in ((["-f", "text", "-g", "x.txt", "-w", "10", "-l", "5"], "-p and -q"),
+                      (["-f", "text", "-g", "x.txt", "-w", "10", "-p", "2", "-q", "0.5"], "-l is required"),
+                      (["-f", "text", "-g", "x.txt", "-w", "10", "-l", "5", "-p", "0", "-q", "1"], "-p and -q")):
+        r = subprocess.run([exe] + argv, capture_output=True, text=True)
+        assert r.returncode == 1 and msg in r.stderr, r.stderr

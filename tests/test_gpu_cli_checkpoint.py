@@ -44,6 +44,14 @@ def test_cli_apps_match_replay(gpu, tmp_path, s16_edges, s16_canon):
     assert r.returncode == 0, r.stderr
     want = oracle.replay_paths(s16_canon, 0, 1000, 10, 7)
     assert np.array_equal(np.fromfile(paths, dtype=np.int32).reshape(1000, 10), want)
+    r = subprocess.run([bin_path("node2vec"), "-f", "text", "-g", str(g), "-w", "1000", "-l", "12",
+                        "-p", "0.5", "-q", "2", "--seed", "9", "--paths-out", str(paths)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    want, _ = oracle.replay_node2vec(s16_canon, 0, 1000, 12, 9, 0.5, 2.0)
+    assert np.array_equal(np.fromfile(paths, dtype=np.int32).reshape(1000, 12), want)
+    r = subprocess.run([bin_path("node2vec"), "-f", "text", "-g", str(g), "-w", "10", "-l", "5"],
+                       capture_output=True, text=True)
+    assert r.returncode != 0 and "-p and -q" in r.stderr
 
 
 def test_resume_equals_uninterrupted(gpu, G16, tmp_path):
