@@ -37,6 +37,9 @@ def main(argv=None):
     p.add_argument("--budget-max", type=float, default=1e5, help="batch: budgets log-uniform in [1e3, this]")
     p.add_argument("--tune", default=None,
                    help="launch parameters as name=value pairs, e.g. block=1024,ilp=2,hot_k=8192")
+    p.add_argument("--batch-tune", default=None,
+                   help="batch: launch parameters of the batched kernel as name=value pairs, e.g. "
+                        "desc_walkers=256,blocks_per_sm=6,group_bytes=402653184,dense_ratio=2,ext_columns=1")
     a = p.parse_args(argv)
 
     import torch
@@ -86,6 +89,9 @@ def main(argv=None):
     if a.tune:
         G.tune = ptw.Tune(**{k: int(v) for k, v in (kv.split("=") for kv in a.tune.split(","))})
         out["tune"] = G.tune.as_dict()
+    if a.batch_tune:
+        ptw.set_batch_tune(G, ptw.BatchTune(**{k: int(v) for k, v in (kv.split("=") for kv in a.batch_tune.split(","))}))
+        out["batch_tune"] = a.batch_tune
     if a.what == "pagerank":
         dev = torch.empty(G.id_bound, dtype=torch.int32, device="cuda")
         ptw.pagerank(G, G.n, a.sp, 1, out=dev)
