@@ -706,6 +706,22 @@ def run_ours(args):
                     "frac": dbytes / (dms / 1000.0) / 1e9 / peak,
                     "path_bytes": 4 * n * L,
                     "kernel": "k_lane_paths" if tune.ext_columns & 2 else "k_paths"}
+        # paths delivered to page-locked host memory through ptw_deepwalk
+        # (walker chunks whose copies overlap the next chunks' walks); host
+        # wall clock per call
+        try:
+            hpaths = torch.empty((n, L), dtype=torch.int32, pin_memory=True)
+            ptw.deepwalk(G, n, L, 6, out=hpaths)
+            w0 = time.perf_counter()
+            for k in range(reps):
+                ptw.deepwalk(G, n, L, 70 + k, out=hpaths)
+            hs = (time.perf_counter() - w0) / reps
+            deepwalk["e2e_host"] = {"steps_per_s": dsteps / hs, "ms_per_call": 1e3 * hs,
+                                    "d2h_bytes_per_call": 4 * n * L,
+                                    "api": "ptw_deepwalk into page-locked host memory (host wall clock)"}
+            del hpaths
+        except Exception as e:  # a side measurement must not cost the line
+            deepwalk["e2e_host"] = {"error": "%s: %s" % (type(e).__name__, e)}
         # node2vec side line (second-order walks, same walkers and length):
         # algorithmic bytes = 64 B per candidate draw (row record + column
         # sector, as a DeepWalk move) + 32 B per neighbour test (one filter

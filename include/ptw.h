@@ -218,7 +218,9 @@ int ptw_rwr_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_pairs, ptw_wa
 /* DeepWalk (src/core/deepwalk.cpp:25-37): n_walkers walks of L vertices
  * (L-1 moves), written as names into h_paths[n_walkers * L] (row-major,
  * int32).  A walk that reaches a vertex without out-edges is padded with -1.
- * cfg->sp and cfg->max_moves are ignored. */
+ * cfg->sp and cfg->max_moves are ignored.  The host variant walks in chunks
+ * whose copies into h_paths overlap the next chunks' walks (page-locked
+ * h_paths copy fastest). */
 int ptw_deepwalk(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *h_paths,
                  ptw_walk_stats *stats);
 int ptw_deepwalk_dev(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *d_paths,

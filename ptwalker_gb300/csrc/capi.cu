@@ -413,6 +413,59 @@ int run_paths(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *d_path
     return PTW_OK;
 }
 
+// Path walks delivered to host memory: the walkers run in chunks (at most 8,
+// at least 2^20 walkers each) into the device staging, every chunk's paths
+// copied to h_paths on the copy stream while the next chunks walk.  All
+// chunk launches are issued before the copies, so a copy into pageable
+// memory (which holds the calling thread) does not hold back the walks.
+// Draws depend on walker ids only, so the paths equal one launch's.
+// launch_chunk(w_begin, w_end, d_paths) issues one chunk on the graph's
+// stream.  Events: ev0 before the first chunk, ev1 after the last, ev2
+// after the last copy (on the graph's stream).
+template <class F>
+int paths_to_host(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t L, int32_t *h_paths, int32_t *stage,
+                  F launch_chunk)
+{
+    const uint64_t W = cfg->n_walkers, w0 = cfg->first_walker;
+    PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
+    if (W == 0 || L == 0) {
+        PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
+        PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+        return PTW_OK;
+    }
+    if (!g->copy_stream) PTW_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+    const uint64_t per = std::max<uint64_t>(1ull << 20, (W + 7) / 8);
+    const uint64_t nc = (W + per - 1) / per;
+    std::vector<cudaEvent_t> ev(nc, nullptr);
+    struct Events {
+        std::vector<cudaEvent_t> &e;
+        ~Events()
+        {
+            for (cudaEvent_t x : e)
+                if (x) cudaEventDestroy(x);
+        }
+    } guard{ev};
+    for (uint64_t c = 0; c < nc; ++c) {
+        PTW_CUDA(cudaEventCreateWithFlags(&ev[c], cudaEventDisableTiming));
+        const uint64_t off = c * per, n = std::min(per, W - off);
+        const int rc = launch_chunk(w0 + off, w0 + off + n, stage + off * L);
+        if (rc) return rc;
+        PTW_CUDA(cudaEventRecord(ev[c], g->stream));
+    }
+    PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
+    for (uint64_t c = 0; c < nc; ++c) {
+        const uint64_t off = c * per, n = std::min(per, W - off);
+        PTW_CUDA(cudaStreamWaitEvent(g->copy_stream, ev[c], 0));
+        PTW_CUDA(cudaMemcpyAsync(h_paths + off * L, stage + off * L, n * (uint64_t)L * 4, cudaMemcpyDeviceToHost,
+                                 g->copy_stream));
+    }
+    PTW_CUDA(cudaEventRecord(ev[nc - 1], g->copy_stream));
+    PTW_CUDA(cudaStreamWaitEvent(g->stream, ev[nc - 1], 0));
+    PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    PTW_CUDA(cudaStreamSynchronize(g->stream));
+    return PTW_OK;
+}
+
 // Acceptance thresholds of the node2vec rejection draw: class weights
 // {1/p (return), 1 (neighbour of the previous vertex), 1/q (other)} over
 // their maximum M, as 32-bit fractions (2^32 = always accept).
@@ -910,11 +963,15 @@ try {
     void *stage = nullptr;
     rc = stage_bytes(g, bytes, &stage);
     if (rc) return rc;
-    rc = run_paths(g, cfg, L, (int32_t *)stage);
+    rc = upload_sources(g, cfg);
     if (rc) return rc;
-    if (bytes) PTW_CUDA(cudaMemcpyAsync(h_paths, stage, bytes, cudaMemcpyDeviceToHost, g->stream));
-    PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
-    PTW_CUDA(cudaStreamSynchronize(g->stream));
+    PTW_CUDA(cudaEventRecord(g->ev[3], g->stream));
+    PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 2 * sizeof(unsigned long long), g->stream));
+    const uint32_t ns = cfg->start_mode == PTW_START_SOURCES ? cfg->n_sources : 0;
+    rc = paths_to_host(g, cfg, L, h_paths, (int32_t *)stage, [&](uint64_t b, uint64_t e, int32_t *d) {
+        return launch_paths(g, b, e, L, cfg->seed, cfg->start_mode, ns, d);
+    });
+    if (rc) return rc;
     if (stats) {
         stats->walkers = cfg->n_walkers;
         stats->moves = L ? cfg->n_walkers * (uint64_t)(L - 1) : 0;
@@ -966,11 +1023,20 @@ try {
     void *stage = nullptr;
     rc = stage_bytes(g, bytes, &stage);
     if (rc) return rc;
-    rc = run_node2vec(g, cfg, L, p, q, thr, (int32_t *)stage);
+    rc = upload_sources(g, cfg);
     if (rc) return rc;
-    if (bytes) PTW_CUDA(cudaMemcpyAsync(h_paths, stage, bytes, cudaMemcpyDeviceToHost, g->stream));
-    PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
-    PTW_CUDA(cudaStreamSynchronize(g->stream));
+    PTW_CUDA(cudaEventRecord(g->ev[3], g->stream));
+    PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 5 * sizeof(unsigned long long), g->stream));
+    if (cfg->n_walkers && L && !(ensure_ext_columns(g) && ensure_edge_filter(g)))
+        return fail(PTW_ENOMEM, "node2vec needs the extended column copy (16 bytes per CSR entry) and "
+                                "the edge filter (2 bytes per CSR entry), which do not fit in device memory");
+    const uint32_t ns = cfg->start_mode == PTW_START_SOURCES ? cfg->n_sources : 0;
+    rc = paths_to_host(g, cfg, L, h_paths, (int32_t *)stage, [&](uint64_t b, uint64_t e, int32_t *d) -> int {
+        // each chunk draws walker ids from a fresh cursor; the counters add up
+        PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, sizeof(unsigned long long), g->stream));
+        return launch_node2vec(g, b, e, L, cfg->seed, cfg->start_mode, ns, p, q, thr, d);
+    });
+    if (rc) return rc;
     return stats ? node2vec_stats(g, cfg, stats) : PTW_OK;
 } catch (...) {
     return host_exception();

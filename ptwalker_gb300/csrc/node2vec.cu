@@ -319,7 +319,10 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
                         hi[s] = trec[s].y;
                         skey[s] = cx[s].w;
                     }
-                    st[s] = kSearch;
+                    // an empty row holds nothing (both rows hold at least
+                    // the edge through v, so this does not happen)
+                    if (hi[s] == 0) verdict = (uint64_t)au[s] < a.thr_out;
+                    else st[s] = kSearch;
                 }
             } else {
                 ++probes;

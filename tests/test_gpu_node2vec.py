@@ -154,6 +154,16 @@ def test_node2vec_device_output_and_app_mirror(gpu, G16, s16_canon):
     assert np.array_equal(app.paths, want)
 
 
+def test_node2vec_host_delivery_in_chunks(gpu, G16, s16_canon):
+    """More than 2^20 walkers: chunks walked with overlapping copies; paths
+    and the draw count equal one replay of all walkers."""
+    W, L, w0 = 2_300_000, 5, 77
+    got, st = gpu.node2vec(G16, W, L, 0.5, 2.0, seed=12, start="uniform", first_walker=w0, stats=True)
+    want, trials = oracle.replay_node2vec(s16_canon, w0, w0 + W, L, 12, 0.5, 2.0, START_UNIFORM, threads=8)
+    assert np.array_equal(got, want)
+    assert st.trials == trials and st.moves == int((want[:, 1:] >= 0).sum())
+
+
 def test_node2vec_rejects_bad_p_q(gpu, G16):
     from ptwalker_gb300 import _capi as C
 

@@ -136,6 +136,24 @@ def test_deepwalk_paths_bit_exact(gpu, G16, s16_canon, L, W, start):
     assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("ext", [0, 2])
+def test_deepwalk_host_delivery_in_chunks(gpu, G16, s16_canon, ext):
+    """More than 2^20 walkers: the host call walks them in chunks whose
+    copies overlap the next chunks' walks; the paths equal the replay."""
+    saved = G16.tune
+    try:
+        t = G16.tune
+        t.ext_columns = ext
+        G16.tune = t
+        W, L, w0 = 2_500_000, 6, 1_000_003
+        got, st = gpu.deepwalk(G16, W, L, 19, "uniform", first_walker=w0, stats=True)
+        want = oracle.replay_paths(s16_canon, w0, w0 + W, L, 19, START_UNIFORM, threads=8)
+        assert np.array_equal(got, want)
+        assert st.total_ms >= st.kernel_ms > 0
+    finally:
+        G16.tune = saved
+
+
 @pytest.mark.parametrize("paths_ilp,hints,named,ext", [(1, 0, 0, 0), (2, 0, 0, 0), (4, 0, 1, 0), (2, 1, 1, 0),
                                                        (4, 1, 0, 0), (1, 1, 1, 0), (1, 1, 0, 2), (2, 1, 1, 3),
                                                        (4, 0, 0, 2), (2, 0, 1, 1)])
