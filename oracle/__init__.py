@@ -13,11 +13,14 @@ Contents
   * ``graph.py``: canonical graph layout (names, CSR in index space) and the
     R-MAT clean-up pipeline, restating the reference loader's semantics.
   * ``power.py``: FP64 power iteration and the exact expected-visit formulas.
+  * ``mlp.py``: FP64 forward / backward / Adam of the learned-budget MLP.
 
-Parity pins: Philox is checked against the SC'11 known-answer vector and,
-on the GPU, against cuRAND's Philox4_32_10; the walker semantics are checked
-statistically against the reference binary built from its own sources
-(``oracle/ref``) and against the FP64 expectation.
+Parity pins: Philox is checked against the three published SC'11
+known-answer vectors, and the GPU's draws equal this file's bit for bit
+through every replay test; the walker semantics are checked statistically
+against the reference binary built from its own sources (``oracle/ref``) and
+against the FP64 expectation, and the node2vec replay against the transition
+law of the reference's node2vec test.
 """
 from .lib import load_lib, build_lib  # noqa: F401
 from .graph import (  # noqa: F401

@@ -20,6 +20,8 @@
  *    moves, so a path holds L vertices.
  *  - Neighbour choice: src/core/sampler.hpp:214-217 (uniform over the CSR row,
  *    multi-edges counted with multiplicity).
+ *  - Second-order (node2vec) walks: the law of the reference's node2vec test
+ *    (see ora_replay_node2vec below).
  *
  * The reference draws from an unseeded xorshift* (include/random.hpp:144-177),
  * so its trajectories cannot be reproduced.  This oracle and the GPU engine
@@ -33,6 +35,7 @@
  *                  out.x -> neighbour index  = mulhi32(out.x, degree)
  *                  out.y -> stop after move  iff out.y < thr, thr = floor(sp * 2^32)
  *    R-MAT edge e, levels 4j..4j+3 : ctr = (e_lo, e_hi, j, PTW_TAG_RMAT)
+ *    node2vec trials 2k, 2k+1 of move `step` : ctr = (wid_lo, wid_hi, step, PTW_TAG_N2V + k)
  *
  * All graph arguments are in canonical index space: vertex i is the i-th
  * smallest vertex name, and each CSR row lists neighbour indices in ascending
