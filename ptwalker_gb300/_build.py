@@ -46,11 +46,34 @@ def up_to_date():
 def build(force=False, verbose=False, extra_flags=()):
     if not force and up_to_date():
         return SO
-    os.makedirs(os.path.join(OUT, "obj"), exist_ok=True)
+    _compile_and_link(OUT, SO, extra_flags, verbose)
+    build_cli()
+    return SO
+
+
+# The checked build (-DPTW_CHECKED): every kernel index the engine derives
+# from data is checked against its bound; a failure is recorded on the
+# device, the access is redirected in bounds, and the entry point returns
+# PTW_ECUDA naming the failing sites.  Loaded instead of the normal library
+# when PTW_CHECKED=1 is set in the environment.
+CHECKED_OUT = os.path.join(OUT, "checked")
+CHECKED_SO = os.path.join(CHECKED_OUT, "libptw.so")
+
+
+def build_checked(force=False, verbose=False):
+    if (not force and os.path.exists(CHECKED_SO)
+            and all(os.path.getmtime(f) <= os.path.getmtime(CHECKED_SO) for f in _deps())):
+        return CHECKED_SO
+    _compile_and_link(CHECKED_OUT, CHECKED_SO, ["-DPTW_CHECKED"], verbose)
+    return CHECKED_SO
+
+
+def _compile_and_link(out_dir, so, extra_flags, verbose):
+    os.makedirs(os.path.join(out_dir, "obj"), exist_ok=True)
     nvcc = _nvcc()
 
     def compile_one(src):
-        obj = os.path.join(OUT, "obj", src.replace(".cu", ".o"))
+        obj = os.path.join(out_dir, "obj", src.replace(".cu", ".o"))
         cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra_flags, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -61,14 +84,12 @@ def build(force=False, verbose=False, extra_flags=()):
 
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    tmp = SO + ".tmp%d" % os.getpid()
+    tmp = so + ".tmp%d" % os.getpid()
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fPIC"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
-    os.replace(tmp, SO)
-    build_cli()
-    return SO
+    os.replace(tmp, so)
 
 
 CLI_SRC = os.path.join(HERE, "cli", "ptw_cli.cpp")

@@ -213,20 +213,30 @@ PTW_NOALLOC_MAX_VERTICES = 1 << 22
 _lib = None
 
 
+def checked():
+    """True when PTW_CHECKED=1 selects the index-checked build of the library."""
+    return os.environ.get("PTW_CHECKED", "") == "1"
+
+
 def lib_path():
-    return _build.SO
+    return _build.CHECKED_SO if checked() else _build.SO
 
 
 def load(build_if_missing=True):
-    """Loads libptw.so; builds it first when it is missing or stale."""
+    """Loads libptw.so (the index-checked build when PTW_CHECKED=1); builds
+    it first when it is missing or stale."""
     global _lib
     if _lib is not None:
         return _lib
-    if build_if_missing and not _build.up_to_date():
+    if checked():
+        if build_if_missing:
+            _build.build_checked()
+    elif build_if_missing and not _build.up_to_date():
         _build.build()
-    if not os.path.exists(_build.SO):
-        raise ImportError("libptw.so is not built; run ptwalker_gb300._build.build()")
-    lib = ctypes.CDLL(_build.SO)
+    path = lib_path()
+    if not os.path.exists(path):
+        raise ImportError("%s is not built; run ptwalker_gb300._build.build()" % path)
+    lib = ctypes.CDLL(path)
     for name, res, args in SIGNATURES:
         fn = getattr(lib, name)
         fn.restype = res

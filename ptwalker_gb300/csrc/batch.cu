@@ -471,6 +471,11 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     a.q_flag = d_flag;
     a.slots = d_slots;
     a.ctrl = d_ctrl;
+    a.check = g->sc.ctrl + 7;
+    a.n_slots = n_slots;
+    a.m = g->dg.m;
+    a.n = g->dg.n;
+    a.nq = nq;
     a.ndesc = (uint32_t)nd;
     a.thr = thr;
     a.key0 = (uint32_t)cfg->seed;
@@ -535,6 +540,7 @@ int run_wave(ptw_graph *g, const std::vector<WaveQuery> &wq, const ptw_batch_cfg
     PTW_CUDA(cudaMemcpyAsync(h_flag.data(), d_flag, nq * 4ull, cudaMemcpyDeviceToHost, st));
     PTW_CUDA(cudaMemcpyAsync(&h_moves, d_ctrl + 1, 8, cudaMemcpyDeviceToHost, st));
     int rc = compact_tables(g, d_slots, h_tab.data(), h_cap.data(), h_dense.data(), nq, &wr.c);
+    if (!rc) rc = check_word_status(g);
     early.join();
     wr.c.pre_join = nullptr;
     wr.c.pre_names.reset();

@@ -56,10 +56,12 @@ __device__ __forceinline__ void tab_add(unsigned long long *slots, uint32_t mask
 // kDenseMask) one fire-and-forget reduction at v's canonical index idx,
 // else a hash-table insert of v.
 __device__ __forceinline__ void count_add(unsigned long long *tab, uint32_t mask, uint32_t v, uint32_t idx,
-                                          uint32_t inc, uint32_t *flag)
+                                          uint32_t inc, uint32_t *flag, uint32_t n, unsigned long long *check)
 {
-    if (mask == kDenseMask) atomicAdd(reinterpret_cast<uint32_t *>(tab) + idx, inc);
+    if (mask == kDenseMask) atomicAdd(reinterpret_cast<uint32_t *>(tab) + PTW_IDX(idx, n, check, kCheckTable), inc);
     else tab_add(tab, mask, v, inc, flag);
+    (void)n;
+    (void)check;
 }
 
 // Work of one launch: descriptor d runs walker ranks desc[d].y ..
@@ -84,6 +86,10 @@ struct BatchArgs {
     uint32_t *q_flag;
     unsigned long long *slots;
     unsigned long long *ctrl;  // [0] descriptor cursor, [1] moves
+    unsigned long long *check; // index-check word (checked build)
+    uint64_t n_slots;          // slots of all tables (index checks)
+    uint64_t m;                // CSR entries (index checks)
+    uint32_t n, nq;            // vertices, query entries (index checks)
     uint32_t ndesc;
     uint64_t thr;
     uint32_t key0, key1, max_moves;
@@ -99,13 +105,14 @@ constexpr int kBatchIlp = 2;
 // query entry q's table, aggregated over the lanes of the warp that visit
 // the same (query, vertex) now.
 __device__ __forceinline__ void visit_agg(unsigned mask_active, bool on, uint32_t q, uint32_t v, uint32_t idx,
-                                          unsigned long long *tab, uint32_t tmask, uint32_t *flag, uint32_t lane)
+                                          unsigned long long *tab, uint32_t tmask, uint32_t *flag, uint32_t lane,
+                                          const BatchArgs &a)
 {
     const unsigned m = __ballot_sync(mask_active, on);
     if (!on) return;
     const unsigned long long key = ((unsigned long long)q << 32) | v;
     const unsigned grp = __match_any_sync(m, key);
-    if ((grp & ((1u << lane) - 1u)) == 0) count_add(tab, tmask, v, idx, __popc(grp), flag);
+    if ((grp & ((1u << lane) - 1u)) == 0) count_add(tab, tmask, v, idx, __popc(grp), flag, a.n, a.check);
 }
 
 // EXT: moves read the extended column copy and keep the row record of the
@@ -166,18 +173,30 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
                 }
             }
             if (got) {
+                q[k] = (uint32_t)PTW_IDX(q[k], a.nq, a.check, kCheckQuery);
                 qid[k] = a.q_qid[q[k]];
                 v[k] = a.q_src[q[k]];
                 tab[k] = a.slots + a.q_tab[q[k]];
                 mask[k] = a.q_mask[q[k]];
+#ifdef PTW_CHECKED
+                {
+                    const uint64_t tslots = mask[k] == kDenseMask ? ((uint64_t)a.n + 1) / 2 : (uint64_t)mask[k] + 1;
+                    if (a.q_tab[q[k]] + tslots > a.n_slots) {  // table outside the slots: count into slot 0
+                        atomicOr(a.check, 1ull << kCheckTable);
+                        tab[k] = a.slots;
+                        mask[k] = 0;
+                    }
+                }
+#endif
                 step[k] = 0;
                 act[k] = true;
                 have[k] = false;
             }
             if (a.app == PTW_APP_VISITS) {
                 // Start visits: one table update per (warp, query) group.
-                const uint32_t sidx = got && mask[k] == kDenseMask ? __ldg(&a.int2idx[v[k]]) : 0u;
-                visit_agg(kBFull, got, q[k], v[k], sidx, tab[k], mask[k], &a.q_flag[q[k]], lane);
+                const uint32_t sidx =
+                    got && mask[k] == kDenseMask ? __ldg(&a.int2idx[PTW_IDX(v[k], a.n, a.check, kCheckCounter)]) : 0u;
+                visit_agg(kBFull, got, q[k], v[k], sidx, tab[k], mask[k], &a.q_flag[q[k]], lane, a);
             }
         }
         bool any = false;
@@ -187,7 +206,7 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
 
 #pragma unroll
         for (int k = 0; k < kBatchIlp; ++k)
-            if (act[k] && !(EXT && have[k])) rec[k] = __ldg(&a.adj[v[k]]);
+            if (act[k] && !(EXT && have[k])) rec[k] = __ldg(&a.adj[PTW_IDX(v[k], a.n, a.check, kCheckRecord)]);
         uint4 r[kBatchIlp];
 #pragma unroll
         for (int k = 0; k < kBatchIlp; ++k)
@@ -200,12 +219,12 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
             if (act[k] && rec[k].y != 0) {
                 const uint32_t e = rec[k].x + __umulhi(r[k].x, rec[k].y);
                 if (EXT) {
-                    const uint4 x = __ldg(&a.col_ext[e]);
+                    const uint4 x = __ldg(&a.col_ext[PTW_IDX(e, a.m, a.check, kCheckColumn)]);
                     nb[k] = x.x;
                     nrec[k] = make_uint2(x.y, x.z);
                     nidx[k] = x.w;  // the neighbour's name: its canonical index when a.ext_idx
                 } else {
-                    nb[k] = __ldg(&a.col[e]);
+                    nb[k] = __ldg(&a.col[PTW_IDX(e, a.m, a.check, kCheckColumn)]);
                 }
             }
         }
@@ -215,7 +234,7 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
 #pragma unroll
         for (int k = 0; k < kBatchIlp; ++k)
             if (act[k] && rec[k].y != 0 && mask[k] == kDenseMask && !(EXT && a.ext_idx))
-                nidx[k] = __ldg(&a.int2idx[nb[k]]);
+                nidx[k] = __ldg(&a.int2idx[PTW_IDX(nb[k], a.n, a.check, kCheckCounter)]);
 #pragma unroll
         for (int k = 0; k < kBatchIlp; ++k) {
             // every lane runs the aggregation calls (warp-collective)
@@ -230,13 +249,15 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a)
                 ++moves;
             }
             if (a.app == PTW_APP_VISITS)
-                visit_agg(kBFull, moved, q[k], v[k], nidx[k], tab[k], mask[k], &a.q_flag[q[k]], lane);
+                visit_agg(kBFull, moved, q[k], v[k], nidx[k], tab[k], mask[k], &a.q_flag[q[k]], lane, a);
             const bool done = act[k] && (!moved || (uint64_t)r[k].y < a.thr || (a.max_moves && step[k] >= a.max_moves));
             if (a.app == PTW_APP_ENDPOINT) {
                 // a walker stuck at its start (no out-edge) ends where it began
                 const uint32_t eidx =
-                    moved ? nidx[k] : done && mask[k] == kDenseMask ? __ldg(&a.int2idx[v[k]]) : 0u;
-                visit_agg(kBFull, done, q[k], v[k], eidx, tab[k], mask[k], &a.q_flag[q[k]], lane);
+                    moved ? nidx[k]
+                          : done && mask[k] == kDenseMask ? __ldg(&a.int2idx[PTW_IDX(v[k], a.n, a.check, kCheckCounter)])
+                                                          : 0u;
+                visit_agg(kBFull, done, q[k], v[k], eidx, tab[k], mask[k], &a.q_flag[q[k]], lane, a);
             }
             if (done) act[k] = false;
         }

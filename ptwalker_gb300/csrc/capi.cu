@@ -524,6 +524,27 @@ int node2vec_stats(ptw_graph *g, const ptw_walk_cfg *cfg, ptw_node2vec_stats *st
 }  // namespace
 }  // namespace ptw
 
+namespace ptw {
+int check_word_status(ptw_graph *g)
+{
+#ifdef PTW_CHECKED
+    unsigned long long w = 0;
+    PTW_CUDA(cudaMemcpyAsync(&w, g->sc.ctrl + 7, sizeof(w), cudaMemcpyDeviceToHost, g->stream));
+    PTW_CUDA(cudaStreamSynchronize(g->stream));
+    if (w) {
+        PTW_CUDA(cudaMemsetAsync(g->sc.ctrl + 7, 0, sizeof(w), g->stream));
+        PTW_CUDA(cudaStreamSynchronize(g->stream));
+        char msg[96];
+        std::snprintf(msg, sizeof msg, "index check failed: site mask 0x%llx", w);
+        return fail(PTW_ECUDA, msg);
+    }
+#else
+    (void)g;
+#endif
+    return PTW_OK;
+}
+}  // namespace ptw
+
 using namespace ptw;
 
 extern "C" const char *ptw_last_error(void) { return g_last_error.c_str(); }
@@ -790,6 +811,7 @@ try {
     rc = run_count(g, cfg, d_counts);
     if (rc) return rc;
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    if ((rc = check_word_status(g))) return rc;
     return finish_stats(g, stats, cfg->n_walkers, true);
 } catch (...) {
     return host_exception();
@@ -810,6 +832,7 @@ try {
                              cudaMemcpyDeviceToHost, g->stream));
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
     PTW_CUDA(cudaStreamSynchronize(g->stream));
+    if ((rc = check_word_status(g))) return rc;
     return finish_stats(g, stats, cfg->n_walkers, true);
 } catch (...) {
     return host_exception();
@@ -869,6 +892,7 @@ try {
     PTW_CUDA(cudaSetDevice(g->device));
     a->ticket = 0;  // the slot is free again whatever happens below
     PTW_CUDA(cudaEventSynchronize(a->ev_copy));
+    if (const int rc = check_word_status(g)) return rc;
     if (stats) {
         stats->walkers = a->walkers;
         stats->moves = *a->h_moves;
@@ -896,6 +920,7 @@ try {
     rc = run_endpoint(g, cfg, d_pairs);
     if (rc) return rc;
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    if ((rc = check_word_status(g))) return rc;
     return finish_stats(g, stats, cfg->n_walkers, false);
 } catch (...) {
     return host_exception();
@@ -917,6 +942,7 @@ try {
         PTW_CUDA(cudaMemcpyAsync(h_pairs, stage, cfg->n_walkers * 8, cudaMemcpyDeviceToHost, g->stream));
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
     PTW_CUDA(cudaStreamSynchronize(g->stream));
+    if ((rc = check_word_status(g))) return rc;
     return finish_stats(g, stats, cfg->n_walkers, false);
 } catch (...) {
     return host_exception();
@@ -934,6 +960,7 @@ try {
     rc = run_paths(g, cfg, L, d_paths);
     if (rc) return rc;
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    if ((rc = check_word_status(g))) return rc;
     if (stats) {
         PTW_CUDA(cudaStreamSynchronize(g->stream));
         stats->walkers = cfg->n_walkers;
@@ -972,6 +999,7 @@ try {
         return launch_paths(g, b, e, L, cfg->seed, cfg->start_mode, ns, d);
     });
     if (rc) return rc;
+    if ((rc = check_word_status(g))) return rc;
     if (stats) {
         stats->walkers = cfg->n_walkers;
         stats->moves = L ? cfg->n_walkers * (uint64_t)(L - 1) : 0;
@@ -1002,6 +1030,7 @@ try {
     rc = run_node2vec(g, cfg, L, p, q, thr, d_paths);
     if (rc) return rc;
     PTW_CUDA(cudaEventRecord(g->ev[2], g->stream));
+    if ((rc = check_word_status(g))) return rc;
     return stats ? node2vec_stats(g, cfg, stats) : PTW_OK;
 } catch (...) {
     return host_exception();
@@ -1037,6 +1066,7 @@ try {
         return launch_node2vec(g, b, e, L, cfg->seed, cfg->start_mode, ns, p, q, thr, d);
     });
     if (rc) return rc;
+    if ((rc = check_word_status(g))) return rc;
     return stats ? node2vec_stats(g, cfg, stats) : PTW_OK;
 } catch (...) {
     return host_exception();

@@ -599,6 +599,7 @@ int build_graph_from_device_edges(ptw_graph *g, uint32_t *d_src, uint32_t *d_dst
     // Scratch reused by every walk.
     PTW_CUDA(device_malloc(&g->sc.counts, (uint64_t)n * 4));
     PTW_CUDA(device_malloc(&g->sc.ctrl, 8 * sizeof(unsigned long long)));
+    PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 8 * sizeof(unsigned long long), st));  // [7]: index checks
     PTW_CUDA(cudaStreamSynchronize(st));
     dg.max_degree = h_maxdeg;
     g->device_bytes = (uint64_t)n * (8 + 4 * 4 + 4) + mm * 4 + 64;

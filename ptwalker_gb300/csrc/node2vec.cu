@@ -107,6 +107,7 @@ struct N2vArgs {
     int32_t *__restrict__ paths;
     unsigned long long *__restrict__ ctrl;  // [0] walker cursor, [1] moves, [2] candidate draws, [3] neighbour tests, [4] row probes
     uint64_t w_begin, n_walk;
+    uint64_t m;                           // CSR entries (index checks)
     uint64_t thr_ret, thr_nb, thr_out;    // acceptance thresholds (2^32 = always)
     uint64_t fold_fx;                     // appendix width a_fx (folding on when fold != 0)
     uint32_t fold;
@@ -174,7 +175,8 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
     // from the first 16-byte boundary of the path row on, single words
     // around them.
     auto flush = [&](int s) {
-        int32_t *dst = a.paths + (wid[s] - a.w_begin) * (uint64_t)a.L;
+        int32_t *dst = a.paths + PTW_IDX((wid[s] - a.w_begin) * (uint64_t)a.L, a.n_walk * (uint64_t)a.L, &a.ctrl[7],
+                                         kCheckPath);
         const int32_t *row = stage[wib][s][lane];
         uint32_t i = c0[s];
         for (; i < p[s] && (reinterpret_cast<uintptr_t>(dst + i) & 15); ++i) dst[i] = row[i - c0[s]];
@@ -225,7 +227,8 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
                 wid[s] = a.w_begin + my;
                 v[s] = walker_start(a.start_mode, a.start_map, a.sources, a.n, a.n_sources, a.key0, a.key1,
                                     wid[s]);
-                const uint4 vx = ld_hint_u4(&a.vtx_ext[v[s]], pol_keep);  // {id, first column, degree, name}
+                // {id, first column, degree, name}
+                const uint4 vx = ld_hint_u4(&a.vtx_ext[PTW_IDX(v[s], a.n, &a.ctrl[7], kCheckRecord)], pol_keep);
                 rec[s] = make_uint2(vx.y, vx.z);
                 vname[s] = vx.w;
                 stage[wib][s][lane][0] = (int32_t)vx.w;
@@ -272,16 +275,20 @@ __global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
                     idx = __umulhi(cu, rec[s].y);
                 }
                 if (appx[s]) x[s] = make_uint4(t[s], trec[s].x, trec[s].y, tname[s]);
-                else x[s] = ld_hint_u4(&a.col_ext[rec[s].x + idx], pol_stream);
+                else
+                    x[s] = ld_hint_u4(&a.col_ext[PTW_IDX((uint64_t)rec[s].x + idx, a.m, &a.ctrl[7], kCheckColumn)],
+                                      pol_stream);
             } else if (st[s] == kFilter) {
                 const FilterKey fk = filter_key(t[s], cx[s].x, a.filter_blocks);
                 fbits[s] = fk.bits;
-                const uint4 *blk = reinterpret_cast<const uint4 *>(a.filter + fk.block * 8);
+                const uint4 *blk = reinterpret_cast<const uint4 *>(
+                    a.filter + PTW_IDX(fk.block, a.filter_blocks, &a.ctrl[7], kCheckFilter) * 8);
                 x[s] = ld_hint_u4(blk, pol_stream);
                 x2[s] = ld_hint_u4(blk + 1, pol_stream);
             } else if (st[s] == kSearch) {
                 mid[s] = lo[s] + ((hi[s] - lo[s]) >> 1);
-                x[s] = ld_hint_u4(&a.col_ext[(uint64_t)soff[s] + mid[s]], pol_stream);
+                x[s] = ld_hint_u4(&a.col_ext[PTW_IDX((uint64_t)soff[s] + mid[s], a.m, &a.ctrl[7], kCheckColumn)],
+                                  pol_stream);
             }
         }
 
@@ -478,6 +485,7 @@ N2vArgs lane_args(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, ui
     a.ctrl = g->sc.ctrl;
     a.w_begin = w_begin;
     a.n_walk = w_end - w_begin;
+    a.m = dg.m;
     a.n = dg.n;
     a.L = L;
     a.key0 = (uint32_t)seed;

@@ -129,6 +129,34 @@ __device__ __forceinline__ uint32_t walker_start(int start_mode, const uint32_t 
     return sources[__umulhi(r.x, n_sources)];
 }
 
+// Index checks of the checked build (nvcc -DPTW_CHECKED; libptw built by
+// ptwalker_gb300._build.build_checked): an index at or above its bound sets
+// bit `site` of the graph's check word (scratch ctrl[7]) and is replaced by
+// 0, so the access stays in bounds and the entry point reports the failure
+// (check_word_status).  The normal build compiles the index unchanged.
+// Sites: see kCheck* below.
+enum : int {
+    kCheckRecord = 0,   // row record / vertex record of a vertex id (< n)
+    kCheckColumn = 1,   // CSR entry (< m)
+    kCheckCounter = 2,  // per-vertex counter or name (< n)
+    kCheckStart = 3,    // start map / source list entry
+    kCheckTable = 4,    // count-table slot of a batched query
+    kCheckQuery = 5,    // query-table entry or work descriptor
+    kCheckPath = 6,     // path position (< walkers * L)
+    kCheckFilter = 7,   // edge-filter block
+};
+#ifdef PTW_CHECKED
+__device__ __forceinline__ uint64_t checked_index(uint64_t i, uint64_t n, unsigned long long *word, int site)
+{
+    if (i < n) return i;
+    atomicOr(word, 1ull << site);
+    return 0;
+}
+#define PTW_IDX(i, n, word, site) ptw::checked_index((i), (n), (word), (site))
+#else
+#define PTW_IDX(i, n, word, site) (i)
+#endif
+
 // L2 eviction-priority policies (PTX createpolicy) for the gathers:
 // kind 0 = normal, 1 = evict_last (keep: row records, visit counters),
 // 2 = evict_first (stream: the column array).
@@ -327,6 +355,11 @@ int launch_counts_by_name(ptw_graph *g, uint32_t *d_out);
 int check_tune(const ptw_tune &t);
 // Frees the column copies the graph's tune no longer reads.
 void drop_unused_columns(ptw_graph *g);
+// Checked build: waits for the graph's stream and fails with PTW_ECUDA
+// naming the sites whose index checks tripped (clearing the word); the
+// normal build returns PTW_OK at once.
+int check_word_status(ptw_graph *g);
+
 // Builds the edge filter of node2vec's neighbour test and checks whether
 // the graph is simple and symmetric, on first use; false, without an error,
 // when the filter does not fit in device memory.  Needs the extended columns.

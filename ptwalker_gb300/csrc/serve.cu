@@ -352,6 +352,11 @@ try {
         a.q_flag = dv.flag;
         a.slots = s->arena;
         a.ctrl = dv.ctrl;
+        a.check = g->sc.ctrl + 7;
+        a.n_slots = s->buddy.capacity();
+        a.m = g->dg.m;
+        a.n = g->dg.n;
+        a.nq = s->S;
         a.ndesc = 0;
         a.thr = s->thr;
         a.key0 = (uint32_t)cfg->seed;
@@ -493,6 +498,7 @@ try {
         }
         PTW_CUDA(cudaEventRecord(s->ev[1], st));
         PTW_CUDA(cudaStreamSynchronize(st));
+        if (const int rc0 = check_word_status(s->g)) return rc0;
         float dev_ms = 0;
         PTW_CUDA(cudaEventElapsedTime(&dev_ms, s->ev[0], s->ev[1]));
         s->st.device_ms += dev_ms;

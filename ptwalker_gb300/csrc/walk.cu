@@ -52,6 +52,7 @@ struct WalkArgs {
     uint64_t w_begin;
     uint64_t n_walk;
     uint64_t thr;
+    uint64_t m;  // CSR entries (index checks)
     uint32_t n;
     uint32_t key0, key1;
     uint32_t n_sources;
@@ -71,7 +72,7 @@ template <bool HOT>
 __device__ __forceinline__ void count_visit(const WalkArgs &a, uint32_t *s_hot, uint32_t v, uint64_t pol)
 {
     if (HOT && v < a.hot_k) atomicAdd(&s_hot[v], 1u);
-    else red_add_hint(&a.counts[v], 1u, pol);
+    else red_add_hint(&a.counts[PTW_IDX(v, a.n, &a.ctrl[7], kCheckCounter)], 1u, pol);
 }
 
 // Warp-aggregated visit (all 32 lanes call it): lanes with `on` set count
@@ -89,7 +90,8 @@ __device__ __forceinline__ void count_visit_agg(const WalkArgs &a, uint32_t *s_h
         return;
     }
     const unsigned grp = __match_any_sync(m, v);
-    if ((grp & lt_mask) == 0) red_add_hint(&a.counts[v], (uint32_t)__popc(grp), pol);
+    if ((grp & lt_mask) == 0)
+        red_add_hint(&a.counts[PTW_IDX(v, a.n, &a.ctrl[7], kCheckCounter)], (uint32_t)__popc(grp), pol);
 }
 
 template <bool ENDPOINT, int ILP, bool HOT, bool EXT, bool AGG = false>
@@ -166,7 +168,8 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
         // ---- one move for every active slot --------------------------------
 #pragma unroll
         for (int k = 0; k < ILP; ++k)
-            if (act[k] && !(EXT && have[k])) rec[k] = ld_hint_u2(&a.adj[v[k]], pol_keep);
+            if (act[k] && !(EXT && have[k]))
+                rec[k] = ld_hint_u2(&a.adj[PTW_IDX(v[k], a.n, &a.ctrl[7], kCheckRecord)], pol_keep);
         uint4 r[ILP];
 #pragma unroll
         for (int k = 0; k < ILP; ++k)
@@ -180,11 +183,11 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
             if (act[k] && rec[k].y != 0) {
                 const uint32_t e = rec[k].x + __umulhi(r[k].x, rec[k].y);
                 if (EXT) {
-                    const uint4 x = ld_hint_u4(&a.col_ext[e], pol_stream);
+                    const uint4 x = ld_hint_u4(&a.col_ext[PTW_IDX(e, a.m, &a.ctrl[7], kCheckColumn)], pol_stream);
                     nb[k] = x.x;
                     nrec[k] = make_uint2(x.y, x.z);
                 } else {
-                    nb[k] = ld_hint_u32(&a.col[e], pol_stream);
+                    nb[k] = ld_hint_u32(&a.col[PTW_IDX(e, a.m, &a.ctrl[7], kCheckColumn)], pol_stream);
                 }
             }
         }
@@ -378,7 +381,8 @@ __global__ void __launch_bounds__(256) k_walk_async(const WalkArgs a)
             const uint4 r = philox(make_uint4((uint32_t)w, (uint32_t)(w >> 32), st, PTW_TAG_WALK), a.key0, a.key1);
             const bool stop = (uint64_t)r.y < a.thr || (a.max_moves && st + 1 >= a.max_moves);
             flag[i] = kSlotActive | kSlotMoved | (stop ? kSlotStop : 0u);
-            cp_async16(&land[i], &a.col_ext[x.y + __umulhi(r.x, x.z)], pol_stream);
+            cp_async16(&land[i], &a.col_ext[PTW_IDX((uint64_t)x.y + __umulhi(r.x, x.z), a.m, &a.ctrl[7], kCheckColumn)],
+                       pol_stream);
         }
         cp_async_wait_all();
 
@@ -434,7 +438,9 @@ struct PathArgs {
     const uint32_t *__restrict__ sources;
     const uint32_t *__restrict__ int2name;
     int32_t *__restrict__ paths;
+    unsigned long long *check;  // index-check word (checked build)
     uint64_t w_begin, n_walk;
+    uint64_t m;  // CSR entries (index checks)
     uint32_t n, L;
     uint32_t key0, key1;
     uint32_t n_sources;
@@ -508,7 +514,7 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
             }
 #pragma unroll
             for (int g = 0; g < G; ++g)
-                if (!dead[g]) rec[g] = ld_hint_u2(&a.adj[v[g]], pol_keep);
+                if (!dead[g]) rec[g] = ld_hint_u2(&a.adj[PTW_IDX(v[g], a.n, a.check, kCheckRecord)], pol_keep);
             uint4 r[G];
 #pragma unroll
             for (int g = 0; g < G; ++g)
@@ -522,18 +528,26 @@ __global__ void __launch_bounds__(kPathWarps * 32) k_paths(const PathArgs a)
                     if (rec[g].y == 0) {
                         dead[g] = true;
                     } else if (MODE == 1) {
-                        const uint2 cn = ld_hint_u2(&a.col_named[rec[g].x + __umulhi(r[g].x, rec[g].y)], pol_stream);
+                        const uint2 cn = ld_hint_u2(
+                            &a.col_named[PTW_IDX((uint64_t)rec[g].x + __umulhi(r[g].x, rec[g].y), a.m, a.check,
+                                                 kCheckColumn)],
+                            pol_stream);
                         v[g] = cn.x;
                         nm[g] = cn.y;
                     } else {
-                        v[g] = ld_hint_u32(&a.col[rec[g].x + __umulhi(r[g].x, rec[g].y)], pol_stream);
+                        v[g] = ld_hint_u32(&a.col[PTW_IDX((uint64_t)rec[g].x + __umulhi(r[g].x, rec[g].y), a.m, a.check,
+                                                          kCheckColumn)],
+                                           pol_stream);
                     }
                 }
             }
 #pragma unroll
             for (int g = 0; g < G; ++g) {
                 int32_t out = -1;
-                if (!dead[g]) out = MODE != 0 ? (int32_t)nm[g] : (int32_t)ld_hint_u32(&a.int2name[v[g]], pol_keep);
+                if (!dead[g])
+                    out = MODE != 0 ? (int32_t)nm[g]
+                                    : (int32_t)ld_hint_u32(&a.int2name[PTW_IDX(v[g], a.n, a.check, kCheckCounter)],
+                                                           pol_keep);
                 stage[wib][g][lane][p - c0] = out;
             }
         }
@@ -734,6 +748,7 @@ int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t)
     a.w_begin = wl.w_begin;
     a.n_walk = wl.w_end - wl.w_begin;
     a.thr = wl.thr;
+    a.m = dg.m;
     a.n = dg.n;
     a.key0 = (uint32_t)wl.seed;
     a.key1 = (uint32_t)(wl.seed >> 32);
@@ -783,8 +798,10 @@ int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uin
     a.sources = g->sc.sources;
     a.int2name = dg.int2name;
     a.paths = paths;
+    a.check = g->sc.ctrl + 7;
     a.w_begin = w_begin;
     a.n_walk = w_end - w_begin;
+    a.m = dg.m;
     a.n = dg.n;
     a.L = L;
     a.key0 = (uint32_t)seed;
