@@ -364,17 +364,23 @@ int run_count(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_by_name)
 {
     int rc = upload_sources(g, cfg);
     if (rc) return rc;
+    // on extended columns the walk counts by name into d_by_name itself;
+    // otherwise by internal id into the scratch, scattered by name after
+    const bool by_name = cfg->n_walkers && count_walk_by_name(g, g->tune);
     PTW_CUDA(cudaEventRecord(g->ev[3], g->stream));
-    PTW_CUDA(cudaMemsetAsync(g->sc.counts, 0, (uint64_t)g->dg.n * 4, g->stream));
+    if (by_name) PTW_CUDA(cudaMemsetAsync(d_by_name, 0, (uint64_t)g->dg.id_bound * 4, g->stream));
+    else PTW_CUDA(cudaMemsetAsync(g->sc.counts, 0, (uint64_t)g->dg.n * 4, g->stream));
     PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
     if (cfg->n_walkers) {
-        rc = launch_walk(g, make_launch(cfg), g->tune);
+        WalkLaunch wl = make_launch(cfg);
+        if (by_name) wl.by_name = d_by_name;
+        rc = launch_walk(g, wl, g->tune);
         if (rc) return rc;
     } else {
         PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 2 * sizeof(unsigned long long), g->stream));
     }
     PTW_CUDA(cudaEventRecord(g->ev[1], g->stream));
-    return launch_counts_by_name(g, d_by_name);
+    return by_name ? PTW_OK : launch_counts_by_name(g, d_by_name);
 }
 
 int run_endpoint(ptw_graph *g, const ptw_walk_cfg *cfg, uint32_t *d_pairs)
@@ -1096,16 +1102,27 @@ try {
     WalkLaunch wl = make_launch(&cfg);
     // Median time per launch of `reps` timings after one warm-up (the warm-up
     // also builds a column copy the candidate asks for); each timing runs
-    // three launches back to back, as a caller's loop of walks does, so the
-    // launch tails and gaps count the way they do there.  A negative time
+    // three walks back to back, as a caller's loop of walks does, so the
+    // launch tails and gaps count the way they do there.  A walk is timed
+    // with what a call does after it: counts by name straight from the walk
+    // on extended columns, a scatter by name otherwise.  A negative time
     // marks a candidate that does not launch.
+    if (!g->sc.by_name) PTW_CUDA(device_malloc(&g->sc.by_name, std::max<uint64_t>((uint64_t)g->dg.id_bound * 4, 4)));
     auto time_walk = [&](const ptw_tune &t, int reps, float *med) -> int {
         std::vector<float> ms(reps);
+        const bool by_name = count_walk_by_name(g, t);
+        WalkLaunch twl = wl;
+        if (by_name) twl.by_name = g->sc.by_name;
         for (int rep = -1; rep < reps; ++rep) {
             PTW_CUDA(cudaEventRecord(g->ev[0], g->stream));
             for (int l = 0; l < 3; ++l) {
-                PTW_CUDA(cudaMemsetAsync(g->sc.counts, 0, (uint64_t)g->dg.n * 4, g->stream));
-                if (launch_walk(g, wl, t) != PTW_OK) {
+                if (by_name) PTW_CUDA(cudaMemsetAsync(g->sc.by_name, 0, (uint64_t)g->dg.id_bound * 4, g->stream));
+                else PTW_CUDA(cudaMemsetAsync(g->sc.counts, 0, (uint64_t)g->dg.n * 4, g->stream));
+                if (launch_walk(g, twl, t) != PTW_OK) {
+                    *med = -1.f;
+                    return PTW_OK;
+                }
+                if (!by_name && launch_counts_by_name(g, g->sc.by_name) != PTW_OK) {
                     *med = -1.f;
                     return PTW_OK;
                 }

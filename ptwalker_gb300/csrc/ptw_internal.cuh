@@ -318,7 +318,12 @@ struct WalkLaunch {
     uint32_t max_moves = 0;
     bool endpoint = false;     // RWR endpoint app instead of counting
     uint32_t *pairs = nullptr; // endpoint output by walker (names)
+    uint32_t *by_name = nullptr; // count walks: count straight into this by-name array (extended
+                                 // columns; see count_walk_by_name), else into the graph's scratch
 };
+// True when the count walk under tune t reads the extended columns (built
+// here if needed) and can count by name directly.
+bool count_walk_by_name(ptw_graph *g, const ptw_tune &t);
 int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t);
 int launch_paths(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed,
                  int start_mode, uint32_t n_sources, int32_t *paths);

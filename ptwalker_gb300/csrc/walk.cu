@@ -61,6 +61,7 @@ struct WalkArgs {
     uint32_t hot_k;
     int start_mode;
     int hints;  // L2 eviction priorities on (see l2_policy)
+    int by_name;  // EXT count walks: counts[] is indexed by vertex name (the caller's output)
 };
 
 __device__ __forceinline__ uint32_t start_vertex(const WalkArgs &a, uint64_t wid)
@@ -68,10 +69,14 @@ __device__ __forceinline__ uint32_t start_vertex(const WalkArgs &a, uint64_t wid
     return walker_start(a.start_mode, a.start_map, a.sources, a.n, a.n_sources, a.key0, a.key1, wid);
 }
 
+// Counts a visit of internal vertex v (name nm): ids below hot_k in shared
+// memory, the others in counts[] by internal id, or by name when by_name.
 template <bool HOT>
-__device__ __forceinline__ void count_visit(const WalkArgs &a, uint32_t *s_hot, uint32_t v, uint64_t pol)
+__device__ __forceinline__ void count_visit(const WalkArgs &a, uint32_t *s_hot, uint32_t v, uint32_t nm,
+                                            uint64_t pol)
 {
     if (HOT && v < a.hot_k) atomicAdd(&s_hot[v], 1u);
+    else if (a.by_name) red_add_hint(&a.counts[nm], 1u, pol);
     else red_add_hint(&a.counts[PTW_IDX(v, a.n, &a.ctrl[7], kCheckCounter)], 1u, pol);
 }
 
@@ -157,7 +162,7 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
                 step[k] = 0;
                 act[k] = true;
                 have[k] = false;
-                if (!ENDPOINT) count_visit<HOT>(a, s_hot, v[k], pol_keep);
+                if (!ENDPOINT && !(EXT && a.by_name)) count_visit<HOT>(a, s_hot, v[k], 0u, pol_keep);
             }
         }
         bool any = false;
@@ -167,25 +172,36 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
 
         // ---- one move for every active slot --------------------------------
 #pragma unroll
-        for (int k = 0; k < ILP; ++k)
-            if (act[k] && !(EXT && have[k]))
+        for (int k = 0; k < ILP; ++k) {
+            if (!act[k] || (EXT && have[k])) continue;
+            if (EXT && a.by_name) {
+                // a walker's first move: its start record, with the start's name
+                // for its start visit
+                const uint4 vx = ld_hint_u4(&a.vtx_ext[PTW_IDX(v[k], a.n, &a.ctrl[7], kCheckRecord)], pol_keep);
+                rec[k] = make_uint2(vx.y, vx.z);
+                if (!ENDPOINT) count_visit<HOT>(a, s_hot, v[k], vx.w, pol_keep);
+            } else {
                 rec[k] = ld_hint_u2(&a.adj[PTW_IDX(v[k], a.n, &a.ctrl[7], kCheckRecord)], pol_keep);
+            }
+        }
         uint4 r[ILP];
 #pragma unroll
         for (int k = 0; k < ILP; ++k)
             if (act[k])
                 r[k] = philox(make_uint4((uint32_t)wid[k], (uint32_t)(wid[k] >> 32), step[k], PTW_TAG_WALK),
                               a.key0, a.key1);
-        uint32_t nb[ILP];
+        uint32_t nb[ILP], nnm[ILP];
         uint2 nrec[ILP];
 #pragma unroll
         for (int k = 0; k < ILP; ++k) {
+            nnm[k] = 0;
             if (act[k] && rec[k].y != 0) {
                 const uint32_t e = rec[k].x + __umulhi(r[k].x, rec[k].y);
                 if (EXT) {
                     const uint4 x = ld_hint_u4(&a.col_ext[PTW_IDX(e, a.m, &a.ctrl[7], kCheckColumn)], pol_stream);
                     nb[k] = x.x;
                     nrec[k] = make_uint2(x.y, x.z);
+                    nnm[k] = x.w;
                 } else {
                     nb[k] = ld_hint_u32(&a.col[PTW_IDX(e, a.m, &a.ctrl[7], kCheckColumn)], pol_stream);
                 }
@@ -208,7 +224,7 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
                     ++moves;
                     if (!ENDPOINT) {
                         if (AGG) counted = true;
-                        else count_visit<HOT>(a, s_hot, v[k], pol_keep);
+                        else count_visit<HOT>(a, s_hot, v[k], nnm[k], pol_keep);
                     }
                     done = (uint64_t)r[k].y < a.thr || (a.max_moves && step[k] >= a.max_moves);
                 }
@@ -232,7 +248,7 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
     if (HOT) {
         __syncthreads();
         for (uint32_t i = threadIdx.x; i < a.hot_k; i += blockDim.x)
-            if (s_hot[i]) atomicAdd(&a.counts[i], s_hot[i]);
+            if (s_hot[i]) atomicAdd(&a.counts[a.by_name ? a.int2name[i] : i], s_hot[i]);
     }
 }
 
@@ -395,12 +411,12 @@ __global__ void __launch_bounds__(256) k_walk_async(const WalkArgs a)
             const uint4 x = land[i];
             if (f & kSlotStart) {
                 s0n[i] = x.w;
-                if (!ENDPOINT) count_visit<HOT>(a, s_hot, x.x, pol_keep);
+                if (!ENDPOINT) count_visit<HOT>(a, s_hot, x.x, 0u, pol_keep);
                 flag[i] = kSlotActive;
             } else if (f & kSlotMoved) {
                 step[i] += 1;
                 ++moves;
-                if (!ENDPOINT) count_visit<HOT>(a, s_hot, x.x, pol_keep);
+                if (!ENDPOINT) count_visit<HOT>(a, s_hot, x.x, 0u, pol_keep);
                 if (f & kSlotStop) {
                     if (ENDPOINT) {
                         const uint64_t j = wid[i] - a.w_begin;
@@ -651,6 +667,11 @@ void *pick_walk(bool endpoint, int ilp, bool hot, int min_blocks, int block, boo
 
 // Builds the extended column copy on first use; false (and no error) when
 // it does not fit in device memory, so the caller walks without it.
+bool count_walk_by_name(ptw_graph *g, const ptw_tune &t)
+{
+    return !t.gather_slots && !t.warp_agg && (t.ext_columns & 1) && ensure_ext_columns(g);
+}
+
 bool ensure_ext_columns(ptw_graph *g)
 {
     if (g->dg.col_ext) return true;
@@ -764,6 +785,14 @@ int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t)
     const bool ext = !slots && (t.ext_columns & 1) && ensure_ext_columns(g);
     a.col_ext = g->dg.col_ext;
     a.vtx_ext = g->dg.vtx_ext;
+    // extended columns carry each neighbour's name: count straight into the
+    // caller's by-name array (no scatter after the walk)
+    a.by_name = 0;
+    if (wl.by_name) {
+        if (!(ext && !t.warp_agg && !wl.endpoint)) return fail(PTW_EINVAL, "counting by name needs the plain walk on extended columns");
+        a.by_name = 1;
+        a.counts = wl.by_name;
+    }
     void *fn = slots ? pick_walk_async(wl.endpoint, hot, t.gather_slots)
                : (t.warp_agg && !wl.endpoint) ? pick_walk_agg(t.ilp, hot, ext)
                                               : pick_walk(wl.endpoint, t.ilp, hot, t.min_blocks, t.block, ext);
