@@ -172,6 +172,36 @@ class BudgetModel:
         b = np.where(np.isfinite(b), np.clip(b, b_min, b_max), fallback)
         return b.astype(np.int64)
 
+    # Model file read by the command-line apps (ppr --budget learned --model FILE):
+    #   magic "PTWBUD1\0", f64 kappa, u64 b_min, b_max, fallback,
+    #   f32 params[4801] (ptw_mlp_get_params order), f32 norm[18].
+    MAGIC = b"PTWBUD1\0"
+
+    def save(self, path, b_min=1000, b_max=1_000_000, fallback=1_000_000):
+        params, norm = self.mlp.params()
+        with open(path, "wb") as f:
+            f.write(self.MAGIC)
+            f.write(np.array([self.kappa], np.float64).tobytes())
+            f.write(np.array([b_min, b_max, fallback], np.uint64).tobytes())
+            f.write(np.ascontiguousarray(params, np.float32).tobytes())
+            f.write(np.ascontiguousarray(norm, np.float32).tobytes())
+
+    @classmethod
+    def load(cls, path):
+        """(model, (b_min, b_max, fallback)) from a file written by save()."""
+        with open(path, "rb") as f:
+            raw = f.read()
+        if raw[:8] != cls.MAGIC:
+            raise ValueError("%s is not a budget model" % path)
+        kappa = float(np.frombuffer(raw, np.float64, 1, 8)[0])
+        lim = np.frombuffer(raw, np.uint64, 3, 16)
+        params = np.frombuffer(raw, np.float32, C.PTW_MLP_NPARAMS, 40).copy()
+        norm = np.frombuffer(raw, np.float32, C.PTW_MLP_NNORM, 40 + 4 * C.PTW_MLP_NPARAMS).copy()
+        m = cls()
+        m.mlp.set_params(params, norm)
+        m.kappa = kappa
+        return m, tuple(int(x) for x in lim)
+
 
 def plain_budgets(n, fixed=1_000_000):
     """The fallback / baseline: the same budget for every query."""

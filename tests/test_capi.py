@@ -209,3 +209,21 @@ def test_cli_node2vec_flags_checked_before_any_gpu_work():
                       (["-f", "text", "-g", "x.txt", "-w", "10", "-l", "5", "-p", "0", "-q", "1"], "-p and -q")):
         r = subprocess.run([exe] + argv, capture_output=True, text=True)
         assert r.returncode == 1 and msg in r.stderr, r.stderr
+
+
+def test_cli_batch_flags_checked_before_any_gpu_work(tmp_path):
+    """ppr --sources / --budget / --model / --tune usage errors are found
+    before the graph is loaded."""
+    import subprocess
+    from ptwalker_gb300 import _build
+    exe = os.path.join(_build.BIN_DIR, "ppr")
+    base = ["-f", "text", "-g", "x.txt", "-w", "10", "--sp", "0.2"]
+    for argv, msg in ((base, "--source or --sources"),
+                      (base + ["--sources", "1,2", "--budget", "magic"], "--budget must be"),
+                      (base + ["--sources", "1,2", "--budget", "learned"], "--model"),
+                      (base + ["--sources", ",,"], "no valid vertex names")):
+        r = subprocess.run([exe] + argv, capture_output=True, text=True)
+        assert r.returncode == 1 and msg in r.stderr, r.stderr
+    r = subprocess.run([os.path.join(_build.BIN_DIR, "pagerank"), "-f", "text", "-g", "x.txt", "-w", "10",
+                        "--sp", "0.2", "--sources", "1"], capture_output=True, text=True)
+    assert r.returncode == 1 and "--sources is for ppr" in r.stderr

@@ -54,6 +54,67 @@ def test_cli_apps_match_replay(gpu, tmp_path, s16_edges, s16_canon):
     assert r.returncode != 0 and "-p and -q" in r.stderr
 
 
+def _read_batch_out(path):
+    raw = np.fromfile(path, dtype=np.uint8)
+    nq = int(raw[:8].view(np.uint64)[0])
+    off = raw[8:8 + 8 * (nq + 1)].view(np.uint64)
+    ne = int(off[-1])
+    rest = raw[8 + 8 * (nq + 1):]
+    return off, rest[:4 * ne].view(np.uint32), rest[4 * ne:8 * ne].view(np.uint32)
+
+
+def test_cli_ppr_sources_fixed_and_learned_budgets(gpu, tmp_path, s16_edges):
+    """ppr --sources runs one batched launch; its lists equal ppr_batch's
+    with the same budgets (fixed -w, or learned from a saved model), and
+    --tune changes no result."""
+    from ptwalker_gb300 import learned
+    g = tmp_path / "g.txt"
+    oracle.write_text_edges(str(g), *s16_edges)
+    G = gpu.Graph.load(str(g), "text")
+    try:
+        rng = np.random.default_rng(5)
+        src = rng.integers(0, G.n, 40).astype(np.uint32)
+        srcf = tmp_path / "src.txt"
+        srcf.write_text("\n".join(str(int(x)) for x in src) + "\n")
+        out, bout = tmp_path / "b.bin", tmp_path / "budgets.u64"
+        r = subprocess.run([bin_path("ppr"), "-f", "text", "-g", str(g), "-w", "3000", "--sp", "0.2", "--seed", "4",
+                            "--sources", str(srcf), "--tune", "512,4,64,8192", "--out", str(out),
+                            "--budgets-out", str(bout)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        off, names, counts = _read_batch_out(out)
+        assert np.array_equal(np.fromfile(bout, dtype=np.uint64), np.full(40, 3000, np.uint64))
+        want = gpu.ppr_batch(G, src, 3000, sp=0.2, seed=4)
+        for i in range(40):
+            wn, wc = want.query(i)
+            assert np.array_equal(names[off[i]:off[i + 1]], wn) and np.array_equal(counts[off[i]:off[i + 1]], wc)
+        want.close()
+        assert r.stdout.startswith("ppr queries 40 entries %d" % int(off[-1]))
+        # learned budgets from a saved model (trained briefly on made-up labels)
+        feats = learned.source_features(G, src)
+        m = learned.BudgetModel(seed=3)
+        m.fit(G, src, np.log(2000 + 50 * feats[:, 0]), epochs=30)
+        model = tmp_path / "model.bin"
+        m.save(str(model), b_min=500, b_max=20000, fallback=7000)
+        m2, lim = learned.BudgetModel.load(str(model))
+        assert lim == (500, 20000, 7000) and m2.kappa == m.kappa
+        r = subprocess.run([bin_path("ppr"), "-f", "text", "-g", str(g), "-w", "1", "--sp", "0.2", "--seed", "6",
+                            "--sources", ",".join(str(int(x)) for x in src), "--budget", "learned",
+                            "--model", str(model), "--tune", "auto", "--out", str(out), "--budgets-out", str(bout)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        used = np.fromfile(bout, dtype=np.uint64).astype(np.int64)
+        expect = m2.budgets(G, src, b_min=500, b_max=20000, fallback=7000)
+        assert np.all(np.abs(used - expect) <= 1) and len(set(used.tolist())) > 1
+        off, names, counts = _read_batch_out(out)
+        want = gpu.ppr_batch(G, src, used, sp=0.2, seed=6)
+        for i in range(40):
+            wn, wc = want.query(i)
+            assert np.array_equal(names[off[i]:off[i + 1]], wn) and np.array_equal(counts[off[i]:off[i + 1]], wc)
+        want.close()
+    finally:
+        G.close()
+
+
 def test_resume_equals_uninterrupted(gpu, G16, tmp_path):
     from ptwalker_gb300.checkpoint import resumable_pagerank
     W = 5 * G16.n + 3
