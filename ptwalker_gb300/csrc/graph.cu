@@ -602,6 +602,9 @@ int build_graph_from_device_edges(ptw_graph *g, uint32_t *d_src, uint32_t *d_dst
     PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 8 * sizeof(unsigned long long), st));  // [7]: index checks
     PTW_CUDA(cudaStreamSynchronize(st));
     dg.max_degree = h_maxdeg;
+    // symmetrised, self-loops dropped and duplicates removed: simple and
+    // symmetric by construction (node2vec then skips its check)
+    dg.simple_symmetric = as_undirected && clean ? 1 : -1;
     g->device_bytes = (uint64_t)n * (8 + 4 * 4 + 4) + mm * 4 + 64;
     return PTW_OK;
 }
