@@ -1,6 +1,7 @@
 """Multi-process walker sharding on CPU (gloo, world size 2): the per-rank
 shards of the global walker stream, summed by one all-reduce, equal the
-single-process run bit for bit; query shards cover every query once; a
+single-process run bit for bit, and so do node2vec path shards gathered in
+rank order; query shards cover every query once; a
 rank that fails before the exchange is detected by the other rank through a
 short collective timeout, on the host."""
 import os
@@ -32,6 +33,16 @@ def _worker(rank, world, port, mode, out_dir):
     dist.init_process_group("gloo", rank=rank, world_size=world, timeout=timeout)
     try:
         canon = oracle.canonical_from_edges(*oracle.rmat_clean_edges(11, 8, seed=4))
+        if mode == "paths":
+            # second-order walks: each rank walks its range of the global
+            # walker ids; the shards, gathered in rank order, are the whole run
+            first, count = shard.strong_range(rank, world, canon.n + 3)
+            paths, _ = oracle.replay_node2vec(canon, first, first + count, 9, 13, 0.5, 2.0)
+            parts = [None] * world
+            dist.all_gather_object(parts, paths)
+            if rank == 0:
+                np.save(os.path.join(out_dir, "paths.npy"), np.concatenate(parts))
+            return
         if mode == "weak":
             first, count = shard.weak_range(rank, world, canon.n)
         else:
@@ -76,6 +87,14 @@ def test_sharded_counts_equal_single_process(mode):
     total = 2 * canon.n if mode == "weak" else 3 * canon.n + 5
     want, _ = oracle.replay_counts(canon, 0, total, 0.15, 77, 0)
     assert np.array_equal(files["sum.npy"], want.astype(np.int64))
+
+
+def test_sharded_node2vec_paths_equal_single_process():
+    files, codes = _run("paths")
+    assert codes == [0, 0]
+    canon = oracle.canonical_from_edges(*oracle.rmat_clean_edges(11, 8, seed=4))
+    want, _ = oracle.replay_node2vec(canon, 0, canon.n + 3, 9, 13, 0.5, 2.0)
+    assert np.array_equal(files["paths.npy"], want)
 
 
 def test_failed_rank_is_detected_by_the_survivor():
