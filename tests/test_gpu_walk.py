@@ -126,6 +126,29 @@ def test_rwr_pairs_bit_exact(gpu, G16, s16_canon, start, W, qid):
     assert st.moves == int(moves.sum())
 
 
+@pytest.mark.parametrize("W_mult,extra,start,sp,seed,max_moves,first", [
+    (1, 0, "per_vertex", 0.15, 1, 0, 0),
+    (3, 17, "per_vertex", 0.15, 2, 0, 12345),
+    (0, 4099, "uniform", 0.2, 0xDEADBEEFCAFEF00D, 0, 1 << 33),
+    (1, 0, "per_vertex", 1.0, 4, 0, 0),
+    (1, 0, "per_vertex", 0.001, 5, 7, 0),
+    (0, 20000, "sources", 0.15, 6, 0, 0),
+])
+def test_counts_by_name_on_extended_columns(gpu, G16, s16_canon, W_mult, extra, start, sp, seed, max_moves, first):
+    """The count walk on extended columns counts straight into the output
+    by name; every start mode, offset and termination equals the replay."""
+    saved = G16.tune
+    try:
+        G16.tune = gpu.Tune(block=768, ilp=2, chunk=64, hot_k=8192, cache_hints=1, ext_columns=3)
+        W = W_mult * G16.n + extra
+        sources = [5, 900, 4242] if start == "sources" else None
+        got, st = gpu.pagerank(G16, W, sp, seed, start, sources, max_moves, first_walker=first, stats=True)
+    finally:
+        G16.tune = saved
+    want, moves = oracle.replay_counts(s16_canon, first, first + W, sp, seed, MODES[start], sources, max_moves)
+    assert np.array_equal(got, want) and st.moves == moves
+
+
 @pytest.mark.parametrize("L,W,start", [(80, None, "per_vertex"), (1, 100, "per_vertex"),
                                        (33, 1000, "uniform"), (64, 4097, "per_vertex"),
                                        (5, 31, "uniform")])
@@ -203,7 +226,8 @@ def test_deepwalk_sources(gpu, G16, s16_canon):
 
 
 @pytest.mark.parametrize("tune", [None, dict(block=256, ilp=2, chunk=64, hot_k=64, gather_slots=16),
-                                  dict(block=128, ilp=2, chunk=5, hot_k=0, gather_slots=8, ext_columns=3)])
+                                  dict(block=128, ilp=2, chunk=5, hot_k=0, gather_slots=8, ext_columns=3),
+                                  dict(block=128, ilp=2, chunk=5, hot_k=64, ext_columns=3)])
 def test_dead_ends_and_sparse_names(gpu, tune):
     rng = np.random.default_rng(1)
     names = np.sort(rng.choice(1 << 20, size=500, replace=False)).astype(np.uint32)
