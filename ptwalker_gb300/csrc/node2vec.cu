@@ -53,7 +53,7 @@ namespace ptw {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kN2vWarps = 4;                // warps per block
+constexpr int kLaneWarps = 4;                // warps per block
 constexpr uint32_t kN2vMaxTrials = 65536u;  // trials per move before the last is taken
 
 // MurmurHash3 64-bit finaliser (Appleby, public domain).
@@ -97,7 +97,8 @@ __global__ void k_build_edge_filter(const uint2 *__restrict__ adj, const uint32_
     }
 }
 
-struct N2vArgs {
+// Arguments of k_lane_paths (DeepWalk and node2vec).
+struct LaneArgs {
     const uint4 *__restrict__ vtx_ext;    // {id, first column, degree, name} per vertex
     const uint4 *__restrict__ col_ext;    // {id, first column, degree, name} per CSR entry
     const uint32_t *__restrict__ filter;  // edge filter, filter_blocks blocks of 8 words
@@ -138,10 +139,10 @@ enum : uint32_t { kIdle = 0, kDraw = 1, kFilter = 2, kSearch = 3 };
 // Philox(ctr = (wid_lo, wid_hi, s, "WALK")), the draw of the other walk
 // kernels.
 template <int ILP>
-__global__ void __launch_bounds__(kN2vWarps * 32) k_lane_paths(const N2vArgs a)
+__global__ void __launch_bounds__(kLaneWarps * 32) k_lane_paths(const LaneArgs a)
 {
     constexpr uint32_t C = 32;
-    __shared__ int32_t stage[kN2vWarps][ILP][32][C + 1];
+    __shared__ int32_t stage[kLaneWarps][ILP][32][C + 1];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t wib = threadIdx.x >> 5;
     const uint32_t lt_mask = (1u << lane) - 1u;
@@ -455,26 +456,26 @@ bool ensure_edge_filter(ptw_graph *g)
 namespace {
 
 // Launches k_lane_paths<ILP>, ILP = 1, 2 or 4.
-int launch_lane_paths(ptw_graph *g, N2vArgs &a, int ilp)
+int launch_lane_paths(ptw_graph *g, LaneArgs &a, int ilp)
 {
     const void *fn = ilp == 1 ? (const void *)k_lane_paths<1>
                               : ilp == 4 ? (const void *)k_lane_paths<4> : (const void *)k_lane_paths<2>;
     int per_sm = 0;
-    PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kN2vWarps * 32, 0));
+    PTW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kLaneWarps * 32, 0));
     per_sm = std::max(per_sm, 1);
-    const uint64_t per_block = (uint64_t)kN2vWarps * 32 * ilp;  // walker slots per block
+    const uint64_t per_block = (uint64_t)kLaneWarps * 32 * ilp;  // walker slots per block
     uint64_t grid = std::min<uint64_t>((uint64_t)g->num_sms * per_sm, (a.n_walk + per_block - 1) / per_block);
     grid = std::max<uint64_t>(grid, 1);
     void *args[] = {&a};
-    PTW_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kN2vWarps * 32), args, 0, g->stream));
+    PTW_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kLaneWarps * 32), args, 0, g->stream));
     return PTW_OK;
 }
 
-N2vArgs lane_args(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed, int start_mode,
+LaneArgs lane_args(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, uint64_t seed, int start_mode,
                   uint32_t n_sources, int32_t *paths)
 {
     const DeviceGraph &dg = g->dg;
-    N2vArgs a{};
+    LaneArgs a{};
     a.vtx_ext = dg.vtx_ext;
     a.col_ext = dg.col_ext;
     a.filter = dg.edge_filter;
@@ -504,7 +505,7 @@ int launch_node2vec(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, 
     if (!ensure_ext_columns(g) || !ensure_edge_filter(g))
         return fail(PTW_ENOMEM, "node2vec needs the extended column copy (16 bytes per CSR entry) and "
                                 "the edge filter (2 bytes per CSR entry), which do not fit in device memory");
-    N2vArgs a = lane_args(g, w_begin, w_end, L, seed, start_mode, n_sources, paths);
+    LaneArgs a = lane_args(g, w_begin, w_end, L, seed, start_mode, n_sources, paths);
     a.thr_ret = thr[0];
     a.thr_nb = thr[1];
     a.thr_out = thr[2];
@@ -533,7 +534,7 @@ int launch_lane_deepwalk(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_
                          int start_mode, uint32_t n_sources, int32_t *paths)
 {
     PTW_CUDA(cudaMemsetAsync(g->sc.ctrl, 0, 2 * sizeof(unsigned long long), g->stream));
-    N2vArgs a = lane_args(g, w_begin, w_end, L, seed, start_mode, n_sources, paths);
+    LaneArgs a = lane_args(g, w_begin, w_end, L, seed, start_mode, n_sources, paths);
     a.thr_ret = a.thr_nb = a.thr_out = 1ull << 32;  // every first candidate accepted
     a.tag = PTW_TAG_WALK;
     return launch_lane_paths(g, a, g->tune.paths_ilp == 1 || g->tune.paths_ilp == 4 ? g->tune.paths_ilp : 2);
