@@ -99,11 +99,11 @@ __global__ void k_build_edge_filter(const uint2 *__restrict__ adj, const uint32_
 
 // Arguments of k_lane_paths (DeepWalk and node2vec).
 struct LaneArgs {
-    const uint4 *__restrict__ vtx_ext;    // {id, first column, degree, name} per vertex
+    const uint4 *__restrict__ vtx_ext;    // {id, first column, degree, name} by canonical index
     const uint4 *__restrict__ col_ext;    // {id, first column, degree, name} per CSR entry
     const uint32_t *__restrict__ filter;  // edge filter, filter_blocks blocks of 8 words
     uint64_t filter_blocks;
-    const uint32_t *__restrict__ start_map;
+    const uint32_t *__restrict__ int2idx;  // internal -> canonical index
     const uint32_t *__restrict__ sources;
     int32_t *__restrict__ paths;
     unsigned long long *__restrict__ ctrl;  // [0] walker cursor, [1] moves, [2] candidate draws, [3] neighbour tests, [4] row probes
@@ -226,10 +226,11 @@ __global__ void __launch_bounds__(kLaneWarps * 32) k_lane_paths(const LaneArgs a
             }
             if (my != ~0ull) {
                 wid[s] = a.w_begin + my;
-                v[s] = walker_start(a.start_mode, a.start_map, a.sources, a.n, a.n_sources, a.key0, a.key1,
-                                    wid[s]);
+                const uint32_t si = walker_start_index(a.start_mode, a.int2idx, a.sources, a.n, a.n_sources,
+                                                       a.key0, a.key1, wid[s]);
                 // {id, first column, degree, name}
-                const uint4 vx = ld_hint_u4(&a.vtx_ext[PTW_IDX(v[s], a.n, &a.ctrl[7], kCheckRecord)], pol_keep);
+                const uint4 vx = ld_hint_u4(&a.vtx_ext[PTW_IDX(si, a.n, &a.ctrl[7], kCheckRecord)], pol_keep);
+                v[s] = vx.x;
                 rec[s] = make_uint2(vx.y, vx.z);
                 vname[s] = vx.w;
                 stage[wib][s][lane][0] = (int32_t)vx.w;
@@ -480,7 +481,7 @@ LaneArgs lane_args(ptw_graph *g, uint64_t w_begin, uint64_t w_end, uint32_t L, u
     a.col_ext = dg.col_ext;
     a.filter = dg.edge_filter;
     a.filter_blocks = dg.filter_blocks;
-    a.start_map = dg.idx2int;
+    a.int2idx = dg.int2idx;
     a.sources = g->sc.sources;
     a.paths = paths;
     a.ctrl = g->sc.ctrl;

@@ -129,6 +129,21 @@ __device__ __forceinline__ uint32_t walker_start(int start_mode, const uint32_t 
     return sources[__umulhi(r.x, n_sources)];
 }
 
+// The same start as walker_start, as a canonical index (name rank): the
+// index into vertex tables kept in name order (vtx_ext).  Consecutive
+// walkers of PTW_START_PER_VERTEX then read consecutive records, and the
+// per-vertex and uniform modes need no index-to-id lookup.
+__device__ __forceinline__ uint32_t walker_start_index(int start_mode, const uint32_t *int2idx,
+                                                       const uint32_t *sources, uint32_t n, uint32_t n_sources,
+                                                       uint32_t key0, uint32_t key1, uint64_t wid)
+{
+    if (start_mode == PTW_START_PER_VERTEX) return wid < n ? (uint32_t)wid : (uint32_t)(wid % n);
+    if (start_mode == PTW_START_SOURCES && n_sources == 1) return int2idx[sources[0]];
+    const uint4 r = philox(make_uint4((uint32_t)wid, (uint32_t)(wid >> 32), 0u, PTW_TAG_START), key0, key1);
+    if (start_mode == PTW_START_UNIFORM) return __umulhi(r.x, n);
+    return int2idx[sources[__umulhi(r.x, n_sources)]];
+}
+
 // Index checks of the checked build (nvcc -DPTW_CHECKED; libptw built by
 // ptwalker_gb300._build.build_checked): an index at or above its bound sets
 // bit `site` of the graph's check word (scratch ctrl[7]) and is replaced by
@@ -238,7 +253,7 @@ struct DeviceGraph {
     uint2 *col_named = nullptr;   // [m] {neighbour internal id, its name}; built on first path walk
     uint4 *col_ext = nullptr;     // [m] {neighbour id, its first column, its degree, its name};
                                   // built on the first walk with tune.ext_columns
-    uint4 *vtx_ext = nullptr;     // [n] {id, first column, degree, name}, built with col_ext
+    uint4 *vtx_ext = nullptr;     // [n] {id, first column, degree, name} by canonical index, built with col_ext
     uint32_t *edge_filter = nullptr; // blocked Bloom filter of the directed edges (u, v): blocks of
                                      // 8 words; built on the first node2vec walk
     uint64_t filter_blocks = 0;      // a power of two

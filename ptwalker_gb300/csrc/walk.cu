@@ -42,8 +42,9 @@ struct WalkArgs {
     const uint2 *__restrict__ adj;
     const uint32_t *__restrict__ col;
     const uint4 *__restrict__ col_ext;       // EXT: {id, first column, degree, name} per entry
-    const uint4 *__restrict__ vtx_ext;       // {id, first column, degree, name} per vertex
+    const uint4 *__restrict__ vtx_ext;       // {id, first column, degree, name} by canonical index
     const uint32_t *__restrict__ start_map;  // canonical index -> internal
+    const uint32_t *__restrict__ int2idx;    // internal -> canonical index
     const uint32_t *__restrict__ sources;    // internal ids
     const uint32_t *__restrict__ int2name;
     uint32_t *__restrict__ counts;
@@ -67,6 +68,11 @@ struct WalkArgs {
 __device__ __forceinline__ uint32_t start_vertex(const WalkArgs &a, uint64_t wid)
 {
     return walker_start(a.start_mode, a.start_map, a.sources, a.n, a.n_sources, a.key0, a.key1, wid);
+}
+
+__device__ __forceinline__ uint32_t start_index(const WalkArgs &a, uint64_t wid)
+{
+    return walker_start_index(a.start_mode, a.int2idx, a.sources, a.n, a.n_sources, a.key0, a.key1, wid);
 }
 
 // Counts a visit of internal vertex v (name nm): ids below hot_k in shared
@@ -157,7 +163,9 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
             }
             if (my != ~0ull) {
                 wid[k] = a.w_begin + my;
-                v[k] = start_vertex(a, wid[k]);
+                // EXT count walks by name hold the start's canonical index
+                // until its record is loaded
+                v[k] = EXT && a.by_name ? start_index(a, wid[k]) : start_vertex(a, wid[k]);
                 s0[k] = v[k];
                 step[k] = 0;
                 act[k] = true;
@@ -178,6 +186,7 @@ __device__ __forceinline__ void walk_body(const WalkArgs &a, uint32_t *s_hot)
                 // a walker's first move: its start record, with the start's name
                 // for its start visit
                 const uint4 vx = ld_hint_u4(&a.vtx_ext[PTW_IDX(v[k], a.n, &a.ctrl[7], kCheckRecord)], pol_keep);
+                v[k] = vx.x;
                 rec[k] = make_uint2(vx.y, vx.z);
                 if (!ENDPOINT) count_visit<HOT>(a, s_hot, v[k], vx.w, pol_keep);
             } else {
@@ -369,7 +378,7 @@ __global__ void __launch_bounds__(256) k_walk_async(const WalkArgs a)
                 wid[i] = w;
                 step[i] = 0;
                 flag[i] = kSlotActive | kSlotStart;
-                cp_async16(&land[i], &a.vtx_ext[start_vertex(a, w)], pol_keep);
+                cp_async16(&land[i], &a.vtx_ext[PTW_IDX(start_index(a, w), a.n, &a.ctrl[7], kCheckRecord)], pol_keep);
             }
         }
         bool any = false;
@@ -589,11 +598,14 @@ __global__ void k_ext_columns(const uint32_t *col, const uint2 *adj, const uint3
     }
 }
 
-__global__ void k_vertex_ext(const uint2 *adj, const uint32_t *int2name, uint32_t n, uint4 *vtx_ext)
+// The vertex records in canonical order (by name rank).
+__global__ void k_vertex_ext(const uint2 *adj, const uint32_t *int2name, const uint32_t *idx2int, uint32_t n,
+                             uint4 *vtx_ext)
 {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t v = idx2int[i];
         const uint2 r = adj[v];
-        vtx_ext[v] = make_uint4(v, r.x, r.y, int2name[v]);
+        vtx_ext[i] = make_uint4(v, r.x, r.y, int2name[v]);
     }
 }
 
@@ -694,7 +706,7 @@ bool ensure_ext_columns(ptw_graph *g)
         return false;
     }
     const unsigned vgrid = (unsigned)std::min<uint64_t>((dg.n + 255) / 256, (uint64_t)g->num_sms * 64);
-    k_vertex_ext<<<std::max(vgrid, 1u), 256, 0, g->stream>>>(dg.adj, dg.int2name, dg.n, vx);
+    k_vertex_ext<<<std::max(vgrid, 1u), 256, 0, g->stream>>>(dg.adj, dg.int2name, dg.idx2int, dg.n, vx);
     if (cudaGetLastError() != cudaSuccess) {
         cudaFree(cx);
         cudaFree(vx);
@@ -761,6 +773,7 @@ int launch_walk(ptw_graph *g, const WalkLaunch &wl, const ptw_tune &t)
     a.adj = dg.adj;
     a.col = dg.col;
     a.start_map = dg.idx2int;
+    a.int2idx = dg.int2idx;
     a.sources = g->sc.sources;
     a.int2name = dg.int2name;
     a.counts = g->sc.counts;
