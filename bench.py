@@ -272,7 +272,7 @@ def degree_sources(G, n, seed):
 # ncu dram__bytes_read.sum + dram__bytes_write.sum over two launches of each
 # launch configuration, divided by the moves of a launch (one-pass capture
 # of the full-size bench command; profiles/k_walk_dram_bytes_rmat-s24.md).
-TRAFFIC_PER_MOVE_S24 = {True: 128.0, False: 130.1}  # extended columns (counting by name) / plain columns
+TRAFFIC_PER_MOVE_S24 = {True: 127.0, False: 130.1}  # extended columns (counting by name) / plain columns
 TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per move of k_walk at R-MAT scale 24 "
                   "(two launches of the %s-column configuration, profiles/k_walk_dram_bytes_rmat-s24.md), "
                   "times this run's moves per launch")
